@@ -1,0 +1,335 @@
+/*
+ * vfd_dfsph.h -- C-ABI of the GB300-native DFSPH simulation step.
+ *
+ * This is the drop-in boundary for VFD's DFSPH solver API. Each entry point
+ * names the reference interface it replaces (paths are relative to the VFD
+ * source tree, VFD/Source/...). Signatures use plain C types only: no CUDA,
+ * torch or C++ types cross this boundary.
+ *
+ * Threading: one handle per host thread; calls on a handle are synchronous
+ * with respect to the host unless the name says otherwise (vfd_steps_async).
+ * Errors: every call returns a VFD_* status code. The library never exits,
+ * traps or hangs; vfd_last_error() returns a message for the calling thread.
+ *
+ * Particle order: every host-side array passed in or out is in the caller's
+ * original particle order (the order given to vfd_set_fluid), which is the
+ * reference's particle index. Internally particles are kept sorted by cell.
+ */
+#ifndef VFD_DFSPH_H
+#define VFD_DFSPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VFD_ABI_VERSION 1
+
+/* Status codes (replace COMPUTE_SAFE -> exit(), Debug/Debug.h:107). */
+enum {
+    VFD_OK = 0,
+    VFD_E_ARG = 1,           /* invalid argument or handle                  */
+    VFD_E_CUDA = 2,          /* a CUDA runtime call failed                   */
+    VFD_E_NONCONVERGED = 3,  /* a solver hit its iteration cap (flag only)   */
+    VFD_E_NAN = 4,           /* non-finite particle state detected           */
+    VFD_E_CAPACITY = 5,      /* grid or buffer capacity exceeded             */
+    VFD_E_STATE = 6,         /* call not valid in the current state          */
+    VFD_E_NOMEM = 7,         /* device or host allocation failed             */
+    VFD_E_NODEVICE = 8       /* no CUDA device                               */
+};
+
+/* Bits of vfd_step_stats.Flags. */
+#define VFD_FLAG_PRESSURE_CAP    0x1u  /* pressure solve stopped at its max iterations   */
+#define VFD_FLAG_DIVERGENCE_CAP  0x2u  /* divergence solve stopped at its max iterations */
+#define VFD_FLAG_VISCOSITY_CAP   0x4u  /* viscosity CG stopped at its max iterations     */
+#define VFD_FLAG_NEIGHBOR_CAP    0x8u  /* some particle reached the 70-neighbour cap     */
+#define VFD_FLAG_NAN             0x10u /* non-finite position or velocity                */
+#define VFD_FLAG_GRID_CAPACITY   0x20u /* search grid larger than the cell table         */
+
+/* Maximum neighbours per particle, ParticleSearchKernels.cuh:7 (CUDA_MAX_NEIGHBORS). */
+#define VFD_MAX_NEIGHBORS 70u
+
+/*
+ * User parameters. Field for field the reference's DFSPHSimulationDescription
+ * (Simulation/DFSPH/Structures/DFSPHSimulationDescription.h:9-49), with bool
+ * fields widened to int32 so the layout is plain C.
+ */
+typedef struct vfd_desc {
+    float TimeStepSize;
+    float MinTimeStepSize;
+    float MaxTimeStepSize;
+    float FrameLength;
+    uint32_t FrameCount;
+
+    uint32_t MinPressureSolverIterations;
+    uint32_t MaxPressureSolverIterations;
+    float MaxPressureSolverError;          /* [%] of rest density x 100 */
+
+    int32_t EnableDivergenceSolverError;
+    uint32_t MinDivergenceSolverIterations;
+    uint32_t MaxDivergenceSolverIterations;
+    float MaxDivergenceSolverError;
+
+    int32_t EnableViscositySolver;
+    uint32_t MinViscositySolverIterations;
+    uint32_t MaxViscositySolverIterations;
+    float MaxViscositySolverError;
+    float Viscosity;                       /* kinematic; dynamic = Viscosity * 1000 */
+    float BoundaryViscosity;
+    float TangentialDistanceFactor;
+
+    int32_t EnableSurfaceTensionSolver;
+    uint32_t SurfaceTensionSmoothPassCount;
+    float SurfaceTension;
+    int32_t TemporalSmoothing;
+    int32_t CSDFix;                        /* sample count per step, <= 0 = use CSD */
+    int32_t CSD;                           /* sample count per particle per second  */
+
+    float ParticleRadius;
+    float Gravity[3];
+} vfd_desc;
+
+/*
+ * A rigid body's volume map, in the reference's SDFDeviceData layout
+ * (Utility/SDF/SDFDeviceData.cuh:549-566): field 0 is the signed distance,
+ * field 1 the boundary volume; cells hold 32 node indices per cell (cubic
+ * serendipity element). Arrays are host memory and are copied by the call.
+ */
+typedef struct vfd_volume_map {
+    const float* nodes;        /* field_count * node_count                    */
+    const uint32_t* cells;     /* field_count * cell_count * 32               */
+    const uint32_t* cell_map;  /* field_count * cell_map_count                */
+    float domain_min[3];
+    float domain_max[3];
+    uint32_t resolution[3];
+    float cell_size[3];
+    float cell_size_inverse[3];
+    uint32_t field_count;
+    uint32_t node_count;
+    uint32_t cell_count;
+    uint32_t cell_map_count;
+} vfd_volume_map;
+
+/*
+ * Per-step solver statistics: DFSPHDebugInfo (Structures/DFSPHDebugInfo.h:8-28)
+ * without the wall-clock timers, plus the step size and search figures.
+ */
+typedef struct vfd_step_stats {
+    uint32_t IterationCount;
+    uint32_t DivergenceSolverIterationCount;
+    uint32_t PressureSolverIterationCount;
+    uint32_t ViscositySolverIterationCount;
+    float DivergenceSolverError;
+    float PressureSolverError;
+    float ViscositySolverError;
+    float FrameTime;
+    uint32_t FrameIndex;
+    float TimeStepSize;          /* dt used by the pressure solve of the step   */
+    float MaxVelocityMagnitude;  /* squared, as GetMaxVelocityMagnitude()        */
+    uint32_t MaxNeighborCount;
+    uint32_t Flags;              /* VFD_FLAG_* of the step                        */
+    uint32_t SurfaceTensionSampleCount;
+} vfd_step_stats;
+
+/* Derived constants: DFSPHSimulationInfo (Structures/DFSPHSimulationInfo.h:5-44). */
+typedef struct vfd_info {
+    uint32_t ParticleCount;
+    uint32_t RigidBodyCount;
+    float SupportRadius;
+    float SupportRadius2;
+    float ParticleRadius;
+    float ParticleDiameter;
+    float TimeStepSize;
+    float TimeStepSize2;
+    float TimeStepSizeInverse;
+    float TimeStepSize2Inverse;
+    float Volume;
+    float Density0;
+    float ParticleMass;
+    float ParticleMassInverse;
+    float Viscosity;
+    float BoundaryViscosity;
+    float DynamicViscosity;
+    float DynamicBoundaryViscosity;
+    float TangentialDistanceFactor;
+    float TangentialDistance;
+    float SurfaceTension;
+    uint32_t SurfaceTensionSampleCount;
+    float ClassifierSlope;
+    float ClassifierConstant;
+    int32_t TemporalSmoothing;
+    float SmoothingFactor;
+    float Factor;
+    float NeighborParticleRadius;
+    float MonteCarloFactor;
+    float Gravity[3];
+} vfd_info;
+
+/* Per-particle fields readable with vfd_get_field (DFSPHParticle, Structures/DFSPHParticle.h:8-33). */
+enum {
+    VFD_FIELD_DENSITY = 0,              /* float    */
+    VFD_FIELD_FACTOR = 1,               /* float    */
+    VFD_FIELD_DENSITY_ADVECTION = 2,    /* float    */
+    VFD_FIELD_PRESSURE_RHO2 = 3,        /* float    */
+    VFD_FIELD_PRESSURE_RHO2_V = 4,      /* float    */
+    VFD_FIELD_PRESSURE_RESIDUUM = 5,    /* float    */
+    VFD_FIELD_PRESSURE_ACCELERATION = 6,/* float[3] */
+    VFD_FIELD_VELOCITY_DIFFERENCE = 7,  /* float[3] */
+    VFD_FIELD_SURFACE_NORMAL = 8,       /* float[3] MonteCarloSurfaceNormal       */
+    VFD_FIELD_SURFACE_CURVATURE = 9,    /* float    MonteCarloSurfaceCurvature    */
+    VFD_FIELD_DELTA_FINAL_CURVATURE = 10,/* float   */
+    VFD_FIELD_BOUNDARY_XJ = 11,         /* float[3] of rigid body `body`          */
+    VFD_FIELD_BOUNDARY_VOLUME = 12,     /* float    of rigid body `body`          */
+    VFD_FIELD_SURFACE_NORMAL_SMOOTH = 13,   /* float[3] */
+    VFD_FIELD_SURFACE_CURVATURE_SMOOTH = 14 /* float    */
+};
+
+typedef struct vfd_sim vfd_sim;
+
+/* Fill `desc` with the reference defaults (DFSPHSimulationDescription.h:11-48). */
+int vfd_desc_default(vfd_desc* desc);
+
+/* DFSPHSimulation::DFSPHSimulation (DFSPHSimulator.cpp:10-18): device check + construct. */
+int vfd_create(const vfd_desc* desc, vfd_sim** out);
+
+/* DFSPHImplementation::~DFSPHImplementation (DFSPHImplementation.cu:23-31). */
+int vfd_destroy(vfd_sim* sim);
+
+/* DFSPHSimulation::SetDescription -> DFSPHImplementation::SetDescription (DFSPHImplementation.cu:318-368). */
+int vfd_set_description(vfd_sim* sim, const vfd_desc* desc);
+
+/* DFSPHSimulation::GetDescription (DFSPHSimulator.cpp:72-75). */
+int vfd_get_description(const vfd_sim* sim, vfd_desc* desc);
+
+/*
+ * DFSPHImplementation::SetFluidObjects (DFSPHImplementation.cu:172-253): the
+ * concatenated positions (xyz, n*3 floats) and velocities (n*3 floats, may be
+ * NULL = zero) of all fluid objects become the initial state.
+ */
+int vfd_set_fluid(vfd_sim* sim, const float* xyz, const float* vel, uint32_t n);
+
+/*
+ * DFSPHImplementation::SetRigidBodies (DFSPHImplementation.cu:255-271), one
+ * body per call, in the reference's order. Call after vfd_set_fluid.
+ */
+int vfd_add_rigid_body(vfd_sim* sim, const vfd_volume_map* map);
+
+/* Removes all rigid bodies (SetRigidBodies with an empty vector). */
+int vfd_clear_rigid_bodies(vfd_sim* sim);
+
+/*
+ * Builds the volume map of an axis-aligned box on the GPU, the work of
+ * RigidBody::RigidBody (RigidBody.cu:10-72) for a box mesh: distance field
+ * sign*(sd - (padding - r)) and the 16^3-point Gauss-Legendre volume field.
+ * Outputs go to caller buffers sized by vfd_box_map_sizes.
+ */
+int vfd_box_map_sizes(const uint32_t resolution[3], uint32_t* node_count, uint32_t* cell_count);
+int vfd_build_box_map(const float box_min[3], const float box_max[3], int32_t inverted,
+                      float padding, const uint32_t resolution[3], float particle_radius,
+                      float* nodes, uint32_t* cells, uint32_t* cell_map, vfd_volume_map* map_out);
+
+/*
+ * DFSPHImplementation::Simulate (DFSPHImplementation.cu:33-61) preamble:
+ * re-uploads the initial particles, resets dt, frame time and counters.
+ */
+int vfd_reset(vfd_sim* sim);
+
+/* DFSPHImplementation::OnUpdate (DFSPHImplementation.cu:63-170): one step. stats may be NULL. */
+int vfd_step(vfd_sim* sim, vfd_step_stats* stats);
+
+/*
+ * `count` OnUpdate steps launched back to back without host synchronisation
+ * between them; waits for the last one. stats (may be NULL) is the last step's.
+ */
+int vfd_steps(vfd_sim* sim, uint32_t count, vfd_step_stats* stats);
+
+/* Same as vfd_steps but returns without waiting; vfd_synchronize waits. */
+int vfd_steps_async(vfd_sim* sim, uint32_t count);
+int vfd_synchronize(vfd_sim* sim, vfd_step_stats* stats);
+
+/* Frame callback for vfd_simulate: x, v, a are n*3 floats in original order. */
+typedef void (*vfd_frame_callback)(uint32_t frame_index, uint32_t n, const float* x,
+                                   const float* v, const float* a, float max_velocity,
+                                   float time_step, void* user);
+
+/*
+ * DFSPHImplementation::Simulate (DFSPHImplementation.cu:33-61) with the frame
+ * capture of OnUpdate (:148-167): resets, then steps until FrameCount frames
+ * were emitted; each frame is handed to `cb` (may be NULL).
+ */
+int vfd_simulate(vfd_sim* sim, vfd_frame_callback cb, void* user);
+
+/*
+ * ConvertParticlesToBuffer (DFSPHKernels.cu:6-22) + the frame D2H copy
+ * (DFSPHImplementation.cu:156-162): positions, velocities, accelerations in
+ * original order; any pointer may be NULL.
+ */
+int vfd_get_state(vfd_sim* sim, float* x, float* v, float* a);
+
+/* Overwrites positions and velocities (original order; vel may be NULL) of the running state. */
+int vfd_set_state(vfd_sim* sim, const float* x, const float* v);
+
+/* One per-particle field (VFD_FIELD_*) of the last step, original order. */
+int vfd_get_field(vfd_sim* sim, int32_t field, uint32_t body, float* out);
+
+/* ParticleSearch::FindNeighbors (ParticleSearch.h:80-93) on the current positions, without stepping. */
+int vfd_find_neighbors(vfd_sim* sim);
+
+/*
+ * The last neighbour search (NeighborSet, NeighborSet.h:8-28, and
+ * ParticleSearch::GetSortIndices, ParticleSearch.h:76-78), in the reference's
+ * index space: counts[n], offsets[n] (exclusive scan), list[capacity]
+ * (original indices, CSR), sort_indices[n] (sorted slot -> original index),
+ * cell_keys[n] (Morton meta-grid cell of each particle). *total receives the
+ * list length; VFD_E_CAPACITY if it exceeds `capacity`. Pointers may be NULL.
+ */
+int vfd_get_neighbors(vfd_sim* sim, uint32_t* counts, uint32_t* offsets, uint32_t* list,
+                      uint32_t capacity, uint32_t* total, uint32_t* sort_indices,
+                      uint32_t* cell_keys);
+
+/* Getters of DFSPHSimulation (DFSPHSimulator.h:24-37). */
+int vfd_get_info(const vfd_sim* sim, vfd_info* info);
+int vfd_get_particle_count(const vfd_sim* sim, uint32_t* n);
+int vfd_get_current_time_step_size(vfd_sim* sim, float* dt);
+int vfd_get_max_velocity_magnitude(vfd_sim* sim, float* v2);
+int vfd_get_debug_info(vfd_sim* sim, vfd_step_stats* stats);
+
+/*
+ * The SPH kernel table (PrecomputedDFSPHCubicKernel, Kernel/DFSPHKernels.h:8-143):
+ * w[10000] and grad_w[10001] as built by SetRadius(4r), plus radius and W(0).
+ */
+int vfd_get_kernel_table(const vfd_sim* sim, float* w, float* grad_w, float* radius, float* w_zero);
+
+/*
+ * Solver execution mode: 1 (default) = the whole step is one CUDA graph with
+ * device-side while loops for the three solvers; 0 = kernels launched from the
+ * host with one flag read per solver iteration (the reference's control flow).
+ */
+int vfd_set_graph_mode(vfd_sim* sim, int32_t enabled);
+
+/* Batched scenes: independent scenes advanced together, one launch per stage.
+ * vfd_create_batch takes one description per scene (same ParticleRadius for all);
+ * scene-scoped calls address one scene. The plain calls act on scene 0. */
+int vfd_create_batch(const vfd_desc* descs, uint32_t scene_count, vfd_sim** out);
+int vfd_get_scene_count(const vfd_sim* sim, uint32_t* scenes);
+int vfd_scene_set_fluid(vfd_sim* sim, uint32_t scene, const float* xyz, const float* vel, uint32_t n);
+int vfd_scene_add_rigid_body(vfd_sim* sim, uint32_t scene, const vfd_volume_map* map);
+int vfd_scene_get_state(vfd_sim* sim, uint32_t scene, float* x, float* v, float* a);
+int vfd_scene_get_stats(vfd_sim* sim, uint32_t scene, vfd_step_stats* stats);
+
+/* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
+int vfd_set_device(int32_t device);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* vfd_last_error(void);
+
+/* VFD_ABI_VERSION of the loaded library. */
+int vfd_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VFD_DFSPH_H */

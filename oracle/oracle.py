@@ -1,0 +1,260 @@
+"""ctypes wrapper of the CPU oracle (oracle/dfsph_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: tests, __graft_entry__.smoke() and bench.py's CPU
+baseline use it as the checker and the timed CPU restatement of the
+reference's DFSPH step. The product (vfd_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+from vfd_gb300 import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libvfd_oracle.so")
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (seconds)."""
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+            os.path.getmtime(os.path.join(HERE, "dfsph_oracle.cpp")),
+            os.path.getmtime(os.path.join(HERE, "..", "include", "vfd_dfsph.h"))):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(LIB_PATH)
+            P = C.c_void_p
+            u32p = C.POINTER(C.c_uint32)
+            f32p = C.POINTER(C.c_float)
+            f64p = C.POINTER(C.c_double)
+            L.orc_create.restype = P
+            L.orc_create.argtypes = [C.POINTER(_abi.vfd_desc), C.c_int]
+            L.orc_destroy.argtypes = [P]
+            L.orc_set_fluid.argtypes = [P, f32p, f32p, C.c_uint32]
+            L.orc_add_rigid_body.argtypes = [P, C.POINTER(_abi.vfd_volume_map)]
+            L.orc_reset.argtypes = [P]
+            L.orc_step.argtypes = [P, C.POINTER(_abi.vfd_step_stats)]
+            L.orc_find_neighbors.argtypes = [P]
+            L.orc_get_neighbors.argtypes = [P, u32p, u32p, u32p, C.c_uint32, u32p, u32p, u32p]
+            L.orc_get_state.argtypes = [P, f64p, f64p, f64p]
+            L.orc_get_field.argtypes = [P, C.c_int, C.c_uint32, f64p]
+            L.orc_get_time_step.argtypes = [P, f64p]
+            L.orc_kernel_table.argtypes = [C.c_float, f32p, f32p, f32p]
+            L.orc_halton.argtypes = [f32p]
+            L.orc_morton3.restype = C.c_uint32
+            L.orc_morton3.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+            L.orc_box_map_sizes.argtypes = [u32p, u32p, u32p]
+            L.orc_build_box_map.argtypes = [f32p, f32p, C.c_int, C.c_float, u32p, C.c_float, f32p, u32p, u32p,
+                                            C.POINTER(_abi.vfd_volume_map)]
+            L.orc_map_interpolate.argtypes = [C.POINTER(_abi.vfd_volume_map), C.c_uint32, f32p, C.c_uint32, f64p,
+                                              f64p]
+            L.orc_set_threads.argtypes = [C.c_int]
+            L.orc_get_threads.restype = C.c_int
+            _lib = L
+    return _lib
+
+
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype)) if a is not None else None
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().orc_get_threads())
+
+
+def kernel_table(radius: float):
+    w = np.zeros(10000, np.float32)
+    g = np.zeros(10001, np.float32)
+    wz = C.c_float()
+    lib().orc_kernel_table(C.c_float(radius), _ptr(w, C.c_float), _ptr(g, C.c_float), C.byref(wz))
+    return w, g, wz.value
+
+
+def halton() -> np.ndarray:
+    out = np.zeros(49152, np.float32)
+    lib().orc_halton(_ptr(out, C.c_float))
+    return out
+
+
+def morton3(x: int, y: int, z: int) -> int:
+    return int(lib().orc_morton3(x, y, z))
+
+
+class VolumeMap:
+    """Holds the arrays of a vfd_volume_map alive together with the struct."""
+
+    def __init__(self, nodes, cells, cell_map, struct):
+        self.nodes, self.cells, self.cell_map, self.struct = nodes, cells, cell_map, struct
+
+    @staticmethod
+    def from_arrays(nodes, cells, cell_map, meta) -> "VolumeMap":
+        m = _abi.vfd_volume_map()
+        nodes = np.ascontiguousarray(nodes, np.float32)
+        cells = np.ascontiguousarray(cells, np.uint32)
+        cell_map = np.ascontiguousarray(cell_map, np.uint32)
+        m.nodes = _ptr(nodes, C.c_float)
+        m.cells = _ptr(cells, C.c_uint32)
+        m.cell_map = _ptr(cell_map, C.c_uint32)
+        for k in ("domain_min", "domain_max", "resolution", "cell_size", "cell_size_inverse"):
+            getattr(m, k)[:] = list(meta[k])
+        for k in ("field_count", "node_count", "cell_count", "cell_map_count"):
+            setattr(m, k, int(meta[k]))
+        return VolumeMap(nodes, cells, cell_map, m)
+
+    def meta(self) -> dict:
+        m = self.struct
+        return dict(domain_min=list(m.domain_min), domain_max=list(m.domain_max), resolution=list(m.resolution),
+                    cell_size=list(m.cell_size), cell_size_inverse=list(m.cell_size_inverse),
+                    field_count=m.field_count, node_count=m.node_count, cell_count=m.cell_count,
+                    cell_map_count=m.cell_map_count)
+
+
+def build_box_map(bmin, bmax, inverted: bool, padding: float, resolution, particle_radius: float) -> VolumeMap:
+    res = np.ascontiguousarray(resolution, np.uint32)
+    nn, nc = C.c_uint32(), C.c_uint32()
+    lib().orc_box_map_sizes(_ptr(res, C.c_uint32), C.byref(nn), C.byref(nc))
+    nodes = np.zeros(2 * nn.value, np.float32)
+    cells = np.zeros(2 * nc.value * 32, np.uint32)
+    cell_map = np.zeros(2 * nc.value, np.uint32)
+    m = _abi.vfd_volume_map()
+    bmin_a, _ = _f32(bmin)
+    bmax_a, _ = _f32(bmax)
+    lib().orc_build_box_map(_ptr(bmin_a, C.c_float), _ptr(bmax_a, C.c_float), int(bool(inverted)),
+                            C.c_float(padding), _ptr(res, C.c_uint32), C.c_float(particle_radius),
+                            _ptr(nodes, C.c_float), _ptr(cells, C.c_uint32), _ptr(cell_map, C.c_uint32),
+                            C.byref(m))
+    return VolumeMap(nodes, cells, cell_map, m)
+
+
+def map_interpolate(vmap: VolumeMap, field: int, points):
+    pts, pp = _f32(points)
+    n = len(pts)
+    phi = np.zeros(n, np.float64)
+    grad = np.zeros((n, 3), np.float64)
+    lib().orc_map_interpolate(C.byref(vmap.struct), field, pp, n, _ptr(phi, C.c_double), _ptr(grad, C.c_double))
+    return phi, grad
+
+
+class OracleSim:
+    """The oracle simulator: precision 32 (FP32 mirror) or 64 (FP64 oracle)."""
+
+    def __init__(self, desc: _abi.vfd_desc, precision: int = 64):
+        self._desc = desc
+        self.precision = precision
+        self.h = lib().orc_create(C.byref(desc), precision)
+        if not self.h:
+            raise ValueError("orc_create failed")
+        self.n = 0
+        self._maps = []
+
+    def close(self):
+        if self.h:
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_fluid(self, x, v=None):
+        xa, xp = _f32(x)
+        if v is not None:
+            va, vp = _f32(v)
+        else:
+            vp = None
+        self.n = len(xa)
+        lib().orc_set_fluid(self.h, xp, vp, self.n)
+
+    def add_rigid_body(self, vmap: VolumeMap):
+        self._maps.append(vmap)
+        rc = lib().orc_add_rigid_body(self.h, C.byref(vmap.struct))
+        if rc != 0:
+            raise RuntimeError(f"orc_add_rigid_body -> {rc}")
+
+    def reset(self):
+        lib().orc_reset(self.h)
+
+    def step(self) -> dict:
+        st = _abi.vfd_step_stats()
+        lib().orc_step(self.h, C.byref(st))
+        return st.as_dict()
+
+    def find_neighbors(self):
+        lib().orc_find_neighbors(self.h)
+
+    def neighbors(self) -> dict:
+        n = self.n
+        counts = np.zeros(n, np.uint32)
+        offsets = np.zeros(n, np.uint32)
+        sort_idx = np.zeros(n, np.uint32)
+        keys = np.zeros(n, np.uint32)
+        total = C.c_uint32()
+        lib().orc_get_neighbors(self.h, _ptr(counts, C.c_uint32), _ptr(offsets, C.c_uint32), None, 0,
+                                C.byref(total), _ptr(sort_idx, C.c_uint32), _ptr(keys, C.c_uint32))
+        lst = np.zeros(max(1, total.value), np.uint32)
+        lib().orc_get_neighbors(self.h, None, None, _ptr(lst, C.c_uint32), total.value, C.byref(total), None, None)
+        return dict(counts=counts, offsets=offsets, list=lst[:total.value], sort_indices=sort_idx, cell_keys=keys)
+
+    def state(self):
+        n = self.n
+        x = np.zeros((n, 3), np.float64)
+        v = np.zeros((n, 3), np.float64)
+        a = np.zeros((n, 3), np.float64)
+        lib().orc_get_state(self.h, _ptr(x, C.c_double), _ptr(v, C.c_double), _ptr(a, C.c_double))
+        return x, v, a
+
+    def field(self, field: int, body: int = 0) -> np.ndarray:
+        n = self.n
+        shape = (n, 3) if field in _abi.VECTOR_FIELDS else (n,)
+        out = np.zeros(shape, np.float64)
+        rc = lib().orc_get_field(self.h, field, body, _ptr(out, C.c_double))
+        if rc != 0:
+            raise ValueError(f"orc_get_field({field}) -> {rc}")
+        return out
+
+    def time_step(self) -> float:
+        d = C.c_double()
+        lib().orc_get_time_step(self.h, C.byref(d))
+        return d.value
+
+
+def scene_oracle(scene: dict, precision: int = 64, desc_overrides: dict | None = None,
+                 maps: list | None = None) -> OracleSim:
+    """An OracleSim loaded with a vfd_gb300.scenes scene (maps built on the CPU unless given)."""
+    d = dict(scene["desc"])
+    if desc_overrides:
+        d.update(desc_overrides)
+    sim = OracleSim(_abi.make_desc(**d), precision)
+    sim.set_fluid(scene["x"], scene["v"])
+    if maps is None:
+        r = d["ParticleRadius"]
+        maps = [build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"], r)
+                for b in scene["boxes"]]
+    for m in maps:
+        sim.add_rigid_body(m)
+    return sim
