@@ -207,7 +207,8 @@ struct KernelTable {
 // ---------------------------------------------------------------------------
 // Surface-tension directions, HaltonVec323.cuh:4: point i of 16384 is
 // (sqrt(1-z^2) cos 2 pi h2(i), sqrt(1-z^2) sin 2 pi h2(i), z = 1 - 2 h3(i)),
-// h_b the radical inverse in base b.
+// h_b the radical inverse in base b; the reference lists the values with 15
+// decimals, so each is rounded to 15 decimals before the float conversion.
 static double radical_inverse(unsigned i, unsigned b) {
     double inv = 1.0 / b, f = inv, r = 0.0;
     while (i > 0) { r += f * (double)(i % b); i /= b; f *= inv; }
@@ -219,9 +220,8 @@ static void halton_table(float* out) {
         const double z = 1.0 - 2.0 * radical_inverse(i, 3);
         const double phi = 2.0 * kPI * radical_inverse(i, 2);
         const double s = std::sqrt(std::max(0.0, 1.0 - z * z));
-        out[3 * i + 0] = (float)(s * std::cos(phi));
-        out[3 * i + 1] = (float)(s * std::sin(phi));
-        out[3 * i + 2] = (float)z;
+        const double v[3] = {s * std::cos(phi), s * std::sin(phi), z};
+        for (int k = 0; k < 3; k++) out[3 * i + k] = (float)(std::nearbyint(v[k] * 1e15) / 1e15 + 0.0);  // +0.0: no negative zeros
     }
 }
 
@@ -495,6 +495,15 @@ static void gauss_legendre(unsigned n, std::vector<double>& x, std::vector<doubl
             z -= dz;
             if (std::fabs(dz) < 1e-17) break;
         }
+        {  // P_n' at the converged root
+            double p0 = 1.0, p1 = z;
+            for (unsigned k = 2; k <= n; k++) {
+                const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+        }
         x[n - 1 - i] = z;  // ascending order
         w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
     }
@@ -763,7 +772,7 @@ struct Sim {
     void update_samples() {
         if (desc.CSDFix > 0) info.stSamples = (uint32_t)desc.CSDFix;
         else info.stSamples = (uint32_t)(int)((T)desc.CSD * info.dt);
-        info.mcFactor = (T)std::asin((double)(info.nbrRadius / info.r));
+        info.mcFactor = std::asin(info.nbrRadius / info.r);
     }
 
     uint32_t nbrCount(uint32_t i) const { return search.counts[i]; }
@@ -1561,6 +1570,29 @@ int orc_map_interpolate(const vfd_volume_map* mp, uint32_t field, const float* x
         }
         phi[i] = interpolate_grad(m, field, cell, c0, N, g, dN);
         if (grad) { grad[3 * i] = g.x; grad[3 * i + 1] = g.y; grad[3 * i + 2] = g.z; }
+    }
+    return VFD_OK;
+}
+
+// n-point Gauss-Legendre abscissae and weights on [-1, 1] (ascending).
+int orc_gauss_legendre(unsigned n, double* x, double* w) {
+    std::vector<double> a, b;
+    gauss_legendre(n, a, b);
+    std::copy(a.begin(), a.end(), x);
+    std::copy(b.begin(), b.end(), w);
+    return VFD_OK;
+}
+
+// Positions of all nodes of a map (SDF::IndexToNodePosition) into out[3 * node_count].
+int orc_map_node_positions(const vfd_volume_map* mp, float* out) {
+    MapData m;
+    for (int k = 0; k < 3; k++) {
+        m.dmin[k] = mp->domain_min[k]; m.dmax[k] = mp->domain_max[k]; m.res[k] = mp->resolution[k];
+        m.cs[k] = mp->cell_size[k]; m.csi[k] = mp->cell_size_inverse[k];
+    }
+    for (uint32_t i = 0; i < mp->node_count; i++) {
+        const V3<float> p = node_position(m, i);
+        out[3 * i] = p.x; out[3 * i + 1] = p.y; out[3 * i + 2] = p.z;
     }
     return VFD_OK;
 }

@@ -62,6 +62,8 @@ def lib():
                                             C.POINTER(_abi.vfd_volume_map)]
             L.orc_map_interpolate.argtypes = [C.POINTER(_abi.vfd_volume_map), C.c_uint32, f32p, C.c_uint32, f64p,
                                               f64p]
+            L.orc_gauss_legendre.argtypes = [C.c_uint, f64p, f64p]
+            L.orc_map_node_positions.argtypes = [C.POINTER(_abi.vfd_volume_map), f32p]
             L.orc_set_threads.argtypes = [C.c_int]
             L.orc_get_threads.restype = C.c_int
             _lib = L
@@ -96,6 +98,19 @@ def kernel_table(radius: float):
 def halton() -> np.ndarray:
     out = np.zeros(49152, np.float32)
     lib().orc_halton(_ptr(out, C.c_float))
+    return out
+
+
+def gauss_legendre(n: int):
+    x = np.zeros(n, np.float64)
+    w = np.zeros(n, np.float64)
+    lib().orc_gauss_legendre(n, _ptr(x, C.c_double), _ptr(w, C.c_double))
+    return x, w
+
+
+def map_node_positions(vmap) -> np.ndarray:
+    out = np.zeros((vmap.struct.node_count, 3), np.float32)
+    lib().orc_map_node_positions(C.byref(vmap.struct), _ptr(out, C.c_float))
     return out
 
 

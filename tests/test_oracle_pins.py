@@ -1,0 +1,185 @@
+"""The CPU oracle against the reference's own tables and closed forms.
+
+The reference has no tests or fixtures for the DFSPH path; these pins come
+from its source text (tests/golden/reference_tables.json, generated by
+tests/golden/make_golden.py) and from the closed forms in the source.
+"""
+import hashlib
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from vfd_gb300 import _abi, scenes
+
+
+def test_halton_table_matches_reference(golden):
+    h = O.halton()
+    assert h.size == golden["halton"]["count"]
+    assert hashlib.sha256(h.astype(np.float32).tobytes()).hexdigest() == golden["halton"]["sha256"]
+    idx = golden["halton"]["sample_index"]
+    np.testing.assert_array_equal(h[idx], np.array(golden["halton"]["sample"], np.float32))
+
+
+def test_gauss_legendre_matches_reference(golden):
+    g = golden["gauss_legendre"]
+    x, w = O.gauss_legendre(g["n"])
+    np.testing.assert_allclose(x, g["abscissae"], rtol=0, atol=1e-15)
+    # the reference's weight table carries ~4e-15 errors in its last digits (a
+    # 40-digit evaluation agrees with this generator to 1e-16); the reference
+    # uses the weights as float, where both are the same numbers
+    np.testing.assert_allclose(w, g["weights"], rtol=0, atol=1e-14)
+    np.testing.assert_array_equal(w.astype(np.float32), np.array(g["weights"]).astype(np.float32))
+
+
+def test_description_defaults_match_reference(golden):
+    ref = golden["description_defaults"]
+    for k, v in ref.items():
+        ours = _abi.DEFAULTS[k]
+        if isinstance(v, list):
+            assert list(ours) == pytest.approx(v)
+        else:
+            assert float(ours) == pytest.approx(v), k
+
+
+def test_kernel_table_closed_form():
+    """W(0) = 8 / (pi h^3); table entries equal the cubic spline at r_i = i h / 9999."""
+    r = 0.025
+    h = 4 * r
+    w, g, wz = O.kernel_table(np.float32(h))
+    assert wz == pytest.approx(8.0 / (math.pi * h ** 3), rel=1e-6)
+    q = np.arange(10000) / 9999.0
+    k = 8.0 / (math.pi * h ** 3)
+    ref = np.where(q <= 0.5, k * (6 * q ** 3 - 6 * q ** 2 + 1), k * 2 * (1 - q) ** 3)
+    np.testing.assert_allclose(w, ref, rtol=2e-5, atol=1e-3)
+    # gradient / r: L q (3q - 2) / (r h) below q = 1/2, -L (1-q)^2 / (r h) above
+    L = 48.0 / (math.pi * h ** 3)
+    rr = q * h
+    with np.errstate(divide="ignore", invalid="ignore"):
+        gref = np.where(q <= 0.5, L * q * (3 * q - 2), -L * (1 - q) ** 2) / (rr * h)
+    sel = (rr > 1e-5) & (np.abs(q - 0.5) > 1e-3)
+    # FP32 cancellation in (1 - q)^2 near q = 1: absolute tolerance on the table's scale
+    np.testing.assert_allclose(g[:10000][sel], gref[sel], rtol=5e-5, atol=1e-6 * np.abs(gref[sel]).max())
+    assert g[10000] == 0.0 and g[0] == 0.0
+
+
+def test_morton_keys():
+    assert O.morton3(0, 0, 0) == 0
+    assert O.morton3(1, 0, 0) == 1
+    assert O.morton3(0, 1, 0) == 2
+    assert O.morton3(0, 0, 1) == 4
+    assert O.morton3(7, 7, 7) == 511
+    rng = np.random.default_rng(3)
+    for x, y, z in rng.integers(0, 1024, size=(200, 3)):
+        ref = 0
+        for b in range(10):
+            ref |= ((int(x) >> b) & 1) << (3 * b)
+            ref |= ((int(y) >> b) & 1) << (3 * b + 1)
+            ref |= ((int(z) >> b) & 1) << (3 * b + 2)
+        assert O.morton3(int(x), int(y), int(z)) == ref
+
+
+def test_shape_functions_reproduce_cubics():
+    """The 32-node element with the reference's cell/node layout interpolates any
+    cubic polynomial exactly, which pins node numbering, cell table and positions."""
+    m = O.build_box_map((0, 0, 0), (0.5, 0.4, 0.3), True, 0.0, (5, 4, 3), 0.01)
+    pos = O.map_node_positions(m).astype(np.float64)
+
+    def f(p):
+        x, y, z = p[..., 0], p[..., 1], p[..., 2]
+        return 0.3 + x - 2 * y + 0.5 * z + x * y - z * z + 0.7 * x ** 3 - y * y * z
+
+    def grad(p):
+        x, y, z = p[..., 0], p[..., 1], p[..., 2]
+        return np.stack([1 + y + 2.1 * x ** 2, -2 + x - 2 * y * z, 0.5 - 2 * z - y * y], -1)
+
+    nn = m.struct.node_count
+    nodes = m.nodes.copy()
+    nodes[:nn] = f(pos).astype(np.float32)
+    mm = O.VolumeMap.from_arrays(nodes, m.cells, m.cell_map, m.meta())
+    rng = np.random.default_rng(1)
+    lo, hi = np.array(m.struct.domain_min), np.array(m.struct.domain_max)
+    pts = (lo + rng.random((500, 3)) * (hi - lo)).astype(np.float32)
+    phi, g = O.map_interpolate(mm, 0, pts)
+    np.testing.assert_allclose(phi, f(pts.astype(np.float64)), atol=2e-6)
+    np.testing.assert_allclose(g, grad(pts.astype(np.float64)), atol=5e-5)
+
+
+def _brute_force(x, h):
+    x = x.astype(np.float32)
+    n = len(x)
+    h2 = np.float32(h) * np.float32(h)
+    out = []
+    for i in range(n):
+        d = x - x[i]
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        out.append(set(np.nonzero((d2 < h2) & (d2 > 0))[0].tolist()))
+    return out
+
+
+@pytest.mark.parametrize("n_side", [6, 10])
+def test_neighbor_sets_match_brute_force(n_side):
+    s = scenes.small_dam_break(n_side=n_side, seed=11)
+    sim = O.OracleSim(_abi.make_desc(**s["desc"]), 32)
+    sim.set_fluid(s["x"], s["v"])
+    sim.find_neighbors()
+    nb = sim.neighbors()
+    ref = _brute_force(s["x"], 4 * s["desc"]["ParticleRadius"])
+    for i in range(len(s["x"])):
+        got = nb["list"][nb["offsets"][i]: nb["offsets"][i] + nb["counts"][i]]
+        assert len(got) == len(set(got.tolist()))
+        assert set(got.tolist()) == ref[i]
+
+
+def test_sort_permutation_rules():
+    """Cell keys ascend along the sort; equal keys keep ascending particle index."""
+    s = scenes.dam_break_c1()
+    sim = O.OracleSim(_abi.make_desc(**s["desc"]), 32)
+    sim.set_fluid(s["x"], s["v"])
+    sim.find_neighbors()
+    nb = sim.neighbors()
+    perm, keys = nb["sort_indices"], nb["cell_keys"]
+    assert sorted(perm.tolist()) == list(range(len(perm)))
+    k = keys[perm]
+    assert np.all(np.diff(k.astype(np.int64)) >= 0)
+    same = np.diff(k.astype(np.int64)) == 0
+    assert np.all(np.diff(perm.astype(np.int64))[same] > 0)
+    assert nb["counts"].max() < _abi.MAX_NEIGHBORS
+
+
+def test_fp32_mirror_tracks_fp64_oracle():
+    s = scenes.small_dam_break(n_side=8)
+    b = s["boxes"][0]
+    m = O.build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"], s["desc"]["ParticleRadius"])
+    a = O.scene_oracle(s, 32, maps=[m])
+    c = O.scene_oracle(s, 64, maps=[m])
+    for _ in range(3):
+        sa, sc = a.step(), c.step()
+        assert sa["PressureSolverIterationCount"] == sc["PressureSolverIterationCount"]
+    xa, va, _ = a.state()
+    xc, vc, _ = c.state()
+    h = 4 * s["desc"]["ParticleRadius"]
+    dx = np.abs(xa - xc).max(axis=1)
+    # bulk: rounding only; tail: a few particles on a discrete branch (neighbour
+    # at exactly h, boundary push-out) that FP32 and FP64 decide differently
+    assert np.median(dx) < 1e-6 * h
+    assert dx.max() < 1e-3 * h
+    assert np.median(np.abs(va - vc)) < 1e-5
+    rel = np.abs(a.field(_abi.FIELD_DENSITY) / c.field(_abi.FIELD_DENSITY) - 1.0)
+    assert np.median(rel) < 1e-6 and np.mean(rel < 1e-4) > 0.99 and rel.max() < 1e-2
+
+
+def test_dam_break_stays_bounded():
+    """Physics sanity of the restatement: particles stay in the box, density error
+    at pressure-solve exit within the 0.1 % bound, no solver hits its cap."""
+    s = scenes.dam_break_c1(n_side=10, box_scale=(2, 1, 1))
+    sim = O.scene_oracle(s, 64)
+    for _ in range(30):
+        st = sim.step()
+        assert st["PressureSolverError"] <= 1.0 + 1e-9  # eta = 10 * 1e-4 * rho0
+        assert st["Flags"] == 0
+    x, v, _ = sim.state()
+    box = np.array(s["boxes"][0]["max"])
+    assert np.all(x > -0.05) and np.all(x < box + 0.05)
+    assert np.linalg.norm(v, axis=1).max() < 5.0

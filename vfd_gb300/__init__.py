@@ -1,0 +1,375 @@
+"""vfd_gb300: a GB300-native DFSPH simulation step behind VFD's solver API.
+
+The compute path is the CUDA library libvfd_dfsph.so (include/vfd_dfsph.h),
+loaded through ctypes. This module mirrors the reference's
+vfd::DFSPHSimulation (Simulation/DFSPH/DFSPHSimulator.h:10-58): same method
+names, same argument meaning; errors raise VFDError instead of exiting the
+process. There is no CPU fallback: without the library or a GPU, calls fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import _abi
+from ._abi import make_desc, vfd_desc, vfd_info, vfd_step_stats, vfd_volume_map  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvfd_dfsph.so")
+
+# Every entry point declared in include/vfd_dfsph.h.
+EXPORTS = [
+    "vfd_desc_default", "vfd_create", "vfd_destroy", "vfd_set_description", "vfd_get_description",
+    "vfd_set_fluid", "vfd_add_rigid_body", "vfd_clear_rigid_bodies", "vfd_box_map_sizes", "vfd_build_box_map",
+    "vfd_reset", "vfd_step", "vfd_steps", "vfd_steps_async", "vfd_synchronize", "vfd_simulate",
+    "vfd_get_state", "vfd_set_state", "vfd_get_field", "vfd_find_neighbors", "vfd_get_neighbors",
+    "vfd_get_info", "vfd_get_particle_count", "vfd_get_current_time_step_size", "vfd_get_max_velocity_magnitude",
+    "vfd_get_debug_info", "vfd_get_kernel_table", "vfd_set_graph_mode", "vfd_create_batch",
+    "vfd_get_scene_count", "vfd_scene_set_fluid", "vfd_scene_add_rigid_body", "vfd_scene_get_state",
+    "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version",
+]
+
+
+class VFDError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str):
+        self.code = code
+        super().__init__(f"{where} -> {_abi.STATUS_NAMES.get(code, code)}: {message}")
+
+
+_lock = threading.Lock()
+_lib = None
+
+FRAME_CALLBACK = C.CFUNCTYPE(None, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                             C.POINTER(C.c_float), C.c_float, C.c_float, C.c_void_p)
+
+
+def lib() -> C.CDLL:
+    """The loaded CUDA library; raises if it was not built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(f"{LIB_PATH} is missing: build it with `python -m vfd_gb300.build` "
+                                  "(the DFSPH step has no CPU implementation)")
+            L = C.CDLL(LIB_PATH)
+            P = C.c_void_p
+            u32p, f32p = C.POINTER(C.c_uint32), C.POINTER(C.c_float)
+            sig = {
+                "vfd_desc_default": [C.POINTER(vfd_desc)],
+                "vfd_create": [C.POINTER(vfd_desc), C.POINTER(P)],
+                "vfd_destroy": [P],
+                "vfd_set_description": [P, C.POINTER(vfd_desc)],
+                "vfd_get_description": [P, C.POINTER(vfd_desc)],
+                "vfd_set_fluid": [P, f32p, f32p, C.c_uint32],
+                "vfd_add_rigid_body": [P, C.POINTER(vfd_volume_map)],
+                "vfd_clear_rigid_bodies": [P],
+                "vfd_box_map_sizes": [u32p, u32p, u32p],
+                "vfd_build_box_map": [f32p, f32p, C.c_int32, C.c_float, u32p, C.c_float, f32p, u32p, u32p,
+                                      C.POINTER(vfd_volume_map)],
+                "vfd_reset": [P],
+                "vfd_step": [P, C.POINTER(vfd_step_stats)],
+                "vfd_steps": [P, C.c_uint32, C.POINTER(vfd_step_stats)],
+                "vfd_steps_async": [P, C.c_uint32],
+                "vfd_synchronize": [P, C.POINTER(vfd_step_stats)],
+                "vfd_simulate": [P, FRAME_CALLBACK, C.c_void_p],
+                "vfd_get_state": [P, f32p, f32p, f32p],
+                "vfd_set_state": [P, f32p, f32p],
+                "vfd_get_field": [P, C.c_int32, C.c_uint32, f32p],
+                "vfd_find_neighbors": [P],
+                "vfd_get_neighbors": [P, u32p, u32p, u32p, C.c_uint32, u32p, u32p, u32p],
+                "vfd_get_info": [P, C.POINTER(vfd_info)],
+                "vfd_get_particle_count": [P, u32p],
+                "vfd_get_current_time_step_size": [P, f32p],
+                "vfd_get_max_velocity_magnitude": [P, f32p],
+                "vfd_get_debug_info": [P, C.POINTER(vfd_step_stats)],
+                "vfd_get_kernel_table": [P, f32p, f32p, f32p, f32p],
+                "vfd_set_graph_mode": [P, C.c_int32],
+                "vfd_create_batch": [C.POINTER(vfd_desc), C.c_uint32, C.POINTER(P)],
+                "vfd_get_scene_count": [P, u32p],
+                "vfd_scene_set_fluid": [P, C.c_uint32, f32p, f32p, C.c_uint32],
+                "vfd_scene_add_rigid_body": [P, C.c_uint32, C.POINTER(vfd_volume_map)],
+                "vfd_scene_get_state": [P, C.c_uint32, f32p, f32p, f32p],
+                "vfd_scene_get_stats": [P, C.c_uint32, C.POINTER(vfd_step_stats)],
+                "vfd_set_device": [C.c_int32],
+                "vfd_last_error": [],
+                "vfd_abi_version": [],
+            }
+            for name, args in sig.items():
+                fn = getattr(L, name)
+                fn.argtypes = args
+                fn.restype = C.c_int
+            L.vfd_last_error.restype = C.c_char_p
+            _lib = L
+    return _lib
+
+
+def _check(rc: int, where: str):
+    if rc != _abi.VFD_OK:
+        msg = lib().vfd_last_error()
+        raise VFDError(rc, where, msg.decode() if msg else "")
+
+
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _u32ptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32)) if a is not None else None
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+class VolumeMap:
+    """A rigid body's volume map (SDFDeviceData layout) with its arrays kept alive."""
+
+    def __init__(self, nodes, cells, cell_map, struct: vfd_volume_map):
+        self.nodes, self.cells, self.cell_map, self.struct = nodes, cells, cell_map, struct
+
+    @staticmethod
+    def from_arrays(nodes, cells, cell_map, meta: dict) -> "VolumeMap":
+        nodes = np.ascontiguousarray(nodes, np.float32)
+        cells = np.ascontiguousarray(cells, np.uint32)
+        cell_map = np.ascontiguousarray(cell_map, np.uint32)
+        m = vfd_volume_map()
+        m.nodes = _fptr(nodes)
+        m.cells = _u32ptr(cells)
+        m.cell_map = _u32ptr(cell_map)
+        for k in ("domain_min", "domain_max", "resolution", "cell_size", "cell_size_inverse"):
+            getattr(m, k)[:] = list(meta[k])
+        for k in ("field_count", "node_count", "cell_count", "cell_map_count"):
+            setattr(m, k, int(meta[k]))
+        return VolumeMap(nodes, cells, cell_map, m)
+
+    def meta(self) -> dict:
+        m = self.struct
+        return dict(domain_min=list(m.domain_min), domain_max=list(m.domain_max), resolution=list(m.resolution),
+                    cell_size=list(m.cell_size), cell_size_inverse=list(m.cell_size_inverse),
+                    field_count=m.field_count, node_count=m.node_count, cell_count=m.cell_count,
+                    cell_map_count=m.cell_map_count)
+
+
+def build_box_map(bmin, bmax, inverted: bool, padding: float, resolution, particle_radius: float) -> VolumeMap:
+    """Volume map of an axis-aligned box, built on the GPU (RigidBody::RigidBody for a box mesh)."""
+    res = np.ascontiguousarray(resolution, np.uint32)
+    nn, nc = C.c_uint32(), C.c_uint32()
+    _check(lib().vfd_box_map_sizes(_u32ptr(res), C.byref(nn), C.byref(nc)), "vfd_box_map_sizes")
+    nodes = np.zeros(2 * nn.value, np.float32)
+    cells = np.zeros(2 * nc.value * 32, np.uint32)
+    cell_map = np.zeros(2 * nc.value, np.uint32)
+    m = vfd_volume_map()
+    lo, lop = _f32(bmin)
+    hi, hip = _f32(bmax)
+    _check(lib().vfd_build_box_map(lop, hip, int(bool(inverted)), C.c_float(padding), _u32ptr(res),
+                                   C.c_float(particle_radius), _fptr(nodes), _u32ptr(cells), _u32ptr(cell_map),
+                                   C.byref(m)), "vfd_build_box_map")
+    return VolumeMap(nodes, cells, cell_map, m)
+
+
+class DFSPHSimulation:
+    """vfd::DFSPHSimulation (DFSPHSimulator.h:10-58) over the CUDA library.
+
+    One instance holds one device simulation. `scenes` > 1 creates a batch of
+    independent scenes advanced together (scene-scoped methods take `scene=`).
+    """
+
+    def __init__(self, desc: vfd_desc | dict | None = None, scenes: list | None = None):
+        if scenes is not None:
+            descs = [d if isinstance(d, vfd_desc) else make_desc(**d) for d in scenes]
+        else:
+            if desc is None:
+                desc = vfd_desc()
+                _check(lib().vfd_desc_default(C.byref(desc)), "vfd_desc_default")
+            descs = [desc if isinstance(desc, vfd_desc) else make_desc(**desc)]
+        arr = (vfd_desc * len(descs))(*descs)
+        h = C.c_void_p()
+        _check(lib().vfd_create_batch(arr, len(descs), C.byref(h)), "vfd_create_batch")
+        self._h = h
+        self._maps: list = []
+        self._counts = [0] * len(descs)
+        self.scene_count = len(descs)
+
+    # lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().vfd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # setters
+    def SetDescription(self, desc: vfd_desc | dict):
+        d = desc if isinstance(desc, vfd_desc) else make_desc(**desc)
+        _check(lib().vfd_set_description(self._h, C.byref(d)), "vfd_set_description")
+
+    def SetFluidObjects(self, positions, velocities=None, scene: int = 0):
+        """Concatenated positions (n, 3) and velocities (n, 3) of all fluid objects."""
+        x, xp = _f32(np.asarray(positions).reshape(-1, 3))
+        vp = None
+        if velocities is not None:
+            v, vp = _f32(np.asarray(velocities).reshape(-1, 3))
+        _check(lib().vfd_scene_set_fluid(self._h, scene, xp, vp, len(x)), "vfd_scene_set_fluid")
+        self._counts[scene] = len(x)
+
+    def SetRigidBodies(self, maps: list, scene: int = 0):
+        """One VolumeMap per rigid body, in order (replaces the scene's bodies when scene == 0 of a plain sim)."""
+        if self.scene_count == 1:
+            _check(lib().vfd_clear_rigid_bodies(self._h), "vfd_clear_rigid_bodies")
+        for m in maps:
+            self.AddRigidBody(m, scene)
+
+    def AddRigidBody(self, vmap: VolumeMap, scene: int = 0):
+        self._maps.append(vmap)
+        _check(lib().vfd_scene_add_rigid_body(self._h, scene, C.byref(vmap.struct)), "vfd_scene_add_rigid_body")
+
+    def SetGraphMode(self, enabled: bool):
+        _check(lib().vfd_set_graph_mode(self._h, int(bool(enabled))), "vfd_set_graph_mode")
+
+    # stepping
+    def Reset(self):
+        _check(lib().vfd_reset(self._h), "vfd_reset")
+
+    def OnUpdate(self) -> dict:
+        st = vfd_step_stats()
+        _check(lib().vfd_step(self._h, C.byref(st)), "vfd_step")
+        return st.as_dict()
+
+    def Steps(self, count: int) -> dict:
+        st = vfd_step_stats()
+        _check(lib().vfd_steps(self._h, count, C.byref(st)), "vfd_steps")
+        return st.as_dict()
+
+    def StepsAsync(self, count: int):
+        _check(lib().vfd_steps_async(self._h, count), "vfd_steps_async")
+
+    def Synchronize(self) -> dict:
+        st = vfd_step_stats()
+        _check(lib().vfd_synchronize(self._h, C.byref(st)), "vfd_synchronize")
+        return st.as_dict()
+
+    def Simulate(self, on_frame=None) -> int:
+        """Runs FrameCount frames from the initial state; on_frame(index, x, v, a, max_v2, dt)."""
+        frames = [0]
+
+        def cb(idx, n, x, v, a, mv, dt, user):
+            frames[0] += 1
+            if on_frame is not None:
+                on_frame(idx, np.ctypeslib.as_array(x, (n, 3)).copy(), np.ctypeslib.as_array(v, (n, 3)).copy(),
+                         np.ctypeslib.as_array(a, (n, 3)).copy(), mv, dt)
+
+        fn = FRAME_CALLBACK(cb)
+        _check(lib().vfd_simulate(self._h, fn, None), "vfd_simulate")
+        return frames[0]
+
+    # getters
+    def GetParticleCount(self) -> int:
+        n = C.c_uint32()
+        _check(lib().vfd_get_particle_count(self._h, C.byref(n)), "vfd_get_particle_count")
+        return n.value
+
+    def GetParticleRadius(self) -> float:
+        return self.GetInfo()["ParticleRadius"]
+
+    def GetCurrentTimeStepSize(self) -> float:
+        dt = C.c_float()
+        _check(lib().vfd_get_current_time_step_size(self._h, C.byref(dt)), "vfd_get_current_time_step_size")
+        return dt.value
+
+    def GetMaxVelocityMagnitude(self) -> float:
+        v = C.c_float()
+        _check(lib().vfd_get_max_velocity_magnitude(self._h, C.byref(v)), "vfd_get_max_velocity_magnitude")
+        return v.value
+
+    def GetDescription(self) -> dict:
+        d = vfd_desc()
+        _check(lib().vfd_get_description(self._h, C.byref(d)), "vfd_get_description")
+        return _abi.desc_to_dict(d)
+
+    def GetInfo(self) -> dict:
+        i = vfd_info()
+        _check(lib().vfd_get_info(self._h, C.byref(i)), "vfd_get_info")
+        return i.as_dict()
+
+    def GetDebugInfo(self, scene: int = 0) -> dict:
+        st = vfd_step_stats()
+        _check(lib().vfd_scene_get_stats(self._h, scene, C.byref(st)), "vfd_scene_get_stats")
+        return st.as_dict()
+
+    def GetKernel(self):
+        w = np.zeros(10000, np.float32)
+        g = np.zeros(10001, np.float32)
+        r, wz = C.c_float(), C.c_float()
+        _check(lib().vfd_get_kernel_table(self._h, _fptr(w), _fptr(g), C.byref(r), C.byref(wz)),
+               "vfd_get_kernel_table")
+        return dict(W=w, GradW=g, radius=r.value, w_zero=wz.value)
+
+    def GetState(self, scene: int = 0):
+        n = self._counts[scene]
+        x = np.zeros((n, 3), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        a = np.zeros((n, 3), np.float32)
+        _check(lib().vfd_scene_get_state(self._h, scene, _fptr(x), _fptr(v), _fptr(a)), "vfd_scene_get_state")
+        return x, v, a
+
+    def SetState(self, x=None, v=None):
+        xp = vp = None
+        if x is not None:
+            xa, xp = _f32(np.asarray(x).reshape(-1, 3))
+        if v is not None:
+            va, vp = _f32(np.asarray(v).reshape(-1, 3))
+        _check(lib().vfd_set_state(self._h, xp, vp), "vfd_set_state")
+
+    def GetField(self, field: int, body: int = 0) -> np.ndarray:
+        n = self._counts[0]
+        shape = (n, 3) if field in _abi.VECTOR_FIELDS else (n,)
+        out = np.zeros(shape, np.float32)
+        _check(lib().vfd_get_field(self._h, field, body, _fptr(out)), "vfd_get_field")
+        return out
+
+    def FindNeighbors(self):
+        _check(lib().vfd_find_neighbors(self._h), "vfd_find_neighbors")
+
+    def GetNeighbors(self) -> dict:
+        n = self._counts[0]
+        counts = np.zeros(n, np.uint32)
+        offsets = np.zeros(n, np.uint32)
+        sort_idx = np.zeros(n, np.uint32)
+        keys = np.zeros(n, np.uint32)
+        total = C.c_uint32()
+        _check(lib().vfd_get_neighbors(self._h, _u32ptr(counts), _u32ptr(offsets), None, 0, C.byref(total),
+                                       _u32ptr(sort_idx), _u32ptr(keys)), "vfd_get_neighbors")
+        lst = np.zeros(max(1, total.value), np.uint32)
+        _check(lib().vfd_get_neighbors(self._h, None, None, _u32ptr(lst), total.value, C.byref(total), None, None),
+               "vfd_get_neighbors")
+        return dict(counts=counts, offsets=offsets, list=lst[:total.value], sort_indices=sort_idx, cell_keys=keys)
+
+
+def scene_simulation(scene: dict, desc_overrides: dict | None = None, maps: list | None = None) -> DFSPHSimulation:
+    """A DFSPHSimulation loaded with a vfd_gb300.scenes scene (volume maps built on the GPU unless given)."""
+    d = dict(scene["desc"])
+    if desc_overrides:
+        d.update(desc_overrides)
+    sim = DFSPHSimulation(make_desc(**d))
+    sim.SetFluidObjects(scene["x"], scene["v"])
+    if maps is None:
+        r = d["ParticleRadius"]
+        maps = [build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"], r)
+                for b in scene["boxes"]]
+    for m in maps:
+        sim.AddRigidBody(m)
+    return sim

@@ -1,0 +1,1322 @@
+// C-ABI of the GB300 DFSPH step (include/vfd_dfsph.h): the host side of
+// DFSPHSimulation / DFSPHImplementation (Simulation/DFSPH/DFSPHSimulator.cpp,
+// DFSPHImplementation.cu). Owns all device memory, uploads scenes, records the
+// step either as one CUDA graph (conditional while nodes for the divergence,
+// viscosity and pressure loops) or as eagerly launched kernels with one flag
+// read per solver iteration, and converts results back to the caller's
+// particle order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/vfd_dfsph.h"
+#include "dfsph_common.cuh"
+
+namespace vfd {
+void launch_search(const Dev& d, cudaStream_t s);
+uint32_t scan_block_count(uint32_t cellCap);
+void launch_boundary(const Dev& d, cudaStream_t s);
+void launch_density(const Dev& d, cudaStream_t s);
+void launch_div_init(const Dev& d, cudaStream_t s);
+void launch_div_iter(const Dev& d, cudaStream_t s);
+void launch_div_finish(const Dev& d, cudaStream_t s);
+void launch_surface_tension(const Dev& d, uint32_t maxPasses, cudaStream_t s);
+void launch_visc_init(const Dev& d, cudaStream_t s);
+void launch_cg_iter(const Dev& d, cudaStream_t s);
+void launch_visc_finish_dt(const Dev& d, cudaStream_t s);
+void launch_pres_init(const Dev& d, cudaStream_t s);
+void launch_pres_iter(const Dev& d, cudaStream_t s);
+void launch_pres_finish(const Dev& d, cudaStream_t s);
+void box_map_sizes(const uint32_t res[3], uint32_t& nodes, uint32_t& cells);
+int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, float padding, const uint32_t res[3],
+                      float r, const float* table, float wZero, float invStep, float* nodes, uint32_t* cells,
+                      uint32_t* cellMap, float dminOut[3], float dmaxOut[3], float csOut[3], float csiOut[3]);
+}  // namespace vfd
+
+using namespace vfd;
+
+namespace {
+
+thread_local std::string g_lastError;
+int g_device = 0;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_lastError = buf;
+    return code;
+}
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(VFD_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                        \
+    } while (0)
+
+// PrecomputedDFSPHCubicKernel::SetRadius (Kernel/DFSPHKernels.h:13-41) in FP32; the
+// library is built with -ffp-contract=off for host code so the table matches it bit for bit.
+struct KernelTable {
+    std::vector<float> W, G;
+    float radius = 0, radius2 = 0, invStep = 0, wZero = 0, K = 0, L = 0;
+    float calcW(float r) const {
+        float res = 0.0f;
+        const float q = r / radius;
+        if (q <= 1.0f) {
+            if (q <= 0.5f) {
+                const float q2 = q * q, q3 = q2 * q;
+                res = K * (6.0f * q3 - 6.0f * q2 + 1.0f);
+            } else {
+                const float q1 = 1.0f - q, q3 = q1 * q1 * q1;
+                res = K * (2.0f * q3);
+            }
+        }
+        return res;
+    }
+    float calcGradWx(float px) const {  // CalculateGradientW({px, 0, 0}).x
+        const float rl = std::sqrt(px * px + 0.0f * 0.0f + 0.0f * 0.0f);
+        const float q = rl / radius;
+        if (rl > 1.0e-5f && q <= 1.0f) {
+            const float gq = px * (1.0f / (rl * radius));
+            if (q <= 0.5f) return ((L * q) * (3.0f * q - 2.0f)) * gq;
+            const float f = 1.0f - q;
+            return (L * (-f * f)) * gq;
+        }
+        return 0.0f;
+    }
+    void setRadius(float r) {
+        const float pi = (float)3.14159265358979323846;
+        W.assign(kTableRes, 0.0f);
+        G.assign(kTableRes + 1, 0.0f);
+        radius = r;
+        radius2 = radius * radius;
+        const float r3 = radius * radius * radius;
+        K = 8.0f / (pi * r3);
+        L = 48.0f / (pi * r3);
+        wZero = calcW(std::sqrt(0.0f));
+        const float step = radius / (float)(kTableRes - 1);
+        invStep = 1.0f / step;
+        for (uint32_t i = 0; i < kTableRes; i++) {
+            const float px = step * (float)i;
+            W[i] = calcW(px);
+            G[i] = px > 1.0e-9f ? calcGradWx(px) / px : 0.0f;
+        }
+        G[kTableRes] = 0.0f;
+    }
+};
+
+// Surface-tension directions (HaltonVec323.cuh:4): the Halton(2,3) points on the unit
+// sphere, each component rounded to the 15 decimals the reference lists.
+void halton_table(std::vector<float>& out) {
+    out.assign(kHaltonCount, 0.0f);
+    auto radical = [](uint32_t i, uint32_t b) {
+        double inv = 1.0 / b, f = inv, r = 0.0;
+        while (i > 0) { r += f * (double)(i % b); i /= b; f *= inv; }
+        return r;
+    };
+    for (uint32_t i = 0; i < kHaltonCount / 3; i++) {
+        const double z = 1.0 - 2.0 * radical(i, 3);
+        const double phi = 2.0 * 3.14159265358979323846 * radical(i, 2);
+        const double s = std::sqrt(std::max(0.0, 1.0 - z * z));
+        const double v[3] = {s * std::cos(phi), s * std::sin(phi), z};
+        for (int k = 0; k < 3; k++) out[3 * i + k] = (float)(std::nearbyint(v[k] * 1e15) / 1e15 + 0.0);  // +0.0: no negative zeros
+    }
+}
+
+struct BodyHost {
+    BodyDev dev{};
+    float* nodes = nullptr;
+    uint32_t* cells = nullptr;
+    uint32_t* cellMap = nullptr;
+    void release() {
+        cudaFree(nodes);
+        cudaFree(cells);
+        cudaFree(cellMap);
+        nodes = nullptr;
+        cells = cellMap = nullptr;
+    }
+};
+
+struct SceneHost {
+    vfd_desc desc{};
+    std::vector<float> x0, v0;
+    std::vector<BodyHost> bodies;
+};
+
+}  // namespace
+
+struct vfd_sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<SceneHost> scenes;
+    KernelTable table;
+    std::vector<float> halton;
+    bool graphMode = true;
+    bool graphFailed = false;
+
+    // layout
+    bool allocated = false, uploaded = false;
+    uint32_t n = 0, stride = 0, cellCap = 0, maxBodies = 0;
+    std::vector<uint32_t> sceneBegin;
+    std::vector<void*> allocs;
+    Dev dev[2]{};
+    int cs = 0;  // set holding the current carried state
+    float4* XB = nullptr;
+    SceneDev* dScenes = nullptr;
+    BodyDev* dBodies = nullptr;
+    uint32_t* dStatus = nullptr;
+    float *dWM = nullptr, *dGM = nullptr, *dHalton = nullptr;
+    uint32_t* hStatus = nullptr;  // pinned
+    std::vector<SceneDev> hScenes;
+    uint32_t maxStPasses = 0;
+    bool anyDiv = false, anyVisc = false, anyST = false;
+
+    // graphs (one per parity)
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    bool searchOnlyPending = false;
+
+    ~vfd_sim() { release(); }
+
+    void releaseGraphs() {
+        for (int k = 0; k < 2; k++) {
+            if (exec[k]) cudaGraphExecDestroy(exec[k]);
+            if (graph[k]) cudaGraphDestroy(graph[k]);
+            exec[k] = nullptr;
+            graph[k] = nullptr;
+        }
+    }
+    void releaseBuffers() {
+        releaseGraphs();
+        for (void* p : allocs) cudaFree(p);
+        allocs.clear();
+        if (hStatus) cudaFreeHost(hStatus);
+        hStatus = nullptr;
+        allocated = false;
+        uploaded = false;
+    }
+    void release() {
+        releaseBuffers();
+        for (auto& s : scenes)
+            for (auto& b : s.bodies) b.release();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+template <class T>
+int dalloc(vfd_sim* s, T** p, size_t count) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(VFD_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    s->allocs.push_back(q);
+    *p = (T*)q;
+    return VFD_OK;
+}
+
+#define TRY(x)                   \
+    do {                         \
+        int rc_ = (x);           \
+        if (rc_ != VFD_OK) return rc_; \
+    } while (0)
+
+int check_desc(const vfd_desc* d) {
+    if (!d) return fail(VFD_E_ARG, "null description");
+    if (!(d->ParticleRadius > 0.0f) || !std::isfinite(d->ParticleRadius))
+        return fail(VFD_E_ARG, "ParticleRadius must be positive and finite");
+    if (!(d->MinTimeStepSize > 0.0f) || !(d->MaxTimeStepSize >= d->MinTimeStepSize) || !(d->TimeStepSize > 0.0f))
+        return fail(VFD_E_ARG, "time step bounds must satisfy 0 < Min <= Max and TimeStepSize > 0");
+    return VFD_OK;
+}
+
+// Estimated cell table size: the reference's grid for the initial bounds with 50 % headroom.
+uint32_t estimate_cells(const vfd_sim* s) {
+    uint64_t total = 0;
+    for (const auto& sc : s->scenes) {
+        const uint32_t n = (uint32_t)(sc.x0.size() / 3);
+        if (n == 0) continue;
+        const float R = 4.0f * sc.desc.ParticleRadius;
+        uint64_t cells = 512;
+        for (int k = 0; k < 3; k++) {
+            float lo = FLT_MAX, hi = -FLT_MAX;
+            for (uint32_t i = 0; i < n; i++) {
+                lo = std::min(lo, sc.x0[3 * i + k]);
+                hi = std::max(hi, sc.x0[3 * i + k]);
+            }
+            // the box may let the fluid spread; take the bodies' domains too
+            for (const auto& b : sc.bodies) {
+                lo = std::min(lo, b.dev.dmin[k]);
+                hi = std::max(hi, b.dev.dmax[k]);
+            }
+            const uint64_t dim = (uint64_t)std::ceil((hi - lo) / R) + 6u;
+            cells *= (dim + 7u) / 8u;
+        }
+        total += cells;
+    }
+    total = total + total / 2 + 4096;
+    return (uint32_t)std::min<uint64_t>(total, 0xF0000000ull);
+}
+
+int allocate(vfd_sim* s) {
+    s->releaseBuffers();
+    uint32_t n = 0, maxBodies = 0;
+    s->sceneBegin.clear();
+    for (const auto& sc : s->scenes) {
+        s->sceneBegin.push_back(n);
+        n += (uint32_t)(sc.x0.size() / 3);
+        maxBodies = std::max<uint32_t>(maxBodies, (uint32_t)sc.bodies.size());
+    }
+    s->n = n;
+    s->stride = std::max<uint32_t>(32u, (n + 31u) & ~31u);
+    s->maxBodies = maxBodies;
+    if (s->cellCap == 0) s->cellCap = estimate_cells(s);
+    const size_t st = s->stride;
+    Dev base{};
+    base.n = n;
+    base.stride = s->stride;
+    base.nscenes = (uint32_t)s->scenes.size();
+    base.maxBodies = maxBodies;
+    base.cellCap = s->cellCap;
+    base.scanBlocks = scan_block_count(s->cellCap);
+    float4* X[2];
+    float4* V[2];
+    float4* DV[2];
+    float* DK[2];
+    uint32_t* PID[2];
+    for (int k = 0; k < 2; k++) {
+        TRY(dalloc(s, &X[k], st));
+        TRY(dalloc(s, &V[k], st));
+        TRY(dalloc(s, &DV[k], st));
+        TRY(dalloc(s, &DK[k], st));
+        TRY(dalloc(s, &PID[k], st));
+    }
+    TRY(dalloc(s, &base.XN, st));
+    TRY(dalloc(s, &base.A, st));
+    TRY(dalloc(s, &base.AP, st));
+    TRY(dalloc(s, &base.GB, st));
+    TRY(dalloc(s, &base.RHO, st));
+    TRY(dalloc(s, &base.ALPHA, st));
+    TRY(dalloc(s, &base.RHOADV, st));
+    TRY(dalloc(s, &base.KAPPA, st));
+    TRY(dalloc(s, &base.KAPPAV, st));
+    TRY(dalloc(s, &base.RES, st));
+    TRY(dalloc(s, &base.XB, st * std::max<uint32_t>(1u, maxBodies)));
+    TRY(dalloc(s, &base.NBR, st * kMaxNeighbors));
+    TRY(dalloc(s, &base.NCNT, st));
+    TRY(dalloc(s, &base.KEY, st));
+    TRY(dalloc(s, &base.KEYS, st));
+    TRY(dalloc(s, &base.TMP, st));
+    TRY(dalloc(s, &base.CELL_START, s->cellCap));
+    TRY(dalloc(s, &base.CELL_COUNT, s->cellCap));
+    TRY(dalloc(s, &base.FILL, s->cellCap));
+    TRY(dalloc(s, &base.SCAN, base.scanBlocks + 1));
+    TRY(dalloc(s, &base.MINV, 3 * st));
+    TRY(dalloc(s, &base.BVM, 3 * st));
+    TRY(dalloc(s, &base.CB, st));
+    TRY(dalloc(s, &base.CG, st));
+    TRY(dalloc(s, &base.CR, st));
+    TRY(dalloc(s, &base.CP, st));
+    TRY(dalloc(s, &base.CZ, st));
+    TRY(dalloc(s, &base.CAP, st));
+    TRY(dalloc(s, &base.STN, st));
+    TRY(dalloc(s, &base.STNS, st));
+    TRY(dalloc(s, &base.SID, st));
+    TRY(dalloc(s, &s->dScenes, base.nscenes));
+    uint32_t bodyTotal = 0;
+    for (const auto& sc : s->scenes) bodyTotal += (uint32_t)sc.bodies.size();
+    TRY(dalloc(s, &s->dBodies, std::max<uint32_t>(1u, bodyTotal)));
+    TRY(dalloc(s, &s->dStatus, 16));
+    TRY(dalloc(s, &s->dWM, kTableRes));
+    TRY(dalloc(s, &s->dGM, kTableRes));
+    TRY(dalloc(s, &s->dHalton, kHaltonCount));
+    CK(cudaMallocHost(&s->hStatus, 16 * sizeof(uint32_t)));
+    base.scenes = s->dScenes;
+    base.bodies = s->dBodies;
+    base.status = s->dStatus;
+    base.WM = s->dWM;
+    base.GM = s->dGM;
+    base.halton = s->dHalton;
+    base.wZero = s->table.wZero;
+    base.invStep = s->table.invStep;
+    base.radius = s->table.radius;
+    base.radius2 = s->table.radius2;
+    for (int k = 0; k < 2; k++) {
+        Dev d = base;
+        d.Xc = X[k]; d.Vc = V[k]; d.DVc = DV[k]; d.DKc = DK[k]; d.PIDc = PID[k];
+        d.X = X[1 - k]; d.V = V[1 - k]; d.DV = DV[1 - k]; d.DK = DK[1 - k]; d.PID = PID[1 - k];
+        s->dev[k] = d;
+    }
+    // static uploads: tables, scene ids, bodies
+    std::vector<float> wm(kTableRes), gm(kTableRes);
+    for (uint32_t i = 0; i + 1 < kTableRes; i++) {
+        wm[i] = 0.5f * (s->table.W[i] + s->table.W[i + 1]);
+        gm[i] = 0.5f * (s->table.G[i] + s->table.G[i + 1]);
+    }
+    wm[kTableRes - 1] = gm[kTableRes - 1] = 0.0f;
+    CK(cudaMemcpy(s->dWM, wm.data(), sizeof(float) * kTableRes, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->dGM, gm.data(), sizeof(float) * kTableRes, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->dHalton, s->halton.data(), sizeof(float) * kHaltonCount, cudaMemcpyHostToDevice));
+    std::vector<uint16_t> sid(st, 0);
+    std::vector<BodyDev> bodies;
+    for (uint32_t k = 0; k < s->scenes.size(); k++) {
+        const uint32_t cnt = (uint32_t)(s->scenes[k].x0.size() / 3);
+        for (uint32_t i = 0; i < cnt; i++) sid[s->sceneBegin[k] + i] = (uint16_t)k;
+        for (const auto& b : s->scenes[k].bodies) bodies.push_back(b.dev);
+    }
+    CK(cudaMemcpy(base.SID, sid.data(), sizeof(uint16_t) * st, cudaMemcpyHostToDevice));
+    if (!bodies.empty())
+        CK(cudaMemcpy(s->dBodies, bodies.data(), sizeof(BodyDev) * bodies.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemset(base.NCNT, 0, sizeof(uint32_t) * st));
+    CK(cudaMemset(base.A, 0, sizeof(float4) * st));
+    CK(cudaMemset(base.AP, 0, sizeof(float4) * st));
+    CK(cudaMemset(base.STN, 0, sizeof(float4) * st));
+    CK(cudaMemset(base.STNS, 0, sizeof(float4) * st));
+    CK(cudaMemset(base.XB, 0, sizeof(float4) * st * std::max<uint32_t>(1u, maxBodies)));
+    s->allocated = true;
+    return VFD_OK;
+}
+
+SceneDev scene_constants(const vfd_desc& d, uint32_t begin, uint32_t count, uint32_t bodyBegin, uint32_t bodyCount) {
+    SceneDev S;
+    std::memset(&S, 0, sizeof(S));
+    S.begin = begin;
+    S.count = count;
+    S.bodyBegin = bodyBegin;
+    S.bodyCount = bodyCount;
+    // DFSPHImplementation::SetDescription (DFSPHImplementation.cu:318-368)
+    S.r = d.ParticleRadius;
+    S.diam = 2.0f * S.r;
+    S.h = 4.0f * S.r;
+    S.h2 = S.h * S.h;
+    S.volume = 0.8f * S.diam * S.diam * S.diam;
+    S.rho0 = 1000.0f;
+    S.mass = S.volume * S.rho0;
+    S.massInv = 1.0f / S.mass;
+    S.dynVisc = d.Viscosity * S.rho0;
+    S.dynBVisc = d.BoundaryViscosity * S.rho0;
+    S.tangDist = d.TangentialDistanceFactor * S.h;
+    S.st = d.SurfaceTension;
+    S.slope = 74.688796680497925f;
+    S.constant = 12.0f;
+    S.smoothing = 0.5f;
+    S.nbrRadius = S.r * 0.8f;
+    S.mcFactor = std::asin(S.nbrRadius / S.r);
+    S.temporal = d.TemporalSmoothing ? 1 : 0;
+    for (int k = 0; k < 3; k++) S.g[k] = d.Gravity[k];
+    S.minIterP = d.MinPressureSolverIterations;
+    S.maxIterP = d.MaxPressureSolverIterations;
+    S.minIterD = d.MinDivergenceSolverIterations;
+    S.maxIterD = d.MaxDivergenceSolverIterations;
+    S.minIterV = d.MinViscositySolverIterations;
+    S.maxIterV = d.MaxViscositySolverIterations;
+    S.maxErrP = d.MaxPressureSolverError;
+    S.maxErrD = d.MaxDivergenceSolverError;
+    S.maxErrV = d.MaxViscositySolverError;
+    S.enableDiv = d.EnableDivergenceSolverError ? 1 : 0;
+    S.enableVisc = d.EnableViscositySolver ? 1 : 0;
+    S.enableST = d.EnableSurfaceTensionSolver ? 1 : 0;
+    S.stPasses = d.SurfaceTensionSmoothPassCount;
+    S.csdFix = d.CSDFix;
+    S.csd = d.CSD;
+    S.minDt = d.MinTimeStepSize;
+    S.maxDt = d.MaxTimeStepSize;
+    // Simulate() preamble (:39-43): dt = TimeStepSize
+    S.dt = d.TimeStepSize;
+    S.dt2 = d.TimeStepSize * d.TimeStepSize;
+    S.dtInv = 1.0f / S.dt;
+    S.dt2Inv = 1.0f / S.dt2;
+    // ComputeTimeStepSize sets the sample count after the first surface-tension pass
+    // (:413-420); the first step uses the one of the initial dt.
+    S.stSamples = d.CSDFix > 0 ? (uint32_t)d.CSDFix : (uint32_t)(int)((float)d.CSD * S.dt);
+    S.stSamplesUsed = S.stSamples;
+    S.frameLength = d.FrameLength;
+    S.frameCount = d.FrameCount;
+    for (int k = 0; k < 3; k++) {
+        S.minCell[k] = INT_MAX;
+        S.maxCell[k] = INT_MIN;
+    }
+    return S;
+}
+
+// Simulate() preamble (DFSPHImplementation.cu:33-51): initial particles to the device,
+// dt and counters reset.
+int upload(vfd_sim* s) {
+    if (!s->allocated) TRY(allocate(s));
+    const size_t st = s->stride;
+    std::vector<float4> xn(st, make_float4(0, 0, 0, 0)), v(st, make_float4(0, 0, 0, 0));
+    std::vector<uint32_t> pid(st, 0);
+    s->hScenes.clear();
+    uint32_t bodyBegin = 0;
+    s->maxStPasses = 0;
+    s->anyDiv = s->anyVisc = s->anyST = false;
+    for (uint32_t k = 0; k < s->scenes.size(); k++) {
+        const SceneHost& sc = s->scenes[k];
+        const uint32_t b = s->sceneBegin[k], cnt = (uint32_t)(sc.x0.size() / 3);
+        for (uint32_t i = 0; i < cnt; i++) {
+            xn[b + i] = make_float4(sc.x0[3 * i], sc.x0[3 * i + 1], sc.x0[3 * i + 2], 0.0f);
+            if (!sc.v0.empty()) v[b + i] = make_float4(sc.v0[3 * i], sc.v0[3 * i + 1], sc.v0[3 * i + 2], 0.0f);
+            pid[b + i] = i;
+        }
+        s->hScenes.push_back(scene_constants(sc.desc, b, cnt, bodyBegin, (uint32_t)sc.bodies.size()));
+        bodyBegin += (uint32_t)sc.bodies.size();
+        if (sc.desc.EnableSurfaceTensionSolver) s->maxStPasses = std::max(s->maxStPasses, sc.desc.SurfaceTensionSmoothPassCount);
+        s->anyDiv |= sc.desc.EnableDivergenceSolverError != 0;
+        s->anyVisc |= sc.desc.EnableViscositySolver != 0;
+        s->anyST |= sc.desc.EnableSurfaceTensionSolver != 0;
+    }
+    s->cs = 0;
+    const Dev& d = s->dev[0];
+    CK(cudaMemcpy(d.XN, xn.data(), sizeof(float4) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.Vc, v.data(), sizeof(float4) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.PIDc, pid.data(), sizeof(uint32_t) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemset(d.DVc, 0, sizeof(float4) * st));
+    CK(cudaMemset(d.DKc, 0, sizeof(float) * st));
+    CK(cudaMemset(d.A, 0, sizeof(float4) * st));
+    CK(cudaMemcpy(s->dScenes, s->hScenes.data(), sizeof(SceneDev) * s->hScenes.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemset(s->dStatus, 0, 16 * sizeof(uint32_t)));
+    CK(cudaDeviceSynchronize());
+    s->uploaded = true;
+    return VFD_OK;
+}
+
+// ---------------------------------------------------------------- step recording
+template <class F>
+cudaError_t add_while(cudaStream_t cap, cudaGraph_t g, cudaGraphConditionalHandle h, std::vector<cudaGraphNode_t>& leaves,
+                      F body) {
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    cudaError_t e = cudaGraphAddNode(&node, g, leaves.data(), nullptr, leaves.size(), &np);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t bodyGraph = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(cap, bodyGraph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    body(cap);
+    e = cudaStreamEndCapture(cap, &bodyGraph);
+    if (e != cudaSuccess) return e;
+    leaves.assign(1, node);
+    return cudaSuccess;
+}
+
+template <class F>
+cudaError_t add_segment(cudaStream_t cap, cudaGraph_t g, std::vector<cudaGraphNode_t>& leaves, F seg) {
+    cudaError_t e = cudaStreamBeginCaptureToGraph(cap, g, leaves.empty() ? nullptr : leaves.data(), nullptr,
+                                                  leaves.size(), cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    seg(cap);
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(cap, &status, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> next(deps, deps + nd);
+    cudaGraph_t out = g;
+    e = cudaStreamEndCapture(cap, &out);
+    if (e != cudaSuccess) return e;
+    if (!next.empty()) leaves = next;
+    return cudaSuccess;
+}
+
+int build_graph(vfd_sim* s, int parity) {
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h[3];
+    for (int k = 0; k < 3; k++) {
+        cudaError_t e = cudaGraphConditionalHandleCreate(&h[k], g, 0, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return fail(VFD_E_CUDA, "cudaGraphConditionalHandleCreate: %s", cudaGetErrorString(e));
+        }
+    }
+    Dev d = s->dev[parity];
+    for (int k = 0; k < 3; k++) d.condHandle[k] = (unsigned long long)h[k];
+    cudaStream_t cap = s->stream;
+    std::vector<cudaGraphNode_t> leaves;
+    const uint32_t passes = s->maxStPasses;
+    const bool anyDiv = s->anyDiv, anyVisc = s->anyVisc, anyST = s->anyST;
+    cudaError_t e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        launch_search(d, st);
+        launch_boundary(d, st);
+        launch_density(d, st);
+        launch_div_init(d, st);
+    });
+    if (e == cudaSuccess && anyDiv) e = add_while(cap, g, h[0], leaves, [&](cudaStream_t st) { launch_div_iter(d, st); });
+    if (e == cudaSuccess)
+        e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+            launch_div_finish(d, st);
+            if (anyST) launch_surface_tension(d, passes, st);
+            if (anyVisc) launch_visc_init(d, st);
+        });
+    if (e == cudaSuccess && anyVisc) e = add_while(cap, g, h[1], leaves, [&](cudaStream_t st) { launch_cg_iter(d, st); });
+    if (e == cudaSuccess)
+        e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+            launch_visc_finish_dt(d, st);
+            launch_pres_init(d, st);
+        });
+    if (e == cudaSuccess) e = add_while(cap, g, h[2], leaves, [&](cudaStream_t st) { launch_pres_iter(d, st); });
+    if (e == cudaSuccess) e = add_segment(cap, g, leaves, [&](cudaStream_t st) { launch_pres_finish(d, st); });
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(g);
+        return fail(VFD_E_CUDA, "step graph construction failed: %s", cudaGetErrorString(e));
+    }
+    s->graph[parity] = g;
+    s->exec[parity] = exec;
+    return VFD_OK;
+}
+
+int read_flag(vfd_sim* s, int idx, uint32_t& v) {
+    CK(cudaMemcpyAsync(s->hStatus + idx, s->dStatus + idx, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    v = s->hStatus[idx];
+    return VFD_OK;
+}
+
+// The reference's host-driven control flow: one flag read per solver iteration.
+int launch_eager(vfd_sim* s) {
+    const Dev& d = s->dev[s->cs];
+    cudaStream_t st = s->stream;
+    uint32_t more = 0;
+    launch_search(d, st);
+    launch_boundary(d, st);
+    launch_density(d, st);
+    launch_div_init(d, st);
+    if (s->anyDiv) {
+        TRY(read_flag(s, 4, more));
+        for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
+            launch_div_iter(d, st);
+            TRY(read_flag(s, 4, more));
+        }
+    }
+    launch_div_finish(d, st);
+    if (s->anyST) launch_surface_tension(d, s->maxStPasses, st);
+    if (s->anyVisc) {
+        launch_visc_init(d, st);
+        TRY(read_flag(s, 5, more));
+        for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
+            launch_cg_iter(d, st);
+            TRY(read_flag(s, 5, more));
+        }
+    }
+    launch_visc_finish_dt(d, st);
+    launch_pres_init(d, st);
+    TRY(read_flag(s, 6, more));
+    for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
+        launch_pres_iter(d, st);
+        TRY(read_flag(s, 6, more));
+    }
+    launch_pres_finish(d, st);
+    CK(cudaGetLastError());
+    return VFD_OK;
+}
+
+int ensure_ready(vfd_sim* s) {
+    if (s->scenes.empty()) return fail(VFD_E_STATE, "no scene");
+    if (!s->uploaded) TRY(upload(s));
+    return VFD_OK;
+}
+
+int launch_one(vfd_sim* s) {
+    if (s->graphMode && !s->graphFailed) {
+        if (!s->exec[s->cs]) {
+            const int rc = build_graph(s, s->cs);
+            if (rc != VFD_OK) {
+                // keep the kernels, drop the graph: eager launches of the same kernels
+                s->graphFailed = true;
+                s->releaseGraphs();
+            }
+        }
+        if (!s->graphFailed) {
+            CK(cudaGraphLaunch(s->exec[s->cs], s->stream));
+            s->cs = 1 - s->cs;
+            return VFD_OK;
+        }
+    }
+    TRY(launch_eager(s));
+    s->cs = 1 - s->cs;
+    return VFD_OK;
+}
+
+// Handles a grid larger than the cell table: the step aborted before touching the
+// carried state, so the table is grown and the same step launched again.
+int finish_steps(vfd_sim* s, vfd_step_stats* stats, uint32_t& flags) {
+    CK(cudaMemcpyAsync(s->hStatus, s->dStatus, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaGetLastError());
+    flags = s->hStatus[0];
+    if (stats) {
+        CK(cudaMemcpy(s->hScenes.data(), s->dScenes, sizeof(SceneDev) * s->hScenes.size(), cudaMemcpyDeviceToHost));
+    }
+    return VFD_OK;
+}
+
+void fill_stats(const SceneDev& S, vfd_step_stats* st) {
+    st->IterationCount = S.iteration;
+    st->DivergenceSolverIterationCount = S.enableDiv ? S.div.it : 0u;
+    st->PressureSolverIterationCount = S.pres.it;
+    st->ViscositySolverIterationCount = S.enableVisc ? S.cgIt : 0u;
+    st->DivergenceSolverError = S.enableDiv ? S.div.err : 0.0f;
+    st->PressureSolverError = S.pres.err;
+    st->ViscositySolverError = S.enableVisc ? S.cgErr : 0.0f;
+    st->FrameTime = S.frameTime;
+    st->FrameIndex = S.frameIndex;
+    st->TimeStepSize = S.dt;
+    st->MaxVelocityMagnitude = S.maxV2;
+    st->MaxNeighborCount = S.maxNbr;
+    st->Flags = S.flags;
+    st->SurfaceTensionSampleCount = S.stSamplesUsed;
+}
+
+int grow_cells(vfd_sim* s) {
+    // keep the state: copy it out, reallocate with a larger table, copy it back
+    const size_t st = s->stride;
+    const Dev& d = s->dev[s->cs];
+    std::vector<float4> xn(st), v(st), dv(st);
+    std::vector<float> dk(st);
+    std::vector<uint32_t> pid(st);
+    CK(cudaMemcpy(xn.data(), d.XN, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), d.Vc, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dv.data(), d.DVc, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dk.data(), d.DKc, sizeof(float) * st, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pid.data(), d.PIDc, sizeof(uint32_t) * st, cudaMemcpyDeviceToHost));
+    std::vector<SceneDev> sc(s->hScenes.size());
+    CK(cudaMemcpy(sc.data(), s->dScenes, sizeof(SceneDev) * sc.size(), cudaMemcpyDeviceToHost));
+    const uint64_t want = (uint64_t)s->cellCap * 2u;
+    if (want > 0xF0000000ull) return fail(VFD_E_CAPACITY, "search grid exceeds the cell table limit");
+    s->cellCap = (uint32_t)want;
+    TRY(allocate(s));
+    const Dev& e = s->dev[0];
+    s->cs = 0;
+    CK(cudaMemcpy(e.XN, xn.data(), sizeof(float4) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.Vc, v.data(), sizeof(float4) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.DVc, dv.data(), sizeof(float4) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.DKc, dk.data(), sizeof(float) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.PIDc, pid.data(), sizeof(uint32_t) * st, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->dScenes, sc.data(), sizeof(SceneDev) * sc.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemset(s->dStatus, 0, 16 * sizeof(uint32_t)));
+    s->uploaded = true;
+    return VFD_OK;
+}
+
+int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
+    if (!s) return fail(VFD_E_ARG, "null handle");
+    TRY(ensure_ready(s));
+    if (s->n == 0) return VFD_OK;
+    uint32_t remaining = count;
+    for (int attempt = 0; remaining > 0 && attempt < 16; attempt++) {
+        const int cs0 = s->cs;
+        for (uint32_t k = 0; k < remaining; k++) TRY(launch_one(s));
+        if (!wait) return VFD_OK;
+        uint32_t flags = 0;
+        TRY(finish_steps(s, stats, flags));
+        // Only the search aborts a step (grid larger than the cell table, or a
+        // non-finite position); an aborted step and the ones after it leave the
+        // carried state where it was, so the state set follows the completed count.
+        const uint32_t completed = s->hStatus[7];
+        s->cs = (completed & 1u) ? 1 - cs0 : cs0;
+        CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
+        if (!s->hStatus[1]) {
+            if (stats) fill_stats(s->hScenes[0], stats);
+            return VFD_OK;
+        }
+        if (flags & 0x10u) return fail(VFD_E_NAN, "non-finite particle position");
+        remaining -= std::min(remaining, completed);
+        TRY(grow_cells(s));
+    }
+    return fail(VFD_E_CAPACITY, "search grid keeps exceeding the cell table");
+}
+
+int check_sim(const vfd_sim* s) { return s ? VFD_OK : fail(VFD_E_ARG, "null handle"); }
+
+int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out) {
+    const uint32_t n = s->n;
+    std::vector<float4> buf(n);
+    std::vector<uint32_t> pid(n);
+    CK(cudaMemcpy(buf.data(), dsrc, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pid.data(), s->dev[s->cs].PIDc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    for (uint32_t p = b; p < b + cnt; p++) {
+        const uint32_t o = pid[p];
+        out[3 * o] = buf[p].x;
+        out[3 * o + 1] = buf[p].y;
+        out[3 * o + 2] = buf[p].z;
+    }
+    return VFD_OK;
+}
+
+int scatter_scalar(vfd_sim* s, uint32_t scene, const float* dsrc, float* out, int comp = -1, const float4* d4 = nullptr) {
+    const uint32_t n = s->n;
+    std::vector<float> buf(n);
+    std::vector<float4> buf4;
+    std::vector<uint32_t> pid(n);
+    if (d4) {
+        buf4.resize(n);
+        CK(cudaMemcpy(buf4.data(), d4, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    } else {
+        CK(cudaMemcpy(buf.data(), dsrc, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    }
+    CK(cudaMemcpy(pid.data(), s->dev[s->cs].PIDc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    for (uint32_t p = b; p < b + cnt; p++) {
+        float v = d4 ? (comp == 3 ? buf4[p].w : (&buf4[p].x)[comp]) : buf[p];
+        out[pid[p]] = v;
+    }
+    return VFD_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C-ABI
+extern "C" {
+
+int vfd_abi_version(void) { return VFD_ABI_VERSION; }
+
+const char* vfd_last_error(void) { return g_lastError.c_str(); }
+
+int vfd_set_device(int32_t device) {
+    int count = 0;
+    CK(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return fail(VFD_E_ARG, "device %d of %d", device, count);
+    g_device = device;
+    return VFD_OK;
+}
+
+int vfd_desc_default(vfd_desc* d) {
+    if (!d) return fail(VFD_E_ARG, "null description");
+    std::memset(d, 0, sizeof(*d));
+    d->TimeStepSize = 0.001f;
+    d->MinTimeStepSize = 0.0001f;
+    d->MaxTimeStepSize = 0.005f;
+    d->FrameLength = 0.0016f;
+    d->FrameCount = 200u;
+    d->MinPressureSolverIterations = 0u;
+    d->MaxPressureSolverIterations = 100u;
+    d->MaxPressureSolverError = 10.0f;
+    d->EnableDivergenceSolverError = 1;
+    d->MinDivergenceSolverIterations = 0u;
+    d->MaxDivergenceSolverIterations = 100u;
+    d->MaxDivergenceSolverError = 10.0f;
+    d->EnableViscositySolver = 1;
+    d->MinViscositySolverIterations = 0u;
+    d->MaxViscositySolverIterations = 100u;
+    d->MaxViscositySolverError = 0.1f;
+    d->Viscosity = 10.0f;
+    d->BoundaryViscosity = 10.0f;
+    d->TangentialDistanceFactor = 0.5f;
+    d->EnableSurfaceTensionSolver = 1;
+    d->SurfaceTensionSmoothPassCount = 1u;
+    d->SurfaceTension = 1.0f;
+    d->TemporalSmoothing = 0;
+    d->CSDFix = -1;
+    d->CSD = 10000;
+    d->ParticleRadius = 0.025f;
+    d->Gravity[0] = 0.0f;
+    d->Gravity[1] = -9.81f;
+    d->Gravity[2] = 0.0f;
+    return VFD_OK;
+}
+
+int vfd_create_batch(const vfd_desc* descs, uint32_t count, vfd_sim** out) {
+    if (!out || !descs || count == 0 || count > 65535u) return fail(VFD_E_ARG, "invalid scene list");
+    *out = nullptr;
+    for (uint32_t k = 0; k < count; k++) {
+        TRY(check_desc(&descs[k]));
+        if (descs[k].ParticleRadius != descs[0].ParticleRadius)
+            return fail(VFD_E_ARG, "all scenes of a batch share one ParticleRadius");
+    }
+    int devCount = 0;
+    cudaError_t e = cudaGetDeviceCount(&devCount);
+    if (e != cudaSuccess || devCount == 0) return fail(VFD_E_NODEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    CK(cudaSetDevice(g_device));
+    vfd_sim* s = new (std::nothrow) vfd_sim();
+    if (!s) return fail(VFD_E_NOMEM, "host allocation");
+    s->device = g_device;
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail(VFD_E_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    s->scenes.resize(count);
+    for (uint32_t k = 0; k < count; k++) s->scenes[k].desc = descs[k];
+    s->table.setRadius(4.0f * descs[0].ParticleRadius);
+    halton_table(s->halton);
+    *out = s;
+    return VFD_OK;
+}
+
+int vfd_create(const vfd_desc* desc, vfd_sim** out) { return vfd_create_batch(desc, 1, out); }
+
+int vfd_destroy(vfd_sim* s) {
+    if (!s) return VFD_OK;
+    cudaSetDevice(s->device);
+    delete s;
+    return VFD_OK;
+}
+
+int vfd_get_scene_count(const vfd_sim* s, uint32_t* n) {
+    TRY(check_sim(s));
+    if (!n) return fail(VFD_E_ARG, "null output");
+    *n = (uint32_t)s->scenes.size();
+    return VFD_OK;
+}
+
+int vfd_set_description(vfd_sim* s, const vfd_desc* desc) {
+    TRY(check_sim(s));
+    TRY(check_desc(desc));
+    if (s->scenes.size() > 1 && desc->ParticleRadius != s->scenes[0].desc.ParticleRadius)
+        return fail(VFD_E_ARG, "all scenes of a batch share one ParticleRadius");
+    CK(cudaSetDevice(s->device));
+    s->scenes[0].desc = *desc;
+    if (desc->ParticleRadius != s->table.radius / 4.0f) s->table.setRadius(4.0f * desc->ParticleRadius);
+    s->releaseBuffers();
+    return VFD_OK;
+}
+
+int vfd_get_description(const vfd_sim* s, vfd_desc* desc) {
+    TRY(check_sim(s));
+    if (!desc) return fail(VFD_E_ARG, "null output");
+    *desc = s->scenes[0].desc;
+    return VFD_OK;
+}
+
+int vfd_scene_set_fluid(vfd_sim* s, uint32_t scene, const float* xyz, const float* vel, uint32_t n) {
+    TRY(check_sim(s));
+    if (scene >= s->scenes.size()) return fail(VFD_E_ARG, "scene %u out of range", scene);
+    if (n > 0 && !xyz) return fail(VFD_E_ARG, "null positions");
+    for (uint64_t i = 0; i < 3ull * n; i++)
+        if (!std::isfinite(xyz[i]) || (vel && !std::isfinite(vel[i])))
+            return fail(VFD_E_NAN, "non-finite input at element %llu", (unsigned long long)i);
+    CK(cudaSetDevice(s->device));
+    SceneHost& sc = s->scenes[scene];
+    sc.x0.assign(xyz, xyz + 3ull * n);
+    if (vel) sc.v0.assign(vel, vel + 3ull * n);
+    else sc.v0.assign(3ull * n, 0.0f);
+    s->releaseBuffers();
+    s->cellCap = 0;
+    return VFD_OK;
+}
+
+int vfd_set_fluid(vfd_sim* s, const float* xyz, const float* vel, uint32_t n) {
+    return vfd_scene_set_fluid(s, 0, xyz, vel, n);
+}
+
+int vfd_scene_add_rigid_body(vfd_sim* s, uint32_t scene, const vfd_volume_map* m) {
+    TRY(check_sim(s));
+    if (scene >= s->scenes.size()) return fail(VFD_E_ARG, "scene %u out of range", scene);
+    if (!m || !m->nodes || !m->cells || !m->cell_map) return fail(VFD_E_ARG, "incomplete volume map");
+    if (m->field_count < 2) return fail(VFD_E_ARG, "a volume map needs fields 0 (distance) and 1 (volume)");
+    const uint64_t cells = (uint64_t)m->resolution[0] * m->resolution[1] * m->resolution[2];
+    if (cells == 0 || cells != m->cell_map_count) return fail(VFD_E_ARG, "cell map size does not match the resolution");
+    for (uint64_t c = 0; c < m->cell_map_count; c++) {
+        const uint32_t j = m->cell_map[c];
+        if (j != UINT_MAX && j >= m->cell_count) return fail(VFD_E_ARG, "cell map entry %u out of range", j);
+    }
+    for (uint64_t k = 0; k < (uint64_t)m->cell_count * 32u; k++)
+        if (m->cells[k] >= m->node_count) return fail(VFD_E_ARG, "cell node index out of range");
+    CK(cudaSetDevice(s->device));
+    BodyHost b;
+    for (int k = 0; k < 3; k++) {
+        b.dev.dmin[k] = m->domain_min[k];
+        b.dev.dmax[k] = m->domain_max[k];
+        b.dev.cs[k] = m->cell_size[k];
+        b.dev.csi[k] = m->cell_size_inverse[k];
+        b.dev.res[k] = m->resolution[k];
+    }
+    b.dev.nodeCount = m->node_count;
+    b.dev.cellCount = m->cell_count;
+    b.dev.cellMapCount = m->cell_map_count;
+    CK(cudaMalloc(&b.nodes, sizeof(float) * 2ull * m->node_count));
+    CK(cudaMalloc(&b.cells, sizeof(uint32_t) * 32ull * m->cell_count));
+    CK(cudaMalloc(&b.cellMap, sizeof(uint32_t) * (size_t)m->cell_map_count));
+    CK(cudaMemcpy(b.nodes, m->nodes, sizeof(float) * 2ull * m->node_count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.cells, m->cells, sizeof(uint32_t) * 32ull * m->cell_count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.cellMap, m->cell_map, sizeof(uint32_t) * (size_t)m->cell_map_count, cudaMemcpyHostToDevice));
+    b.dev.nodes = b.nodes;
+    b.dev.cells = b.cells;
+    b.dev.cellMap = b.cellMap;
+    s->scenes[scene].bodies.push_back(b);
+    s->releaseBuffers();
+    return VFD_OK;
+}
+
+int vfd_add_rigid_body(vfd_sim* s, const vfd_volume_map* m) { return vfd_scene_add_rigid_body(s, 0, m); }
+
+int vfd_clear_rigid_bodies(vfd_sim* s) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    for (auto& sc : s->scenes) {
+        for (auto& b : sc.bodies) b.release();
+        sc.bodies.clear();
+    }
+    s->releaseBuffers();
+    return VFD_OK;
+}
+
+int vfd_box_map_sizes(const uint32_t resolution[3], uint32_t* node_count, uint32_t* cell_count) {
+    if (!resolution || !node_count || !cell_count) return fail(VFD_E_ARG, "null argument");
+    for (int k = 0; k < 3; k++)
+        if (resolution[k] == 0 || resolution[k] > 1024) return fail(VFD_E_ARG, "resolution must be in 1..1024");
+    box_map_sizes(resolution, *node_count, *cell_count);
+    return VFD_OK;
+}
+
+int vfd_build_box_map(const float box_min[3], const float box_max[3], int32_t inverted, float padding,
+                      const uint32_t resolution[3], float particle_radius, float* nodes, uint32_t* cells,
+                      uint32_t* cell_map, vfd_volume_map* out) {
+    if (!box_min || !box_max || !resolution || !nodes || !cells || !cell_map || !out)
+        return fail(VFD_E_ARG, "null argument");
+    if (!(particle_radius > 0.0f)) return fail(VFD_E_ARG, "particle radius must be positive");
+    for (int k = 0; k < 3; k++)
+        if (!(box_max[k] > box_min[k])) return fail(VFD_E_ARG, "empty box");
+    uint32_t nn = 0, nc = 0;
+    TRY(vfd_box_map_sizes(resolution, &nn, &nc));
+    int devCount = 0;
+    if (cudaGetDeviceCount(&devCount) != cudaSuccess || devCount == 0) return fail(VFD_E_NODEVICE, "no CUDA device");
+    CK(cudaSetDevice(g_device));
+    KernelTable t;
+    t.setRadius(4.0f * particle_radius);
+    const int e = build_box_map_gpu(box_min, box_max, inverted != 0, padding, resolution, particle_radius,
+                                    t.W.data(), t.wZero, t.invStep, nodes, cells, cell_map, out->domain_min,
+                                    out->domain_max, out->cell_size, out->cell_size_inverse);
+    if (e != 0) return fail(VFD_E_CUDA, "volume map build: %s", cudaGetErrorString((cudaError_t)e));
+    out->nodes = nodes;
+    out->cells = cells;
+    out->cell_map = cell_map;
+    for (int k = 0; k < 3; k++) out->resolution[k] = resolution[k];
+    out->field_count = 2;
+    out->node_count = nn;
+    out->cell_count = nc;
+    out->cell_map_count = nc;
+    return VFD_OK;
+}
+
+int vfd_reset(vfd_sim* s) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    if (s->scenes.empty()) return fail(VFD_E_STATE, "no scene");
+    return upload(s);
+}
+
+int vfd_set_graph_mode(vfd_sim* s, int32_t enabled) {
+    TRY(check_sim(s));
+    s->graphMode = enabled != 0;
+    s->graphFailed = false;
+    return VFD_OK;
+}
+
+int vfd_step(vfd_sim* s, vfd_step_stats* stats) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    vfd_step_stats tmp;
+    TRY(run_steps(s, 1, stats ? stats : &tmp, true));
+    const uint32_t f = s->hStatus ? s->hStatus[0] : 0u;
+    if (f & 0x10u) return fail(VFD_E_NAN, "non-finite particle state");
+    return VFD_OK;
+}
+
+int vfd_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    if (count == 0) return VFD_OK;
+    vfd_step_stats tmp;
+    TRY(run_steps(s, count, stats ? stats : &tmp, true));
+    if (s->hStatus && (s->hStatus[0] & 0x10u)) return fail(VFD_E_NAN, "non-finite particle state");
+    return VFD_OK;
+}
+
+int vfd_steps_async(vfd_sim* s, uint32_t count) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    return run_steps(s, count, nullptr, false);
+}
+
+int vfd_synchronize(vfd_sim* s, vfd_step_stats* stats) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    if (!s->uploaded) return VFD_OK;
+    uint32_t flags = 0;
+    TRY(finish_steps(s, stats, flags));
+    CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
+    if (s->hStatus[1]) {
+        if (flags & 0x10u) return fail(VFD_E_NAN, "non-finite particle position");
+        return fail(VFD_E_CAPACITY, "search grid exceeded the cell table during an asynchronous step");
+    }
+    if (stats) fill_stats(s->hScenes[0], stats);
+    return VFD_OK;
+}
+
+int vfd_get_state(vfd_sim* s, float* x, float* v, float* a) { return vfd_scene_get_state(s, 0, x, v, a); }
+
+int vfd_scene_get_state(vfd_sim* s, uint32_t scene, float* x, float* v, float* a) {
+    TRY(check_sim(s));
+    if (scene >= s->scenes.size()) return fail(VFD_E_ARG, "scene %u out of range", scene);
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    CK(cudaStreamSynchronize(s->stream));
+    const Dev& d = s->dev[s->cs];
+    if (x) TRY(scatter_vec(s, scene, d.XN, x));
+    if (v) TRY(scatter_vec(s, scene, d.Vc, v));
+    if (a) TRY(scatter_vec(s, scene, d.A, a));
+    return VFD_OK;
+}
+
+int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    CK(cudaStreamSynchronize(s->stream));
+    const Dev& d = s->dev[s->cs];
+    const uint32_t cnt = (uint32_t)(s->scenes[0].x0.size() / 3);
+    std::vector<uint32_t> pid(cnt);
+    CK(cudaMemcpy(pid.data(), d.PIDc, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
+    std::vector<float4> buf(cnt);
+    if (x) {
+        CK(cudaMemcpy(buf.data(), d.XN, sizeof(float4) * cnt, cudaMemcpyDeviceToHost));
+        for (uint32_t p = 0; p < cnt; p++) {
+            const uint32_t o = pid[p];
+            buf[p].x = x[3 * o]; buf[p].y = x[3 * o + 1]; buf[p].z = x[3 * o + 2];
+        }
+        CK(cudaMemcpy(d.XN, buf.data(), sizeof(float4) * cnt, cudaMemcpyHostToDevice));
+    }
+    if (v) {
+        CK(cudaMemcpy(buf.data(), d.Vc, sizeof(float4) * cnt, cudaMemcpyDeviceToHost));
+        for (uint32_t p = 0; p < cnt; p++) {
+            const uint32_t o = pid[p];
+            buf[p].x = v[3 * o]; buf[p].y = v[3 * o + 1]; buf[p].z = v[3 * o + 2];
+        }
+        CK(cudaMemcpy(d.Vc, buf.data(), sizeof(float4) * cnt, cudaMemcpyHostToDevice));
+    }
+    return VFD_OK;
+}
+
+int vfd_get_field(vfd_sim* s, int32_t field, uint32_t body, float* out) {
+    TRY(check_sim(s));
+    if (!out) return fail(VFD_E_ARG, "null output");
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    CK(cudaStreamSynchronize(s->stream));
+    const Dev& d = s->dev[s->cs];
+    const uint32_t cnt = (uint32_t)(s->scenes[0].x0.size() / 3);
+    switch (field) {
+        case VFD_FIELD_DENSITY: return scatter_scalar(s, 0, d.RHO, out);
+        case VFD_FIELD_FACTOR: return scatter_scalar(s, 0, d.ALPHA, out);
+        case VFD_FIELD_DENSITY_ADVECTION: return scatter_scalar(s, 0, d.RHOADV, out);
+        case VFD_FIELD_PRESSURE_RHO2: return scatter_scalar(s, 0, d.KAPPA, out);
+        case VFD_FIELD_PRESSURE_RHO2_V: return scatter_scalar(s, 0, d.KAPPAV, out);
+        case VFD_FIELD_PRESSURE_RESIDUUM: return scatter_scalar(s, 0, d.RES, out);
+        case VFD_FIELD_PRESSURE_ACCELERATION: return scatter_vec(s, 0, d.AP, out);
+        case VFD_FIELD_VELOCITY_DIFFERENCE: return scatter_vec(s, 0, d.DVc, out);
+        case VFD_FIELD_SURFACE_NORMAL: return scatter_vec(s, 0, d.STN, out);
+        case VFD_FIELD_SURFACE_CURVATURE: return scatter_scalar(s, 0, nullptr, out, 3, d.STN);
+        case VFD_FIELD_DELTA_FINAL_CURVATURE: return scatter_scalar(s, 0, d.DKc, out);
+        case VFD_FIELD_SURFACE_NORMAL_SMOOTH: return scatter_vec(s, 0, d.STNS, out);
+        case VFD_FIELD_SURFACE_CURVATURE_SMOOTH: return scatter_scalar(s, 0, nullptr, out, 3, d.STNS);
+        case VFD_FIELD_BOUNDARY_XJ:
+        case VFD_FIELD_BOUNDARY_VOLUME:
+            if (body >= s->scenes[0].bodies.size()) return fail(VFD_E_ARG, "body %u out of range", body);
+            if (field == VFD_FIELD_BOUNDARY_XJ) return scatter_vec(s, 0, d.XB + (size_t)body * s->stride, out);
+            return scatter_scalar(s, 0, nullptr, out, 3, d.XB + (size_t)body * s->stride);
+        default:
+            (void)cnt;
+            return fail(VFD_E_ARG, "unknown field %d", field);
+    }
+}
+
+int vfd_find_neighbors(vfd_sim* s) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    if (s->n == 0) return VFD_OK;
+    for (int attempt = 0; attempt < 8; attempt++) {
+        const Dev& d = s->dev[s->cs];
+        launch_search(d, s->stream);
+        CK(cudaGetLastError());
+        uint32_t flags = 0;
+        TRY(finish_steps(s, nullptr, flags));
+        if (s->hStatus[1]) {
+            if (flags & 0x10u) return fail(VFD_E_NAN, "non-finite particle position");
+            TRY(grow_cells(s));
+            continue;
+        }
+        // the sorted set becomes the current state; positions follow the new order
+        CK(cudaMemcpyAsync(d.XN, d.X, sizeof(float4) * s->n, cudaMemcpyDeviceToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        s->cs = 1 - s->cs;
+        return VFD_OK;
+    }
+    return fail(VFD_E_CAPACITY, "search grid too large");
+}
+
+int vfd_get_neighbors(vfd_sim* s, uint32_t* counts, uint32_t* offsets, uint32_t* list, uint32_t capacity,
+                      uint32_t* total, uint32_t* sort_indices, uint32_t* cell_keys) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    CK(cudaStreamSynchronize(s->stream));
+    const Dev& d = s->dev[s->cs];
+    const uint32_t cnt = (uint32_t)(s->scenes[0].x0.size() / 3);
+    std::vector<uint32_t> pid(cnt), ncnt(cnt), keys(cnt);
+    CK(cudaMemcpy(pid.data(), d.PIDc, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ncnt.data(), d.NCNT, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(keys.data(), d.KEYS, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
+    std::vector<SceneDev> sc(1);
+    CK(cudaMemcpy(sc.data(), s->dScenes, sizeof(SceneDev), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> c(cnt), off(cnt);
+    for (uint32_t p = 0; p < cnt; p++) c[pid[p]] = ncnt[p] & kCountMask;
+    uint64_t tot = 0;
+    for (uint32_t i = 0; i < cnt; i++) {
+        off[i] = (uint32_t)tot;
+        tot += c[i];
+    }
+    if (total) *total = (uint32_t)tot;
+    if (counts) std::copy(c.begin(), c.end(), counts);
+    if (offsets) std::copy(off.begin(), off.end(), offsets);
+    if (sort_indices) std::copy(pid.begin(), pid.end(), sort_indices);
+    if (cell_keys)
+        for (uint32_t p = 0; p < cnt; p++) cell_keys[pid[p]] = keys[p] - sc[0].cellBase;
+    if (list) {
+        if (tot > capacity) return fail(VFD_E_CAPACITY, "list needs %llu entries", (unsigned long long)tot);
+        std::vector<uint32_t> ell((size_t)s->stride * kMaxNeighbors);
+        CK(cudaMemcpy(ell.data(), d.NBR, sizeof(uint32_t) * ell.size(), cudaMemcpyDeviceToHost));
+        for (uint32_t p = 0; p < cnt; p++) {
+            const uint32_t o = pid[p];
+            for (uint32_t j = 0; j < c[o]; j++) list[off[o] + j] = pid[ell[(size_t)j * s->stride + p]];
+        }
+    }
+    return VFD_OK;
+}
+
+int vfd_get_info(const vfd_sim* s, vfd_info* info) {
+    TRY(check_sim(s));
+    if (!info) return fail(VFD_E_ARG, "null output");
+    const vfd_desc& d = s->scenes[0].desc;
+    SceneDev S = scene_constants(d, 0, (uint32_t)(s->scenes[0].x0.size() / 3), 0, (uint32_t)s->scenes[0].bodies.size());
+    std::memset(info, 0, sizeof(*info));
+    info->ParticleCount = S.count;
+    info->RigidBodyCount = S.bodyCount;
+    info->SupportRadius = S.h;
+    info->SupportRadius2 = S.h2;
+    info->ParticleRadius = S.r;
+    info->ParticleDiameter = S.diam;
+    float dt = S.dt;
+    if (s->uploaded && !s->hScenes.empty()) dt = s->hScenes[0].dt;
+    info->TimeStepSize = dt;
+    info->TimeStepSize2 = dt * dt;
+    info->TimeStepSizeInverse = 1.0f / dt;
+    info->TimeStepSize2Inverse = 1.0f / (dt * dt);
+    info->Volume = S.volume;
+    info->Density0 = S.rho0;
+    info->ParticleMass = S.mass;
+    info->ParticleMassInverse = S.massInv;
+    info->Viscosity = d.Viscosity;
+    info->BoundaryViscosity = d.BoundaryViscosity;
+    info->DynamicViscosity = S.dynVisc;
+    info->DynamicBoundaryViscosity = S.dynBVisc;
+    info->TangentialDistanceFactor = d.TangentialDistanceFactor;
+    info->TangentialDistance = S.tangDist;
+    info->SurfaceTension = S.st;
+    info->SurfaceTensionSampleCount = S.stSamples;
+    info->ClassifierSlope = S.slope;
+    info->ClassifierConstant = S.constant;
+    info->TemporalSmoothing = S.temporal;
+    info->SmoothingFactor = S.smoothing;
+    info->Factor = 0.8f;
+    info->NeighborParticleRadius = S.nbrRadius;
+    info->MonteCarloFactor = S.mcFactor;
+    for (int k = 0; k < 3; k++) info->Gravity[k] = S.g[k];
+    return VFD_OK;
+}
+
+int vfd_get_particle_count(const vfd_sim* s, uint32_t* n) {
+    TRY(check_sim(s));
+    if (!n) return fail(VFD_E_ARG, "null output");
+    *n = (uint32_t)(s->scenes[0].x0.size() / 3);
+    return VFD_OK;
+}
+
+int vfd_scene_get_stats(vfd_sim* s, uint32_t scene, vfd_step_stats* st) {
+    TRY(check_sim(s));
+    if (!st) return fail(VFD_E_ARG, "null output");
+    if (scene >= s->scenes.size()) return fail(VFD_E_ARG, "scene %u out of range", scene);
+    CK(cudaSetDevice(s->device));
+    std::memset(st, 0, sizeof(*st));
+    if (!s->uploaded) return VFD_OK;
+    CK(cudaStreamSynchronize(s->stream));
+    SceneDev S;
+    CK(cudaMemcpy(&S, s->dScenes + scene, sizeof(SceneDev), cudaMemcpyDeviceToHost));
+    fill_stats(S, st);
+    return VFD_OK;
+}
+
+int vfd_get_debug_info(vfd_sim* s, vfd_step_stats* st) { return vfd_scene_get_stats(s, 0, st); }
+
+int vfd_get_current_time_step_size(vfd_sim* s, float* dt) {
+    vfd_step_stats st;
+    TRY(vfd_scene_get_stats(s, 0, &st));
+    if (!dt) return fail(VFD_E_ARG, "null output");
+    *dt = s->uploaded ? st.TimeStepSize : s->scenes[0].desc.TimeStepSize;
+    return VFD_OK;
+}
+
+int vfd_get_max_velocity_magnitude(vfd_sim* s, float* v2) {
+    vfd_step_stats st;
+    TRY(vfd_scene_get_stats(s, 0, &st));
+    if (!v2) return fail(VFD_E_ARG, "null output");
+    *v2 = st.MaxVelocityMagnitude;
+    return VFD_OK;
+}
+
+int vfd_get_kernel_table(const vfd_sim* s, float* w, float* grad_w, float* radius, float* w_zero) {
+    TRY(check_sim(s));
+    if (w) std::copy(s->table.W.begin(), s->table.W.end(), w);
+    if (grad_w) std::copy(s->table.G.begin(), s->table.G.end(), grad_w);
+    if (radius) *radius = s->table.radius;
+    if (w_zero) *w_zero = s->table.wZero;
+    return VFD_OK;
+}
+
+int vfd_simulate(vfd_sim* s, vfd_frame_callback cb, void* user) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    TRY(upload(s));
+    const uint32_t n = (uint32_t)(s->scenes[0].x0.size() / 3);
+    std::vector<float> x(3ull * n), v(3ull * n), a(3ull * n);
+    const uint32_t frames = s->scenes[0].desc.FrameCount;
+    uint32_t lastFrame = 0;
+    for (uint64_t guard = 0; guard < 100000000ull; guard++) {
+        vfd_step_stats st;
+        TRY(vfd_step(s, &st));
+        if (st.FrameIndex != lastFrame) {
+            lastFrame = st.FrameIndex;
+            if (cb) {
+                TRY(vfd_get_state(s, x.data(), v.data(), a.data()));
+                cb(st.FrameIndex - 1, n, x.data(), v.data(), a.data(), st.MaxVelocityMagnitude, st.TimeStepSize, user);
+            }
+        }
+        if (st.FrameIndex >= frames) return VFD_OK;
+        if (n == 0) return VFD_OK;
+    }
+    return fail(VFD_E_STATE, "frame clock did not advance");
+}
+
+}  // extern "C"

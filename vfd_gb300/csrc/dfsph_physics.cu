@@ -1,0 +1,805 @@
+// DFSPH physics kernels of one step (Simulation/DFSPH/DFSPHKernels.cu:24-1046)
+// and the device-side control of its three solver loops
+// (DFSPHImplementation.cu:443-808). One thread per particle slot, neighbours
+// through the ELL list, carried state in cell order.
+//
+// Fusions relative to the reference's 22 kernels:
+//   K2+K3 (density, factor) -> k_density_factor, which also stores the summed
+//         boundary gradient GB = sum_b Vb gradW(x - xb) that K4-K7, K17-K20 reuse;
+//   K7+K8 -> k_div_finish; K15+T1 (CFL max) -> k_visc_finish;
+//   K20+K21 -> k_pres_finish; K6/K19 fused with their FP64 residual reduction;
+//   the CG's thrust transforms and reductions -> k_cg_update / k_cg_p (FP64 dots);
+//   the boundary part of the viscosity SpMV is a per-particle 3x3 matrix built once
+//   per step by k_visc_precond.
+// Loop control: after each iteration a one-block controller updates every
+// scene's iteration count, error and active flag and sets the CUDA-graph while
+// condition (or, in eager mode, a flag the host reads).
+#include <cfloat>
+
+#include "dfsph_common.cuh"
+
+namespace vfd {
+
+enum LoopId { kLoopDiv = 0, kLoopCG = 1, kLoopPres = 2 };
+
+__device__ __forceinline__ bool aborted_p(const Dev& d) { return *(volatile uint32_t*)(d.status + 1) != 0u; }
+
+__device__ __forceinline__ void set_condition(const Dev& d, int loop, uint32_t value) {
+    if (d.condHandle[loop]) cudaGraphSetConditional((cudaGraphConditionalHandle)d.condHandle[loop], value);
+    d.status[4 + loop] = value;
+}
+
+struct Nbr {
+    const uint32_t* list;
+    uint32_t stride, count, flags;
+    __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return __ldg(list + (size_t)j * stride); }
+};
+__device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
+    const uint32_t w = d.NCNT[p];
+    return Nbr{d.NBR + p, d.stride, w & kCountMask, w};
+}
+
+// W and gradW of one pair from one table position (GetW / GetGradientW keep their own
+// range tests: |r|^2 <= R^2 for W, |r| <= R for gradW).
+__device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, float& gs) {
+    const float r2 = dot3(r, r);
+    const float rl = sqrtf(r2);
+    const uint32_t pos = table_pos(d, rl);
+    w = r2 <= d.radius2 ? __ldg(d.WM + pos) : 0.0f;
+    gs = rl <= d.radius ? __ldg(d.GM + pos) : 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// K2 + K3: ComputeDensityKernel (:152-187) and ComputeDFSPHFactorKernel (:189-231).
+__global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    const float3 xi = f3(d.X[p]);
+    const Nbr nb = neighbors(d, p);
+    float wsum = 0.0f, g2 = 0.0f;
+    float3 gi = make_float3(0.f, 0.f, 0.f);
+    const float V = S.volume;
+    for (uint32_t j = 0; j < nb.count; j++) {
+        const uint32_t q = nb[j];
+        const float3 r = xi - f3(d.X[q]);
+        float w, gs;
+        kernel_wg(d, r, w, gs);
+        wsum += w;
+        const float3 gj = (-V * gs) * r;
+        g2 += dot3(gj, gj);
+        gi -= gj;
+    }
+    float rhoB = 0.0f;
+    float3 gb = make_float3(0.f, 0.f, 0.f);
+    if (nb.flags & kHasBoundary) {
+        for (uint32_t b = 0; b < S.bodyCount; b++) {
+            const float4 xb = d.XB[(size_t)b * d.stride + p];
+            if (xb.w > 0.0f) {
+                const float3 r = xi - f3(xb);
+                float w, gs;
+                kernel_wg(d, r, w, gs);
+                rhoB += xb.w * w;
+                gb += (xb.w * gs) * r;
+            }
+        }
+    }
+    gi += gb;
+    d.RHO[p] = (V * d.wZero + V * wsum + rhoB) * S.rho0;
+    g2 += dot3(gi, gi);
+    d.ALPHA[p] = g2 > kEps ? 1.0f / g2 : 0.0f;
+    d.GB[p] = f4(gb, 0.0f);
+}
+
+// Sum_j (vi - vj) . gradW_ij * V + vi . GB  (K4 :498-522, K17 :253-271).
+__device__ __forceinline__ float velocity_divergence(const Dev& d, uint32_t p, const SceneDev& S, const Nbr& nb,
+                                                     float3 xi, float3 vi) {
+    float s = 0.0f;
+    for (uint32_t j = 0; j < nb.count; j++) {
+        const uint32_t q = nb[j];
+        const float3 r = xi - f3(d.X[q]);
+        s += dot3(vi - f3(d.V[q]), kernel_grad(d, r));
+    }
+    s *= S.volume;
+    if (nb.flags & kHasBoundary) s += dot3(vi, f3(d.GB[p]));
+    return s;
+}
+
+// K4: ComputeDensityChangeKernel (:483-529).
+__global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!S.enableDiv) return;
+    const Nbr nb = neighbors(d, p);
+    float rhoAdv = velocity_divergence(d, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    rhoAdv = nb.count < 20u ? 0.0f : fmaxf(rhoAdv, 0.0f);
+    d.RHOADV[p] = rhoAdv;
+    const float alpha = d.ALPHA[p] * S.dtInv;
+    d.ALPHA[p] = alpha;
+    d.KAPPAV[p] = rhoAdv * alpha;
+}
+
+// Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481).
+template <bool DIV>
+__device__ __forceinline__ float3 pressure_accel(const Dev& d, uint32_t p, const SceneDev& S, const Nbr& nb) {
+    const float* kap = DIV ? d.KAPPAV : d.KAPPA;
+    const float ki = kap[p];
+    const float3 xi = f3(d.X[p]);
+    const float V = S.volume;
+    float3 a = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t j = 0; j < nb.count; j++) {
+        const uint32_t q = nb[j];
+        const float sum = ki + __ldg(kap + q);
+        if (fabsf(sum) > kEps) {
+            const float3 g = (-V) * kernel_grad(d, xi - f3(d.X[q]));
+            a += sum * g;
+        }
+    }
+    if (fabsf(ki) > kEps && (nb.flags & kHasBoundary)) a += ki * (-f3(d.GB[p]));
+    return a;
+}
+
+// K5 / K18.
+template <bool DIV>
+__global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!(DIV ? S.div.active : S.pres.active)) return;
+    const Nbr nb = neighbors(d, p);
+    d.AP[p] = f4(pressure_accel<DIV>(d, p, S, nb), 0.0f);
+}
+
+// K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
+// each with ComputeDensityPressureForce (:280-315) and the FP64 residual sum.
+template <bool DIV>
+__global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool valid = inRange && (DIV ? S.div.active : S.pres.active);
+    double res = 0.0;
+    if (valid) {
+        const Nbr nb = neighbors(d, p);
+        const float3 xi = f3(d.X[p]);
+        const float3 ai = f3(d.AP[p]);
+        float f = 0.0f;
+        for (uint32_t j = 0; j < nb.count; j++) {
+            const uint32_t q = nb[j];
+            f += dot3(ai - f3(d.AP[q]), kernel_grad(d, xi - f3(d.X[q])));
+        }
+        f *= S.volume;
+        if (nb.flags & kHasBoundary) f += dot3(ai, f3(d.GB[p]));
+        float r;
+        if (DIV) {
+            f *= S.dt;
+            r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
+            d.KAPPAV[p] -= r * d.ALPHA[p];
+        } else {
+            f *= S.dt2;
+            r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
+            d.KAPPA[p] -= r * d.ALPHA[p];
+        }
+        d.RES[p] = r;
+        res = (double)r;
+    }
+    const double v[1] = {res};
+    const int slot[1] = {0};
+    scene_accumulate<1>(d, sid, valid, v, slot);
+}
+
+// Loop start: the reference's while condition evaluated with error 0, iteration 0
+// (DFSPHImplementation.cu:461, :532).
+template <bool DIV>
+__global__ void k_ctrl_jacobi_init(Dev d) {
+    __shared__ uint32_t any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    const bool ab = aborted_p(d);
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        LoopState& L = DIV ? S.div : S.pres;
+        L.it = 0;
+        L.err = 0.0f;
+        S.acc[0] = 0.0;
+        const uint32_t mn = DIV ? S.minIterD : S.minIterP, mx = DIV ? S.maxIterD : S.maxIterP;
+        const bool enabled = (DIV ? S.enableDiv != 0 : true) && S.count > 0 && !ab;
+        const float eta = DIV ? S.dtInv * S.maxErrD * 0.0001f * S.rho0 : S.maxErrP * 0.0001f * S.rho0;
+        L.active = (enabled && ((0.0f > eta) || 0u < mn) && 0u < mx) ? 1u : 0u;
+        if (L.active) atomicOr(&any, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) set_condition(d, DIV ? kLoopDiv : kLoopPres, any);
+}
+
+// After an iteration: error = -rho0 * sum(res) / N (order-independent form of the
+// reference's thrust::minus fold, DFSPHImplementation.cu:483-491, :554-563).
+template <bool DIV>
+__global__ void k_ctrl_jacobi(Dev d) {
+    __shared__ uint32_t any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        LoopState& L = DIV ? S.div : S.pres;
+        if (!L.active) continue;
+        const double err = -(double)S.rho0 * S.acc[0] / (double)S.count;
+        S.acc[0] = 0.0;
+        L.err = (float)err;
+        L.it++;
+        const uint32_t mn = DIV ? S.minIterD : S.minIterP, mx = DIV ? S.maxIterD : S.maxIterP;
+        const float eta = DIV ? S.dtInv * S.maxErrD * 0.0001f * S.rho0 : S.maxErrP * 0.0001f * S.rho0;
+        const bool again = (err > (double)eta || L.it < mn) && L.it < mx;
+        if (!again && L.it >= mx && err > (double)eta) S.flags |= DIV ? 0x2u : 0x1u;
+        L.active = again ? 1u : 0u;
+        if (again) atomicOr(&any, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) set_condition(d, DIV ? kLoopDiv : kLoopPres, aborted_p(d) ? 0u : any);
+}
+
+// K7 ComputePressureAccelerationAndFactorKernel (:555-602) + K8 ClearAccelerationKernel (:24-37).
+__global__ void __launch_bounds__(kBlock) k_div_finish(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (S.enableDiv) {
+        const Nbr nb = neighbors(d, p);
+        const float3 a = pressure_accel<true>(d, p, S, nb);
+        d.AP[p] = f4(a, 0.0f);
+        const float4 v = d.V[p];
+        d.V[p] = f4(f3(v) + S.dt * a, v.w);
+        d.ALPHA[p] *= S.dt;
+    }
+    d.A[p] = make_float4(S.g[0], S.g[1], S.g[2], 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Surface tension (DFSPHImplementation.cu:810-839).
+// K9: ComputeSurfaceTensionClassificationKernel (DFSPHKernels.cu:881-958).
+__global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!S.enableST) return;
+    const Nbr nb = neighbors(d, p);
+    const float3 xi = f3(d.X[p]);
+    if (nb.count == 0) {
+        d.STN[p] = make_float4(0.f, 0.f, 0.f, 1.0f / S.h);
+        return;
+    }
+    float3 com = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t j = 0; j < nb.count; j++) com += f3(d.X[nb[j]]) - xi;
+    com = make_float3(com.x / S.h, com.y / S.h, com.z / S.h);
+    const float input = sqrtf(dot3(com, com)) / (float)nb.count;
+    float3 nsum = make_float3(0.f, 0.f, 0.f);
+    float curv = 0.0f;
+    if ((float)nb.count <= S.slope * input + S.constant + 0.0f) {
+        const uint32_t samples = S.stSamples;
+        const uint32_t s0 = d.PID[p] * samples / 3u * 3u;
+        const float ratio = S.nbrRadius / S.r;
+        const float lim = ratio * ratio * S.h2;
+        uint32_t count = 0;
+        for (uint32_t k = 0; k < samples; k++) {
+            const uint32_t i3 = s0 + 3u * k;
+            const float3 pt = S.h * make_float3(__ldg(d.halton + i3 % kHaltonCount),
+                                                __ldg(d.halton + (i3 + 1u) % kHaltonCount),
+                                                __ldg(d.halton + (i3 + 2u) % kHaltonCount));
+            bool covered = false;
+            for (uint32_t j = 0; j < nb.count; j++) {
+                const float3 v = pt - (f3(d.X[nb[j]]) - xi);
+                if (dot3(v, v) <= lim) { covered = true; break; }
+            }
+            if (!covered) { nsum += pt; count++; }
+        }
+        if (count > 0) {
+            if (dot3(nsum, nsum) > 0.0f) nsum = normalize3(nsum);
+            curv = 1.0f / S.h * -2.0f * sqrtf(1.0f - S.nbrRadius * S.nbrRadius / (S.r * S.r)) *
+                   cosf(acosf(1.0f - 2.0f * ((float)count / (float)samples)) + S.mcFactor);
+        } else {
+            nsum = make_float3(0.f, 0.f, 0.f);
+        }
+    }
+    d.STN[p] = f4(nsum, curv);
+}
+
+__device__ __forceinline__ bool nonzero3(float4 a) { return a.x != 0.0f || a.y != 0.0f || a.z != 0.0f; }
+
+// K10: ComputeSurfaceTensionNormalsAndCurvatureKernel (:960-1006).
+__global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!S.enableST) return;
+    const float4 ni = d.STN[p];
+    if (!nonzero3(ni)) return;
+    const Nbr nb = neighbors(d, p);
+    const float3 xi = f3(d.X[p]);
+    float3 nc = make_float3(0.f, 0.f, 0.f);
+    float cc = 0.0f, cf = 0.0f;
+    for (uint32_t j = 0; j < nb.count; j++) {
+        const uint32_t q = nb[j];
+        const float4 nj = d.STN[q];
+        if (nonzero3(nj)) {
+            const float3 dx = f3(d.X[q]) - xi;
+            const float num = 1.0f - sqrtf(dot3(dx, dx)) / S.h;
+            nc += f3(nj) * num;
+            cc += nj.w * num;
+            cf += num;
+        }
+    }
+    if (dot3(nc, nc) > 0.0f) nc = normalize3(nc);
+    const float sf = S.smoothing;
+    float3 ns = (1.0f - sf) * f3(ni) + sf * nc;
+    if (dot3(ns, ns) > 0.0f) ns = normalize3(ns);
+    d.STNS[p] = f4(ns, ((1.0f - sf) * ni.w + sf * cc) / (1.0f - sf + sf * cf));
+}
+
+// K11: ComputeSurfaceTensionBlendingKernel (:1008-1046), pass `pass` of SurfaceTensionSmoothPassCount.
+__global__ void __launch_bounds__(kBlock) k_st_blend(Dev d, uint32_t pass) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!S.enableST || pass >= S.stPasses) return;
+    if (nonzero3(d.STN[p])) {
+        const float4 ns = d.STNS[p];
+        float fc = ns.w;
+        if (S.temporal) fc = 0.05f * fc + 0.95f * d.DK[p];
+        const float3 force = f3(ns) * S.st * fc;
+        const float4 a = d.A[p];
+        d.A[p] = f4(f3(a) - S.massInv * force, a.w);
+        d.DK[p] = fc;
+    } else {
+        d.DK[p] = S.temporal ? 0.95f * d.DK[p] : 0.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Viscosity (Weiler 2018 implicit, block-Jacobi PCG), DFSPHImplementation.cu:577-808.
+struct Mat3 {
+    float3 r0, r1, r2;
+};
+__device__ __forceinline__ float3 mul(const Mat3& m, float3 v) {
+    return make_float3(dot3(m.r0, v), dot3(m.r1, v), dot3(m.r2, v));
+}
+__device__ __forceinline__ void add_outer(Mat3& m, float c, float3 a, float3 b) {  // m += c a b^T
+    m.r0 += (c * a.x) * b;
+    m.r1 += (c * a.y) * b;
+    m.r2 += (c * a.z) * b;
+}
+__device__ __forceinline__ Mat3 load_mat(const float4* M, size_t stride, uint32_t p) {
+    Mat3 m;
+    m.r0 = f3(M[p]);
+    m.r1 = f3(M[stride + p]);
+    m.r2 = f3(M[2 * stride + p]);
+    return m;
+}
+__device__ __forceinline__ void store_mat(float4* M, size_t stride, uint32_t p, const Mat3& m) {
+    M[p] = f4(m.r0, 0.f);
+    M[stride + p] = f4(m.r1, 0.f);
+    M[2 * stride + p] = f4(m.r2, 0.f);
+}
+__device__ __forceinline__ Mat3 inverse3(const Mat3& a) {  // cofactors / determinant
+    const float c00 = a.r1.y * a.r2.z - a.r1.z * a.r2.y;
+    const float c01 = a.r1.z * a.r2.x - a.r1.x * a.r2.z;
+    const float c02 = a.r1.x * a.r2.y - a.r1.y * a.r2.x;
+    const float det = a.r0.x * c00 + a.r0.y * c01 + a.r0.z * c02;
+    const float id = 1.0f / det;
+    Mat3 r;
+    r.r0 = make_float3(c00 * id, (a.r0.z * a.r2.y - a.r0.y * a.r2.z) * id, (a.r0.y * a.r1.z - a.r0.z * a.r1.y) * id);
+    r.r1 = make_float3(c01 * id, (a.r0.x * a.r2.z - a.r0.z * a.r2.x) * id, (a.r0.z * a.r1.x - a.r0.x * a.r1.z) * id);
+    r.r2 = make_float3(c02 * id, (a.r0.y * a.r2.x - a.r0.x * a.r2.y) * id, (a.r0.x * a.r1.y - a.r0.y * a.r1.x) * id);
+    return r;
+}
+
+// K12 ComputeViscosityPreconditionerKernel (:604-684) + K13 ComputeViscosityGradientKernel
+// (:686-756, whose boundary term dots a zero vector: b = v) + the boundary matrix BV of
+// the SpMV's boundary term (:793-839): BV p_i = sum_k c_k (p_i . d_k) gradW_k.
+__global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!S.enableVisc) return;
+    const Nbr nb = neighbors(d, p);
+    const float3 xi = f3(d.X[p]);
+    const float eps2 = 0.01f * S.h2;
+    const float cmu = 10.0f * S.dynVisc;
+    Mat3 m = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+    for (uint32_t j = 0; j < nb.count; j++) {
+        const uint32_t q = nb[j];
+        const float3 r = xi - f3(d.X[q]);
+        const float3 g = kernel_grad(d, r);
+        const float c = cmu * (S.mass / d.RHO[q]) / (dot3(r, r) + eps2);
+        add_outer(m, c, r, g);
+    }
+    Mat3 bv = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+    bool hasBV = false;
+    if (S.dynBVisc != 0.0f && (nb.flags & kHasBoundary)) {
+        for (uint32_t b = 0; b < S.bodyCount; b++) {
+            const float4 xb4 = d.XB[(size_t)b * d.stride + p];
+            if (!(xb4.w > 0.0f)) continue;
+            const float3 xb = f3(xb4);
+            float3 normal = -(xi - xb);
+            const float nl = sqrtf(dot3(normal, normal));
+            if (!(nl > 0.0001f)) continue;
+            normal = make_float3(normal.x / nl, normal.y / nl, normal.z / nl);
+            float3 t1, t2;
+            orthogonal_vectors(normal, t1, t2);
+            const float td = S.tangDist;
+            const float3 pos[4] = {xb - t1 * td, xb + t1 * td, xb - t2 * td, xb + t2 * td};
+            const float vol = 0.25f * xb4.w;
+            const float3 d1 = xi - pos[0];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float3 dk = xi - pos[k];
+                const float3 gk = kernel_grad(d, dk);
+                const float c = 10.0f * S.dynBVisc * vol / (dot3(dk, dk) + eps2);
+                add_outer(m, c, d1, gk);  // positionDirection1 in all four terms (:674-677)
+                add_outer(bv, c, gk, dk);
+            }
+            hasBV = true;
+        }
+    }
+    const float f = S.dt / d.RHO[p];
+    Mat3 a;
+    a.r0 = make_float3(1.0f - f * m.r0.x, -f * m.r0.y, -f * m.r0.z);
+    a.r1 = make_float3(-f * m.r1.x, 1.0f - f * m.r1.y, -f * m.r1.z);
+    a.r2 = make_float3(-f * m.r2.x, -f * m.r2.y, 1.0f - f * m.r2.z);
+    store_mat(d.MINV, d.stride, p, inverse3(a));
+    if (hasBV) {
+        store_mat(d.BVM, d.stride, p, bv);
+        d.NCNT[p] = nb.flags | kHasBoundaryVisc;
+    } else if (nb.flags & kHasBoundaryVisc) {
+        d.NCNT[p] = nb.flags & ~kHasBoundaryVisc;
+    }
+    const float4 v = d.V[p];
+    d.CB[p] = v;
+    d.CG[p] = f4(f3(v) + f3(d.DV[p]), 0.0f);
+}
+
+// ComputeMatrixVecProdFunctionKernel (:758-842): (A x)_i.
+__device__ __forceinline__ float3 visc_matvec(const Dev& d, uint32_t p, const SceneDev& S, const float4* vec,
+                                              float3 vi) {
+    const Nbr nb = neighbors(d, p);
+    const float3 xi = f3(d.X[p]);
+    const float eps2 = 0.01f * S.h2;
+    const float cmu = 10.0f * S.dynVisc;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t j = 0; j < nb.count; j++) {
+        const uint32_t q = nb[j];
+        const float3 r = xi - f3(d.X[q]);
+        const float3 g = kernel_grad(d, r);
+        acc += (cmu * (S.mass / d.RHO[q]) * dot3(vi - f3(vec[q]), r) / (dot3(r, r) + eps2)) * g;
+    }
+    if (nb.flags & kHasBoundaryVisc) acc += mul(load_mat(d.BVM, d.stride, p), vi);
+    return vi - (S.dt / d.RHO[p]) * acc;
+}
+
+// Initial residual r = b - A g and the norms |b|^2, |r|^2 (:627-669).
+__global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool valid = inRange && S.enableVisc;
+    double bb = 0.0, rr = 0.0;
+    if (valid) {
+        const float3 g = f3(d.CG[p]);
+        const float3 ag = visc_matvec(d, p, S, d.CG, g);
+        const float3 b = f3(d.CB[p]);
+        const float3 r = b - ag;
+        d.CR[p] = f4(r, 0.0f);
+        bb = (double)b.x * b.x + (double)b.y * b.y + (double)b.z * b.z;
+        rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+    }
+    const double v[2] = {bb, rr};
+    const int slot[2] = {0, 1};
+    scene_accumulate<2>(d, sid, valid, v, slot);
+}
+
+// Early outs of SolveViscosity (:646-675).
+__global__ void k_ctrl_cg0(Dev d) {
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        S.cgIt = 0;
+        S.cgActive = 0;
+        S.cgUpdateP = 0;
+        S.cgZeroG = 0;
+        S.cgDone = 1;
+        S.cgErr = 0.0f;
+        if (!S.enableVisc || aborted_p(d)) continue;
+        const double rhs = S.acc[0], rr = S.acc[1];
+        S.acc[0] = S.acc[1] = S.acc[2] = 0.0;
+        S.cgRhs = rhs;
+        S.cgRR = rr;
+        if (rhs == 0.0) {
+            S.cgZeroG = 1;
+            continue;
+        }
+        const double e = (double)S.maxErrV;
+        S.cgThr = fmax(e * e * 0.0001 * rhs, (double)FLT_MIN);
+        if (rr < S.cgThr) {
+            S.cgErr = (float)sqrt(rr / rhs);
+            continue;
+        }
+        S.cgDone = 0;
+    }
+}
+
+// p = M^-1 r and |r . p| (:677-691).
+__global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool valid = inRange && S.enableVisc && !S.cgDone;
+    double rz = 0.0;
+    if (valid) {
+        const float3 r = f3(d.CR[p]);
+        const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
+        d.CP[p] = f4(z, 0.0f);
+        rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+    }
+    const double v[1] = {rz};
+    const int slot[1] = {0};
+    scene_accumulate<1>(d, sid, valid, v, slot);
+}
+
+__global__ void k_ctrl_cg1(Dev d) {
+    __shared__ uint32_t any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        if (!S.enableVisc || S.cgDone) continue;
+        S.cgAbsNew = fabs(S.acc[0]);
+        S.acc[0] = 0.0;
+        S.cgErr = (float)sqrt(S.cgRR / S.cgRhs);
+        const bool run = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
+        S.cgActive = run ? 1u : 0u;
+        if (run) atomicOr(&any, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
+}
+
+// Loop body 1: Ap and p . Ap (:695-720).
+__global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool valid = inRange && S.cgActive;
+    double pap = 0.0;
+    if (valid) {
+        const float3 pv = f3(d.CP[p]);
+        const float3 ap = visc_matvec(d, p, S, d.CP, pv);
+        d.CAP[p] = f4(ap, 0.0f);
+        pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
+    }
+    const double v[1] = {pap};
+    const int slot[1] = {0};
+    scene_accumulate<1>(d, sid, valid, v, slot);
+}
+
+// Loop body 2: g += alpha p, r -= alpha Ap, |r|^2, z = M^-1 r, r . z (:722-784).
+__global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool valid = inRange && S.cgActive;
+    double rr = 0.0, rz = 0.0;
+    if (valid) {
+        const float alpha = (float)(S.cgAbsNew / S.acc[0]);
+        const float3 pv = f3(d.CP[p]);
+        const float3 g = f3(d.CG[p]) + pv * alpha;
+        const float3 r = f3(d.CR[p]) - f3(d.CAP[p]) * alpha;
+        d.CG[p] = f4(g, 0.0f);
+        d.CR[p] = f4(r, 0.0f);
+        const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
+        d.CZ[p] = f4(z, 0.0f);
+        rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+        rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+    }
+    const double v[2] = {rr, rz};
+    const int slot[2] = {1, 2};
+    scene_accumulate<2>(d, sid, valid, v, slot);
+}
+
+// Loop control: break on |r|^2 < threshold, else beta and the next iteration (:754-805).
+__global__ void k_ctrl_cg(Dev d) {
+    __shared__ uint32_t any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        S.cgUpdateP = 0;
+        if (!S.cgActive) continue;
+        const double rr = S.acc[1], rz = S.acc[2];
+        S.acc[0] = S.acc[1] = S.acc[2] = 0.0;
+        S.cgRR = rr;
+        S.cgErr = (float)sqrt(rr / S.cgRhs);
+        if (rr < S.cgThr) {
+            S.cgActive = 0;
+            S.cgDone = 1;
+            continue;
+        }
+        const double absOld = S.cgAbsNew;
+        S.cgAbsNew = fabs(rz);
+        S.cgBeta = (float)(S.cgAbsNew / absOld);
+        S.cgIt++;
+        S.cgUpdateP = 1;
+        const bool again = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
+        if (!again) S.flags |= 0x4u;
+        S.cgActive = again ? 1u : 0u;
+        if (again) atomicOr(&any, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
+}
+
+// Loop body 3: p = beta p + z (:786-802).
+__global__ void __launch_bounds__(kBlock) k_cg_p(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!S.cgUpdateP) return;
+    d.CP[p] = f4(f3(d.CP[p]) * S.cgBeta + f3(d.CZ[p]), 0.0f);
+}
+
+// K15 ApplyViscosityForceKernel (:844-862) + T1, the CFL maximum of |v + a dt|^2
+// (ComputeMaxVelocityMagnitude, DFSPHImplementation.cu:430-441).
+__global__ void __launch_bounds__(kBlock) k_visc_finish(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < d.n && !aborted_p(d);
+    const uint32_t sid = valid ? scene_of(d, p) : 0u;
+    float m = 0.0f;
+    if (valid) {
+        const SceneDev& S = d.scenes[sid];
+        const float3 v = f3(d.V[p]);
+        float3 a = f3(d.A[p]);
+        if (S.enableVisc) {
+            const float3 g = S.cgZeroG ? make_float3(0.f, 0.f, 0.f) : f3(d.CG[p]);
+            a += 1.0f / S.dt * (g - v);
+            d.A[p] = f4(a, 0.0f);
+            d.DV[p] = f4(g - v, 0.0f);
+        }
+        const float3 w = v + a * S.dt;
+        m = dot3(w, w);
+    }
+    scene_max_float(d, sid, valid, m);
+}
+
+// ComputeTimeStepSize (DFSPHImplementation.cu:395-428) + the frame clock (:148-167).
+__global__ void k_ctrl_dt(Dev d) {
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        if (aborted_p(d)) continue;
+        float mv = fmaxf(0.1f, __uint_as_float(S.maxV2Bits));
+        if (mv < 1.0e-9f) mv = 1.0e-9f;
+        S.maxV2 = mv;
+        float dt = 0.4f * (S.diam / sqrtf(mv));
+        dt = fminf(dt, S.maxDt);
+        dt = fmaxf(dt, S.minDt);
+        S.dt = dt;
+        S.dt2 = dt * dt;
+        S.dtInv = 1.0f / dt;
+        S.dt2Inv = 1.0f / S.dt2;
+        S.stSamplesUsed = S.stSamples;
+        S.stSamples = S.csdFix > 0 ? (uint32_t)S.csdFix : (uint32_t)(int)((float)S.csd * dt);
+        S.frameTime += dt;
+    }
+}
+
+// K16 ComputeVelocityKernel (:39-52).
+__global__ void __launch_bounds__(kBlock) k_velocity(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    const float4 v = d.V[p];
+    d.V[p] = f4(f3(v) + S.dt * f3(d.A[p]), v.w);
+}
+
+// K17 ComputeDensityAdvectionKernel (:233-278).
+__global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    const Nbr nb = neighbors(d, p);
+    const float delta = velocity_divergence(d, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    const float rhoAdv = d.RHO[p] / S.rho0 + S.dt * delta;
+    d.RHOADV[p] = rhoAdv;
+    const float alpha = d.ALPHA[p] * S.dt2Inv;
+    d.ALPHA[p] = alpha;
+    d.KAPPA[p] = -fminf(1.0f - rhoAdv, 0.0f) * alpha;
+}
+
+// K20 ComputePressureAccelerationAndVelocityKernel (:434-481) + K21 ComputePositionKernel (:54-67);
+// positions go to XN so that the neighbours' positions read here stay unchanged.
+__global__ void __launch_bounds__(kBlock) k_pres_finish(Dev d) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || aborted_p(d)) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    const Nbr nb = neighbors(d, p);
+    const float3 a = pressure_accel<false>(d, p, S, nb);
+    d.AP[p] = f4(a, 0.0f);
+    const float3 v = f3(d.V[p]) + S.dt * a;
+    d.V[p] = f4(v, 0.0f);
+    const float3 x = f3(d.X[p]) + S.dt * v;
+    d.XN[p] = f4(x, 0.0f);
+    if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(d.status, 0x10u);
+}
+
+// End of step: frame clock and iteration counter (DFSPHImplementation.cu:148-169);
+// status[7] counts the steps completed since the host last looked.
+__global__ void k_ctrl_end(Dev d) {
+    if (threadIdx.x == 0 && !aborted_p(d)) d.status[7]++;
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        if (aborted_p(d)) continue;
+        S.frameDue = 0;
+        if (S.frameIndex < S.frameCount && S.frameTime >= S.frameLength) {
+            S.frameDue = 1;
+            S.frameTime = 0.0f;
+            S.frameIndex++;
+        }
+        S.iteration++;
+        atomicOr(d.status, S.flags);
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_density(const Dev& d, cudaStream_t s) {
+    k_density_factor<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+}
+void launch_div_init(const Dev& d, cudaStream_t s) {
+    k_div_init<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d);
+}
+void launch_div_iter(const Dev& d, cudaStream_t s) {
+    k_pressure_accel<true><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_jacobi_iter<true><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d);
+}
+void launch_div_finish(const Dev& d, cudaStream_t s) { k_div_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d); }
+void launch_surface_tension(const Dev& d, uint32_t maxPasses, cudaStream_t s) {
+    k_st_classify<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_st_smooth<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    for (uint32_t pass = 0; pass < maxPasses; pass++) k_st_blend<<<blocks_for(d.n), kBlock, 0, s>>>(d, pass);
+}
+void launch_visc_init(const Dev& d, cudaStream_t s) {
+    k_visc_precond<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_visc_setup<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_cg0<<<1, 256, 0, s>>>(d);
+    k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_cg1<<<1, 256, 0, s>>>(d);
+}
+void launch_cg_iter(const Dev& d, cudaStream_t s) {
+    k_cg_spmv<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_cg<<<1, 256, 0, s>>>(d);
+    k_cg_p<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+}
+void launch_visc_finish_dt(const Dev& d, cudaStream_t s) {
+    k_visc_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_dt<<<1, 256, 0, s>>>(d);
+    k_velocity<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+}
+void launch_pres_init(const Dev& d, cudaStream_t s) {
+    k_pres_init<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_jacobi_init<false><<<1, 256, 0, s>>>(d);
+}
+void launch_pres_iter(const Dev& d, cudaStream_t s) {
+    k_pressure_accel<false><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_jacobi_iter<false><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d);
+}
+void launch_pres_finish(const Dev& d, cudaStream_t s) {
+    k_pres_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    k_ctrl_end<<<1, 256, 0, s>>>(d);
+}
+
+}  // namespace vfd
