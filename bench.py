@@ -1,0 +1,316 @@
+"""Benchmark of the DFSPH step: particle-steps/s on the 1M-particle viscous dam break.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (BASELINE config 2): 100^3 jittered lattice (r = 0.005, a 1 m block) in
+a 2 x 1.5 x 1 m box (volume-map boundary), dynamic viscosity 50 Pa s with the
+implicit CG solve (relative tolerance 1e-4), surface tension 0.05, CFL time
+steps, pressure solve to <= 0.1 % mean density error. Synthetic seeded data.
+
+value : particle-steps/s with the state resident in HBM (whole step as one
+        CUDA graph, timed with CUDA events on the library's stream).
+e2e   : the same metric through the C-ABI with host buffers: each step uploads
+        positions and velocities from pinned host memory, steps, and reads back
+        positions, velocities and accelerations.
+roofline: the kernel with the largest share of the step, timed per launch with
+        CUDA events (eager launches), against the measured HBM copy bandwidth.
+cpu_baseline: the CPU restatement of the reference method (oracle, FP32, all
+        host threads) on a 64k-particle sample of the same configuration.
+--impl reference: that CPU restatement alone (the reference has no CPU DFSPH and
+        its CUDA path needs Windows headers and a missing glm submodule).
+Multi-GPU: replicas only (one independent scene per rank, weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @1M, ≤0.1% density err: plain vs batched vs fwd+adjoint"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per particle of each kernel: the fields it must read and write
+# once (float3 = 12 B, float = 4 B), neighbour fields assumed cache-served and the
+# neighbour list not counted (it is an implementation choice).
+ALGO_BYTES = {
+    "k_cg_spmv": 12 + 4 + 12 + 12,          # x, rho, p -> Ap (+ dot)
+    "k_cg_update": 12 * 4 + 36 + 12 * 3,    # p, g, r, Ap, Minv -> g, r, z
+    "k_cg_p": 12 * 2 + 12,                  # p, z -> p
+    "k_pressure_accel": 12 + 4 + 12,        # x, kappa -> a_p
+    "k_jacobi_iter": 12 + 12 + 4 + 4 + 4 + 4,  # x, a_p, rho_adv, alpha, kappa -> kappa, res
+    "k_density_factor": 12 + 4 + 4,         # x -> rho, alpha
+    "k_neighbors": 12 + 4,                  # x -> count (list excluded)
+    "k_visc_precond": 12 + 4 + 12 + 12 + 36 + 12 + 12,
+    "k_visc_setup": 12 + 4 + 12 + 12 + 12,
+    "k_st_classify": 12 + 16,
+    "k_boundary": 12 + 16,
+    "k_pres_finish": 12 + 4 + 12 + 12 + 12,
+    "k_pres_init": 12 + 12 + 4 + 4 + 4 + 4 + 4,
+    "k_div_init": 12 + 12 + 4 + 4 + 4 + 4,
+    "k_div_finish": 12 + 4 + 12 + 4 + 12 + 12,
+    "k_rank_gather": 4 + 4 + 12 + 12 + 12 + 4 + 4 + 4 + 4 + 12 + 12 + 12 + 4 + 4,
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines: list[str] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, fl in rows for k, v in enumerate(fl) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+def c2_config(n_side: int) -> dict:
+    edge = n_side * 0.01
+    return {"workload": f"viscous dam break, {n_side ** 3} particles ({n_side}^3 lattice, r=0.005)",
+            "particles": n_side ** 3, "box_m": [round(2 * edge + 0.02, 4), round(1.5 * edge + 0.02, 4),
+                                                 round(edge + 0.02, 4)],
+            "dynamic_viscosity_pa_s": 50.0, "cg_relative_tolerance": 1e-4, "surface_tension": 0.05,
+            "pressure_error_bound": "0.1% of rho0 (MaxPressureSolverError=10)", "min_solver_iterations": 2,
+            "boundary": "volume map (GPU-built, 40x30x20 cells)", "parallelism": "replicas",
+            "l2": "inputs larger than L2 (state ~0.5 GB for 1M particles)"}
+
+
+def cpu_baseline(n_side: int, steps: int, warmup: int):
+    """The oracle (FP32, all host threads) on a c2-parameter sample."""
+    from oracle import oracle as O
+    from vfd_gb300 import scenes
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    s = scenes.viscous_dam_break(n_side=n_side)
+    sim = O.scene_oracle(s, 32)
+    for _ in range(warmup):
+        sim.step()
+    t = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    el = time.perf_counter() - t
+    n = len(s["x"])
+    return n * steps / el, el, n, O.get_threads()
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    n_side = 40
+    value, el, n, cores = cpu_baseline(n_side, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(c2_config(100), sample=f"{n} particles ({n_side}^3) with the same parameters"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"c2 parameters at {n} particles, {args.steps} steps after {args.warmup}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference's DFSPH step (no CPU DFSPH exists in the reference)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-side", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+
+    import vfd_gb300 as V
+    from vfd_gb300 import scenes
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    V.lib().vfd_set_device(local)
+
+    s = scenes.viscous_dam_break(n_side=args.n_side, seed=scenes.config_seed(2) + rank)
+    n = len(s["x"])
+    sim = V.scene_simulation(s)
+    sim.Steps(1)
+    lanes = sim.Autotune(2)  # per-kernel lanes per particle, state restored
+    sim.Steps(args.warmup)
+    stream = torch.cuda.ExternalStream(sim.GetStream())
+
+    def timed(k):
+        sim.GetLaunchCount(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.StepsAsync(k)
+        e1.record(stream)
+        st = sim.Synchronize()
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        return e0.elapsed_time(e1), st, sim.GetLaunchCount()
+
+    with ClockSampler(local) as clk:
+        try:
+            ms, st, launches = timed(args.steps)
+        except V.VFDError as e:  # grid grew past the table mid-run: the table was enlarged, time again
+            log("retiming after", e)
+            sim.Steps(1)
+            ms, st, launches = timed(args.steps)
+    clocks = clk.summary()
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = n * ws * args.steps / (ms_max / 1e3)
+
+    # end to end through the C-ABI with pinned host buffers
+    pin = lambda: torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+    xh, vh, ah = pin(), pin(), pin()
+    sim.GetStateInto(xh, vh, ah)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sim.SetState(xh, vh)
+        sim.OnUpdate()
+        sim.GetStateInto(xh, vh, ah)
+    el = time.perf_counter() - t0
+    t = torch.tensor([el], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e = {"value": n * ws * args.e2e_steps / float(t.item()), "unit": UNIT, "h2d_bytes_per_step": 24 * n,
+           "d2h_bytes_per_step": 36 * n}
+
+    # per-kernel event timing of eager launches -> dominant kernel and roofline
+    prof = sim.ProfileKernels(3)
+    tot = sum(v[1] for v in prof.values())
+    name, (cnt, kms) = max(prof.items(), key=lambda kv: kv[1][1])
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if name in ALGO_BYTES and cnt:
+        bytes_launch = ALGO_BYTES[name] * n
+        achieved = bytes_launch / (kms / cnt / 1e3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            with open(tp) as f:
+                tr = json.load(f).get(name)
+            if tr:
+                traffic = tr["bytes_per_particle"] * n
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": kms / cnt,
+                "share_of_step": kms / tot}
+    shares = {k: round(v[1] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:8]}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 reductions)", "data": "synthetic (seeded jittered lattice)",
+        "config": c2_config(args.n_side), "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
+        "roofline": roof, "kernel_shares": shares, "lanes_per_particle": lanes,
+        "solver": {k: st[k] for k in ("DivergenceSolverIterationCount", "PressureSolverIterationCount",
+                                      "ViscositySolverIterationCount", "PressureSolverError", "TimeStepSize",
+                                      "MaxNeighborCount", "Flags")},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"oracle FP32 on c2 parameters at {nc} particles (40^3), "
+                                          f"{args.cpu_steps} steps after 2 ({el:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

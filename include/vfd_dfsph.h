@@ -319,6 +319,48 @@ int vfd_scene_add_rigid_body(vfd_sim* sim, uint32_t scene, const vfd_volume_map*
 int vfd_scene_get_state(vfd_sim* sim, uint32_t scene, float* x, float* v, float* a);
 int vfd_scene_get_stats(vfd_sim* sim, uint32_t scene, vfd_step_stats* stats);
 
+/* Per-kernel time of eagerly launched steps (CUDA events on the launch stream). */
+typedef struct vfd_kernel_time {
+    char name[48];
+    uint32_t launches;
+    double total_ms;
+} vfd_kernel_time;
+
+/*
+ * Runs `steps` steps with every kernel launched from the host and bracketed by
+ * CUDA events, and reports each kernel's launch count and summed time (no
+ * counterpart in the reference, whose DFSPHDebugInfo timers are host wall
+ * clocks around synchronised phases, Structures/DFSPHDebugInfo.h:10-15).
+ */
+int vfd_profile_kernels(vfd_sim* sim, uint32_t steps, vfd_kernel_time* out, uint32_t capacity, uint32_t* count);
+
+/*
+ * Lanes per particle (4, 8 or 16) of the neighbour-loop kernels, in the order
+ * density+factor, density change, pressure acceleration, Jacobi iteration,
+ * divergence finish, surface classification, surface smoothing, viscosity
+ * preconditioner, viscosity setup, CG matrix-vector product, density advection,
+ * pressure finish, neighbour search (no counterpart in the reference, which
+ * launches every kernel with 256 threads, one per particle).
+ */
+int vfd_set_lanes(vfd_sim* sim, const uint8_t* lanes, uint32_t count);
+int vfd_get_lanes(const vfd_sim* sim, uint8_t* lanes, uint32_t count);
+
+/*
+ * Autotuner: runs `steps` steps from a snapshot of the current state once per
+ * lane count, times every neighbour-loop kernel with CUDA events, keeps the
+ * fastest lane count per kernel and restores the state exactly (positions,
+ * velocities, accelerations and all carried solver state; the simulation does not
+ * advance). Per-step diagnostics (vfd_get_field, vfd_get_neighbors) reflect the
+ * last tuning step until the next step. lanes_out (may be NULL) receives the choice.
+ */
+int vfd_autotune(vfd_sim* sim, uint32_t steps, uint8_t* lanes_out, uint32_t count);
+
+/* The cudaStream_t all work of `sim` is issued on (for events recorded by the caller). */
+int vfd_get_stream(vfd_sim* sim, void** stream);
+
+/* Number of kernel launches executed since creation (or the last reset), counted on the device. */
+int vfd_get_launch_count(vfd_sim* sim, uint64_t* launches, int32_t reset);
+
 /* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
 int vfd_set_device(int32_t device);
 

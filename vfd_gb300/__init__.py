@@ -29,8 +29,16 @@ EXPORTS = [
     "vfd_get_info", "vfd_get_particle_count", "vfd_get_current_time_step_size", "vfd_get_max_velocity_magnitude",
     "vfd_get_debug_info", "vfd_get_kernel_table", "vfd_set_graph_mode", "vfd_create_batch",
     "vfd_get_scene_count", "vfd_scene_set_fluid", "vfd_scene_add_rigid_body", "vfd_scene_get_state",
-    "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version",
+    "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version", "vfd_profile_kernels",
+    "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
 ]
+
+TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
+                 "st_smooth", "visc_precond", "visc_setup", "cg_spmv", "pres_init", "pres_finish", "neighbors"]
+
+
+class vfd_kernel_time(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
 
 
 class VFDError(RuntimeError):
@@ -94,6 +102,12 @@ def lib() -> C.CDLL:
                 "vfd_scene_get_state": [P, C.c_uint32, f32p, f32p, f32p],
                 "vfd_scene_get_stats": [P, C.c_uint32, C.POINTER(vfd_step_stats)],
                 "vfd_set_device": [C.c_int32],
+                "vfd_profile_kernels": [P, C.c_uint32, C.POINTER(vfd_kernel_time), C.c_uint32, u32p],
+                "vfd_get_stream": [P, C.POINTER(C.c_void_p)],
+                "vfd_get_launch_count": [P, C.POINTER(C.c_uint64), C.c_int32],
+                "vfd_set_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
+                "vfd_get_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
+                "vfd_autotune": [P, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_last_error": [],
                 "vfd_abi_version": [],
             }
@@ -326,6 +340,13 @@ class DFSPHSimulation:
         _check(lib().vfd_scene_get_state(self._h, scene, _fptr(x), _fptr(v), _fptr(a)), "vfd_scene_get_state")
         return x, v, a
 
+    def GetStateInto(self, x=None, v=None, a=None, scene: int = 0):
+        """GetState into caller arrays (float32, C-contiguous, (n, 3)), e.g. pinned host memory."""
+        for arr in (x, v, a):
+            if arr is not None and (arr.dtype != np.float32 or not arr.flags.c_contiguous):
+                raise ValueError("arrays must be C-contiguous float32")
+        _check(lib().vfd_scene_get_state(self._h, scene, _fptr(x), _fptr(v), _fptr(a)), "vfd_scene_get_state")
+
     def SetState(self, x=None, v=None):
         xp = vp = None
         if x is not None:
@@ -340,6 +361,39 @@ class DFSPHSimulation:
         out = np.zeros(shape, np.float32)
         _check(lib().vfd_get_field(self._h, field, body, _fptr(out)), "vfd_get_field")
         return out
+
+    def ProfileKernels(self, steps: int) -> dict:
+        """{kernel name: (launches, total ms)} over `steps` eagerly launched steps."""
+        cap = 64
+        arr = (vfd_kernel_time * cap)()
+        cnt = C.c_uint32()
+        _check(lib().vfd_profile_kernels(self._h, steps, arr, cap, C.byref(cnt)), "vfd_profile_kernels")
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(cnt.value)}
+
+    def Autotune(self, steps: int = 2) -> dict:
+        """Per-kernel lanes per particle chosen by timing (state restored afterwards)."""
+        arr = (C.c_uint8 * 16)()
+        _check(lib().vfd_autotune(self._h, steps, arr, 16), "vfd_autotune")
+        return {k: arr[i] for i, k in enumerate(TUNED_KERNELS)}
+
+    def SetLanes(self, lanes):
+        arr = (C.c_uint8 * len(lanes))(*lanes)
+        _check(lib().vfd_set_lanes(self._h, arr, len(lanes)), "vfd_set_lanes")
+
+    def GetLanes(self) -> list:
+        arr = (C.c_uint8 * 16)()
+        _check(lib().vfd_get_lanes(self._h, arr, 16), "vfd_get_lanes")
+        return list(arr)[:len(TUNED_KERNELS)]
+
+    def GetStream(self) -> int:
+        p = C.c_void_p()
+        _check(lib().vfd_get_stream(self._h, C.byref(p)), "vfd_get_stream")
+        return p.value or 0
+
+    def GetLaunchCount(self, reset: bool = False) -> int:
+        c = C.c_uint64()
+        _check(lib().vfd_get_launch_count(self._h, C.byref(c), int(reset)), "vfd_get_launch_count")
+        return c.value
 
     def FindNeighbors(self):
         _check(lib().vfd_find_neighbors(self._h), "vfd_find_neighbors")

@@ -43,6 +43,43 @@ int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, f
                       uint32_t* cellMap, float dminOut[3], float dmaxOut[3], float csOut[3], float csiOut[3]);
 }  // namespace vfd
 
+namespace vfd {
+LaunchProfiler* g_profiler = nullptr;
+
+// Original-order export of a per-slot float4 field (x, y, z) of slots [begin, begin + count).
+__global__ void k_export3(const uint32_t* pid, const float4* src, float* out, uint32_t begin, uint32_t count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t p = begin + k;
+    const uint32_t o = pid[p];
+    if (o >= count) return;
+    const float4 v = src[p];
+    out[3 * (size_t)o] = v.x;
+    out[3 * (size_t)o + 1] = v.y;
+    out[3 * (size_t)o + 2] = v.z;
+}
+// Original-order export of a scalar field (float, or component `comp` of a float4 field).
+__global__ void k_export1(const uint32_t* pid, const float* src, const float4* src4, int comp, float* out,
+                          uint32_t begin, uint32_t count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t p = begin + k;
+    const uint32_t o = pid[p];
+    if (o >= count) return;
+    out[o] = src4 ? (&src4[p].x)[comp] : src[p];
+}
+// Original-order import into a float4 field (w kept).
+__global__ void k_import3(const uint32_t* pid, const float* in, float4* dst, uint32_t begin, uint32_t count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t p = begin + k;
+    const uint32_t o = pid[p];
+    if (o >= count) return;
+    const float4 w = dst[p];
+    dst[p] = make_float4(in[3 * (size_t)o], in[3 * (size_t)o + 1], in[3 * (size_t)o + 2], w.w);
+}
+}  // namespace vfd
+
 using namespace vfd;
 
 namespace {
@@ -166,6 +203,7 @@ struct vfd_sim {
     std::vector<float> halton;
     bool graphMode = true;
     bool graphFailed = false;
+    uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
 
     // layout
     bool allocated = false, uploaded = false;
@@ -175,6 +213,7 @@ struct vfd_sim {
     Dev dev[2]{};
     int cs = 0;  // set holding the current carried state
     float4* XB = nullptr;
+    float* dStage = nullptr;     // 3 floats per particle, original order
     SceneDev* dScenes = nullptr;
     BodyDev* dBodies = nullptr;
     uint32_t* dStatus = nullptr;
@@ -273,6 +312,20 @@ uint32_t estimate_cells(const vfd_sim* s) {
     return (uint32_t)std::min<uint64_t>(total, 0xF0000000ull);
 }
 
+// Reduction buckets to their identities (sums 0, max 0, min cell INT_MAX, max cell INT_MIN).
+int reset_buckets(vfd_sim* s, const Dev& d) {
+    const size_t ns = d.nscenes;
+    CK(cudaMemset(d.ACCB, 0, sizeof(double) * ns * kAccSlots * kBuckets * 16u));
+    CK(cudaMemset(d.MAXB, 0, sizeof(uint32_t) * ns * 2u * kBuckets * 32u));
+    std::vector<int32_t> mm(ns * 6u * kBuckets * 32u);
+    for (size_t sc = 0; sc < ns; sc++)
+        for (uint32_t k = 0; k < 6; k++)
+            for (uint32_t b = 0; b < kBuckets * 32u; b++)
+                mm[(sc * 6u + k) * kBuckets * 32u + b] = k < 3 ? INT_MAX : INT_MIN;
+    CK(cudaMemcpy(d.MMB, mm.data(), sizeof(int32_t) * mm.size(), cudaMemcpyHostToDevice));
+    return VFD_OK;
+}
+
 int allocate(vfd_sim* s) {
     s->releaseBuffers();
     uint32_t n = 0, maxBodies = 0;
@@ -294,6 +347,7 @@ int allocate(vfd_sim* s) {
     base.maxBodies = maxBodies;
     base.cellCap = s->cellCap;
     base.scanBlocks = scan_block_count(s->cellCap);
+    std::memcpy(base.lanes, s->lanes, sizeof(base.lanes));
     float4* X[2];
     float4* V[2];
     float4* DV[2];
@@ -317,7 +371,7 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.KAPPAV, st));
     TRY(dalloc(s, &base.RES, st));
     TRY(dalloc(s, &base.XB, st * std::max<uint32_t>(1u, maxBodies)));
-    TRY(dalloc(s, &base.NBR, st * kMaxNeighbors));
+    TRY(dalloc(s, &base.NBR, st * kRow));
     TRY(dalloc(s, &base.NCNT, st));
     TRY(dalloc(s, &base.KEY, st));
     TRY(dalloc(s, &base.KEYS, st));
@@ -342,6 +396,10 @@ int allocate(vfd_sim* s) {
     for (const auto& sc : s->scenes) bodyTotal += (uint32_t)sc.bodies.size();
     TRY(dalloc(s, &s->dBodies, std::max<uint32_t>(1u, bodyTotal)));
     TRY(dalloc(s, &s->dStatus, 16));
+    TRY(dalloc(s, &s->dStage, 3 * st));
+    TRY(dalloc(s, &base.ACCB, (size_t)base.nscenes * kAccSlots * kBuckets * 16u));
+    TRY(dalloc(s, &base.MAXB, (size_t)base.nscenes * 2u * kBuckets * 32u));
+    TRY(dalloc(s, &base.MMB, (size_t)base.nscenes * 6u * kBuckets * 32u));
     TRY(dalloc(s, &s->dWM, kTableRes));
     TRY(dalloc(s, &s->dGM, kTableRes));
     TRY(dalloc(s, &s->dHalton, kHaltonCount));
@@ -388,6 +446,7 @@ int allocate(vfd_sim* s) {
     CK(cudaMemset(base.STN, 0, sizeof(float4) * st));
     CK(cudaMemset(base.STNS, 0, sizeof(float4) * st));
     CK(cudaMemset(base.XB, 0, sizeof(float4) * st * std::max<uint32_t>(1u, maxBodies)));
+    TRY(reset_buckets(s, base));
     s->allocated = true;
     return VFD_OK;
 }
@@ -490,6 +549,7 @@ int upload(vfd_sim* s) {
     CK(cudaMemset(d.A, 0, sizeof(float4) * st));
     CK(cudaMemcpy(s->dScenes, s->hScenes.data(), sizeof(SceneDev) * s->hScenes.size(), cudaMemcpyHostToDevice));
     CK(cudaMemset(s->dStatus, 0, 16 * sizeof(uint32_t)));
+    TRY(reset_buckets(s, d));
     CK(cudaDeviceSynchronize());
     s->uploaded = true;
     return VFD_OK;
@@ -749,40 +809,65 @@ int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
 int check_sim(const vfd_sim* s) { return s ? VFD_OK : fail(VFD_E_ARG, "null handle"); }
 
 int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out) {
-    const uint32_t n = s->n;
-    std::vector<float4> buf(n);
-    std::vector<uint32_t> pid(n);
-    CK(cudaMemcpy(buf.data(), dsrc, sizeof(float4) * n, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(pid.data(), s->dev[s->cs].PIDc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
     const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
-    for (uint32_t p = b; p < b + cnt; p++) {
-        const uint32_t o = pid[p];
-        out[3 * o] = buf[p].x;
-        out[3 * o + 1] = buf[p].y;
-        out[3 * o + 2] = buf[p].z;
-    }
+    if (cnt == 0) return VFD_OK;
+    k_export3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, dsrc, s->dStage, b, cnt);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->dStage, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
 
 int scatter_scalar(vfd_sim* s, uint32_t scene, const float* dsrc, float* out, int comp = -1, const float4* d4 = nullptr) {
-    const uint32_t n = s->n;
-    std::vector<float> buf(n);
-    std::vector<float4> buf4;
-    std::vector<uint32_t> pid(n);
-    if (d4) {
-        buf4.resize(n);
-        CK(cudaMemcpy(buf4.data(), d4, sizeof(float4) * n, cudaMemcpyDeviceToHost));
-    } else {
-        CK(cudaMemcpy(buf.data(), dsrc, sizeof(float) * n, cudaMemcpyDeviceToHost));
-    }
-    CK(cudaMemcpy(pid.data(), s->dev[s->cs].PIDc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
     const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
-    for (uint32_t p = b; p < b + cnt; p++) {
-        float v = d4 ? (comp == 3 ? buf4[p].w : (&buf4[p].x)[comp]) : buf[p];
-        out[pid[p]] = v;
-    }
+    if (cnt == 0) return VFD_OK;
+    k_export1<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, dsrc, d4, comp, s->dStage, b, cnt);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->dStage, sizeof(float) * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
+
+int gather_vec(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
+    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    if (cnt == 0) return VFD_OK;
+    CK(cudaMemcpyAsync(s->dStage, in, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyHostToDevice, s->stream));
+    k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, s->dStage, ddst, b, cnt);
+    CK(cudaGetLastError());
+    return VFD_OK;
+}
+
+// Event-timed eager launches (vfd_profile_kernels).
+struct EventProfiler : LaunchProfiler {
+    struct Rec {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    cudaError_t err = cudaSuccess;
+    cudaEvent_t get() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) { err = r; return nullptr; }
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    void begin(const char* name, cudaStream_t st) override {
+        Rec r{name, get(), get()};
+        if (r.a) cudaEventRecord(r.a, st);
+        recs.push_back(r);
+    }
+    void end(cudaStream_t st) override {
+        if (!recs.empty() && recs.back().b) cudaEventRecord(recs.back().b, st);
+    }
+    ~EventProfiler() override {
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
 
 }  // namespace
 
@@ -1072,7 +1157,6 @@ int vfd_scene_get_state(vfd_sim* s, uint32_t scene, float* x, float* v, float* a
     if (scene >= s->scenes.size()) return fail(VFD_E_ARG, "scene %u out of range", scene);
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
-    CK(cudaStreamSynchronize(s->stream));
     const Dev& d = s->dev[s->cs];
     if (x) TRY(scatter_vec(s, scene, d.XN, x));
     if (v) TRY(scatter_vec(s, scene, d.Vc, v));
@@ -1084,28 +1168,10 @@ int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
     TRY(check_sim(s));
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
-    CK(cudaStreamSynchronize(s->stream));
     const Dev& d = s->dev[s->cs];
-    const uint32_t cnt = (uint32_t)(s->scenes[0].x0.size() / 3);
-    std::vector<uint32_t> pid(cnt);
-    CK(cudaMemcpy(pid.data(), d.PIDc, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
-    std::vector<float4> buf(cnt);
-    if (x) {
-        CK(cudaMemcpy(buf.data(), d.XN, sizeof(float4) * cnt, cudaMemcpyDeviceToHost));
-        for (uint32_t p = 0; p < cnt; p++) {
-            const uint32_t o = pid[p];
-            buf[p].x = x[3 * o]; buf[p].y = x[3 * o + 1]; buf[p].z = x[3 * o + 2];
-        }
-        CK(cudaMemcpy(d.XN, buf.data(), sizeof(float4) * cnt, cudaMemcpyHostToDevice));
-    }
-    if (v) {
-        CK(cudaMemcpy(buf.data(), d.Vc, sizeof(float4) * cnt, cudaMemcpyDeviceToHost));
-        for (uint32_t p = 0; p < cnt; p++) {
-            const uint32_t o = pid[p];
-            buf[p].x = v[3 * o]; buf[p].y = v[3 * o + 1]; buf[p].z = v[3 * o + 2];
-        }
-        CK(cudaMemcpy(d.Vc, buf.data(), sizeof(float4) * cnt, cudaMemcpyHostToDevice));
-    }
+    if (x) TRY(gather_vec(s, 0, x, d.XN));
+    if (v) TRY(gather_vec(s, 0, v, d.Vc));
+    CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
 
@@ -1196,11 +1262,11 @@ int vfd_get_neighbors(vfd_sim* s, uint32_t* counts, uint32_t* offsets, uint32_t*
         for (uint32_t p = 0; p < cnt; p++) cell_keys[pid[p]] = keys[p] - sc[0].cellBase;
     if (list) {
         if (tot > capacity) return fail(VFD_E_CAPACITY, "list needs %llu entries", (unsigned long long)tot);
-        std::vector<uint32_t> ell((size_t)s->stride * kMaxNeighbors);
-        CK(cudaMemcpy(ell.data(), d.NBR, sizeof(uint32_t) * ell.size(), cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> rows((size_t)cnt * kRow);
+        CK(cudaMemcpy(rows.data(), d.NBR, sizeof(uint32_t) * rows.size(), cudaMemcpyDeviceToHost));
         for (uint32_t p = 0; p < cnt; p++) {
             const uint32_t o = pid[p];
-            for (uint32_t j = 0; j < c[o]; j++) list[off[o] + j] = pid[ell[(size_t)j * s->stride + p]];
+            for (uint32_t j = 0; j < c[o]; j++) list[off[o] + j] = pid[rows[(size_t)p * kRow + j]];
         }
     }
     return VFD_OK;
@@ -1317,6 +1383,180 @@ int vfd_simulate(vfd_sim* s, vfd_frame_callback cb, void* user) {
         if (n == 0) return VFD_OK;
     }
     return fail(VFD_E_STATE, "frame clock did not advance");
+}
+
+int vfd_profile_kernels(vfd_sim* s, uint32_t steps, vfd_kernel_time* out, uint32_t capacity, uint32_t* count) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    if (count) *count = 0;
+    if (s->n == 0 || steps == 0) return VFD_OK;
+    EventProfiler prof;
+    int rc = VFD_OK;
+    g_profiler = &prof;
+    for (uint32_t k = 0; k < steps && rc == VFD_OK; k++) {
+        rc = launch_eager(s);
+        if (rc == VFD_OK) s->cs = 1 - s->cs;
+    }
+    g_profiler = nullptr;
+    TRY(rc);
+    uint32_t flags = 0;
+    TRY(finish_steps(s, nullptr, flags));
+    const uint32_t completed = s->hStatus[7];
+    CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
+    if (s->hStatus[1] || completed != steps) return fail(VFD_E_STATE, "a profiled step aborted; run vfd_step first");
+    if (prof.err != cudaSuccess) return fail(VFD_E_CUDA, "event creation: %s", cudaGetErrorString(prof.err));
+    std::vector<vfd_kernel_time> acc;
+    for (const auto& r : prof.recs) {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, r.a, r.b));
+        auto it = std::find_if(acc.begin(), acc.end(), [&](const vfd_kernel_time& t) { return r.name == t.name; });
+        if (it == acc.end()) {
+            vfd_kernel_time t;
+            std::memset(&t, 0, sizeof(t));
+            std::snprintf(t.name, sizeof(t.name), "%s", r.name.c_str());
+            acc.push_back(t);
+            it = acc.end() - 1;
+        }
+        it->launches++;
+        it->total_ms += ms;
+    }
+    if (count) *count = (uint32_t)std::min<size_t>(acc.size(), capacity);
+    if (out) std::copy(acc.begin(), acc.begin() + std::min<size_t>(acc.size(), capacity), out);
+    return VFD_OK;
+}
+
+int vfd_set_lanes(vfd_sim* s, const uint8_t* lanes, uint32_t count) {
+    TRY(check_sim(s));
+    if (!lanes || count == 0 || count > 16) return fail(VFD_E_ARG, "lanes: 1..16 entries");
+    for (uint32_t k = 0; k < count; k++)
+        if (lanes[k] != 4 && lanes[k] != 8 && lanes[k] != 16) return fail(VFD_E_ARG, "lanes must be 4, 8 or 16");
+    std::memcpy(s->lanes, lanes, count);
+    for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+    s->releaseGraphs();
+    return VFD_OK;
+}
+
+int vfd_get_lanes(const vfd_sim* s, uint8_t* lanes, uint32_t count) {
+    TRY(check_sim(s));
+    if (!lanes || count == 0 || count > 16) return fail(VFD_E_ARG, "lanes: 1..16 entries");
+    std::memcpy(lanes, s->lanes, count);
+    return VFD_OK;
+}
+
+int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count) {
+    TRY(check_sim(s));
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    if (s->n == 0 || steps == 0) return VFD_OK;
+    static const char* names[kTunedCount] = {"k_density_factor", "k_div_init", "k_pressure_accel", "k_jacobi_iter",
+                                             "k_div_finish", "k_st_classify", "k_st_smooth", "k_visc_precond",
+                                             "k_visc_setup", "k_cg_spmv", "k_pres_init", "k_pres_finish",
+                                             "k_neighbors"};
+    const uint8_t cand[3] = {4, 8, 16};
+    // snapshot of everything a step carries: positions, the current state set, scenes
+    const size_t st = s->stride;
+    const int cs0 = s->cs;
+    const Dev d0 = s->dev[cs0];
+    float4 *xn = nullptr, *v = nullptr, *dv = nullptr, *acc = nullptr;
+    float* dk = nullptr;
+    uint32_t* pid = nullptr;
+    SceneDev* sc = nullptr;
+    uint32_t* stat = nullptr;
+    auto release = [&]() {
+        cudaFree(xn); cudaFree(v); cudaFree(dv); cudaFree(acc); cudaFree(dk); cudaFree(pid); cudaFree(sc);
+        cudaFree(stat);
+    };
+    cudaError_t e = cudaMalloc(&xn, sizeof(float4) * st);
+    if (e == cudaSuccess) e = cudaMalloc(&v, sizeof(float4) * st);
+    if (e == cudaSuccess) e = cudaMalloc(&dv, sizeof(float4) * st);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(float4) * st);
+    if (e == cudaSuccess) e = cudaMalloc(&dk, sizeof(float) * st);
+    if (e == cudaSuccess) e = cudaMalloc(&pid, sizeof(uint32_t) * st);
+    if (e == cudaSuccess) e = cudaMalloc(&sc, sizeof(SceneDev) * s->hScenes.size());
+    if (e == cudaSuccess) e = cudaMalloc(&stat, sizeof(uint32_t) * 16);
+    auto copy_all = [&](bool save) -> cudaError_t {
+        cudaError_t r = cudaSuccess;
+        auto cp = [&](void* a, void* b, size_t bytes) {
+            if (r == cudaSuccess) r = cudaMemcpyAsync(save ? a : b, save ? b : a, bytes, cudaMemcpyDeviceToDevice, s->stream);
+        };
+        cp(xn, d0.XN, sizeof(float4) * st);
+        cp(v, d0.Vc, sizeof(float4) * st);
+        cp(dv, d0.DVc, sizeof(float4) * st);
+        cp(acc, d0.A, sizeof(float4) * st);
+        cp(dk, d0.DKc, sizeof(float) * st);
+        cp(pid, d0.PIDc, sizeof(uint32_t) * st);
+        cp(sc, s->dScenes, sizeof(SceneDev) * s->hScenes.size());
+        cp(stat, s->dStatus, sizeof(uint32_t) * 16);
+        if (r == cudaSuccess) r = cudaStreamSynchronize(s->stream);
+        return r;
+    };
+    if (e == cudaSuccess) e = copy_all(true);
+    if (e != cudaSuccess) {
+        release();
+        return fail(VFD_E_CUDA, "autotune snapshot: %s", cudaGetErrorString(e));
+    }
+    double times[kTunedCount][3] = {};
+    int rc = VFD_OK;
+    for (int c = 0; c < 3 && rc == VFD_OK; c++) {
+        for (int k = 0; k < 2; k++)
+            for (int t = 0; t < kTunedCount; t++) s->dev[k].lanes[t] = cand[c];
+        EventProfiler prof;
+        g_profiler = &prof;
+        for (uint32_t k = 0; k < steps && rc == VFD_OK; k++) {
+            rc = launch_eager(s);
+            if (rc == VFD_OK) s->cs = 1 - s->cs;
+        }
+        g_profiler = nullptr;
+        if (rc == VFD_OK) {
+            cudaError_t r = cudaStreamSynchronize(s->stream);
+            if (r != cudaSuccess) rc = fail(VFD_E_CUDA, "autotune: %s", cudaGetErrorString(r));
+        }
+        for (const auto& rec : prof.recs) {
+            float ms = 0.0f;
+            if (rc == VFD_OK && cudaEventElapsedTime(&ms, rec.a, rec.b) == cudaSuccess)
+                for (int t = 0; t < kTunedCount; t++)
+                    if (rec.name == names[t]) times[t][c] += ms;
+        }
+        s->cs = cs0;
+        e = copy_all(false);
+        if (e != cudaSuccess && rc == VFD_OK) rc = fail(VFD_E_CUDA, "autotune restore: %s", cudaGetErrorString(e));
+    }
+    release();
+    if (rc != VFD_OK) {
+        for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+        return rc;
+    }
+    for (int t = 0; t < kTunedCount; t++) {
+        int best = 1;
+        for (int c = 0; c < 3; c++)
+            if (times[t][c] > 0.0 && times[t][c] < times[t][best]) best = c;
+        s->lanes[t] = cand[best];
+    }
+    for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+    s->releaseGraphs();
+    if (lanes_out) std::memcpy(lanes_out, s->lanes, std::min<uint32_t>(count, 16));
+    return VFD_OK;
+}
+
+int vfd_get_stream(vfd_sim* s, void** stream) {
+    TRY(check_sim(s));
+    if (!stream) return fail(VFD_E_ARG, "null output");
+    *stream = (void*)s->stream;
+    return VFD_OK;
+}
+
+int vfd_get_launch_count(vfd_sim* s, uint64_t* launches, int32_t reset) {
+    TRY(check_sim(s));
+    if (!launches) return fail(VFD_E_ARG, "null output");
+    CK(cudaSetDevice(s->device));
+    *launches = 0;
+    if (!s->allocated) return VFD_OK;
+    uint32_t v = 0;
+    TRY(read_flag(s, 8, v));
+    *launches = v;
+    if (reset) CK(cudaMemsetAsync(s->dStatus + 8, 0, sizeof(uint32_t), s->stream));
+    return VFD_OK;
 }
 
 }  // extern "C"

@@ -119,8 +119,9 @@ __device__ __forceinline__ MapSample map_lookup(const BodyDev& m, float3 p) {
 
 // K1: ComputeVolumeAndBoundaryKernel (DFSPHKernels.cu:69-150).
 __global__ void __launch_bounds__(kBlock) k_boundary(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || *(volatile uint32_t*)(d.status + 1)) return;
+    if (p >= d.n || is_aborted(d)) return;
     const SceneDev& S = d.scenes[scene_of(d, p)];
     uint32_t flags = d.NCNT[p] & ~kHasBoundary;
     if (S.bodyCount == 0) {

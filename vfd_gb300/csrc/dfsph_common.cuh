@@ -11,7 +11,8 @@
 //   XN   float4 positions written by the integrator, read by the next search
 //   per-step fields: A, AP, GB float4; RHO, ALPHA, RHOADV, KAPPA, KAPPAV, RES float
 //   XB   float4 [body slot][slot] boundary sample (xb, Vb) per rigid body
-//   NBR  u32 [70][slot] neighbour slots (ELL, column = neighbour rank)
+//   NBR  u32 [slot][72] neighbour slots, one row per particle in the reference's
+//        z, y, x cell order (at most 70 used), read by groups of G lanes
 //   NCNT u32 [slot] neighbour count | flag bits
 // The reference keeps one 120-byte AoS DFSPHParticle per particle
 // (Structures/DFSPHParticle.h:8-33) in original order.
@@ -26,12 +27,22 @@ constexpr uint32_t kMaxNeighbors = 70u;      // ParticleSearchKernels.cuh:7
 constexpr uint32_t kTableRes = 10000u;       // Kernel/DFSPHKernels.h:143
 constexpr uint32_t kHaltonCount = 49152u;    // HaltonVec323.cuh:4
 constexpr uint32_t kBlock = 128u;            // threads per particle kernel
+constexpr uint32_t kRow = 72u;               // neighbour row length (70 rounded up to 8)
+constexpr uint32_t kGroup = 8u;              // lanes per particle in neighbour loops
+constexpr uint32_t kBuckets = 32u;           // reduction buckets per scene and quantity
+constexpr uint32_t kAccSlots = 4u;           // FP64 accumulators per scene
 constexpr float kEps = 1.0e-5f;              // Core/Math/Math.h:6
 
 // NCNT flag bits (above the 7-bit count).
 constexpr uint32_t kCountMask = 0xFFu;
 constexpr uint32_t kHasBoundary = 1u << 8;   // some body gave this particle Vb > 0
 constexpr uint32_t kHasBoundaryVisc = 1u << 9;
+
+// Neighbour-loop kernels whose lanes per particle (4, 8 or 16) the autotuner picks.
+enum TunedKernel {
+    kTDensity = 0, kTDivInit, kTPAccel, kTJacobi, kTDivFinish, kTStClassify, kTStSmooth, kTViscPrecond,
+    kTViscSetup, kTSpmv, kTPresInit, kTPresFinish, kTNeighbors, kTunedCount
+};
 
 // Per-scene solver loop state (one Jacobi or CG loop).
 struct LoopState {
@@ -79,7 +90,6 @@ struct SceneDev {
     float cgErr;
     double cgRhs, cgThr, cgAbsNew, cgRR;
     float cgAlpha, cgBeta;
-    double acc[4];             // FP64 reduction accumulators of the current sub-stage
 };
 
 // Rigid body volume map (SDFDeviceData, Utility/SDF/SDFDeviceData.cuh:549-566).
@@ -122,7 +132,13 @@ struct Dev {
     float wZero, invStep, radius, radius2;
     const float* halton;
     uint32_t* status;          // [0] sticky error flags, [1] abort (capacity)
+    // Reduction buckets, 128 B apart so that concurrent atomics land in different
+    // L2 slices; blocks pick bucket blockIdx % 32, controllers fold and reset them.
+    double* ACCB;              // [scene][kAccSlots][kBuckets] x16: FP64 sums
+    uint32_t* MAXB;            // [scene][2][kBuckets] x32: max |v + a dt|^2 bits, max neighbours
+    int32_t* MMB;              // [scene][6][kBuckets] x32: min cell xyz, max cell xyz
     unsigned long long condHandle[3];  // while-node handles (div, cg, pres); 0 = eager
+    uint8_t lanes[16];                 // lanes per particle of each TunedKernel
 };
 
 // ---------------------------------------------------------------- float3 math
@@ -172,17 +188,49 @@ __device__ __forceinline__ void orthogonal_vectors(float3 vec, float3& x, float3
 __device__ __forceinline__ uint32_t scene_of(const Dev& d, uint32_t i) { return d.nscenes == 1 ? 0u : (uint32_t)d.SID[i]; }
 
 // ------------------------------------------------------------ reductions
-// Adds `v` into scenes[sid].acc[k] (FP64). Warps whose lanes share one scene
-// reduce with shuffles first; a block whose slots lie in one scene reduces in
-// shared memory and issues one atomic.
-template <int K>
+__device__ __forceinline__ double* acc_bucket(const Dev& d, uint32_t s, int slot, uint32_t b) {
+    return d.ACCB + ((size_t)(s * kAccSlots + (uint32_t)slot) * kBuckets + b) * 16u;
+}
+__device__ __forceinline__ uint32_t* max_bucket(const Dev& d, uint32_t s, int k, uint32_t b) {
+    return d.MAXB + ((size_t)(s * 2u + (uint32_t)k) * kBuckets + b) * 32u;
+}
+__device__ __forceinline__ int32_t* mm_bucket(const Dev& d, uint32_t s, int k, uint32_t b) {
+    return d.MMB + ((size_t)(s * 6u + (uint32_t)k) * kBuckets + b) * 32u;
+}
+// Controller side: sum (and zero) one accumulator's buckets.
+__device__ __forceinline__ double fold_acc(const Dev& d, uint32_t s, int slot) {
+    double t = 0.0;
+    for (uint32_t b = 0; b < kBuckets; b++) {
+        double* q = acc_bucket(d, s, slot, b);
+        t += *q;
+        *q = 0.0;
+    }
+    return t;
+}
+__device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
+    uint32_t t = 0u;
+    for (uint32_t b = 0; b < kBuckets; b++) {
+        uint32_t* q = max_bucket(d, s, k, b);
+        t = max(t, *q);
+        *q = 0u;
+    }
+    return t;
+}
+
+// Adds `v` into scene `sid`'s FP64 accumulators `slot` (bucket blockIdx % 32). A block
+// whose particles lie in one scene reduces in shared memory and issues one atomic per
+// accumulator; otherwise each valid thread adds its own value. Kernels running G lanes
+// per particle pass G (a block then covers blockDim.x / G particles); all threads of
+// the block must call this.
+template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, bool valid, const double (&v)[K],
                                                  const int (&slot)[K]) {
     __shared__ double sm[kBlock / 32][4];
     __shared__ int uniformBlock;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t first = blockIdx.x * blockDim.x;
-    const uint32_t last = min(first + blockDim.x, d.n) - 1u;
+    const uint32_t first = blockIdx.x * (blockDim.x / G);
+    const uint32_t last = min(first + blockDim.x / G, d.n) - 1u;
+    const uint32_t bucket = blockIdx.x % kBuckets;
     if (threadIdx.x == 0) uniformBlock = (first < d.n) && (scene_of(d, first) == scene_of(d, last)) ? 1 : 0;
     __syncthreads();
     if (uniformBlock) {
@@ -203,30 +251,91 @@ __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, boo
             for (int k = 0; k < K; k++) {
                 double t = 0.0;
                 for (uint32_t w = 0; w < blockDim.x / 32u; w++) t += sm[w][k];
-                atomicAdd(&d.scenes[sc].acc[slot[k]], t);
+                if (t != 0.0) atomicAdd(acc_bucket(d, sc, slot[k], bucket), t);
             }
         }
     } else if (valid) {
 #pragma unroll
-        for (int k = 0; k < K; k++) atomicAdd(&d.scenes[sid].acc[slot[k]], v[k]);
+        for (int k = 0; k < K; k++) atomicAdd(acc_bucket(d, sid, slot[k], bucket), v[k]);
     }
 }
 
+// Max of non-negative floats (they order like their bit patterns) into max bucket 0.
 __device__ __forceinline__ void scene_max_float(const Dev& d, uint32_t sid, bool valid, float v) {
-    // non-negative floats order like their bit patterns
     float m = valid ? v : 0.0f;
     const uint32_t s0 = __shfl_sync(0xffffffffu, sid, 0);
     const bool uniform = __all_sync(0xffffffffu, sid == s0 || !valid);
+    const uint32_t bucket = blockIdx.x % kBuckets;
     if (uniform) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((threadIdx.x & 31u) == 0 && m > 0.0f) atomicMax(&d.scenes[s0].maxV2Bits, __float_as_uint(m));
+        const uint32_t mb = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+        if ((threadIdx.x & 31u) == 0 && mb > 0u) atomicMax(max_bucket(d, s0, 0, bucket), mb);
     } else if (valid) {
-        atomicMax(&d.scenes[sid].maxV2Bits, __float_as_uint(m));
+        atomicMax(max_bucket(d, sid, 0, bucket), __float_as_uint(m));
     }
 }
 
+// Every kernel of the step counts its own launch in status[8] (block 0, thread 0),
+// so graph runs with data-dependent loop counts report how many kernels ran.
+#define VFD_COUNT_LAUNCH(d)                                                     \
+    do {                                                                        \
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd((d).status + 8, 1u); \
+    } while (0)
+
+// The abort flag is raised only by the search kernels; later kernels read it through
+// the read-only path (one L2 request per SM instead of one per thread).
+__device__ __forceinline__ bool is_aborted(const Dev& d) { return __ldg(d.status + 1) != 0u; }
+
+// G consecutive lanes of a warp that share one particle in a neighbour loop;
+// lanes stride the neighbour row and reduce their partial sums with shuffles.
+template <uint32_t G>
+struct Group {
+    uint32_t p, lane, mask;
+    __device__ __forceinline__ Group() {
+        const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+        p = t / G;
+        lane = t % G;
+        mask = G == 32u ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(G - 1u)));
+    }
+    __device__ __forceinline__ float sum(float v) const {
+#pragma unroll
+        for (uint32_t o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+        return v;
+    }
+    __device__ __forceinline__ float3 sum(float3 v) const { return make_float3(sum(v.x), sum(v.y), sum(v.z)); }
+    __device__ __forceinline__ uint32_t sum(uint32_t v) const {
+#pragma unroll
+        for (uint32_t o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+        return v;
+    }
+};
+
 // Host-side launch helpers.
 inline uint32_t blocks_for(uint32_t n, uint32_t block = kBlock) { return (n + block - 1) / block; }
+
+// Optional per-launch timing of eagerly launched kernels (CUDA events on the launch
+// stream); set only while vfd_profile_kernels runs, never during graph capture.
+struct LaunchProfiler {
+    virtual void begin(const char* name, cudaStream_t s) = 0;
+    virtual void end(cudaStream_t s) = 0;
+    virtual ~LaunchProfiler() {}
+};
+extern LaunchProfiler* g_profiler;
+#define VFD_LAUNCH(name, stream, ...)                          \
+    do {                                                       \
+        if (::vfd::g_profiler) ::vfd::g_profiler->begin(name, stream); \
+        __VA_ARGS__;                                           \
+        if (::vfd::g_profiler) ::vfd::g_profiler->end(stream); \
+    } while (0)
+
+// Launch of a neighbour-loop kernel with the tuned lanes per particle; KERNEL(G) names
+// the instantiation (a function-like macro).
+#define VFD_LAUNCH_LANES(name, id, KERNEL)                                                          \
+    do {                                                                                            \
+        switch (d.lanes[id]) {                                                                      \
+            case 4: VFD_LAUNCH(name, s, KERNEL(4)<<<blocks_for(d.n * 4u), kBlock, 0, s>>>(d)); break;   \
+            case 16: VFD_LAUNCH(name, s, KERNEL(16)<<<blocks_for(d.n * 16u), kBlock, 0, s>>>(d)); break; \
+            default: VFD_LAUNCH(name, s, KERNEL(8)<<<blocks_for(d.n * 8u), kBlock, 0, s>>>(d)); break;  \
+        }                                                                                           \
+    } while (0)
 
 }  // namespace vfd

@@ -1,7 +1,11 @@
 // DFSPH physics kernels of one step (Simulation/DFSPH/DFSPHKernels.cu:24-1046)
 // and the device-side control of its three solver loops
-// (DFSPHImplementation.cu:443-808). One thread per particle slot, neighbours
-// through the ELL list, carried state in cell order.
+// (DFSPHImplementation.cu:443-808).
+//
+// Neighbour loops run G lanes per particle (Group<G>): the lanes stride the
+// particle's neighbour row, so one warp-wide gather reads a few runs of
+// consecutive cell-sorted slots instead of 32 scattered ones, and the partial
+// sums meet in a shuffle tree. Element-wise kernels run one thread per particle.
 //
 // Fusions relative to the reference's 22 kernels:
 //   K2+K3 (density, factor) -> k_density_factor, which also stores the summed
@@ -22,7 +26,7 @@ namespace vfd {
 
 enum LoopId { kLoopDiv = 0, kLoopCG = 1, kLoopPres = 2 };
 
-__device__ __forceinline__ bool aborted_p(const Dev& d) { return *(volatile uint32_t*)(d.status + 1) != 0u; }
+__device__ __forceinline__ bool aborted_p(const Dev& d) { return is_aborted(d); }
 
 __device__ __forceinline__ void set_condition(const Dev& d, int loop, uint32_t value) {
     if (d.condHandle[loop]) cudaGraphSetConditional((cudaGraphConditionalHandle)d.condHandle[loop], value);
@@ -30,13 +34,41 @@ __device__ __forceinline__ void set_condition(const Dev& d, int loop, uint32_t v
 }
 
 struct Nbr {
-    const uint32_t* list;
-    uint32_t stride, count, flags;
-    __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return __ldg(list + (size_t)j * stride); }
+    const uint32_t* row;
+    uint32_t count, flags;
+    __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return __ldg(row + j); }
 };
 __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
-    return Nbr{d.NBR + p, d.stride, w & kCountMask, w};
+    return Nbr{d.NBR + (size_t)p * kRow, w & kCountMask, w};
+}
+
+// Neighbour loop of one group. Each lane owns 4 consecutive entries of the row and
+// loads them with one 16-byte load; the group covers 4G entries per round. The first
+// round's load does not wait for the count (rows have 72 slots, entries past the count
+// are masked), so the count, the indices and the particle's own fields are fetched
+// together, and a lane's 4 gathers are independent and usually touch one cell's run
+// of consecutive slots. Masked entries use the particle itself as a stand-in index.
+template <uint32_t G, class F>
+__device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb, uint32_t self, F&& f) {
+    static_assert(4u * G <= kRow, "first round must stay inside the row");
+    const uint4* rows4 = reinterpret_cast<const uint4*>(nb.row);
+    uint4 q4 = __ldg(rows4 + grp.lane);
+    for (uint32_t base = 4u * grp.lane; base < nb.count;) {
+        const uint32_t q[4] = {base + 0u < nb.count ? q4.x : self, base + 1u < nb.count ? q4.y : self,
+                               base + 2u < nb.count ? q4.z : self, base + 3u < nb.count ? q4.w : self};
+        const uint32_t next = base + 4u * G;
+        if (next < nb.count) q4 = __ldg(rows4 + next / 4u);
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; u++) f(q[u], base + u < nb.count);
+        base = next;
+    }
+}
+
+// gradW factor of one pair: GetGradientW(r) = gs * r (Kernel/DFSPHKernels.h:67-80).
+__device__ __forceinline__ float grad_factor(const Dev& d, float3 r) {
+    const float rl = sqrtf(dot3(r, r));
+    return rl <= d.radius ? __ldg(d.GM + table_pos(d, rl)) : 0.0f;
 }
 
 // W and gradW of one pair from one table position (GetW / GetGradientW keep their own
@@ -49,27 +81,37 @@ __device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, floa
     gs = rl <= d.radius ? __ldg(d.GM + pos) : 0.0f;
 }
 
+#define GROUP_PROLOGUE(G)                    \
+    const Group<G> grp;                      \
+    const uint32_t p = grp.p;                \
+    if (p >= d.n || aborted_p(d)) return;
+
 // ---------------------------------------------------------------------------
 // K2 + K3: ComputeDensityKernel (:152-187) and ComputeDFSPHFactorKernel (:189-231).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     const float3 xi = f3(d.X[p]);
     const Nbr nb = neighbors(d, p);
     float wsum = 0.0f, g2 = 0.0f;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     const float V = S.volume;
-    for (uint32_t j = 0; j < nb.count; j++) {
-        const uint32_t q = nb[j];
+    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
         const float3 r = xi - f3(d.X[q]);
         float w, gs;
         kernel_wg(d, r, w, gs);
+        if (!ok) return;
         wsum += w;
         const float3 gj = (-V * gs) * r;
         g2 += dot3(gj, gj);
         gi -= gj;
-    }
+    });
+    wsum = grp.sum(wsum);
+    g2 = grp.sum(g2);
+    gi = grp.sum(gi);
+    if (grp.lane != 0) return;
     float rhoB = 0.0f;
     float3 gb = make_float3(0.f, 0.f, 0.f);
     if (nb.flags & kHasBoundary) {
@@ -91,28 +133,32 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     d.GB[p] = f4(gb, 0.0f);
 }
 
-// Sum_j (vi - vj) . gradW_ij * V + vi . GB  (K4 :498-522, K17 :253-271).
-__device__ __forceinline__ float velocity_divergence(const Dev& d, uint32_t p, const SceneDev& S, const Nbr& nb,
-                                                     float3 xi, float3 vi) {
+// Sum_j (vi - vj) . gradW_ij * V + vi . GB  (K4 :498-522, K17 :253-271); valid on lane 0.
+template <uint32_t G>
+__device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
+                                                     const Nbr& nb, float3 xi, float3 vi) {
     float s = 0.0f;
-    for (uint32_t j = 0; j < nb.count; j++) {
-        const uint32_t q = nb[j];
+    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
         const float3 r = xi - f3(d.X[q]);
-        s += dot3(vi - f3(d.V[q]), kernel_grad(d, r));
-    }
-    s *= S.volume;
+        const float3 vq = f3(d.V[q]);
+        const float t = dot3(vi - vq, grad_factor(d, r) * r);
+        if (ok) s += t;
+    });
+    s = grp.sum(s) * S.volume;
     if (nb.flags & kHasBoundary) s += dot3(vi, f3(d.GB[p]));
     return s;
 }
 
 // K4: ComputeDensityChangeKernel (:483-529).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableDiv) return;
     const Nbr nb = neighbors(d, p);
-    float rhoAdv = velocity_divergence(d, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    float rhoAdv = velocity_divergence<G>(d, grp, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    if (grp.lane != 0) return;
     rhoAdv = nb.count < 20u ? 0.0f : fmaxf(rhoAdv, 0.0f);
     d.RHOADV[p] = rhoAdv;
     const float alpha = d.ALPHA[p] * S.dtInv;
@@ -120,80 +166,88 @@ __global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
     d.KAPPAV[p] = rhoAdv * alpha;
 }
 
-// Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481).
-template <bool DIV>
-__device__ __forceinline__ float3 pressure_accel(const Dev& d, uint32_t p, const SceneDev& S, const Nbr& nb) {
+// Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481);
+// valid on lane 0.
+template <bool DIV, uint32_t G>
+__device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
+                                                 const Nbr& nb) {
     const float* kap = DIV ? d.KAPPAV : d.KAPPA;
     const float ki = kap[p];
     const float3 xi = f3(d.X[p]);
     const float V = S.volume;
     float3 a = make_float3(0.f, 0.f, 0.f);
-    for (uint32_t j = 0; j < nb.count; j++) {
-        const uint32_t q = nb[j];
+    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
         const float sum = ki + __ldg(kap + q);
-        if (fabsf(sum) > kEps) {
-            const float3 g = (-V) * kernel_grad(d, xi - f3(d.X[q]));
-            a += sum * g;
-        }
-    }
+        const float3 r = xi - f3(d.X[q]);
+        if (ok && fabsf(sum) > kEps) a += (sum * (-V * grad_factor(d, r))) * r;
+    });
+    a = grp.sum(a);
     if (fabsf(ki) > kEps && (nb.flags & kHasBoundary)) a += ki * (-f3(d.GB[p]));
     return a;
 }
 
 // K5 / K18.
-template <bool DIV>
+template <bool DIV, uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!(DIV ? S.div.active : S.pres.active)) return;
     const Nbr nb = neighbors(d, p);
-    d.AP[p] = f4(pressure_accel<DIV>(d, p, S, nb), 0.0f);
+    const float3 a = pressure_accel<DIV, G>(d, grp, p, S, nb);
+    if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
 }
 
 // K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
 // each with ComputeDensityPressureForce (:280-315) and the FP64 residual sum.
-template <bool DIV>
+template <bool DIV, uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    VFD_COUNT_LAUNCH(d);
+    const Group<G> grp;
+    const uint32_t p = grp.p;
     const bool inRange = p < d.n && !aborted_p(d);
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
-    const bool valid = inRange && (DIV ? S.div.active : S.pres.active);
+    const bool active = inRange && (DIV ? S.div.active : S.pres.active);
     double res = 0.0;
-    if (valid) {
+    if (active) {
         const Nbr nb = neighbors(d, p);
         const float3 xi = f3(d.X[p]);
         const float3 ai = f3(d.AP[p]);
         float f = 0.0f;
-        for (uint32_t j = 0; j < nb.count; j++) {
-            const uint32_t q = nb[j];
-            f += dot3(ai - f3(d.AP[q]), kernel_grad(d, xi - f3(d.X[q])));
+        for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+            const float3 r = xi - f3(d.X[q]);
+            const float3 aq = f3(d.AP[q]);
+            const float t = dot3(ai - aq, grad_factor(d, r) * r);
+            if (ok) f += t;
+        });
+        f = grp.sum(f) * S.volume;
+        if (grp.lane == 0) {
+            if (nb.flags & kHasBoundary) f += dot3(ai, f3(d.GB[p]));
+            float r;
+            if (DIV) {
+                f *= S.dt;
+                r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
+                d.KAPPAV[p] -= r * d.ALPHA[p];
+            } else {
+                f *= S.dt2;
+                r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
+                d.KAPPA[p] -= r * d.ALPHA[p];
+            }
+            d.RES[p] = r;
+            res = (double)r;
         }
-        f *= S.volume;
-        if (nb.flags & kHasBoundary) f += dot3(ai, f3(d.GB[p]));
-        float r;
-        if (DIV) {
-            f *= S.dt;
-            r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
-            d.KAPPAV[p] -= r * d.ALPHA[p];
-        } else {
-            f *= S.dt2;
-            r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
-            d.KAPPA[p] -= r * d.ALPHA[p];
-        }
-        d.RES[p] = r;
-        res = (double)r;
     }
     const double v[1] = {res};
     const int slot[1] = {0};
-    scene_accumulate<1>(d, sid, valid, v, slot);
+    scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
 }
 
 // Loop start: the reference's while condition evaluated with error 0, iteration 0
 // (DFSPHImplementation.cu:461, :532).
 template <bool DIV>
 __global__ void k_ctrl_jacobi_init(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
@@ -203,7 +257,6 @@ __global__ void k_ctrl_jacobi_init(Dev d) {
         LoopState& L = DIV ? S.div : S.pres;
         L.it = 0;
         L.err = 0.0f;
-        S.acc[0] = 0.0;
         const uint32_t mn = DIV ? S.minIterD : S.minIterP, mx = DIV ? S.maxIterD : S.maxIterP;
         const bool enabled = (DIV ? S.enableDiv != 0 : true) && S.count > 0 && !ab;
         const float eta = DIV ? S.dtInv * S.maxErrD * 0.0001f * S.rho0 : S.maxErrP * 0.0001f * S.rho0;
@@ -218,6 +271,7 @@ __global__ void k_ctrl_jacobi_init(Dev d) {
 // reference's thrust::minus fold, DFSPHImplementation.cu:483-491, :554-563).
 template <bool DIV>
 __global__ void k_ctrl_jacobi(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
@@ -225,8 +279,7 @@ __global__ void k_ctrl_jacobi(Dev d) {
         SceneDev& S = d.scenes[s];
         LoopState& L = DIV ? S.div : S.pres;
         if (!L.active) continue;
-        const double err = -(double)S.rho0 * S.acc[0] / (double)S.count;
-        S.acc[0] = 0.0;
+        const double err = -(double)S.rho0 * fold_acc(d, s, 0) / (double)S.count;
         L.err = (float)err;
         L.it++;
         const uint32_t mn = DIV ? S.minIterD : S.minIterP, mx = DIV ? S.maxIterD : S.maxIterP;
@@ -241,37 +294,43 @@ __global__ void k_ctrl_jacobi(Dev d) {
 }
 
 // K7 ComputePressureAccelerationAndFactorKernel (:555-602) + K8 ClearAccelerationKernel (:24-37).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_div_finish(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (S.enableDiv) {
         const Nbr nb = neighbors(d, p);
-        const float3 a = pressure_accel<true>(d, p, S, nb);
-        d.AP[p] = f4(a, 0.0f);
-        const float4 v = d.V[p];
-        d.V[p] = f4(f3(v) + S.dt * a, v.w);
-        d.ALPHA[p] *= S.dt;
+        const float3 a = pressure_accel<true, G>(d, grp, p, S, nb);
+        if (grp.lane == 0) {
+            d.AP[p] = f4(a, 0.0f);
+            const float4 v = d.V[p];
+            d.V[p] = f4(f3(v) + S.dt * a, v.w);
+            d.ALPHA[p] *= S.dt;
+        }
     }
-    d.A[p] = make_float4(S.g[0], S.g[1], S.g[2], 0.0f);
+    if (grp.lane == 0) d.A[p] = make_float4(S.g[0], S.g[1], S.g[2], 0.0f);
 }
 
 // ---------------------------------------------------------------------------
 // Surface tension (DFSPHImplementation.cu:810-839).
-// K9: ComputeSurfaceTensionClassificationKernel (DFSPHKernels.cu:881-958).
+// K9: ComputeSurfaceTensionClassificationKernel (DFSPHKernels.cu:881-958); the
+// Monte-Carlo samples are split over the group's lanes.
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableST) return;
     const Nbr nb = neighbors(d, p);
     const float3 xi = f3(d.X[p]);
     if (nb.count == 0) {
-        d.STN[p] = make_float4(0.f, 0.f, 0.f, 1.0f / S.h);
+        if (grp.lane == 0) d.STN[p] = make_float4(0.f, 0.f, 0.f, 1.0f / S.h);
         return;
     }
     float3 com = make_float3(0.f, 0.f, 0.f);
-    for (uint32_t j = 0; j < nb.count; j++) com += f3(d.X[nb[j]]) - xi;
+    for (uint32_t j = grp.lane; j < nb.count; j += G) com += f3(d.X[nb[j]]) - xi;
+    com = grp.sum(com);
     com = make_float3(com.x / S.h, com.y / S.h, com.z / S.h);
     const float input = sqrtf(dot3(com, com)) / (float)nb.count;
     float3 nsum = make_float3(0.f, 0.f, 0.f);
@@ -282,7 +341,7 @@ __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
         const float ratio = S.nbrRadius / S.r;
         const float lim = ratio * ratio * S.h2;
         uint32_t count = 0;
-        for (uint32_t k = 0; k < samples; k++) {
+        for (uint32_t k = grp.lane; k < samples; k += G) {
             const uint32_t i3 = s0 + 3u * k;
             const float3 pt = S.h * make_float3(__ldg(d.halton + i3 % kHaltonCount),
                                                 __ldg(d.halton + (i3 + 1u) % kHaltonCount),
@@ -294,6 +353,8 @@ __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
             }
             if (!covered) { nsum += pt; count++; }
         }
+        nsum = grp.sum(nsum);
+        count = grp.sum(count);
         if (count > 0) {
             if (dot3(nsum, nsum) > 0.0f) nsum = normalize3(nsum);
             curv = 1.0f / S.h * -2.0f * sqrtf(1.0f - S.nbrRadius * S.nbrRadius / (S.r * S.r)) *
@@ -302,15 +363,16 @@ __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
             nsum = make_float3(0.f, 0.f, 0.f);
         }
     }
-    d.STN[p] = f4(nsum, curv);
+    if (grp.lane == 0) d.STN[p] = f4(nsum, curv);
 }
 
 __device__ __forceinline__ bool nonzero3(float4 a) { return a.x != 0.0f || a.y != 0.0f || a.z != 0.0f; }
 
 // K10: ComputeSurfaceTensionNormalsAndCurvatureKernel (:960-1006).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableST) return;
     const float4 ni = d.STN[p];
@@ -319,17 +381,20 @@ __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
     const float3 xi = f3(d.X[p]);
     float3 nc = make_float3(0.f, 0.f, 0.f);
     float cc = 0.0f, cf = 0.0f;
-    for (uint32_t j = 0; j < nb.count; j++) {
-        const uint32_t q = nb[j];
+    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
         const float4 nj = d.STN[q];
-        if (nonzero3(nj)) {
-            const float3 dx = f3(d.X[q]) - xi;
+        const float3 dx = f3(d.X[q]) - xi;
+        if (ok && nonzero3(nj)) {
             const float num = 1.0f - sqrtf(dot3(dx, dx)) / S.h;
             nc += f3(nj) * num;
             cc += nj.w * num;
             cf += num;
         }
-    }
+    });
+    nc = grp.sum(nc);
+    cc = grp.sum(cc);
+    cf = grp.sum(cf);
+    if (grp.lane != 0) return;
     if (dot3(nc, nc) > 0.0f) nc = normalize3(nc);
     const float sf = S.smoothing;
     float3 ns = (1.0f - sf) * f3(ni) + sf * nc;
@@ -339,6 +404,7 @@ __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
 
 // K11: ComputeSurfaceTensionBlendingKernel (:1008-1046), pass `pass` of SurfaceTensionSmoothPassCount.
 __global__ void __launch_bounds__(kBlock) k_st_blend(Dev d, uint32_t pass) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n || aborted_p(d)) return;
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -397,9 +463,11 @@ __device__ __forceinline__ Mat3 inverse3(const Mat3& a) {  // cofactors / determ
 // K12 ComputeViscosityPreconditionerKernel (:604-684) + K13 ComputeViscosityGradientKernel
 // (:686-756, whose boundary term dots a zero vector: b = v) + the boundary matrix BV of
 // the SpMV's boundary term (:793-839): BV p_i = sum_k c_k (p_i . d_k) gradW_k.
+// CG.w and CP.w hold m / rho (read by the SpMV's neighbours) from here on.
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableVisc) return;
     const Nbr nb = neighbors(d, p);
@@ -407,13 +475,18 @@ __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     Mat3 m = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    for (uint32_t j = 0; j < nb.count; j++) {
-        const uint32_t q = nb[j];
+    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
         const float3 r = xi - f3(d.X[q]);
-        const float3 g = kernel_grad(d, r);
-        const float c = cmu * (S.mass / d.RHO[q]) / (dot3(r, r) + eps2);
+        const float rho = d.RHO[q];
+        if (!ok) return;
+        const float3 g = grad_factor(d, r) * r;
+        const float c = cmu * (S.mass / rho) / (dot3(r, r) + eps2);
         add_outer(m, c, r, g);
-    }
+    });
+    m.r0 = grp.sum(m.r0);
+    m.r1 = grp.sum(m.r1);
+    m.r2 = grp.sum(m.r2);
+    if (grp.lane != 0) return;
     Mat3 bv = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
     bool hasBV = false;
     if (S.dynBVisc != 0.0f && (nb.flags & kHasBoundary)) {
@@ -442,7 +515,8 @@ __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
             hasBV = true;
         }
     }
-    const float f = S.dt / d.RHO[p];
+    const float rho = d.RHO[p];
+    const float f = S.dt / rho;
     Mat3 a;
     a.r0 = make_float3(1.0f - f * m.r0.x, -f * m.r0.y, -f * m.r0.z);
     a.r1 = make_float3(-f * m.r1.x, 1.0f - f * m.r1.y, -f * m.r1.z);
@@ -456,51 +530,60 @@ __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
     }
     const float4 v = d.V[p];
     d.CB[p] = v;
-    d.CG[p] = f4(f3(v) + f3(d.DV[p]), 0.0f);
+    d.CG[p] = f4(f3(v) + f3(d.DV[p]), S.mass / rho);
 }
 
-// ComputeMatrixVecProdFunctionKernel (:758-842): (A x)_i.
-__device__ __forceinline__ float3 visc_matvec(const Dev& d, uint32_t p, const SceneDev& S, const float4* vec,
-                                              float3 vi) {
+// ComputeMatrixVecProdFunctionKernel (:758-842): (A x)_i with vec[q].w = m / rho_q; lane 0.
+template <uint32_t G>
+__device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
+                                              const float4* vec, float3 vi) {
     const Nbr nb = neighbors(d, p);
     const float3 xi = f3(d.X[p]);
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    for (uint32_t j = 0; j < nb.count; j++) {
-        const uint32_t q = nb[j];
+    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
         const float3 r = xi - f3(d.X[q]);
-        const float3 g = kernel_grad(d, r);
-        acc += (cmu * (S.mass / d.RHO[q]) * dot3(vi - f3(vec[q]), r) / (dot3(r, r) + eps2)) * g;
-    }
+        const float4 vq = vec[q];
+        const float r2 = dot3(r, r);
+        const float3 t = (cmu * vq.w * dot3(vi - f3(vq), r) / (r2 + eps2) * grad_factor(d, r)) * r;
+        if (ok) acc += t;
+    });
+    acc = grp.sum(acc);
     if (nb.flags & kHasBoundaryVisc) acc += mul(load_mat(d.BVM, d.stride, p), vi);
     return vi - (S.dt / d.RHO[p]) * acc;
 }
 
 // Initial residual r = b - A g and the norms |b|^2, |r|^2 (:627-669).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    VFD_COUNT_LAUNCH(d);
+    const Group<G> grp;
+    const uint32_t p = grp.p;
     const bool inRange = p < d.n && !aborted_p(d);
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
     const bool valid = inRange && S.enableVisc;
     double bb = 0.0, rr = 0.0;
     if (valid) {
-        const float3 g = f3(d.CG[p]);
-        const float3 ag = visc_matvec(d, p, S, d.CG, g);
-        const float3 b = f3(d.CB[p]);
-        const float3 r = b - ag;
-        d.CR[p] = f4(r, 0.0f);
-        bb = (double)b.x * b.x + (double)b.y * b.y + (double)b.z * b.z;
-        rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+        const float4 g4 = d.CG[p];
+        const float3 ag = visc_matvec<G>(d, grp, p, S, d.CG, f3(g4));
+        if (grp.lane == 0) {
+            const float3 b = f3(d.CB[p]);
+            const float3 r = b - ag;
+            d.CR[p] = f4(r, 0.0f);
+            bb = (double)b.x * b.x + (double)b.y * b.y + (double)b.z * b.z;
+            rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+        }
     }
     const double v[2] = {bb, rr};
     const int slot[2] = {0, 1};
-    scene_accumulate<2>(d, sid, valid, v, slot);
+    scene_accumulate<2, G>(d, sid, valid && grp.lane == 0, v, slot);
 }
 
 // Early outs of SolveViscosity (:646-675).
 __global__ void k_ctrl_cg0(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
         S.cgIt = 0;
@@ -509,9 +592,9 @@ __global__ void k_ctrl_cg0(Dev d) {
         S.cgZeroG = 0;
         S.cgDone = 1;
         S.cgErr = 0.0f;
-        if (!S.enableVisc || aborted_p(d)) continue;
-        const double rhs = S.acc[0], rr = S.acc[1];
-        S.acc[0] = S.acc[1] = S.acc[2] = 0.0;
+        if (!S.enableVisc) continue;
+        const double rhs = fold_acc(d, s, 0), rr = fold_acc(d, s, 1);
+        if (aborted_p(d)) continue;
         S.cgRhs = rhs;
         S.cgRR = rr;
         if (rhs == 0.0) {
@@ -528,8 +611,9 @@ __global__ void k_ctrl_cg0(Dev d) {
     }
 }
 
-// p = M^-1 r and |r . p| (:677-691).
+// p = M^-1 r (with p.w = m / rho) and |r . p| (:677-691).
 __global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool inRange = p < d.n && !aborted_p(d);
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
@@ -539,7 +623,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
     if (valid) {
         const float3 r = f3(d.CR[p]);
         const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
-        d.CP[p] = f4(z, 0.0f);
+        d.CP[p] = f4(z, d.CG[p].w);
         rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
     }
     const double v[1] = {rz};
@@ -548,14 +632,14 @@ __global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
 }
 
 __global__ void k_ctrl_cg1(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
         if (!S.enableVisc || S.cgDone) continue;
-        S.cgAbsNew = fabs(S.acc[0]);
-        S.acc[0] = 0.0;
+        S.cgAbsNew = fabs(fold_acc(d, s, 0));
         S.cgErr = (float)sqrt(S.cgRR / S.cgRhs);
         const bool run = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
         S.cgActive = run ? 1u : 0u;
@@ -566,8 +650,11 @@ __global__ void k_ctrl_cg1(Dev d) {
 }
 
 // Loop body 1: Ap and p . Ap (:695-720).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    VFD_COUNT_LAUNCH(d);
+    const Group<G> grp;
+    const uint32_t p = grp.p;
     const bool inRange = p < d.n && !aborted_p(d);
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
@@ -575,17 +662,30 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
     double pap = 0.0;
     if (valid) {
         const float3 pv = f3(d.CP[p]);
-        const float3 ap = visc_matvec(d, p, S, d.CP, pv);
-        d.CAP[p] = f4(ap, 0.0f);
-        pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
+        const float3 ap = visc_matvec<G>(d, grp, p, S, d.CP, pv);
+        if (grp.lane == 0) {
+            d.CAP[p] = f4(ap, 0.0f);
+            pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
+        }
     }
     const double v[1] = {pap};
     const int slot[1] = {0};
-    scene_accumulate<1>(d, sid, valid, v, slot);
+    scene_accumulate<1, G>(d, sid, valid && grp.lane == 0, v, slot);
+}
+
+// alpha = |r . z| / (p . Ap) (:714-720).
+__global__ void k_ctrl_cg_alpha(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
+        SceneDev& S = d.scenes[s];
+        if (!S.cgActive) continue;
+        S.cgAlpha = (float)(S.cgAbsNew / fold_acc(d, s, 0));
+    }
 }
 
 // Loop body 2: g += alpha p, r -= alpha Ap, |r|^2, z = M^-1 r, r . z (:722-784).
 __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool inRange = p < d.n && !aborted_p(d);
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
@@ -593,11 +693,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     const bool valid = inRange && S.cgActive;
     double rr = 0.0, rz = 0.0;
     if (valid) {
-        const float alpha = (float)(S.cgAbsNew / S.acc[0]);
+        const float alpha = S.cgAlpha;
         const float3 pv = f3(d.CP[p]);
-        const float3 g = f3(d.CG[p]) + pv * alpha;
+        const float4 g4 = d.CG[p];
+        const float3 g = f3(g4) + pv * alpha;
         const float3 r = f3(d.CR[p]) - f3(d.CAP[p]) * alpha;
-        d.CG[p] = f4(g, 0.0f);
+        d.CG[p] = f4(g, g4.w);
         d.CR[p] = f4(r, 0.0f);
         const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
         d.CZ[p] = f4(z, 0.0f);
@@ -611,6 +712,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
 
 // Loop control: break on |r|^2 < threshold, else beta and the next iteration (:754-805).
 __global__ void k_ctrl_cg(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
@@ -618,8 +720,7 @@ __global__ void k_ctrl_cg(Dev d) {
         SceneDev& S = d.scenes[s];
         S.cgUpdateP = 0;
         if (!S.cgActive) continue;
-        const double rr = S.acc[1], rz = S.acc[2];
-        S.acc[0] = S.acc[1] = S.acc[2] = 0.0;
+        const double rr = fold_acc(d, s, 1), rz = fold_acc(d, s, 2);
         S.cgRR = rr;
         S.cgErr = (float)sqrt(rr / S.cgRhs);
         if (rr < S.cgThr) {
@@ -641,18 +742,21 @@ __global__ void k_ctrl_cg(Dev d) {
     if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
 }
 
-// Loop body 3: p = beta p + z (:786-802).
+// Loop body 3: p = beta p + z (:786-802), p.w = m / rho kept.
 __global__ void __launch_bounds__(kBlock) k_cg_p(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n || aborted_p(d)) return;
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.cgUpdateP) return;
-    d.CP[p] = f4(f3(d.CP[p]) * S.cgBeta + f3(d.CZ[p]), 0.0f);
+    const float4 pv = d.CP[p];
+    d.CP[p] = f4(f3(pv) * S.cgBeta + f3(d.CZ[p]), pv.w);
 }
 
 // K15 ApplyViscosityForceKernel (:844-862) + T1, the CFL maximum of |v + a dt|^2
 // (ComputeMaxVelocityMagnitude, DFSPHImplementation.cu:430-441).
 __global__ void __launch_bounds__(kBlock) k_visc_finish(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < d.n && !aborted_p(d);
     const uint32_t sid = valid ? scene_of(d, p) : 0u;
@@ -675,10 +779,11 @@ __global__ void __launch_bounds__(kBlock) k_visc_finish(Dev d) {
 
 // ComputeTimeStepSize (DFSPHImplementation.cu:395-428) + the frame clock (:148-167).
 __global__ void k_ctrl_dt(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
         if (aborted_p(d)) continue;
-        float mv = fmaxf(0.1f, __uint_as_float(S.maxV2Bits));
+        float mv = fmaxf(0.1f, __uint_as_float(fold_max(d, s, 0)));
         if (mv < 1.0e-9f) mv = 1.0e-9f;
         S.maxV2 = mv;
         float dt = 0.4f * (S.diam / sqrtf(mv));
@@ -696,6 +801,7 @@ __global__ void k_ctrl_dt(Dev d) {
 
 // K16 ComputeVelocityKernel (:39-52).
 __global__ void __launch_bounds__(kBlock) k_velocity(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n || aborted_p(d)) return;
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -704,12 +810,14 @@ __global__ void __launch_bounds__(kBlock) k_velocity(Dev d) {
 }
 
 // K17 ComputeDensityAdvectionKernel (:233-278).
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     const Nbr nb = neighbors(d, p);
-    const float delta = velocity_divergence(d, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    const float delta = velocity_divergence<G>(d, grp, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    if (grp.lane != 0) return;
     const float rhoAdv = d.RHO[p] / S.rho0 + S.dt * delta;
     d.RHOADV[p] = rhoAdv;
     const float alpha = d.ALPHA[p] * S.dt2Inv;
@@ -719,12 +827,14 @@ __global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
 
 // K20 ComputePressureAccelerationAndVelocityKernel (:434-481) + K21 ComputePositionKernel (:54-67);
 // positions go to XN so that the neighbours' positions read here stay unchanged.
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_pres_finish(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || aborted_p(d)) return;
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     const Nbr nb = neighbors(d, p);
-    const float3 a = pressure_accel<false>(d, p, S, nb);
+    const float3 a = pressure_accel<false, G>(d, grp, p, S, nb);
+    if (grp.lane != 0) return;
     d.AP[p] = f4(a, 0.0f);
     const float3 v = f3(d.V[p]) + S.dt * a;
     d.V[p] = f4(v, 0.0f);
@@ -736,6 +846,7 @@ __global__ void __launch_bounds__(kBlock) k_pres_finish(Dev d) {
 // End of step: frame clock and iteration counter (DFSPHImplementation.cu:148-169);
 // status[7] counts the steps completed since the host last looked.
 __global__ void k_ctrl_end(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     if (threadIdx.x == 0 && !aborted_p(d)) d.status[7]++;
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
@@ -747,59 +858,75 @@ __global__ void k_ctrl_end(Dev d) {
             S.frameIndex++;
         }
         S.iteration++;
+        S.maxNbr = fold_max(d, s, 1);
         atomicOr(d.status, S.flags);
     }
 }
 
 // ---------------------------------------------------------------- launchers
-void launch_density(const Dev& d, cudaStream_t s) {
-    k_density_factor<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-}
+#define K_DENSITY(G) k_density_factor<G>
+#define K_DIV_INIT(G) k_div_init<G>
+#define K_PACCEL_D(G) k_pressure_accel<true, G>
+#define K_PACCEL_P(G) k_pressure_accel<false, G>
+#define K_JACOBI_D(G) k_jacobi_iter<true, G>
+#define K_JACOBI_P(G) k_jacobi_iter<false, G>
+#define K_DIV_FINISH(G) k_div_finish<G>
+#define K_ST_CLASSIFY(G) k_st_classify<G>
+#define K_ST_SMOOTH(G) k_st_smooth<G>
+#define K_VISC_PRECOND(G) k_visc_precond<G>
+#define K_VISC_SETUP(G) k_visc_setup<G>
+#define K_SPMV(G) k_cg_spmv<G>
+#define K_PRES_INIT(G) k_pres_init<G>
+#define K_PRES_FINISH(G) k_pres_finish<G>
+
+void launch_density(const Dev& d, cudaStream_t s) { VFD_LAUNCH_LANES("k_density_factor", kTDensity, K_DENSITY); }
 void launch_div_init(const Dev& d, cudaStream_t s) {
-    k_div_init<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_div_init", kTDivInit, K_DIV_INIT);
+    VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d));
 }
 void launch_div_iter(const Dev& d, cudaStream_t s) {
-    k_pressure_accel<true><<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_jacobi_iter<true><<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_pressure_accel", kTPAccel, K_PACCEL_D);
+    VFD_LAUNCH_LANES("k_jacobi_iter", kTJacobi, K_JACOBI_D);
+    VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
 }
-void launch_div_finish(const Dev& d, cudaStream_t s) { k_div_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d); }
+void launch_div_finish(const Dev& d, cudaStream_t s) { VFD_LAUNCH_LANES("k_div_finish", kTDivFinish, K_DIV_FINISH); }
 void launch_surface_tension(const Dev& d, uint32_t maxPasses, cudaStream_t s) {
-    k_st_classify<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_st_smooth<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    for (uint32_t pass = 0; pass < maxPasses; pass++) k_st_blend<<<blocks_for(d.n), kBlock, 0, s>>>(d, pass);
+    VFD_LAUNCH_LANES("k_st_classify", kTStClassify, K_ST_CLASSIFY);
+    VFD_LAUNCH_LANES("k_st_smooth", kTStSmooth, K_ST_SMOOTH);
+    for (uint32_t pass = 0; pass < maxPasses; pass++)
+        VFD_LAUNCH("k_st_blend", s, k_st_blend<<<blocks_for(d.n), kBlock, 0, s>>>(d, pass));
 }
 void launch_visc_init(const Dev& d, cudaStream_t s) {
-    k_visc_precond<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_visc_setup<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_cg0<<<1, 256, 0, s>>>(d);
-    k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_cg1<<<1, 256, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_visc_precond", kTViscPrecond, K_VISC_PRECOND);
+    VFD_LAUNCH_LANES("k_visc_setup", kTViscSetup, K_VISC_SETUP);
+    VFD_LAUNCH("k_ctrl_cg0", s, k_ctrl_cg0<<<1, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_cg_p0", s, k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_ctrl_cg1", s, k_ctrl_cg1<<<1, 256, 0, s>>>(d));
 }
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
-    k_cg_spmv<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_cg<<<1, 256, 0, s>>>(d);
-    k_cg_p<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_cg_spmv", kTSpmv, K_SPMV);
+    VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_cg_update", s, k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_cg_p", s, k_cg_p<<<blocks_for(d.n), kBlock, 0, s>>>(d));
 }
 void launch_visc_finish_dt(const Dev& d, cudaStream_t s) {
-    k_visc_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_dt<<<1, 256, 0, s>>>(d);
-    k_velocity<<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    VFD_LAUNCH("k_visc_finish", s, k_visc_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_ctrl_dt", s, k_ctrl_dt<<<1, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_velocity", s, k_velocity<<<blocks_for(d.n), kBlock, 0, s>>>(d));
 }
 void launch_pres_init(const Dev& d, cudaStream_t s) {
-    k_pres_init<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_jacobi_init<false><<<1, 256, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_pres_init", kTPresInit, K_PRES_INIT);
+    VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_iter(const Dev& d, cudaStream_t s) {
-    k_pressure_accel<false><<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_jacobi_iter<false><<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_pressure_accel", kTPAccel, K_PACCEL_P);
+    VFD_LAUNCH_LANES("k_jacobi_iter", kTJacobi, K_JACOBI_P);
+    VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_finish(const Dev& d, cudaStream_t s) {
-    k_pres_finish<<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    k_ctrl_end<<<1, 256, 0, s>>>(d);
+    VFD_LAUNCH_LANES("k_pres_finish", kTPresFinish, K_PRES_FINISH);
+    VFD_LAUNCH("k_ctrl_end", s, k_ctrl_end<<<1, 256, 0, s>>>(d));
 }
 
 }  // namespace vfd

@@ -33,10 +33,11 @@ __device__ __forceinline__ uint32_t cell_key(const SceneDev& s, int cx, int cy, 
                           part1by2((uint32_t)cx & 7u));
 }
 
-__device__ __forceinline__ bool aborted(const Dev& d) { return *(volatile uint32_t*)(d.status + 1) != 0u; }
+__device__ __forceinline__ bool aborted(const Dev& d) { return is_aborted(d); }
 
 // N1: ComputeMinMaxKernel (ParticleSearchKernels.cu:40-62) on the current positions.
 __global__ void __launch_bounds__(kBlock) k_minmax(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n;
     const uint32_t sid = valid ? scene_of(d, i) : 0u;
@@ -65,21 +66,22 @@ __global__ void __launch_bounds__(kBlock) k_minmax(Dev d) {
     }
     const uint32_t s0 = __shfl_sync(0xffffffffu, sid, 0);
     const bool uniform = __all_sync(0xffffffffu, !valid || sid == s0);
+    const uint32_t bucket = blockIdx.x % kBuckets;
     if (uniform) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const int mn = __reduce_min_sync(0xffffffffu, c[k]);
             const int mx = __reduce_max_sync(0xffffffffu, cmax[k]);
             if ((threadIdx.x & 31u) == 0 && mn != INT_MAX) {
-                atomicMin(&d.scenes[s0].minCell[k], mn);
-                atomicMax(&d.scenes[s0].maxCell[k], mx);
+                atomicMin(mm_bucket(d, s0, k, bucket), mn);
+                atomicMax(mm_bucket(d, s0, 3 + k, bucket), mx);
             }
         }
     } else if (valid) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            atomicMin(&d.scenes[sid].minCell[k], c[k]);
-            atomicMax(&d.scenes[sid].maxCell[k], cmax[k]);
+            atomicMin(mm_bucket(d, sid, k, bucket), c[k]);
+            atomicMax(mm_bucket(d, sid, 3 + k, bucket), cmax[k]);
         }
     }
 }
@@ -87,9 +89,24 @@ __global__ void __launch_bounds__(kBlock) k_minmax(Dev d) {
 // ParticleSearch::ComputeMinMax tail + ComputeCellInformation (ParticleSearch.cu:50-86),
 // per scene, then the scene cell bases (exclusive scan) and the capacity check.
 __global__ void k_grid(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     __shared__ uint32_t total;
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
+        for (int k = 0; k < 3; k++) {  // fold the N1 buckets, reset them for the next step
+            int mn = INT_MAX, mx = INT_MIN;
+            for (uint32_t b = 0; b < kBuckets; b++) {
+                int32_t* qa = mm_bucket(d, s, k, b);
+                int32_t* qb = mm_bucket(d, s, 3 + k, b);
+                mn = min(mn, *qa);
+                mx = max(mx, *qb);
+                *qa = INT_MAX;
+                *qb = INT_MIN;
+            }
+            S.minCell[k] = mn;
+            S.maxCell[k] = mx;
+        }
+        for (uint32_t b = 0; b < kBuckets; b++) *max_bucket(d, s, 1, b) = 0u;
         const float R = S.h;
         uint32_t cells = 1u;
         bool ok = S.count > 0;
@@ -107,11 +124,7 @@ __global__ void k_grid(Dev d) {
             cells = (cells > 0xFFFFFFFFu / 8u) ? 0xFFFFFFFFu : cells * S.meta[k];
         }
         S.cellCount = (!ok) ? 0u : ((cells > 0xFFFFFFFFu / 512u) ? 0xFFFFFFFFu : cells * 512u);
-        // reset for the next step's N1
-        for (int k = 0; k < 3; k++) { S.minCell[k] = INT_MAX; S.maxCell[k] = INT_MIN; }
         S.flags = 0u;
-        S.maxNbr = 0u;
-        S.maxV2Bits = 0u;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -130,6 +143,7 @@ __global__ void k_grid(Dev d) {
 }
 
 __global__ void __launch_bounds__(256) k_clear_cells(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     if (aborted(d)) return;
     const uint32_t total = d.status[2];
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
@@ -140,6 +154,7 @@ __global__ void __launch_bounds__(256) k_clear_cells(Dev d) {
 
 // N2: InsertParticlesMortonKernel (ParticleSearchKernels.cu:64-78), count part.
 __global__ void __launch_bounds__(kBlock) k_keys(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n || aborted(d)) return;
     const SceneDev& S = d.scenes[scene_of(d, i)];
@@ -162,6 +177,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(Dev d) {
 // N3: exclusive scan of the cell counts (thrust::exclusive_scan, ParticleSearch.cu:111-115),
 // three phases over the device-known number of cells.
 __global__ void __launch_bounds__(256) k_scan_reduce(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     if (aborted(d)) return;
     const uint32_t total = d.status[2];
     const uint32_t base = blockIdx.x * kScanItems;
@@ -211,6 +227,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_1024(uint32_t v, uint32
 }
 
 __global__ void __launch_bounds__(1024) k_scan_top(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     if (aborted(d)) return;
     const uint32_t total = d.status[2];
     const uint32_t nb = (total + kScanItems - 1) / kScanItems;
@@ -226,6 +243,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(Dev d) {
 }
 
 __global__ void __launch_bounds__(256) k_scan_down(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     if (aborted(d)) return;
     const uint32_t total = d.status[2];
     const uint32_t base = blockIdx.x * kScanItems;
@@ -261,6 +279,7 @@ __global__ void __launch_bounds__(256) k_scan_down(Dev d) {
 
 // N4 (first half): CountingSortIndicesKernel's slot, here through a per-cell fill counter.
 __global__ void __launch_bounds__(kBlock) k_slots(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n || aborted(d)) return;
     const uint32_t key = d.KEY[i];
@@ -271,6 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_slots(Dev d) {
 // N4 (second half): the deterministic in-cell rank (ascending original index) and the
 // gather of the carried state into the new cell order.
 __global__ void __launch_bounds__(kBlock) k_rank_gather(Dev d) {
+    VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n || aborted(d)) return;
     const uint32_t i = d.TMP[p];
@@ -289,10 +309,15 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(Dev d) {
 }
 
 // N6-N8: ComputeCountsKernel + NeighborhoodQueryWithCountsKernel (ParticleSearchKernels.cu:93-193)
-// in one pass; the squared distance is computed without contraction, x^2 + y^2 + z^2
-// left to right, as the FP32 oracle does.
+// in one pass. G lanes test consecutive candidates of a cell together and compact the
+// hits with a ballot, so the row keeps the reference's order (z, y, x cells, then cell
+// order) and its cap of 70. The squared distance is computed without contraction,
+// x^2 + y^2 + z^2 left to right, as the FP32 oracle does.
+template <uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    VFD_COUNT_LAUNCH(d);
+    const Group<G> grp;
+    const uint32_t p = grp.p;
     if (p >= d.n || aborted(d)) return;
     const uint32_t sid = scene_of(d, p);
     const SceneDev& S = d.scenes[sid];
@@ -302,9 +327,10 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
 #pragma unroll
     for (int k = 0; k < 3; k++) gc[k] = (int)floorf(__fmul_rn(__fsub_rn(pos[k], S.gridMin[k]), S.gridDelta[k]));
     const float h2 = S.h2;
+    const uint32_t shift = (threadIdx.x & 31u) & ~(G - 1u);
+    const uint32_t below = (1u << grp.lane) - 1u;
     uint32_t count = 0;
-    uint32_t* out = d.NBR + p;
-    const uint32_t stride = d.stride;
+    uint32_t* row = d.NBR + (size_t)p * kRow;
     for (int dz = -1; dz < 2; dz++) {
         for (int dy = -1; dy < 2; dy++) {
             for (int dx = -1; dx < 2; dx++) {
@@ -312,39 +338,60 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                 if (fx < 0 || fy < 0 || fz < 0 || fx >= (int)S.dim[0] || fy >= (int)S.dim[1] || fz >= (int)S.dim[2])
                     continue;
                 const uint32_t c = S.cellBase + cell_key(S, fx, fy, fz);
-                const uint32_t start = d.CELL_START[c], num = d.CELL_COUNT[c];
-                for (uint32_t q = start; q < start + num; q++) {
-                    const float4 xj = d.X[q];
-                    const float ex = __fsub_rn(xj.x, xi.x), ey = __fsub_rn(xj.y, xi.y), ez = __fsub_rn(xj.z, xi.z);
-                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
-                    if (d2 < h2 && d2 > 0.0f) {
-                        out[(size_t)count * stride] = q;
-                        count++;
-                        if (count == kMaxNeighbors) goto done;
+                const uint32_t start = d.CELL_START[c], end = start + d.CELL_COUNT[c];
+                for (uint32_t base = start; base < end; base += G) {
+                    const uint32_t q = base + grp.lane;
+                    bool hit = false;
+                    if (q < end) {
+                        const float4 xj = d.X[q];
+                        const float ex = __fsub_rn(xj.x, xi.x), ey = __fsub_rn(xj.y, xi.y), ez = __fsub_rn(xj.z, xi.z);
+                        const float d2 =
+                            __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
+                        hit = d2 < h2 && d2 > 0.0f;
+                    }
+                    const uint32_t bits = (__ballot_sync(grp.mask, hit) >> shift) & (G == 32u ? 0xffffffffu : ((1u << G) - 1u));
+                    const uint32_t at = count + __popc(bits & below);
+                    if (hit && at < kMaxNeighbors) row[at] = q;
+                    count += __popc(bits);
+                    if (count >= kMaxNeighbors) {
+                        count = kMaxNeighbors;
+                        goto done;
                     }
                 }
             }
         }
     }
 done:
-    d.NCNT[p] = count;
-    atomicMax(&d.scenes[sid].maxNbr, count);
-    if (count == kMaxNeighbors) atomicOr(&d.scenes[sid].flags, 0x8u);
+    if (grp.lane == 0) {
+        d.NCNT[p] = count;
+        if (count == kMaxNeighbors) atomicOr(&d.scenes[sid].flags, 0x8u);
+    }
+    // one max per warp (per scene) into the bucket
+    const uint32_t active = __activemask();
+    const uint32_t leader = __ffs(active) - 1u;
+    const uint32_t s0 = __shfl_sync(active, sid, leader);
+    if (__all_sync(active, sid == s0)) {
+        const uint32_t m = __reduce_max_sync(active, count);
+        if ((threadIdx.x & 31u) == leader) atomicMax(max_bucket(d, s0, 1, blockIdx.x % kBuckets), m);
+    } else if (grp.lane == 0) {
+        atomicMax(max_bucket(d, sid, 1, blockIdx.x % kBuckets), count);
+    }
 }
 
 // ---------------------------------------------------------------- launchers
 void launch_search(const Dev& d, cudaStream_t s) {
     const uint32_t nb = blocks_for(d.n);
-    k_minmax<<<nb, kBlock, 0, s>>>(d);
-    k_grid<<<1, 256, 0, s>>>(d);
-    k_clear_cells<<<1216, 256, 0, s>>>(d);
-    k_keys<<<nb, kBlock, 0, s>>>(d);
-    k_scan_reduce<<<d.scanBlocks, 256, 0, s>>>(d);
-    k_scan_top<<<1, 1024, 0, s>>>(d);
-    k_scan_down<<<d.scanBlocks, 256, 0, s>>>(d);
-    k_slots<<<nb, kBlock, 0, s>>>(d);
-    k_rank_gather<<<nb, kBlock, 0, s>>>(d);
-    k_neighbors<<<nb, kBlock, 0, s>>>(d);
+    VFD_LAUNCH("k_minmax", s, k_minmax<<<nb, kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_grid", s, k_grid<<<1, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_clear_cells", s, k_clear_cells<<<1216, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_keys", s, k_keys<<<nb, kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_scan_reduce", s, k_scan_reduce<<<d.scanBlocks, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_scan_top", s, k_scan_top<<<1, 1024, 0, s>>>(d));
+    VFD_LAUNCH("k_scan_down", s, k_scan_down<<<d.scanBlocks, 256, 0, s>>>(d));
+    VFD_LAUNCH("k_slots", s, k_slots<<<nb, kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_rank_gather", s, k_rank_gather<<<nb, kBlock, 0, s>>>(d));
+#define K_NEIGHBORS(G) k_neighbors<G>
+    VFD_LAUNCH_LANES("k_neighbors", kTNeighbors, K_NEIGHBORS);
 }
 
 uint32_t scan_block_count(uint32_t cellCap) { return (cellCap + kScanItems - 1) / kScanItems; }
