@@ -14,6 +14,10 @@
 //   NBR  u32 [slot][72] neighbour slots, one row per particle in the reference's
 //        z, y, x cell order (at most 70 used), read by groups of G lanes
 //   NCNT u32 [slot] neighbour count | flag bits
+//   GS   f32 [slot][72] gradW / r of each pair, written once per step by the density
+//        pass and streamed by every later neighbour loop instead of a table lookup
+//   X.w  mirrors kappa_v during the divergence solve and kappa during the pressure
+//        solve, so the pressure-acceleration gather brings it with the position
 // The reference keeps one 120-byte AoS DFSPHParticle per particle
 // (Structures/DFSPHParticle.h:8-33) in original order.
 #pragma once
@@ -119,6 +123,7 @@ struct Dev {
     float *RHO, *ALPHA, *RHOADV, *KAPPA, *KAPPAV, *RES;
     float4* XB;
     uint32_t *NBR, *NCNT;
+    float* GS;                 // [slot][72] gradW factor of each neighbour pair (row layout)
     // search scratch
     uint32_t *KEY, *KEYS, *TMP, *CELL_START, *CELL_COUNT, *FILL, *SCAN;
     // viscosity CG
@@ -157,6 +162,15 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
 }
 __device__ __forceinline__ float3 normalize3(float3 a) { return a * (1.0f / sqrtf(dot3(a, a))); }
 
+// Approximate square root (PTX sqrt.approx.f32). The reference is compiled with
+// -use_fast_math, which selects the same approximate instruction for its sqrt and
+// divisions; the neighbour loops use it and __fdividef, the search does not.
+__device__ __forceinline__ float fast_sqrt(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // -------------------------------------------------------- SPH kernel lookups
 // PrecomputedDFSPHCubicKernel::GetW / GetGradientW (Kernel/DFSPHKernels.h:54-80):
 // index = min(trunc(|r| / step), R - 2), value = midpoint of two table entries.
@@ -166,11 +180,11 @@ __device__ __forceinline__ uint32_t table_pos(const Dev& d, float rl) {
 }
 __device__ __forceinline__ float kernel_w(const Dev& d, float3 r) {
     const float r2 = dot3(r, r);
-    if (r2 <= d.radius2) return __ldg(d.WM + table_pos(d, sqrtf(r2)));
+    if (r2 <= d.radius2) return __ldg(d.WM + table_pos(d, fast_sqrt(r2)));
     return 0.0f;
 }
 __device__ __forceinline__ float3 kernel_grad(const Dev& d, float3 r) {
-    const float rl = sqrtf(dot3(r, r));
+    const float rl = fast_sqrt(dot3(r, r));
     if (rl <= d.radius) return __ldg(d.GM + table_pos(d, rl)) * r;
     return make_float3(0.f, 0.f, 0.f);
 }

@@ -35,39 +35,57 @@ __device__ __forceinline__ void set_condition(const Dev& d, int loop, uint32_t v
 
 struct Nbr {
     const uint32_t* row;
+    const float* gs;
     uint32_t count, flags;
     __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return __ldg(row + j); }
 };
 __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
-    return Nbr{d.NBR + (size_t)p * kRow, w & kCountMask, w};
+    return Nbr{d.NBR + (size_t)p * kRow, d.GS + (size_t)p * kRow, w & kCountMask, w};
 }
 
-// Neighbour loop of one group. Each lane owns 4 consecutive entries of the row and
-// loads them with one 16-byte load; the group covers 4G entries per round. The first
-// round's load does not wait for the count (rows have 72 slots, entries past the count
-// are masked), so the count, the indices and the particle's own fields are fetched
-// together, and a lane's 4 gathers are independent and usually touch one cell's run
-// of consecutive slots. Masked entries use the particle itself as a stand-in index.
-template <uint32_t G, class F>
+// kappa (or kappa_v) of particle p, mirrored into X[p].w for the neighbours' gathers.
+__device__ __forceinline__ void set_kappa(const Dev& d, uint32_t p, float k) { reinterpret_cast<float*>(d.X)[4 * (size_t)p + 3] = k; }
+
+// Neighbour loop of one group. In a round the group covers 4G consecutive row
+// entries and lane l takes entries l, l + G, l + 2G, l + 3G, so at each of the four
+// steps the group's lanes read consecutive entries -- usually consecutive slots of one
+// cell, which the gathers then fetch in one or two sectors. The first round's index
+// loads do not wait for the count (rows have 72 slots, entries past the count are
+// masked), so the count, the indices and the particle's own fields are fetched
+// together; within a round the four gathers per lane are independent. Masked entries
+// use the particle itself as a stand-in index.
+template <uint32_t G, bool WITH_GS, class F>
 __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb, uint32_t self, F&& f) {
     static_assert(4u * G <= kRow, "first round must stay inside the row");
-    const uint4* rows4 = reinterpret_cast<const uint4*>(nb.row);
-    uint4 q4 = __ldg(rows4 + grp.lane);
-    for (uint32_t base = 4u * grp.lane; base < nb.count;) {
-        const uint32_t q[4] = {base + 0u < nb.count ? q4.x : self, base + 1u < nb.count ? q4.y : self,
-                               base + 2u < nb.count ? q4.z : self, base + 3u < nb.count ? q4.w : self};
-        const uint32_t next = base + 4u * G;
-        if (next < nb.count) q4 = __ldg(rows4 + next / 4u);
+    uint32_t q[4];
+    float g[4];
 #pragma unroll
-        for (uint32_t u = 0; u < 4u; u++) f(q[u], base + u < nb.count);
-        base = next;
+    for (uint32_t u = 0; u < 4u; u++) {
+        q[u] = __ldg(nb.row + grp.lane + u * G);
+        g[u] = WITH_GS ? __ldg(nb.gs + grp.lane + u * G) : 0.0f;
+    }
+    for (uint32_t base = 0; base < nb.count; base += 4u * G) {
+        if (base > 0) {
+#pragma unroll
+            for (uint32_t u = 0; u < 4u; u++) {
+                const uint32_t j = base + grp.lane + u * G;
+                q[u] = j < nb.count ? __ldg(nb.row + j) : self;
+                g[u] = (WITH_GS && j < nb.count) ? __ldg(nb.gs + j) : 0.0f;
+            }
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; u++) {
+            const uint32_t j = base + grp.lane + u * G;
+            const bool ok = j < nb.count;
+            f(ok ? q[u] : self, g[u], j, ok);
+        }
     }
 }
 
 // gradW factor of one pair: GetGradientW(r) = gs * r (Kernel/DFSPHKernels.h:67-80).
 __device__ __forceinline__ float grad_factor(const Dev& d, float3 r) {
-    const float rl = sqrtf(dot3(r, r));
+    const float rl = fast_sqrt(dot3(r, r));
     return rl <= d.radius ? __ldg(d.GM + table_pos(d, rl)) : 0.0f;
 }
 
@@ -75,7 +93,7 @@ __device__ __forceinline__ float grad_factor(const Dev& d, float3 r) {
 // range tests: |r|^2 <= R^2 for W, |r| <= R for gradW).
 __device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, float& gs) {
     const float r2 = dot3(r, r);
-    const float rl = sqrtf(r2);
+    const float rl = fast_sqrt(r2);
     const uint32_t pos = table_pos(d, rl);
     w = r2 <= d.radius2 ? __ldg(d.WM + pos) : 0.0f;
     gs = rl <= d.radius ? __ldg(d.GM + pos) : 0.0f;
@@ -98,11 +116,13 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     float wsum = 0.0f, g2 = 0.0f;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     const float V = S.volume;
-    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+    float* gsRow = d.GS + (size_t)p * kRow;
+    for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t j, bool ok) {
         const float3 r = xi - f3(d.X[q]);
         float w, gs;
         kernel_wg(d, r, w, gs);
         if (!ok) return;
+        gsRow[j] = gs;
         wsum += w;
         const float3 gj = (-V * gs) * r;
         g2 += dot3(gj, gj);
@@ -138,10 +158,10 @@ template <uint32_t G>
 __device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
                                                      const Nbr& nb, float3 xi, float3 vi) {
     float s = 0.0f;
-    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float3 r = xi - f3(d.X[q]);
         const float3 vq = f3(d.V[q]);
-        const float t = dot3(vi - vq, grad_factor(d, r) * r);
+        const float t = dot3(vi - vq, gs * r);
         if (ok) s += t;
     });
     s = grp.sum(s) * S.volume;
@@ -164,6 +184,7 @@ __global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
     const float alpha = d.ALPHA[p] * S.dtInv;
     d.ALPHA[p] = alpha;
     d.KAPPAV[p] = rhoAdv * alpha;
+    set_kappa(d, p, rhoAdv * alpha);
 }
 
 // Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481);
@@ -176,10 +197,11 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
     const float3 xi = f3(d.X[p]);
     const float V = S.volume;
     float3 a = make_float3(0.f, 0.f, 0.f);
-    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
-        const float sum = ki + __ldg(kap + q);
-        const float3 r = xi - f3(d.X[q]);
-        if (ok && fabsf(sum) > kEps) a += (sum * (-V * grad_factor(d, r))) * r;
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
+        const float4 xq = d.X[q];
+        const float sum = ki + xq.w;
+        const float3 r = xi - f3(xq);
+        if (ok && fabsf(sum) > kEps) a += (sum * (-V * gs)) * r;
     });
     a = grp.sum(a);
     if (fabsf(ki) > kEps && (nb.flags & kHasBoundary)) a += ki * (-f3(d.GB[p]));
@@ -215,10 +237,10 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
         const float3 xi = f3(d.X[p]);
         const float3 ai = f3(d.AP[p]);
         float f = 0.0f;
-        for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+        for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
             const float3 r = xi - f3(d.X[q]);
             const float3 aq = f3(d.AP[q]);
-            const float t = dot3(ai - aq, grad_factor(d, r) * r);
+            const float t = dot3(ai - aq, gs * r);
             if (ok) f += t;
         });
         f = grp.sum(f) * S.volume;
@@ -228,11 +250,15 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
             if (DIV) {
                 f *= S.dt;
                 r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
-                d.KAPPAV[p] -= r * d.ALPHA[p];
+                const float k = d.KAPPAV[p] - r * d.ALPHA[p];
+                d.KAPPAV[p] = k;
+                set_kappa(d, p, k);
             } else {
                 f *= S.dt2;
                 r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
-                d.KAPPA[p] -= r * d.ALPHA[p];
+                const float k = d.KAPPA[p] - r * d.ALPHA[p];
+                d.KAPPA[p] = k;
+                set_kappa(d, p, k);
             }
             d.RES[p] = r;
             res = (double)r;
@@ -381,11 +407,11 @@ __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
     const float3 xi = f3(d.X[p]);
     float3 nc = make_float3(0.f, 0.f, 0.f);
     float cc = 0.0f, cf = 0.0f;
-    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+    for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t, bool ok) {
         const float4 nj = d.STN[q];
         const float3 dx = f3(d.X[q]) - xi;
         if (ok && nonzero3(nj)) {
-            const float num = 1.0f - sqrtf(dot3(dx, dx)) / S.h;
+            const float num = 1.0f - __fdividef(fast_sqrt(dot3(dx, dx)), S.h);
             nc += f3(nj) * num;
             cc += nj.w * num;
             cf += num;
@@ -475,12 +501,12 @@ __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     Mat3 m = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float3 r = xi - f3(d.X[q]);
         const float rho = d.RHO[q];
         if (!ok) return;
-        const float3 g = grad_factor(d, r) * r;
-        const float c = cmu * (S.mass / rho) / (dot3(r, r) + eps2);
+        const float3 g = gs * r;
+        const float c = __fdividef(cmu * __fdividef(S.mass, rho), dot3(r, r) + eps2);
         add_outer(m, c, r, g);
     });
     m.r0 = grp.sum(m.r0);
@@ -542,11 +568,11 @@ __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp,
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    for_neighbors(grp, nb, p, [&](uint32_t q, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float3 r = xi - f3(d.X[q]);
         const float4 vq = vec[q];
         const float r2 = dot3(r, r);
-        const float3 t = (cmu * vq.w * dot3(vi - f3(vq), r) / (r2 + eps2) * grad_factor(d, r)) * r;
+        const float3 t = (__fdividef(cmu * vq.w * dot3(vi - f3(vq), r), r2 + eps2) * gs) * r;
         if (ok) acc += t;
     });
     acc = grp.sum(acc);
@@ -822,7 +848,9 @@ __global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
     d.RHOADV[p] = rhoAdv;
     const float alpha = d.ALPHA[p] * S.dt2Inv;
     d.ALPHA[p] = alpha;
-    d.KAPPA[p] = -fminf(1.0f - rhoAdv, 0.0f) * alpha;
+    const float k = -fminf(1.0f - rhoAdv, 0.0f) * alpha;
+    d.KAPPA[p] = k;
+    set_kappa(d, p, k);
 }
 
 // K20 ComputePressureAccelerationAndVelocityKernel (:434-481) + K21 ComputePositionKernel (:54-67);
