@@ -19,6 +19,11 @@
 // operation order as the reference, no FMA contraction: build with
 // -ffp-contract=off), T = double is the FP64 oracle.
 //
+// Parity pinning: partial. The reference cannot be built here (Windows headers, the glm
+// submodule is absent) and ships no tests or fixtures; the oracle is pinned against the
+// tables and constants of the reference's source (tests/golden/reference_tables.json)
+// and closed forms, not against outputs of the reference's step.
+//
 // Deterministic rules where the reference is not deterministic:
 //   * in-cell order of the counting sort: ascending original particle index
 //     (the reference's atomicAdd rank, ParticleSearchKernels.cu:78, gives any
