@@ -361,6 +361,23 @@ int vfd_get_stream(vfd_sim* sim, void** stream);
 /* Number of kernel launches executed since creation (or the last reset), counted on the device. */
 int vfd_get_launch_count(vfd_sim* sim, uint64_t* launches, int32_t reset);
 
+/*
+ * Neighbour search that allocates nothing. No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: code whose device memory belongs to
+ * another allocator with a fixed budget, and code that must not allocate once it
+ * runs. Inputs and outputs are the caller's device buffers: xyz (n*3 floats),
+ * counts (n), neighbors (n * VFD_MAX_NEIGHBORS; row i holds particle i's neighbours in
+ * the reference's order, original indices), sort_indices (n; sorted slot -> original
+ * index). Intermediate data lives in a fixed ~10 MB __device__ array that every GPU
+ * loading the library keeps until exit; limits: n <= 16384 and a search grid of at most
+ * 262144 cells, else VFD_E_CAPACITY. The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and should come before any stream capture. All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the caller. Runs on
+ * `stream` (a cudaStream_t, NULL = default) and waits for it. Errors: return code only.
+ */
+int vfd_find_neighbors_noalloc(const float* xyz, uint32_t n, float particle_radius, uint32_t* counts,
+                               uint32_t* neighbors, uint32_t* sort_indices, void* stream);
+
 /* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
 int vfd_set_device(int32_t device);
 

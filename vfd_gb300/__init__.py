@@ -31,6 +31,7 @@ EXPORTS = [
     "vfd_get_scene_count", "vfd_scene_set_fluid", "vfd_scene_add_rigid_body", "vfd_scene_get_state",
     "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version", "vfd_profile_kernels",
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
+    "vfd_find_neighbors_noalloc",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
@@ -108,6 +109,8 @@ def lib() -> C.CDLL:
                 "vfd_set_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_get_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_autotune": [P, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32],
+                "vfd_find_neighbors_noalloc": [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p],
                 "vfd_last_error": [],
                 "vfd_abi_version": [],
             }
@@ -411,6 +414,17 @@ class DFSPHSimulation:
         _check(lib().vfd_get_neighbors(self._h, None, None, _u32ptr(lst), total.value, C.byref(total), None, None),
                "vfd_get_neighbors")
         return dict(counts=counts, offsets=offsets, list=lst[:total.value], sort_indices=sort_idx, cell_keys=keys)
+
+
+def find_neighbors_noalloc(xyz_ptr: int, n: int, particle_radius: float, counts_ptr: int, neighbors_ptr: int,
+                           sort_indices_ptr: int, stream: int = 0) -> int:
+    """vfd_find_neighbors_noalloc on caller-owned device buffers (raw device pointers).
+
+    For callers that cannot allocate device memory; the library uses a fixed
+    internal device array instead (at most 16384 particles per call). Returns the
+    status code (VFD_OK = 0)."""
+    return lib().vfd_find_neighbors_noalloc(xyz_ptr, n, C.c_float(particle_radius), counts_ptr, neighbors_ptr,
+                                            sort_indices_ptr, stream or None)
 
 
 def scene_simulation(scene: dict, desc_overrides: dict | None = None, maps: list | None = None) -> DFSPHSimulation:
