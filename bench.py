@@ -60,6 +60,14 @@ ALGO_BYTES = {
     "k_div_init": 12 + 12 + 4 + 4 + 4 + 4,
     "k_div_finish": 12 + 4 + 12 + 4 + 12 + 12,
     "k_rank_gather": 4 + 4 + 12 + 12 + 12 + 4 + 4 + 4 + 4 + 12 + 12 + 12 + 4 + 4,
+    "k_minmax": 12,
+    "k_keys": 12 + 4,
+    "k_slots": 4 + 4,
+    "k_st_smooth": 12 + 16 + 16 + 16,
+    "k_st_blend": 16 + 16 + 12,
+    "k_cg_p0": 12 + 12,
+    "k_visc_finish": 12 * 5,
+    "k_velocity": 12 * 3,
 }
 
 
@@ -149,6 +157,48 @@ def c2_config(n_side: int) -> dict:
             "l2": "inputs larger than L2 (state ~0.5 GB for 1M particles)"}
 
 
+def batched_form(V, scenes, steps: int, warmup: int, plain_every: int):
+    """The uneven-scene batch (256 scenes, 2k-64k particles each) advanced as one
+    simulation, against the plain step run scene by scene on every `plain_every`-th
+    scene. Both in particle-steps/s, timed with CUDA events on the library's stream."""
+    import torch
+    batch = scenes.uneven_batch()
+    counts = [len(s["x"]) for s in batch]
+    maps = [[V.build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"],
+                             s["desc"]["ParticleRadius"]) for b in s["boxes"]] for s in batch]
+
+    def run(sim, k):
+        stream = torch.cuda.ExternalStream(sim.GetStream())
+        sim.Steps(warmup)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.StepsAsync(k)
+        e1.record(stream)
+        sim.Synchronize()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    sim = V.batch_simulation(batch, maps)
+    ms_b = run(sim, steps)
+    errs = [sim.GetDebugInfo(scene=k)["PressureSolverError"] for k in range(len(batch))]
+    del sim
+    plain_n, plain_ms = 0, 0.0
+    for k in range(0, len(batch), plain_every):
+        one = V.scene_simulation(batch[k], maps=maps[k])
+        plain_ms += run(one, steps)
+        plain_n += counts[k]
+        del one
+    batched = sum(counts) * steps / (ms_b / 1e3)
+    plain = plain_n * steps / (plain_ms / 1e3)
+    return {"workload": f"{len(batch)} uneven scenes (dam breaks and drops, 2k-64k particles, "
+                        f"mu log-uniform 0.01-100 Pa s), {sum(counts)} particles in all",
+            "steps": steps, "batched": batched, "batched_ms_per_step": ms_b / steps,
+            "plain_scene_by_scene": plain, "plain_sample": f"every {plain_every}th scene run alone "
+                                                          f"({plain_n} particles)",
+            "batched_over_plain": batched / plain, "max_pressure_error": max(errs)}
+
+
 def cpu_baseline(n_side: int, steps: int, warmup: int):
     """The oracle (FP32, all host threads) on a c2-parameter sample."""
     from oracle import oracle as O
@@ -194,8 +244,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-side", type=int, default=100)
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=150)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched-scene measurement")
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--eager", action="store_true",
+                    help="launch the timed steps kernel by kernel instead of as CUDA graphs (same kernels, same "
+                         "results); profilers cannot see the kernels inside graphs with conditional nodes")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -218,6 +273,7 @@ def main():
     sim = V.scene_simulation(s)
     sim.Steps(1)
     lanes = sim.Autotune(2)  # per-kernel lanes per particle, state restored
+    sim.SetGraphMode(not args.eager)
     sim.Steps(args.warmup)
     stream = torch.cuda.ExternalStream(sim.GetStream())
 
@@ -227,11 +283,13 @@ def main():
         if ws > 1:
             dist.barrier()
         torch.cuda.synchronize()
+        torch.cuda.profiler.start()  # `ncu --profile-from-start off` records the timed steps only
         e0.record(stream)
         sim.StepsAsync(k)
         e1.record(stream)
         st = sim.Synchronize()
         torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
         if ws > 1:
             dist.barrier()
         return e0.elapsed_time(e1), st, sim.GetLaunchCount()
@@ -289,18 +347,27 @@ def main():
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": kms / cnt,
                 "share_of_step": kms / tot}
+    # the whole step: algorithmic bytes of every launch over the summed kernel time
+    step_bytes = sum(ALGO_BYTES.get(k, 0) * n * c for k, (c, _) in prof.items())
+    step_achieved = step_bytes / (tot / 1e3) / 1e9
+    step_roof = {"achieved": step_achieved, "peak": peak, "unit": "GB/s", "frac": step_achieved / peak,
+                 "algorithmic_bytes_per_step": step_bytes / 3, "kernel_ms_per_step": tot / 3}
     shares = {k: round(v[1] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:8]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (f64 reductions)", "data": "synthetic (seeded jittered lattice)",
-        "config": c2_config(args.n_side), "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
-        "roofline": roof, "kernel_shares": shares, "lanes_per_particle": lanes,
+        "config": dict(c2_config(args.n_side), launch="eager" if args.eager else "cuda graph per step"),
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
+        "roofline": roof, "step_roofline": step_roof, "kernel_shares": shares, "lanes_per_particle": lanes,
         "solver": {k: st[k] for k in ("DivergenceSolverIterationCount", "PressureSolverIterationCount",
                                       "ViscositySolverIterationCount", "PressureSolverError", "TimeStepSize",
                                       "MaxNeighborCount", "Flags")},
+        "mean_density_error_pct": 100.0 * st["PressureSolverError"] / 1000.0,
     }
+    if not args.no_forms:
+        line["forms"] = {"batched": batched_form(V, scenes, args.batch_steps, 3, 16)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

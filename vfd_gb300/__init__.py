@@ -427,6 +427,20 @@ def find_neighbors_noalloc(xyz_ptr: int, n: int, particle_radius: float, counts_
                                             sort_indices_ptr, stream or None)
 
 
+def batch_simulation(scene_list: list, maps: list | None = None) -> DFSPHSimulation:
+    """One DFSPHSimulation advancing every vfd_gb300.scenes scene of `scene_list` together
+    (volume maps built on the GPU unless given as one list of maps per scene)."""
+    sim = DFSPHSimulation(scenes=[make_desc(**s["desc"]) for s in scene_list])
+    for k, s in enumerate(scene_list):
+        sim.SetFluidObjects(s["x"], s["v"], scene=k)
+        r = s["desc"]["ParticleRadius"]
+        ms = maps[k] if maps is not None else [
+            build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"], r) for b in s["boxes"]]
+        for m in ms:
+            sim.AddRigidBody(m, scene=k)
+    return sim
+
+
 def scene_simulation(scene: dict, desc_overrides: dict | None = None, maps: list | None = None) -> DFSPHSimulation:
     """A DFSPHSimulation loaded with a vfd_gb300.scenes scene (volume maps built on the GPU unless given)."""
     d = dict(scene["desc"])
