@@ -1,0 +1,214 @@
+// Host-side state of one simulation handle (struct vfd_sim) and the helpers that
+// the C-ABI translation units share: the step launchers, the error and allocation
+// helpers, and the host copies of the kernel table and the scenes. Internal to the
+// library; the public interface is include/vfd_dfsph.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/vfd_dfsph.h"
+#include "dfsph_common.cuh"
+
+namespace vfd {
+void launch_search(const Dev& d, cudaStream_t s);
+uint32_t scan_block_count(uint32_t cellCap);
+void launch_boundary(const Dev& d, cudaStream_t s);
+void launch_density(const Dev& d, cudaStream_t s);
+void launch_div_init(const Dev& d, cudaStream_t s);
+void launch_div_iter(const Dev& d, cudaStream_t s);
+void launch_div_finish(const Dev& d, cudaStream_t s);
+void launch_surface_tension(const Dev& d, uint32_t maxPasses, cudaStream_t s);
+void launch_visc_init(const Dev& d, cudaStream_t s);
+void launch_cg_iter(const Dev& d, cudaStream_t s);
+void launch_visc_finish_dt(const Dev& d, cudaStream_t s);
+void launch_pres_init(const Dev& d, cudaStream_t s);
+void launch_pres_iter(const Dev& d, cudaStream_t s);
+void launch_pres_finish(const Dev& d, cudaStream_t s);
+void box_map_sizes(const uint32_t res[3], uint32_t& nodes, uint32_t& cells);
+int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, float padding, const uint32_t res[3],
+                      float r, const float* table, float wZero, float invStep, float* nodes, uint32_t* cells,
+                      uint32_t* cellMap, float dminOut[3], float dmaxOut[3], float csOut[3], float csiOut[3]);
+}  // namespace vfd
+
+namespace vfd {
+namespace host {
+
+// Records the message returned by vfd_last_error() and returns `code`.
+int fail(int code, const char* fmt, ...);
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(VFD_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                        \
+    } while (0)
+
+#define TRY(x)                         \
+    do {                               \
+        int rc_ = (x);                 \
+        if (rc_ != VFD_OK) return rc_; \
+    } while (0)
+
+// PrecomputedDFSPHCubicKernel::SetRadius (Kernel/DFSPHKernels.h:13-41) in FP32; the
+// library is built with -ffp-contract=off for host code so the table matches it bit for bit.
+struct KernelTable {
+    std::vector<float> W, G;
+    float radius = 0, radius2 = 0, invStep = 0, wZero = 0, K = 0, L = 0;
+    float calcW(float r) const {
+        float res = 0.0f;
+        const float q = r / radius;
+        if (q <= 1.0f) {
+            if (q <= 0.5f) {
+                const float q2 = q * q, q3 = q2 * q;
+                res = K * (6.0f * q3 - 6.0f * q2 + 1.0f);
+            } else {
+                const float q1 = 1.0f - q, q3 = q1 * q1 * q1;
+                res = K * (2.0f * q3);
+            }
+        }
+        return res;
+    }
+    float calcGradWx(float px) const {  // CalculateGradientW({px, 0, 0}).x
+        const float rl = std::sqrt(px * px + 0.0f * 0.0f + 0.0f * 0.0f);
+        const float q = rl / radius;
+        if (rl > 1.0e-5f && q <= 1.0f) {
+            const float gq = px * (1.0f / (rl * radius));
+            if (q <= 0.5f) return ((L * q) * (3.0f * q - 2.0f)) * gq;
+            const float f = 1.0f - q;
+            return (L * (-f * f)) * gq;
+        }
+        return 0.0f;
+    }
+    void setRadius(float r) {
+        const float pi = (float)3.14159265358979323846;
+        W.assign(kTableRes, 0.0f);
+        G.assign(kTableRes + 1, 0.0f);
+        radius = r;
+        radius2 = radius * radius;
+        const float r3 = radius * radius * radius;
+        K = 8.0f / (pi * r3);
+        L = 48.0f / (pi * r3);
+        wZero = calcW(std::sqrt(0.0f));
+        const float step = radius / (float)(kTableRes - 1);
+        invStep = 1.0f / step;
+        for (uint32_t i = 0; i < kTableRes; i++) {
+            const float px = step * (float)i;
+            W[i] = calcW(px);
+            G[i] = px > 1.0e-9f ? calcGradWx(px) / px : 0.0f;
+        }
+        G[kTableRes] = 0.0f;
+    }
+};
+
+struct BodyHost {
+    BodyDev dev{};
+    float* nodes = nullptr;
+    uint32_t* cells = nullptr;
+    uint32_t* cellMap = nullptr;
+    void release() {
+        cudaFree(nodes);
+        cudaFree(cells);
+        cudaFree(cellMap);
+        nodes = nullptr;
+        cells = cellMap = nullptr;
+    }
+};
+
+struct SceneHost {
+    vfd_desc desc{};
+    std::vector<float> x0, v0;
+    std::vector<BodyHost> bodies;
+};
+
+}  // namespace host
+}  // namespace vfd
+
+struct vfd_sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<vfd::host::SceneHost> scenes;
+    vfd::host::KernelTable table;
+    std::vector<float> halton;
+    bool graphMode = true;
+    bool graphFailed = false;
+    uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+
+    // layout
+    bool allocated = false, uploaded = false;
+    uint32_t n = 0, stride = 0, cellCap = 0, maxBodies = 0;
+    std::vector<uint32_t> sceneBegin;
+    std::vector<void*> allocs;
+    vfd::Dev dev[2]{};
+    int cs = 0;  // set holding the current carried state
+    float4* XB = nullptr;
+    float* dStage = nullptr;     // 3 floats per particle, original order
+    vfd::SceneDev* dScenes = nullptr;
+    vfd::BodyDev* dBodies = nullptr;
+    uint32_t* dStatus = nullptr;
+    float *dWM = nullptr, *dGM = nullptr, *dHalton = nullptr;
+    uint32_t* hStatus = nullptr;  // pinned
+    std::vector<vfd::SceneDev> hScenes;
+    uint32_t maxStPasses = 0;
+    bool anyDiv = false, anyVisc = false, anyST = false;
+
+    // graphs (one per parity)
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    bool searchOnlyPending = false;
+
+    ~vfd_sim() { release(); }
+
+    void releaseGraphs() {
+        for (int k = 0; k < 2; k++) {
+            if (exec[k]) cudaGraphExecDestroy(exec[k]);
+            if (graph[k]) cudaGraphDestroy(graph[k]);
+            exec[k] = nullptr;
+            graph[k] = nullptr;
+        }
+    }
+    void releaseBuffers() {
+        releaseGraphs();
+        for (void* p : allocs) cudaFree(p);
+        allocs.clear();
+        if (hStatus) cudaFreeHost(hStatus);
+        hStatus = nullptr;
+        allocated = false;
+        uploaded = false;
+    }
+    void release() {
+        releaseBuffers();
+        for (auto& s : scenes)
+            for (auto& b : s.bodies) b.release();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace vfd {
+namespace host {
+
+template <class T>
+int dalloc(vfd_sim* s, T** p, size_t count) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(VFD_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    s->allocs.push_back(q);
+    *p = (T*)q;
+    return VFD_OK;
+}
+
+int ensure_ready(vfd_sim* s);
+int read_flag(vfd_sim* s, int idx, uint32_t& v);
+int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait);
+int finish_steps(vfd_sim* s, vfd_step_stats* stats, uint32_t& flags);
+int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out);
+int gather_vec(vfd_sim* s, uint32_t scene, const float* in, float4* ddst);
+
+}  // namespace host
+}  // namespace vfd
