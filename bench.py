@@ -199,6 +199,63 @@ def batched_form(V, scenes, steps: int, warmup: int, plain_every: int):
             "batched_over_plain": batched / plain, "max_pressure_error": max(errs)}
 
 
+def adjoint_form(V, scenes, steps: int = 60, every: int = 10):
+    """The viscous drop (32k particles, mu = 10 Pa s), `steps` steps: the plain forward
+    run, then the forward run with checkpoints every `every` steps plus the adjoint,
+    both from the same initial state and timed on the host around synchronised calls.
+    Loss = mean |x_T - y|^2, y a jittered copy of the drop moved by (0.05, -0.2, 0);
+    its gradient is checked against central differences (relative step 1e-3) in the
+    viscosity and along one random initial-velocity direction."""
+    s = scenes.viscous_drop_c4()
+    n = len(s["x"])
+    rng = np.random.default_rng(scenes.config_seed(4))
+    target = s["x"].astype(np.float64) + np.array([0.05, -0.2, 0.0]) + 0.25 * s["desc"]["ParticleRadius"] * \
+        rng.standard_normal(s["x"].shape)
+    sim = V.scene_simulation(s)
+    sim.Steps(2)  # builds the step graphs
+
+    def restart(x=None, v=None, nu=None):
+        d = dict(s["desc"])
+        if nu is not None:
+            d["Viscosity"] = d["BoundaryViscosity"] = nu
+        sim.SetDescription(d)
+        sim.SetFluidObjects(s["x"] if x is None else x, s["v"] if v is None else v)
+
+    def loss(**kw):
+        restart(**kw)
+        sim.Steps(steps)
+        x, _, _ = sim.GetState()
+        return float(np.mean(np.sum((x.astype(np.float64) - target) ** 2, axis=1)))
+
+    loss()  # warm-up of the forward path at this size
+    restart()
+    t0 = time.perf_counter()
+    sim.Steps(steps)
+    t_fwd = time.perf_counter() - t0
+    restart()
+    t0 = time.perf_counter()
+    sim.AdjointForward(steps, every)
+    x, v, _ = sim.GetState()
+    xb = (2.0 / n) * (x.astype(np.float64) - target)
+    x0b, v0b, pb = sim.AdjointBackward(xb.astype(np.float32), np.zeros_like(v))
+    t_adj = time.perf_counter() - t0
+    nu = s["desc"]["Viscosity"]
+    eps = 1e-3
+    fd_nu = (loss(nu=nu * (1 + eps)) - loss(nu=nu * (1 - eps))) / (2 * eps * nu)
+    g_nu = float(pb[0] + pb[1])
+    d = np.random.default_rng(1).standard_normal(s["v"].shape).astype(np.float32)
+    fd_v = (loss(v=s["v"] + eps * d) - loss(v=s["v"] - eps * d)) / (2 * eps)
+    g_v = float(np.sum(v0b.astype(np.float64) * d))
+    return {"workload": f"viscous drop, {n} particles (sphere r = 0.1 m), mu = 10 Pa s, {steps} steps, "
+                        f"checkpoint every {every}",
+            "forward": n * steps / t_fwd, "fwd_adjoint": n * steps / t_adj, "adjoint_over_forward": t_adj / t_fwd,
+            "forward_s": t_fwd, "fwd_adjoint_s": t_adj,
+            "grad_check": {"dL_dmu_adjoint": g_nu, "dL_dmu_central_difference": fd_nu,
+                           "rel_err_mu": abs(g_nu - fd_nu) / abs(fd_nu),
+                           "dL_dv0_dir_adjoint": g_v, "dL_dv0_dir_central_difference": fd_v,
+                           "rel_err_v0": abs(g_v - fd_v) / abs(fd_v), "relative_step": eps}}
+
+
 def cpu_baseline(n_side: int, steps: int, warmup: int):
     """The oracle (FP32, all host threads) on a c2-parameter sample."""
     from oracle import oracle as O
@@ -367,7 +424,8 @@ def main():
         "mean_density_error_pct": 100.0 * st["PressureSolverError"] / 1000.0,
     }
     if not args.no_forms:
-        line["forms"] = {"batched": batched_form(V, scenes, args.batch_steps, 3, 16)}
+        line["forms"] = {"batched": batched_form(V, scenes, args.batch_steps, 3, 16),
+                         "fwd_adjoint": adjoint_form(V, scenes)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

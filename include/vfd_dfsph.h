@@ -378,6 +378,28 @@ int vfd_get_launch_count(vfd_sim* sim, uint64_t* launches, int32_t reset);
 int vfd_find_neighbors_noalloc(const float* xyz, uint32_t n, float particle_radius, uint32_t* counts,
                                uint32_t* neighbors, uint32_t* sort_indices, void* stream);
 
+/*
+ * Adjoint of the step. No counterpart in the reference (its step is not
+ * differentiable code). vfd_adjoint_forward runs `steps` OnUpdate steps from the
+ * current state like vfd_steps, keeping a checkpoint of the carried state every
+ * `checkpoint_every` steps. vfd_adjoint_backward then takes the cotangents of the
+ * final positions and velocities (x_bar, v_bar: n*3 floats, original order) and
+ * returns those of the initial positions and velocities (x0_bar, v0_bar; either may
+ * be NULL) and param_bar[0] = d/d Viscosity, param_bar[1] = d/d BoundaryViscosity
+ * (may be NULL). It re-runs each segment from its checkpoint, recording neighbour
+ * rows and solver iterates, and leaves the simulation at the end of the forward run.
+ * Per step the neighbour sets, solver iteration counts and clamp decisions are those
+ * of the forward run; the viscosity solve is differentiated at its converged
+ * solution (a second CG solve with the same tolerance). Requires one scene, surface
+ * tension off and no particle at the 70-neighbour cap (VFD_E_ARG / VFD_E_CAPACITY);
+ * VFD_E_STATE if the simulation was reset after vfd_adjoint_forward.
+ */
+int vfd_adjoint_forward(vfd_sim* sim, uint32_t steps, uint32_t checkpoint_every, vfd_step_stats* stats);
+int vfd_adjoint_backward(vfd_sim* sim, const float* x_bar, const float* v_bar, float* x0_bar, float* v0_bar,
+                         float* param_bar);
+/* Frees the checkpoints and tapes of the recorded run. */
+int vfd_adjoint_release(vfd_sim* sim);
+
 /* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
 int vfd_set_device(int32_t device);
 

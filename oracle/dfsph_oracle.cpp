@@ -1548,9 +1548,10 @@ int orc_build_box_map(const float bmin[3], const float bmax[3], int inverted, fl
     return VFD_OK;
 }
 
-// Distance and gradient of field `field` at n points (FP64 lookup of the map).
-int orc_map_interpolate(const vfd_volume_map* mp, uint32_t field, const float* x, uint32_t n, double* phi,
-                        double* grad) {
+// Distance and gradient of field `field` at n points (FP64 lookup of the map), the
+// points given in double precision.
+int orc_map_interpolate_d(const vfd_volume_map* mp, uint32_t field, const double* x, uint32_t n, double* phi,
+                          double* grad) {
     MapData m;
     m.fieldCount = mp->field_count;
     m.nodeCount = mp->node_count;
@@ -1577,6 +1578,13 @@ int orc_map_interpolate(const vfd_volume_map* mp, uint32_t field, const float* x
         if (grad) { grad[3 * i] = g.x; grad[3 * i + 1] = g.y; grad[3 * i + 2] = g.z; }
     }
     return VFD_OK;
+}
+
+// The same with single-precision points.
+int orc_map_interpolate(const vfd_volume_map* mp, uint32_t field, const float* x, uint32_t n, double* phi,
+                        double* grad) {
+    std::vector<double> xd(x, x + 3 * (size_t)n);
+    return orc_map_interpolate_d(mp, field, xd.data(), n, phi, grad);
 }
 
 // n-point Gauss-Legendre abscissae and weights on [-1, 1] (ascending).

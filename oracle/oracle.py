@@ -62,6 +62,8 @@ def lib():
                                             C.POINTER(_abi.vfd_volume_map)]
             L.orc_map_interpolate.argtypes = [C.POINTER(_abi.vfd_volume_map), C.c_uint32, f32p, C.c_uint32, f64p,
                                               f64p]
+            L.orc_map_interpolate_d.argtypes = [C.POINTER(_abi.vfd_volume_map), C.c_uint32, f64p, C.c_uint32, f64p,
+                                                f64p]
             L.orc_gauss_legendre.argtypes = [C.c_uint, f64p, f64p]
             L.orc_map_node_positions.argtypes = [C.POINTER(_abi.vfd_volume_map), f32p]
             L.orc_set_threads.argtypes = [C.c_int]
@@ -162,6 +164,17 @@ def build_box_map(bmin, bmax, inverted: bool, padding: float, resolution, partic
                             _ptr(nodes, C.c_float), _ptr(cells, C.c_uint32), _ptr(cell_map, C.c_uint32),
                             C.byref(m))
     return VolumeMap(nodes, cells, cell_map, m)
+
+
+def map_interpolate_d(vmap: VolumeMap, field: int, points):
+    """FP64 value and gradient of map field `field` at double-precision points (FLT_MAX outside)."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    n = len(pts)
+    phi = np.zeros(n, np.float64)
+    grad = np.zeros((n, 3), np.float64)
+    lib().orc_map_interpolate_d(C.byref(vmap.struct), field, _ptr(pts, C.c_double), n, _ptr(phi, C.c_double),
+                                _ptr(grad, C.c_double))
+    return phi, grad
 
 
 def map_interpolate(vmap: VolumeMap, field: int, points):

@@ -31,7 +31,7 @@ EXPORTS = [
     "vfd_get_scene_count", "vfd_scene_set_fluid", "vfd_scene_add_rigid_body", "vfd_scene_get_state",
     "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version", "vfd_profile_kernels",
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
-    "vfd_find_neighbors_noalloc",
+    "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
@@ -111,6 +111,9 @@ def lib() -> C.CDLL:
                 "vfd_autotune": [P, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_find_neighbors_noalloc": [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p],
+                "vfd_adjoint_forward": [P, C.c_uint32, C.c_uint32, C.POINTER(vfd_step_stats)],
+                "vfd_adjoint_backward": [P, f32p, f32p, f32p, f32p, f32p],
+                "vfd_adjoint_release": [P],
                 "vfd_last_error": [],
                 "vfd_abi_version": [],
             }
@@ -364,6 +367,30 @@ class DFSPHSimulation:
         out = np.zeros(shape, np.float32)
         _check(lib().vfd_get_field(self._h, field, body, _fptr(out)), "vfd_get_field")
         return out
+
+    # adjoint (no counterpart in the reference)
+    def AdjointForward(self, steps: int, checkpoint_every: int = 10) -> dict:
+        """`steps` steps from the current state, checkpointed for AdjointBackward."""
+        st = vfd_step_stats()
+        _check(lib().vfd_adjoint_forward(self._h, steps, checkpoint_every, C.byref(st)), "vfd_adjoint_forward")
+        return st.as_dict()
+
+    def AdjointBackward(self, x_bar, v_bar):
+        """Cotangents of the final (x, v) -> those of the initial (x, v) and of
+        (Viscosity, BoundaryViscosity), for the run of the last AdjointForward."""
+        n = self.GetParticleCount()
+        xb, xbp = _f32(np.asarray(x_bar).reshape(n, 3))
+        vb, vbp = _f32(np.asarray(v_bar).reshape(n, 3))
+        x0 = np.empty((n, 3), np.float32)
+        v0 = np.empty((n, 3), np.float32)
+        pb = np.zeros(2, np.float32)
+        _check(lib().vfd_adjoint_backward(self._h, xbp, vbp, x0.ctypes.data_as(C.POINTER(C.c_float)),
+                                          v0.ctypes.data_as(C.POINTER(C.c_float)),
+                                          pb.ctypes.data_as(C.POINTER(C.c_float))), "vfd_adjoint_backward")
+        return x0, v0, pb
+
+    def AdjointRelease(self):
+        _check(lib().vfd_adjoint_release(self._h), "vfd_adjoint_release")
 
     def ProfileKernels(self, steps: int) -> dict:
         """{kernel name: (launches, total ms)} over `steps` eagerly launched steps."""

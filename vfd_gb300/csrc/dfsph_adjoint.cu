@@ -1,0 +1,1184 @@
+// Reverse-mode derivative (adjoint) of the DFSPH step: the gradient of a function
+// of the final positions and velocities after `steps` OnUpdate steps with respect
+// to the initial positions, the initial velocities, Viscosity and BoundaryViscosity.
+//
+// The reference has no derivative of its step. The forward computation
+// differentiated here is the step of DFSPHImplementation::OnUpdate
+// (Simulation/DFSPH/DFSPHImplementation.cu:63-170) exactly as dfsph_physics.cu runs
+// it. Per step, with neighbour sets N(i), the solver iteration counts and the
+// clamp/skip decisions of the step frozen:
+//   density    rho_i = rho0 (V W0 + V sum_j W_ij + sum_b Vb W(pd_b))
+//              alpha_i = 1 / (sum_j |V gradW_ij|^2 + |V sum_j gradW_ij + GB_i|^2)
+//   operators  D_i(w) = V sum_j (w_i - w_j).gradW_ij + w_i.GB_i          (K4, K6, K17, K19)
+//              P_i(k) = -V sum_j (k_i + k_j) gradW_ij - k_i GB_i         (K5, K7, K18, K20)
+//   divergence rho_adv = max(D(v0), 0); k0 = rho_adv alpha / dt_o;
+//              k <- k + m_k (alpha / dt_o) (rho_adv + dt_o D(P(k)))      (unrolled, m_k = clamp active)
+//              v1 = v0 + dt_o P(k)
+//   viscosity  A(x, rho) g = v1 (Weiler 2018), solved by CG; through the implicit
+//              function theorem the adjoint solves A lambda = g_bar with the same CG
+//              (A is symmetric) and differentiates A g = v1 for x, rho, the two
+//              viscosities and dt_o
+//   CFL        dt_n = 0.4 d / sqrt(max_i |g_i + dt_o gravity|^2)   (through the argmax)
+//   velocity   v2 = v1 + dt_n (gravity + (g - v1) / dt_o)
+//   pressure   rho_adv = rho / rho0 + dt_n D(v2); k0 = max(rho_adv - 1, 0) alpha / dt_n^2;
+//              k <- k - m_k (alpha / dt_n^2) (1 - rho_adv - dt_n^2 D(P(k)))
+//              v3 = v2 + dt_n P(k); x' = x + dt_n v3
+// D and P are transposes of each other up to sign (P = -D^T), so the adjoint of
+// every linear solve step is again a pass of the same two operators. Their
+// dependence on positions goes through gradW(x_i - x_j), whose derivative is the
+// kernel Hessian H = gs I + gs'/|r| r r^T of the analytic cubic spline (the
+// reference's midpoint table lookup is piecewise constant in |r|; its values are
+// used wherever the forward uses them). Boundary samples: x - xb = pd n with
+// pd = max(phi0 + r/2, 2r) and Vb = phi1 of the volume map; phi0, phi1 are
+// differentiated through the shape-function gradients, the normal n is held
+// fixed (exact on planar walls). The push-out of particles inside a wall moves
+// them by a constant 0.1 r along n (identity Jacobian) and zeroes their velocity.
+//
+// Memory: states are checkpointed every `checkpoint_every` steps during the
+// forward run; the backward pass re-runs each segment eagerly from its checkpoint,
+// recording per step the neighbour rows, four velocity fields and the Jacobi
+// iterates, and then walks the segment's steps in reverse.
+// Limits: one scene, surface tension off; neighbour sets must be symmetric, so a
+// particle at the 70-neighbour cap is rejected.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "dfsph_map.cuh"
+#include "dfsph_sim.h"
+
+namespace vfd {
+
+namespace {
+
+constexpr uint32_t kAG = 8;  // lanes per particle of the adjoint neighbour loops
+
+// Cotangent arrays of the backward pass (slot order unless stated).
+struct AdjDev {
+    float4 *XBAR, *VBAR;      // x and v of the point of the step being differentiated
+    float4 *ABAR, *AK;        // pressure-acceleration cotangent, recomputed acceleration
+    float4 *GBAR, *GSUM;      // viscosity-solution cotangent; (sum gradW + GB, S bar)
+    float4* BD;               // [3][body][stride]: (n, Vb), (grad pd, pd), (grad Vb, -)
+    float *KBAR, *U, *RABAR, *APBAR, *DBAR, *RHOBAR, *ALBAR;
+    uint32_t* STOP;           // 1 where the boundary zeroed the velocity
+    double* SC;               // [0] dt_o bar, [1] dt_n bar, [2] Viscosity bar, [3] BoundaryViscosity bar
+    uint32_t* CLAIM;          // [0] largest recomputed CFL |w|^2 (bits), [1] argmax claimed
+    float4 *XBO, *VBO;        // x and v cotangents in original particle order
+};
+
+// The reference's cubic spline (Kernel/DFSPHKernels.h:86-131) and its derivatives.
+struct Spline {
+    float h, K;
+    __device__ explicit Spline(float radius) : h(radius), K(8.0f / (3.14159265358979f * radius * radius * radius)) {}
+    __device__ float w(float s) const {
+        const float q = s / h;
+        if (q <= 0.5f) return K * (6.0f * q * q * q - 6.0f * q * q + 1.0f);
+        if (q <= 1.0f) {
+            const float f = 1.0f - q;
+            return 2.0f * K * f * f * f;
+        }
+        return 0.0f;
+    }
+    // W'(s) and W''(s).
+    __device__ void d12(float s, float& w1, float& w2) const {
+        const float q = s / h;
+        if (q <= 0.5f) {
+            w1 = K * (18.0f * q * q - 12.0f * q) / h;
+            w2 = K * (36.0f * q - 12.0f) / (h * h);
+        } else if (q <= 1.0f) {
+            const float f = 1.0f - q;
+            w1 = -6.0f * K * f * f / h;
+            w2 = 12.0f * K * f / (h * h);
+        } else {
+            w1 = w2 = 0.0f;
+        }
+    }
+    // gs = W'(s) / s and gq = gs'(s) / s: gradW(r) = gs r, d gradW / dr = gs I + gq r r^T.
+    __device__ void hess(float s, float& gs, float& gq) const {
+        const float q = s / h;
+        if (q <= 0.5f) {
+            gs = K * (18.0f * q - 12.0f) / (h * h);
+            gq = 18.0f * K / (h * h * h * s);
+        } else if (q <= 1.0f) {
+            const float f = 1.0f - q;
+            gs = -6.0f * K * f * f / (h * s);
+            const float w2 = 12.0f * K * f / (h * h);
+            gq = (w2 - gs) / (s * s);
+        } else {
+            gs = gq = 0.0f;
+        }
+    }
+};
+
+__device__ __forceinline__ float3 hmul(float gs, float gq, float3 r, float3 w) { return gs * w + (gq * dot3(r, w)) * r; }
+
+struct Row {
+    const uint32_t* nbr;
+    const float* gs;
+    uint32_t count, flags;
+};
+__device__ __forceinline__ Row row_of(const Dev& d, uint32_t p) {
+    const uint32_t w = d.NCNT[p];
+    return Row{d.NBR + (size_t)p * kRow, d.GS + (size_t)p * kRow, w & kCountMask, w};
+}
+
+__device__ __forceinline__ float4 bd(const AdjDev& a, const Dev& d, uint32_t k, uint32_t b, uint32_t p) {
+    return a.BD[((size_t)k * d.maxBodies + b) * d.stride + p];
+}
+
+// J_GB^T y: GB_i = sum_b Vb W'(pd) n, so d(GB . y)/dx = sum_b (n . y)(W'(pd) grad Vb + Vb W''(pd) grad pd).
+__device__ float3 jgb_t(const Dev& d, const AdjDev& a, const Spline& sp, uint32_t nb, uint32_t p, float3 y) {
+    float3 out = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t b = 0; b < nb; b++) {
+        const float4 b0 = bd(a, d, 0, b, p);
+        if (!(b0.w > 0.0f)) continue;
+        const float4 b1 = bd(a, d, 1, b, p), b2 = bd(a, d, 2, b, p);
+        float w1, w2;
+        sp.d12(b1.w, w1, w2);
+        const float ny = dot3(f3(b0), y);
+        out += ny * (w1 * f3(b2) + (b0.w * w2) * f3(b1));
+    }
+    return out;
+}
+
+// Adds v into dst (one atomic per block); every thread of the block must call it.
+__device__ void block_add(double* dst, double v) {
+    __shared__ double part[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) part[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (uint32_t w = 0; w < (blockDim.x + 31u) / 32u; w++) t += part[w];
+        if (t != 0.0) atomicAdd(dst, t);
+    }
+}
+
+__device__ __forceinline__ double dot3d(float3 a, float3 b) {
+    return (double)a.x * b.x + (double)a.y * b.y + (double)a.z * b.z;
+}
+
+#define ADJ_GROUP                                          \
+    const Group<kAG> grp;                                  \
+    const uint32_t p = grp.p;                              \
+    const bool live = p < d.n;                             \
+    const uint32_t pp = live ? p : 0u;                     \
+    (void)pp;
+
+// ---------------------------------------------------------------- boundary data
+// The boundary kernel's decisions (k_boundary, ComputeVolumeAndBoundaryKernel
+// DFSPHKernels.cu:69-150) replayed on the positions before it ran, keeping what the
+// adjoint needs: per body (n, Vb), (grad pd, pd), (grad Vb), and the velocity reset.
+__global__ void k_adj_bdata(Dev d, AdjDev a) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    const SceneDev& S = d.scenes[0];
+    float3 x = f3(d.X[p]);
+    uint32_t stop = 0;
+    for (uint32_t b = 0; b < S.bodyCount; b++) {
+        const BodyDev& m = d.bodies[S.bodyBegin + b];
+        const MapSample s = map_lookup<true>(m, x);
+        const float dist = s.inside ? s.phi0 : FLT_MAX;
+        float4 b0 = make_float4(0.f, 0.f, 0.f, 0.f), b1 = b0, b2 = b0;
+        if (dist > 0.0f && dist < S.h) {
+            const float volume = s.phi1;
+            if (volume > 0.0f && volume != FLT_MAX) {
+                const float nl = sqrtf(dot3(s.grad0, s.grad0));
+                if (nl > 1.0e-9f) {
+                    const float3 n = make_float3(s.grad0.x / nl, s.grad0.y / nl, s.grad0.z / nl);
+                    const float raw = dist + 0.5f * S.r;
+                    const float pd = fmaxf(raw, S.diam);
+                    b0 = f4(n, volume);
+                    b1 = f4(raw > S.diam ? s.grad0 : make_float3(0.f, 0.f, 0.f), pd);
+                    b2 = f4(s.grad1, 0.0f);
+                }
+            }
+        } else if (dist <= 0.0f) {
+            const float nl = sqrtf(dot3(s.grad0, s.grad0));
+            if (nl > 1.0e-5f) {
+                const float3 n = make_float3(s.grad0.x / nl, s.grad0.y / nl, s.grad0.z / nl);
+                x += fminf(S.diam - dist, 0.1f * S.r) * n;
+                stop = 1;
+            }
+        }
+        a.BD[((size_t)0 * d.maxBodies + b) * d.stride + p] = b0;
+        a.BD[((size_t)1 * d.maxBodies + b) * d.stride + p] = b1;
+        a.BD[((size_t)2 * d.maxBodies + b) * d.stride + p] = b2;
+    }
+    a.STOP[p] = stop;
+}
+
+// ---------------------------------------------------------------- Jacobi passes
+// AK = P(kap) as the forward computes it (masks |k_i + k_j| > eps, |k_i| > eps);
+// with U: ABAR = c D^T(U) = c (V sum_j (u_i + u_j) gradW_ij + u_i GB_i).
+template <bool HAS_U>
+__global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const float* __restrict__ kap, float c) {
+    ADJ_GROUP
+    const SceneDev& S = d.scenes[0];
+    const float V = S.volume;
+    float3 acc = make_float3(0.f, 0.f, 0.f), ab = acc;
+    Row rw{};
+    float ki = 0.f, ui = 0.f;
+    float3 xi = acc;
+    if (live) {
+        rw = row_of(d, p);
+        ki = kap[p];
+        ui = HAS_U ? a.U[p] : 0.f;
+        xi = f3(d.X[p]);
+        for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
+            const uint32_t q = __ldg(rw.nbr + j);
+            const float gs = __ldg(rw.gs + j);
+            const float3 r = xi - f3(d.X[q]);
+            const float kq = kap[q];
+            const float sum = ki + kq;
+            if (fabsf(sum) > kEps) acc += (sum * (-V * gs)) * r;
+            if (HAS_U) ab += ((ui + a.U[q]) * (V * gs)) * r;
+        }
+    }
+    acc = grp.sum(acc);
+    if (HAS_U) ab = grp.sum(ab);
+    if (!live || grp.lane != 0) return;
+    const float3 gb = f3(d.GB[p]);
+    if (fabsf(ki) > kEps && (rw.flags & kHasBoundary)) acc += ki * (-gb);
+    a.AK[p] = f4(acc, 0.0f);
+    if (HAS_U) a.ABAR[p] = f4(c * (ab + ui * gb), 0.0f);
+}
+
+// KBAR += P^T(ABAR) (masked like P); XBAR += XP(kap, ABAR) + c XD(AK, U), where
+// XP(k, ab)_i = -V sum_j e_ij (k_i + k_j) H_ij (ab_i - ab_j) - k_i J_GB^T ab_i and
+// XD(w, u)_i = V sum_j H_ij (w_i - w_j)(u_i + u_j) + u_i J_GB^T w_i.
+template <bool HAS_U>
+__global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a, const float* __restrict__ kap, float c) {
+    ADJ_GROUP
+    const SceneDev& S = d.scenes[0];
+    const Spline sp(d.radius);
+    const float V = S.volume;
+    float kb = 0.f;
+    float3 xp = make_float3(0.f, 0.f, 0.f), xd = xp;
+    Row rw{};
+    float ki = 0.f, ui = 0.f;
+    float3 xi = xp, abi = xp, aki = xp;
+    if (live) {
+        rw = row_of(d, p);
+        ki = kap[p];
+        xi = f3(d.X[p]);
+        abi = f3(a.ABAR[p]);
+        if (HAS_U) {
+            ui = a.U[p];
+            aki = f3(a.AK[p]);
+        }
+        for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
+            const uint32_t q = __ldg(rw.nbr + j);
+            const float gsT = __ldg(rw.gs + j);
+            const float3 r = xi - f3(d.X[q]);
+            const float s = sqrtf(dot3(r, r));
+            float gs, gq;
+            sp.hess(s, gs, gq);
+            const float kq = kap[q];
+            const float3 dab = abi - f3(a.ABAR[q]);
+            if (fabsf(ki + kq) > kEps) {
+                kb += -V * gsT * dot3(r, dab);
+                xp += (-V * (ki + kq)) * hmul(gs, gq, r, dab);
+            }
+            if (HAS_U) xd += (V * (ui + a.U[q])) * hmul(gs, gq, r, aki - f3(a.AK[q]));
+        }
+    }
+    kb = grp.sum(kb);
+    xp = grp.sum(xp);
+    if (HAS_U) xd = grp.sum(xd);
+    if (!live || grp.lane != 0) return;
+    if (rw.flags & kHasBoundary) {
+        if (fabsf(ki) > kEps) {
+            kb += -dot3(f3(d.GB[p]), abi);
+            xp += -ki * jgb_t(d, a, sp, S.bodyCount, p, abi);
+        }
+        if (HAS_U) xd += ui * jgb_t(d, a, sp, S.bodyCount, p, aki);
+    }
+    a.KBAR[p] += kb;
+    a.XBAR[p] = f4(f3(a.XBAR[p]) + xp + c * xd, 0.0f);
+}
+
+// VBAR += D^T(DBAR); XBAR += XD(w, DBAR); with DT also SC[1] += sum RABAR_i D_i(w).
+template <bool DT>
+__global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const float4* __restrict__ w) {
+    ADJ_GROUP
+    const SceneDev& S = d.scenes[0];
+    const Spline sp(d.radius);
+    const float V = S.volume;
+    float3 vb = make_float3(0.f, 0.f, 0.f), xd = vb, wi = vb, xi = vb;
+    float di = 0.f, dv = 0.f;
+    Row rw{};
+    if (live) {
+        rw = row_of(d, p);
+        xi = f3(d.X[p]);
+        wi = f3(w[p]);
+        di = a.DBAR[p];
+        for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
+            const uint32_t q = __ldg(rw.nbr + j);
+            const float gsT = __ldg(rw.gs + j);
+            const float3 r = xi - f3(d.X[q]);
+            const float s = sqrtf(dot3(r, r));
+            float gs, gq;
+            sp.hess(s, gs, gq);
+            const float dq = a.DBAR[q];
+            const float3 dw = wi - f3(w[q]);
+            vb += ((di + dq) * (V * gsT)) * r;
+            xd += (V * (di + dq)) * hmul(gs, gq, r, dw);
+            if (DT) dv += gsT * dot3(dw, r);
+        }
+    }
+    vb = grp.sum(vb);
+    xd = grp.sum(xd);
+    if (DT) dv = grp.sum(dv);
+    double acc = 0.0;
+    if (live && grp.lane == 0) {
+        if (rw.flags & kHasBoundary) {
+            const float3 gb = f3(d.GB[p]);
+            vb += di * gb;
+            xd += di * jgb_t(d, a, sp, S.bodyCount, p, wi);
+            dv = V * dv + dot3(wi, gb);
+        } else {
+            dv = V * dv;
+        }
+        a.VBAR[p] = f4(f3(a.VBAR[p]) + vb, 0.0f);
+        a.XBAR[p] = f4(f3(a.XBAR[p]) + xd, 0.0f);
+        if (DT) acc = (double)a.RABAR[p] * (double)dv;
+    }
+    if (DT) block_add(a.SC + 1, acc);
+}
+
+// ---------------------------------------------------------------- density and factor
+// GSUM = (G_i, S bar_i) with G_i = V sum_j gradW_ij + GB_i and S bar = -alpha_bar alpha^2.
+__global__ void __launch_bounds__(kBlock) k_adj_gsum(Dev d, AdjDev a) {
+    ADJ_GROUP
+    const SceneDev& S = d.scenes[0];
+    const float V = S.volume;
+    float3 g = make_float3(0.f, 0.f, 0.f);
+    float g2 = 0.0f;
+    Row rw{};
+    if (live) {
+        rw = row_of(d, p);
+        const float3 xi = f3(d.X[p]);
+        for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
+            const uint32_t q = __ldg(rw.nbr + j);
+            const float3 gj = (V * __ldg(rw.gs + j)) * (xi - f3(d.X[q]));
+            g += gj;
+            g2 += dot3(gj, gj);
+        }
+    }
+    g = grp.sum(g);
+    g2 = grp.sum(g2);
+    if (!live || grp.lane != 0) return;
+    if (rw.flags & kHasBoundary) g += f3(d.GB[p]);
+    g2 += dot3(g, g);
+    const float al = d.ALPHA[p];
+    const float sbar = g2 > kEps ? -a.ALBAR[p] * al * al : 0.0f;
+    a.GSUM[p] = f4(g, sbar);
+}
+
+// XBAR += rho0 V sum_j gradW_ij (rb_i + rb_j) + rb_i rho0 sum_b (W(pd) grad Vb + Vb W'(pd) grad pd)
+//       + 2 V^2 sum_j (sb_i + sb_j) H_ij gradW_ij + V sum_j H_ij (Gb_i - Gb_j) + J_GB^T Gb_i,
+// with Gb = 2 sb G.
+__global__ void __launch_bounds__(kBlock) k_adj_density(Dev d, AdjDev a) {
+    ADJ_GROUP
+    const SceneDev& S = d.scenes[0];
+    const Spline sp(d.radius);
+    const float V = S.volume;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    Row rw{};
+    float rbi = 0.f, sbi = 0.f;
+    float3 gbi = acc;
+    if (live) {
+        rw = row_of(d, p);
+        const float3 xi = f3(d.X[p]);
+        rbi = a.RHOBAR[p];
+        const float4 gi = a.GSUM[p];
+        sbi = gi.w;
+        gbi = (2.0f * gi.w) * f3(gi);
+        for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
+            const uint32_t q = __ldg(rw.nbr + j);
+            const float3 r = xi - f3(d.X[q]);
+            const float s = sqrtf(dot3(r, r));
+            float gs, gq;
+            sp.hess(s, gs, gq);
+            const float4 gj = a.GSUM[q];
+            const float3 gw = gs * r;
+            acc += (S.rho0 * V * (rbi + a.RHOBAR[q])) * gw;
+            acc += (2.0f * V * V * (sbi + gj.w)) * hmul(gs, gq, r, gw);
+            acc += V * hmul(gs, gq, r, gbi - (2.0f * gj.w) * f3(gj));
+        }
+    }
+    acc = grp.sum(acc);
+    if (!live || grp.lane != 0) return;
+    if (rw.flags & kHasBoundary) {
+        for (uint32_t b = 0; b < S.bodyCount; b++) {
+            const float4 b0 = bd(a, d, 0, b, p);
+            if (!(b0.w > 0.0f)) continue;
+            const float4 b1 = bd(a, d, 1, b, p), b2 = bd(a, d, 2, b, p);
+            float w1, w2;
+            sp.d12(b1.w, w1, w2);
+            acc += (rbi * S.rho0) * (sp.w(b1.w) * f3(b2) + (b0.w * w1) * f3(b1));
+        }
+        acc += jgb_t(d, a, sp, S.bodyCount, p, gbi);
+    }
+    a.XBAR[p] = f4(f3(a.XBAR[p]) + acc, 0.0f);
+}
+
+// ---------------------------------------------------------------- viscosity
+// lambda = d.CG solves A lambda = g_bar. With lt_i = (dt / rho_i) lambda_i and
+// Q_i = sum_j T_ij + B_i g_i (A g = g - (dt / rho) Q):
+//   XBAR += R(r, g_ij, cmu m (lt_i / rho_j - lt_j / rho_i)) over j, plus the boundary terms,
+//   RHOBAR += -lt_i . Q_i / rho_i + sum_j (cmu m / rho_i^2)(g_ij . r) phi (lt_j . r),
+//   SC[0] += lambda_i . Q_i / rho_i, SC[2] += rho0 lt_i . dQ_i/d mu, SC[3] += rho0 lt_i . dQ_i/d mu_b,
+// where T_ij = cmu (m / rho_j)(g_ij . r) phi(|r|) r, phi = gs / (|r|^2 + eps2) and
+// R(r, g, w) = phi ((r . w) g + (g . r) w) + (g . r)(r . w)(phi' / |r|) r.
+__global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const float4* __restrict__ G, float dt) {
+    ADJ_GROUP
+    const SceneDev& S = d.scenes[0];
+    const Spline sp(d.radius);
+    const float eps2 = 0.01f * S.h2;
+    const float cmu = 10.0f * S.dynVisc;
+    const float m = S.mass;
+    float3 xacc = make_float3(0.f, 0.f, 0.f), q1 = xacc, qf = xacc;
+    float racc = 0.f;
+    Row rw{};
+    float rhoi = 1.f;
+    float3 xi = xacc, gi = xacc, lti = xacc, li = xacc;
+    if (live) {
+        rw = row_of(d, p);
+        xi = f3(d.X[p]);
+        gi = f3(G[p]);
+        rhoi = d.RHO[p];
+        li = f3(d.CG[p]);
+        lti = (dt / rhoi) * li;
+        for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
+            const uint32_t q = __ldg(rw.nbr + j);
+            const float gsT = __ldg(rw.gs + j);
+            const float3 r = xi - f3(d.X[q]);
+            const float s2 = dot3(r, r);
+            const float s = sqrtf(s2);
+            float gs, gq;
+            sp.hess(s, gs, gq);
+            const float rhoq = d.RHO[q];
+            const float3 ltq = (dt / rhoq) * f3(d.CG[q]);
+            const float3 g = gi - f3(G[q]);
+            const float gr = dot3(g, r);
+            const float den = s2 + eps2;
+            const float phiT = gsT / den;
+            // values (table gradient, as the forward)
+            const float3 t1 = (10.0f * (m / rhoq) * gr * phiT) * r;
+            q1 += t1;
+            qf += S.dynVisc * t1;
+            racc += (cmu * m / (rhoi * rhoi)) * gr * phiT * dot3(ltq, r);
+            // position derivative (analytic spline)
+            const float phi = gs / den;
+            const float phis = gq / den - 2.0f * gs / (den * den);
+            const float3 w = (cmu * m) * ((1.0f / rhoq) * lti - (1.0f / rhoi) * ltq);
+            const float rw_ = dot3(r, w);
+            xacc += phi * (rw_ * g + gr * w) + (gr * rw_ * phis) * r;
+        }
+    }
+    xacc = grp.sum(xacc);
+    q1 = grp.sum(q1);
+    qf = grp.sum(qf);
+    racc = grp.sum(racc);
+    double s0 = 0.0, s2v = 0.0, s3v = 0.0;
+    if (live && grp.lane == 0) {
+        float3 b1 = make_float3(0.f, 0.f, 0.f);  // B g per unit dynamic boundary viscosity
+        if (S.dynBVisc != 0.0f && (rw.flags & kHasBoundary)) {
+            for (uint32_t b = 0; b < S.bodyCount; b++) {
+                const float4 b0 = bd(a, d, 0, b, p);
+                if (!(b0.w > 0.0f)) continue;
+                const float4 bp = bd(a, d, 1, b, p), bv = bd(a, d, 2, b, p);
+                const float3 n = f3(b0);
+                const float pd = bp.w;
+                float3 t1, t2;
+                orthogonal_vectors(-n, t1, t2);
+                const float td = S.tangDist;
+                const float3 off[4] = {-td * t1, td * t1, -td * t2, td * t2};
+                const float c1 = 10.0f * 0.25f * b0.w;  // per unit dynamic boundary viscosity
+                float dpd = 0.0f, dvb = 0.0f;
+                for (int k = 0; k < 4; k++) {
+                    const float3 dk = pd * n - off[k];
+                    const float s2 = dot3(dk, dk);
+                    const float s = sqrtf(s2);
+                    const float den = s2 + eps2;
+                    const float3 gk = kernel_grad(d, dk);
+                    const float dg = dot3(dk, gi), dl = dot3(dk, lti);
+                    // value: c (d . g) gradW(d)
+                    b1 += (c1 * dg / den) * gk;
+                    dvb += S.dynBVisc * c1 * dg / den * dot3(gk, lti);
+                    float gs, gq;
+                    sp.hess(s, gs, gq);
+                    const float C = S.dynBVisc * c1;
+                    const float beta = C * gs / den;
+                    const float betas = C * (gq / den - 2.0f * gs / (den * den));
+                    dpd += betas * dot3(dk, n) * dg * dl + beta * (dot3(n, gi) * dl + dg * dot3(n, lti));
+                }
+                xacc += dpd * f3(bp) + (dvb / b0.w) * f3(bv);
+            }
+        }
+        const float3 Q = qf + S.dynBVisc * b1;
+        racc += -dot3(lti, Q) / rhoi;
+        a.XBAR[p] = f4(f3(a.XBAR[p]) + xacc, 0.0f);
+        a.RHOBAR[p] += racc;
+        s0 = dot3d(li, Q) / (double)rhoi;
+        s2v = (double)S.rho0 * dot3d(lti, q1);
+        s3v = (double)S.rho0 * dot3d(lti, b1);
+    }
+    block_add(a.SC + 0, s0);
+    block_add(a.SC + 2, s2v);
+    block_add(a.SC + 3, s3v);
+}
+
+// ---------------------------------------------------------------- element-wise steps
+__global__ void k_adj_load(Dev d, AdjDev a, const uint32_t* pid) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    const uint32_t o = pid[p];
+    a.XBAR[p] = a.XBO[o];
+    a.VBAR[p] = a.VBO[o];
+    a.RHOBAR[p] = 0.f;
+    a.ALBAR[p] = 0.f;
+}
+
+// The boundary's velocity reset, then back to original order.
+__global__ void k_adj_store(Dev d, AdjDev a, const uint32_t* pid) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    const uint32_t o = pid[p];
+    a.XBO[o] = a.XBAR[p];
+    a.VBO[o] = a.STOP[p] ? make_float4(0.f, 0.f, 0.f, 0.f) : a.VBAR[p];
+}
+
+// x' = x + dt_n v3, v3 = v2 + dt_n a_p (K20 + K21): v3 bar, dt_n bar; ABAR = dt_n v3 bar.
+__global__ void k_adj_pres_out(Dev d, AdjDev a, const float4* V2, float dtn) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (p < d.n) {
+        const float3 ap = f3(a.AK[p]);
+        const float3 v3 = f3(V2[p]) + dtn * ap;
+        const float3 xb = f3(a.XBAR[p]);
+        const float3 vb = f3(a.VBAR[p]) + dtn * xb;
+        acc = dot3d(v3, xb) + dot3d(ap, vb);
+        a.VBAR[p] = f4(vb, 0.f);
+        a.ABAR[p] = f4(dtn * vb, 0.f);
+        a.KBAR[p] = 0.f;
+        a.RABAR[p] = 0.f;
+        a.APBAR[p] = 0.f;
+    }
+    block_add(a.SC + 1, acc);
+}
+
+// v1 = v0 + dt_o a_d (K7): dt_o bar; ABAR = dt_o v1 bar.
+__global__ void k_adj_div_out(Dev d, AdjDev a, float dto) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (p < d.n) {
+        const float3 vb = f3(a.VBAR[p]);
+        acc = dot3d(f3(a.AK[p]), vb);
+        a.ABAR[p] = f4(dto * vb, 0.f);
+        a.KBAR[p] = 0.f;
+        a.RABAR[p] = 0.f;
+        a.APBAR[p] = 0.f;
+    }
+    block_add(a.SC + 0, acc);
+}
+
+// One Jacobi update k <- k - r alpha', r = min(c0 - rho_adv - f, 0) (c0 = 0 divergence,
+// 1 pressure; r = 0 where skipped): U = [r < 0] alpha' k_bar; rho_adv bar += U,
+// alpha' bar += -r k_bar; f = scale * D(P(k)) gives SC[slot] += fdt * U f.
+template <bool DIV>
+__global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, float alphaScale, float fdt) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (p < d.n) {
+        const float r = res[p];
+        const float kb = a.KBAR[p];
+        const float u = r < 0.0f ? d.ALPHA[p] * alphaScale * kb : 0.0f;
+        a.U[p] = u;
+        a.RABAR[p] += u;
+        a.APBAR[p] += -r * kb;
+        if (u != 0.0f) {
+            const float f = (DIV ? 0.0f : 1.0f) - rhoadv[p] - r;
+            acc = (double)fdt * (double)u * (double)f;
+        }
+    }
+    block_add(a.SC + (DIV ? 0 : 1), acc);
+}
+
+// Pressure solve start (K17): k0 = max(rho_adv - 1, 0) alpha'', rho_adv = rho / rho0 + dt_n D(v2),
+// alpha'' = alpha / dt_n^2.
+__global__ void k_adj_pres_init(Dev d, AdjDev a, const float* rhoadv, float dtn) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (p < d.n) {
+        const SceneDev& S = d.scenes[0];
+        const float ra = rhoadv[p];
+        const float al = d.ALPHA[p];
+        const float a2 = al / (dtn * dtn);
+        const float kb = a.KBAR[p];
+        const float rab = a.RABAR[p] + (ra > 1.0f ? a2 * kb : 0.0f);
+        const float apb = a.APBAR[p] + fmaxf(ra - 1.0f, 0.0f) * kb;
+        a.RABAR[p] = rab;
+        a.RHOBAR[p] += rab / S.rho0;
+        a.DBAR[p] = dtn * rab;
+        a.ALBAR[p] += apb / (dtn * dtn);
+        acc = -2.0 * (double)apb * (double)al / ((double)dtn * dtn * dtn);
+    }
+    block_add(a.SC + 1, acc);
+}
+
+// Divergence solve start (K4): k0 = rho_adv alpha', rho_adv = [n >= 20] max(D(v0), 0),
+// alpha' = alpha / dt_o.
+__global__ void k_adj_div_init(Dev d, AdjDev a, const float* rhoadv, float dto) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (p < d.n) {
+        const float ra = rhoadv[p];
+        const float al = d.ALPHA[p];
+        const float kb = a.KBAR[p];
+        const float rab = a.RABAR[p] + al / dto * kb;
+        const float apb = a.APBAR[p] + ra * kb;
+        const bool counted = (d.NCNT[p] & kCountMask) >= 20u;
+        a.DBAR[p] = (counted && ra > 0.0f) ? rab : 0.0f;
+        a.ALBAR[p] += apb / dto;
+        acc = -(double)apb * (double)al / ((double)dto * dto);
+    }
+    block_add(a.SC + 0, acc);
+}
+
+// v2 = v1 + dt_n a with a = gravity (+ (g - v1) / dt_o with viscosity; g = 0 when the CG
+// right-hand side was zero). mode: 0 no viscosity, 1 viscosity, 2 viscosity with g = 0.
+__global__ void k_adj_velocity(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, float dtn, int mode) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    double sn = 0.0, so = 0.0;
+    if (p < d.n) {
+        const SceneDev& S = d.scenes[0];
+        const float3 grav = make_float3(S.g[0], S.g[1], S.g[2]);
+        const float3 vb = f3(a.VBAR[p]);
+        if (mode == 0) {
+            sn = dot3d(vb, grav);
+            a.GBAR[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            const float3 v1 = f3(V1[p]);
+            const float3 g = mode == 1 ? f3(G[p]) : make_float3(0.f, 0.f, 0.f);
+            const float3 dg = g - v1;
+            sn = dot3d(vb, grav + (1.0f / dto) * dg);
+            so = -(double)(dtn / (dto * dto)) * dot3d(vb, dg);
+            a.GBAR[p] = mode == 1 ? f4((dtn / dto) * vb, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+            a.VBAR[p] = f4((1.0f - dtn / dto) * vb, 0.f);
+        }
+    }
+    block_add(a.SC + 1, sn);
+    block_add(a.SC + 0, so);
+}
+
+// CFL (k_visc_finish + k_ctrl_dt): dt_n = 0.4 d / sqrt(|w*|^2) for the particle with the
+// largest |w|^2 = |v1 + a dt_o|^2; d dt_n / d w = -dt_n w / |w|^2. The first kernel finds
+// the largest recomputed |w|^2, the second gives its particle the derivative.
+__device__ __forceinline__ float3 cfl_w(const Dev& d, const float4* V1, const float4* G, uint32_t p, float dto,
+                                        int mode) {
+    const SceneDev& S = d.scenes[0];
+    const float3 v1 = f3(V1[p]);
+    float3 acc = make_float3(S.g[0], S.g[1], S.g[2]);
+    if (mode != 0) {
+        const float3 g = mode == 1 ? f3(G[p]) : make_float3(0.f, 0.f, 0.f);
+        acc += 1.0f / dto * (g - v1);
+    }
+    return v1 + acc * dto;
+}
+__global__ void k_adj_cfl_max(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, int mode) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    const float3 w = cfl_w(d, V1, G, p, dto, mode);
+    atomicMax(a.CLAIM, __float_as_uint(dot3(w, w)));
+}
+__global__ void k_adj_cfl(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, float dtn, float maxV2,
+                          int mode) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    const float3 w = cfl_w(d, V1, G, p, dto, mode);
+    if (__float_as_uint(dot3(w, w)) != a.CLAIM[0]) return;
+    if (atomicExch(a.CLAIM + 1, 1u) != 0u) return;
+    const SceneDev& S = d.scenes[0];
+    const float3 grav = make_float3(S.g[0], S.g[1], S.g[2]);
+    const float dtnb = (float)a.SC[1];
+    const float3 wb = (-dtnb * dtn / maxV2) * w;
+    atomicAdd(a.SC + 0, dot3d(wb, grav));
+    if (mode == 1) a.GBAR[p] = f4(f3(a.GBAR[p]) + wb, 0.f);
+    else if (mode == 0) a.VBAR[p] = f4(f3(a.VBAR[p]) + wb, 0.f);
+}
+
+__global__ void k_adj_add_lambda(Dev d, AdjDev a) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    a.VBAR[p] = f4(f3(a.VBAR[p]) + f3(d.CG[p]), 0.f);
+}
+
+// dt_o of this step is dt_n of the step before.
+__global__ void k_adj_carry(AdjDev a) {
+    a.SC[1] = a.SC[0];
+    a.SC[0] = 0.0;
+    a.CLAIM[0] = 0u;
+    a.CLAIM[1] = 0u;
+}
+
+// ---------------------------------------------------------------- host side
+#define ADJ_LAUNCH(kernel, grid, ...) kernel<<<(grid), kBlock, 0, st>>>(__VA_ARGS__)
+
+struct StepMeta {
+    SceneDev pre;          // scene state before the step (dt of the divergence and viscosity solves)
+    float dto, dtn, maxV2;
+    bool cfl;              // dt_n came from an unclamped CFL maximum above the 0.1 floor
+    bool div, visc, zeroG;
+};
+
+struct StepTape {
+    float4 *Xpre = nullptr, *V0 = nullptr, *V1 = nullptr, *G = nullptr, *V2 = nullptr;
+    uint32_t *PID = nullptr, *NCNT = nullptr, *NBR = nullptr;
+    float *RAD = nullptr, *RAP = nullptr;
+    std::vector<float*> KD, RD, KP, RP;  // kappa^0..K, res^0..K-1 of each solve
+    StepMeta meta{};
+};
+
+struct Checkpoint {
+    float4 *XN = nullptr, *V = nullptr, *DV = nullptr;
+    float* DK = nullptr;
+    uint32_t* PID = nullptr;
+    std::vector<SceneDev> scenes;
+    uint32_t status[16] = {};
+    int cs = 0;
+};
+
+}  // namespace
+
+struct AdjointState {
+    uint32_t steps = 0, every = 0, n = 0, stride = 0;
+    uint64_t generation = 0;
+    std::vector<Checkpoint> ckpt;  // ckpt[k]: before step k * every; back(): after the last step
+    std::vector<StepTape> tapes;   // one segment
+    std::vector<float*> pool;      // free iterate arrays
+    std::vector<void*> allocs;
+    AdjDev a{};
+    ~AdjointState() {
+        for (void* p : allocs) cudaFree(p);
+    }
+};
+
+namespace {
+
+using namespace vfd::host;
+
+template <class T>
+int aalloc(AdjointState* A, T** p, size_t count) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+    const cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(VFD_E_NOMEM, "adjoint: cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    A->allocs.push_back(q);
+    *p = (T*)q;
+    return VFD_OK;
+}
+
+int take_array(AdjointState* A, float** out) {
+    if (!A->pool.empty()) {
+        *out = A->pool.back();
+        A->pool.pop_back();
+        return VFD_OK;
+    }
+    return aalloc(A, out, A->stride);
+}
+
+void recycle(AdjointState* A, StepTape& t) {
+    for (auto* v : {&t.KD, &t.RD, &t.KP, &t.RP}) {
+        for (float* f : *v) A->pool.push_back(f);
+        v->clear();
+    }
+}
+
+int save_checkpoint(vfd_sim* s, AdjointState* A, Checkpoint& c) {
+    const size_t st = s->stride;
+    if (!c.XN) {
+        TRY(aalloc(A, &c.XN, st));
+        TRY(aalloc(A, &c.V, st));
+        TRY(aalloc(A, &c.DV, st));
+        TRY(aalloc(A, &c.DK, st));
+        TRY(aalloc(A, &c.PID, st));
+    }
+    const Dev& d = s->dev[s->cs];
+    cudaStream_t st_ = s->stream;
+    CK(cudaMemcpyAsync(c.XN, d.XN, sizeof(float4) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(c.V, d.Vc, sizeof(float4) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(c.DV, d.DVc, sizeof(float4) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(c.DK, d.DKc, sizeof(float) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(c.PID, d.PIDc, sizeof(uint32_t) * st, cudaMemcpyDeviceToDevice, st_));
+    c.scenes.resize(s->hScenes.size());
+    CK(cudaMemcpyAsync(c.scenes.data(), s->dScenes, sizeof(SceneDev) * c.scenes.size(), cudaMemcpyDeviceToHost, st_));
+    CK(cudaMemcpyAsync(c.status, s->dStatus, sizeof(c.status), cudaMemcpyDeviceToHost, st_));
+    CK(cudaStreamSynchronize(st_));
+    c.cs = s->cs;
+    return VFD_OK;
+}
+
+int restore_checkpoint(vfd_sim* s, const Checkpoint& c) {
+    const size_t st = s->stride;
+    s->cs = c.cs;
+    const Dev& d = s->dev[s->cs];
+    cudaStream_t st_ = s->stream;
+    CK(cudaMemcpyAsync(d.XN, c.XN, sizeof(float4) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(d.Vc, c.V, sizeof(float4) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(d.DVc, c.DV, sizeof(float4) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(d.DKc, c.DK, sizeof(float) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(d.PIDc, c.PID, sizeof(uint32_t) * st, cudaMemcpyDeviceToDevice, st_));
+    CK(cudaMemcpyAsync(s->dScenes, c.scenes.data(), sizeof(SceneDev) * c.scenes.size(), cudaMemcpyHostToDevice, st_));
+    CK(cudaMemcpyAsync(s->dStatus, c.status, sizeof(c.status), cudaMemcpyHostToDevice, st_));
+    CK(cudaStreamSynchronize(st_));
+    s->hScenes = c.scenes;
+    return VFD_OK;
+}
+
+int read_scene(vfd_sim* s, SceneDev& S) {
+    CK(cudaMemcpyAsync(&S, s->dScenes, sizeof(SceneDev), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return VFD_OK;
+}
+
+#define COPY(dst, src, bytes) CK(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st))
+
+// One eagerly launched step (the kernels of launch_eager) that records the tape.
+int record_step(vfd_sim* s, AdjointState* A, StepTape& t) {
+    const size_t n4 = sizeof(float4) * s->stride, n1 = sizeof(float) * s->stride;
+    cudaStream_t st = s->stream;
+    if (!t.Xpre) {
+        TRY(aalloc(A, &t.Xpre, s->stride));
+        TRY(aalloc(A, &t.V0, s->stride));
+        TRY(aalloc(A, &t.V1, s->stride));
+        TRY(aalloc(A, &t.G, s->stride));
+        TRY(aalloc(A, &t.V2, s->stride));
+        TRY(aalloc(A, &t.PID, s->stride));
+        TRY(aalloc(A, &t.NCNT, s->stride));
+        TRY(aalloc(A, &t.NBR, (size_t)s->stride * kRow));
+        TRY(aalloc(A, &t.RAD, s->stride));
+        TRY(aalloc(A, &t.RAP, s->stride));
+    }
+    recycle(A, t);
+    TRY(read_scene(s, t.meta.pre));
+    const Dev& d = s->dev[s->cs];
+    uint32_t more = 0;
+    launch_search(d, st);
+    COPY(t.Xpre, d.X, n4);
+    COPY(t.PID, d.PID, sizeof(uint32_t) * s->stride);
+    COPY(t.NCNT, d.NCNT, sizeof(uint32_t) * s->stride);
+    COPY(t.NBR, d.NBR, sizeof(uint32_t) * s->stride * kRow);
+    launch_boundary(d, st);
+    COPY(t.V0, d.V, n4);
+    launch_density(d, st);
+    launch_div_init(d, st);
+    t.meta.div = s->anyDiv;
+    if (s->anyDiv) {
+        float* k0;
+        TRY(take_array(A, &k0));
+        COPY(k0, d.KAPPAV, n1);
+        t.KD.push_back(k0);
+        COPY(t.RAD, d.RHOADV, n1);
+        TRY(read_flag(s, 4, more));
+        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
+            launch_div_iter(d, st);
+            float *r, *k;
+            TRY(take_array(A, &r));
+            TRY(take_array(A, &k));
+            COPY(r, d.RES, n1);
+            COPY(k, d.KAPPAV, n1);
+            t.RD.push_back(r);
+            t.KD.push_back(k);
+            TRY(read_flag(s, 4, more));
+        }
+    }
+    launch_div_finish(d, st);
+    COPY(t.V1, d.V, n4);
+    t.meta.visc = s->anyVisc;
+    if (s->anyVisc) {
+        launch_visc_init(d, st);
+        TRY(read_flag(s, 5, more));
+        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
+            launch_cg_iter(d, st);
+            TRY(read_flag(s, 5, more));
+        }
+        COPY(t.G, d.CG, n4);
+    }
+    launch_visc_finish_dt(d, st);
+    COPY(t.V2, d.V, n4);
+    launch_pres_init(d, st);
+    {
+        float* k0;
+        TRY(take_array(A, &k0));
+        COPY(k0, d.KAPPA, n1);
+        t.KP.push_back(k0);
+        COPY(t.RAP, d.RHOADV, n1);
+    }
+    TRY(read_flag(s, 6, more));
+    for (uint32_t guard = 0; more && guard < 100000u; guard++) {
+        launch_pres_iter(d, st);
+        float *r, *k;
+        TRY(take_array(A, &r));
+        TRY(take_array(A, &k));
+        COPY(r, d.RES, n1);
+        COPY(k, d.KAPPA, n1);
+        t.RP.push_back(r);
+        t.KP.push_back(k);
+        TRY(read_flag(s, 6, more));
+    }
+    launch_pres_finish(d, st);
+    CK(cudaGetLastError());
+    SceneDev post;
+    TRY(read_scene(s, post));
+    CK(cudaMemcpyAsync(s->hStatus, s->dStatus, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (s->hStatus[1]) return fail(VFD_E_STATE, "adjoint: a recomputed step aborted (grid or non-finite position)");
+    if (post.maxNbr >= kMaxNeighbors)
+        return fail(VFD_E_CAPACITY, "adjoint: a particle reached the %u-neighbour cap (neighbour sets must be symmetric)",
+                    kMaxNeighbors);
+    t.meta.dto = t.meta.pre.dt;
+    t.meta.dtn = post.dt;
+    t.meta.maxV2 = post.maxV2;
+    t.meta.zeroG = s->anyVisc && post.cgZeroG;
+    const float raw = 0.4f * (post.diam / sqrtf(post.maxV2));
+    t.meta.cfl = post.maxV2 > 0.1f && raw == post.dt;
+    s->cs = 1 - s->cs;
+    return VFD_OK;
+}
+
+// Backward pass of one recorded step; A->a.XBO / VBO hold the cotangents of its
+// outputs on entry and of its inputs on return.
+int backward_step(vfd_sim* s, AdjointState* A, const StepTape& t) {
+    cudaStream_t st = s->stream;
+    const Dev& d = s->dev[0];
+    AdjDev& a = A->a;
+    const StepMeta& M = t.meta;
+    const uint32_t n = s->n;
+    const uint32_t g1 = blocks_for(n), gG = blocks_for(n * kAG);
+    // the forward arrays of this step
+    CK(cudaMemcpyAsync(s->dScenes, &M.pre, sizeof(SceneDev), cudaMemcpyHostToDevice, st));
+    COPY(d.X, t.Xpre, sizeof(float4) * s->stride);
+    COPY(d.NCNT, t.NCNT, sizeof(uint32_t) * s->stride);
+    COPY(d.NBR, t.NBR, sizeof(uint32_t) * s->stride * kRow);
+    CK(cudaMemsetAsync(s->dStatus, 0, 16 * sizeof(uint32_t), st));
+    ADJ_LAUNCH(k_adj_bdata, g1, d, a);
+    launch_boundary(d, st);
+    launch_density(d, st);
+    ADJ_LAUNCH(k_adj_load, g1, d, a, t.PID);
+
+    // pressure solve, K20 + K21 (v3 and x')
+    const float dtn = M.dtn, dto = M.dto;
+    const uint32_t kp = (uint32_t)t.RP.size();
+    ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, t.KP[kp], 0.0f);
+    ADJ_LAUNCH(k_adj_pres_out, g1, d, a, t.V2, dtn);
+    ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, t.KP[kp], 0.0f);
+    for (uint32_t k = kp; k-- > 0;) {
+        ADJ_LAUNCH(k_adj_u<false>, g1, d, a, t.RP[k], t.RAP, 1.0f / (dtn * dtn), 2.0f / dtn);
+        ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, t.KP[k], dtn * dtn);
+        ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, t.KP[k], dtn * dtn);
+    }
+    ADJ_LAUNCH(k_adj_pres_init, g1, d, a, t.RAP, dtn);
+    ADJ_LAUNCH(k_adj_div_b<true>, gG, d, a, t.V2);
+
+    // K16 velocity update and the CFL time step
+    const int mode = !M.visc ? 0 : (M.zeroG ? 2 : 1);
+    ADJ_LAUNCH(k_adj_velocity, g1, d, a, t.V1, t.G, dto, dtn, mode);
+    if (M.cfl) {
+        ADJ_LAUNCH(k_adj_cfl_max, g1, d, a, t.V1, t.G, dto, mode);
+        ADJ_LAUNCH(k_adj_cfl, g1, d, a, t.V1, t.G, dto, dtn, M.maxV2, mode);
+    }
+
+    // viscosity: A lambda = g_bar with the forward's CG, then the derivative of A g = v1
+    if (mode == 1) {
+        COPY(d.V, a.GBAR, sizeof(float4) * s->stride);
+        CK(cudaMemsetAsync(d.DV, 0, sizeof(float4) * s->stride, st));
+        uint32_t more = 0;
+        launch_visc_init(d, st);
+        TRY(read_flag(s, 5, more));
+        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
+            launch_cg_iter(d, st);
+            TRY(read_flag(s, 5, more));
+        }
+        SceneDev sc;
+        TRY(read_scene(s, sc));
+        if (!sc.cgZeroG) {
+            ADJ_LAUNCH(k_adj_add_lambda, g1, d, a);
+            ADJ_LAUNCH(k_adj_visc, gG, d, a, t.G, dto);
+        }
+    }
+
+    // divergence solve, K4-K7
+    if (M.div) {
+        const uint32_t kd = (uint32_t)t.RD.size();
+        ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, t.KD[kd], 0.0f);
+        ADJ_LAUNCH(k_adj_div_out, g1, d, a, dto);
+        ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, t.KD[kd], 0.0f);
+        for (uint32_t k = kd; k-- > 0;) {
+            ADJ_LAUNCH(k_adj_u<true>, g1, d, a, t.RD[k], t.RAD, 1.0f / dto, 1.0f / dto);
+            ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, t.KD[k], dto);
+            ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, t.KD[k], dto);
+        }
+        ADJ_LAUNCH(k_adj_div_init, g1, d, a, t.RAD, dto);
+        ADJ_LAUNCH(k_adj_div_b<false>, gG, d, a, t.V0);
+    }
+
+    // density and factor (K2 + K3), then the boundary's velocity reset and original order
+    ADJ_LAUNCH(k_adj_gsum, gG, d, a);
+    ADJ_LAUNCH(k_adj_density, gG, d, a);
+    ADJ_LAUNCH(k_adj_store, g1, d, a, t.PID);
+    k_adj_carry<<<1, 1, 0, st>>>(a);
+    CK(cudaGetLastError());
+    return VFD_OK;
+}
+
+int check_adjoint_scene(vfd_sim* s) {
+    if (s->scenes.size() != 1) return fail(VFD_E_ARG, "adjoint: one scene per simulation");
+    if (s->scenes[0].desc.EnableSurfaceTensionSolver) return fail(VFD_E_ARG, "adjoint: surface tension is not differentiated");
+    return VFD_OK;
+}
+
+int alloc_cotangents(vfd_sim* s, AdjointState* A) {
+    const size_t st = s->stride;
+    AdjDev& a = A->a;
+    TRY(aalloc(A, &a.XBAR, st));
+    TRY(aalloc(A, &a.VBAR, st));
+    TRY(aalloc(A, &a.ABAR, st));
+    TRY(aalloc(A, &a.AK, st));
+    TRY(aalloc(A, &a.GBAR, st));
+    TRY(aalloc(A, &a.GSUM, st));
+    TRY(aalloc(A, &a.BD, 3 * st * std::max<uint32_t>(1u, s->maxBodies)));
+    TRY(aalloc(A, &a.KBAR, st));
+    TRY(aalloc(A, &a.U, st));
+    TRY(aalloc(A, &a.RABAR, st));
+    TRY(aalloc(A, &a.APBAR, st));
+    TRY(aalloc(A, &a.DBAR, st));
+    TRY(aalloc(A, &a.RHOBAR, st));
+    TRY(aalloc(A, &a.ALBAR, st));
+    TRY(aalloc(A, &a.STOP, st));
+    TRY(aalloc(A, &a.SC, 8));
+    TRY(aalloc(A, &a.CLAIM, 2));
+    TRY(aalloc(A, &a.XBO, st));
+    TRY(aalloc(A, &a.VBO, st));
+    return VFD_OK;
+}
+
+__global__ void k_adj_pack(float4* dst, const float* src, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = make_float4(src[3 * (size_t)i], src[3 * (size_t)i + 1], src[3 * (size_t)i + 2], 0.f);
+}
+__global__ void k_adj_unpack(float* dst, const float4* src, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = src[i];
+    dst[3 * (size_t)i] = v.x;
+    dst[3 * (size_t)i + 1] = v.y;
+    dst[3 * (size_t)i + 2] = v.z;
+}
+
+}  // namespace
+
+void adjoint_release(vfd_sim* s) {
+    delete s->adjoint;
+    s->adjoint = nullptr;
+}
+
+}  // namespace vfd
+
+using namespace vfd;
+using namespace vfd::host;
+
+extern "C" {
+
+int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, vfd_step_stats* stats) {
+    if (!s) return fail(VFD_E_ARG, "null handle");
+    if (steps == 0 || checkpoint_every == 0) return fail(VFD_E_ARG, "adjoint: steps and checkpoint_every must be positive");
+    TRY(check_adjoint_scene(s));
+    TRY(ensure_ready(s));
+    adjoint_release(s);
+    auto A = std::make_unique<AdjointState>();
+    A->steps = steps;
+    A->every = checkpoint_every;
+    A->n = s->n;
+    A->stride = s->stride;
+    const uint32_t segs = (steps + checkpoint_every - 1) / checkpoint_every;
+    A->ckpt.resize(segs + 1);
+    for (uint32_t k = 0; k < segs; k++) {
+        TRY(save_checkpoint(s, A.get(), A->ckpt[k]));
+        const uint32_t cnt = std::min(checkpoint_every, steps - k * checkpoint_every);
+        TRY(run_steps(s, cnt, stats, true));
+    }
+    TRY(save_checkpoint(s, A.get(), A->ckpt[segs]));
+    A->generation = s->generation;
+    s->adjoint = A.release();
+    return VFD_OK;
+}
+
+int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, float* x0_bar, float* v0_bar,
+                         float* param_bar) {
+    if (!s) return fail(VFD_E_ARG, "null handle");
+    AdjointState* A = s->adjoint;
+    if (!A) return fail(VFD_E_STATE, "adjoint: no recorded forward run (call vfd_adjoint_forward first)");
+    if (A->generation != s->generation || A->n != s->n)
+        return fail(VFD_E_STATE, "adjoint: the simulation was reset after the recorded forward run");
+    if (!x_bar || !v_bar) return fail(VFD_E_ARG, "adjoint: null cotangent");
+    const uint32_t n = s->n;
+    cudaStream_t st = s->stream;
+    if (!A->a.XBAR) TRY(alloc_cotangents(s, A));
+    AdjDev& a = A->a;
+    // cotangents of the final state, original order
+    CK(cudaMemcpyAsync(s->dStage, x_bar, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+    k_adj_pack<<<blocks_for(n, 256), 256, 0, st>>>(a.XBO, s->dStage, n);
+    CK(cudaMemcpyAsync(s->dStage, v_bar, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+    k_adj_pack<<<blocks_for(n, 256), 256, 0, st>>>(a.VBO, s->dStage, n);
+    CK(cudaMemsetAsync(a.SC, 0, 8 * sizeof(double), st));
+    CK(cudaMemsetAsync(a.CLAIM, 0, 2 * sizeof(uint32_t), st));
+    const uint32_t segs = (uint32_t)A->ckpt.size() - 1;
+    A->tapes.resize(A->every);
+    int rc = VFD_OK;
+    for (uint32_t k = segs; k-- > 0 && rc == VFD_OK;) {
+        rc = restore_checkpoint(s, A->ckpt[k]);
+        const uint32_t cnt = std::min(A->every, A->steps - k * A->every);
+        for (uint32_t t = 0; t < cnt && rc == VFD_OK; t++) rc = record_step(s, A, A->tapes[t]);
+        for (uint32_t t = cnt; t-- > 0 && rc == VFD_OK;) rc = backward_step(s, A, A->tapes[t]);
+    }
+    // leave the simulation where the forward run ended
+    const int rc2 = restore_checkpoint(s, A->ckpt[segs]);
+    if (rc != VFD_OK) return rc;
+    if (rc2 != VFD_OK) return rc2;
+    if (x0_bar) {
+        k_adj_unpack<<<blocks_for(n, 256), 256, 0, st>>>(s->dStage, a.XBO, n);
+        CK(cudaMemcpyAsync(x0_bar, s->dStage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (v0_bar) {
+        k_adj_unpack<<<blocks_for(n, 256), 256, 0, st>>>(s->dStage, a.VBO, n);
+        CK(cudaMemcpyAsync(v0_bar, s->dStage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (param_bar) {
+        double sc[8];
+        CK(cudaMemcpyAsync(sc, a.SC, sizeof(sc), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        param_bar[0] = (float)sc[2];
+        param_bar[1] = (float)sc[3];
+    }
+    CK(cudaGetLastError());
+    return VFD_OK;
+}
+
+int vfd_adjoint_release(vfd_sim* s) {
+    if (!s) return fail(VFD_E_ARG, "null handle");
+    adjoint_release(s);
+    return VFD_OK;
+}
+
+}  // extern "C"

@@ -384,6 +384,7 @@ int upload(vfd_sim* s) {
     TRY(reset_buckets(s, d));
     CK(cudaDeviceSynchronize());
     s->uploaded = true;
+    s->generation++;
     return VFD_OK;
 }
 

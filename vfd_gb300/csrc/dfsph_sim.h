@@ -128,6 +128,11 @@ struct SceneHost {
 }  // namespace host
 }  // namespace vfd
 
+namespace vfd {
+struct AdjointState;
+void adjoint_release(vfd_sim* s);  // frees the recorded forward run of the adjoint
+}  // namespace vfd
+
 struct vfd_sim {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -161,6 +166,11 @@ struct vfd_sim {
     cudaGraph_t graph[2] = {nullptr, nullptr};
     bool searchOnlyPending = false;
 
+    // adjoint: checkpoints and tapes of the last vfd_adjoint_forward; `generation`
+    // counts uploads, so a reset after the recorded run is detected
+    vfd::AdjointState* adjoint = nullptr;
+    uint64_t generation = 0;
+
     ~vfd_sim() { release(); }
 
     void releaseGraphs() {
@@ -181,6 +191,7 @@ struct vfd_sim {
         uploaded = false;
     }
     void release() {
+        vfd::adjoint_release(this);
         releaseBuffers();
         for (auto& s : scenes)
             for (auto& b : s.bodies) b.release();
