@@ -230,6 +230,13 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.ACCB, (size_t)base.nscenes * kAccSlots * kBuckets * 16u));
     TRY(dalloc(s, &base.MAXB, (size_t)base.nscenes * 2u * kBuckets * 32u));
     TRY(dalloc(s, &base.MMB, (size_t)base.nscenes * 6u * kBuckets * 32u));
+    base.workStride = 2u + 2u * base.nscenes;
+    TRY(dalloc(s, &base.WORK, 3 * (size_t)base.workStride));
+    {
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+        base.batchBlocks = (uint32_t)std::max(1, sms) * (2048u / kBlock);
+    }
     TRY(dalloc(s, &s->dWM, kTableRes));
     TRY(dalloc(s, &s->dGM, kTableRes));
     TRY(dalloc(s, &s->dHalton, kHaltonCount));

@@ -144,6 +144,12 @@ struct Dev {
     int32_t* MMB;              // [scene][6][kBuckets] x32: min cell xyz, max cell xyz
     unsigned long long condHandle[3];  // while-node handles (div, cg, pres); 0 = eager
     uint8_t lanes[16];                 // lanes per particle of each TunedKernel
+    // Batches: per solver loop (div, cg, pres) the controllers list the scenes still
+    // iterating, [0] particles in them, [1] their count, then prefix[nscenes] (first
+    // virtual index of each listed scene) and begin[nscenes] (its first slot); the loop
+    // kernels of a batch walk this list with a fixed grid of batchBlocks blocks.
+    uint32_t* WORK;
+    uint32_t workStride, batchBlocks;
 };
 
 // ---------------------------------------------------------------- float3 math
@@ -236,6 +242,41 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
 // accumulator; otherwise each valid thread adds its own value. Kernels running G lanes
 // per particle pass G (a block then covers blockDim.x / G particles); all threads of
 // the block must call this.
+// Core of scene_accumulate: `uniformScene` is the scene of every particle the block
+// serves, or -1 when they belong to several scenes.
+template <int K>
+__device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformScene, uint32_t sid, bool valid,
+                                                      const double (&v)[K], const int (&slot)[K]) {
+    __shared__ double sm[kBlock / 32][4];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t bucket = blockIdx.x % kBuckets;
+    if (uniformScene >= 0) {
+        double s[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            s[k] = valid ? v[k] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+        }
+        __syncthreads();
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < K; k++) sm[warp][k] = s[k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                double t = 0.0;
+                for (uint32_t w = 0; w < blockDim.x / 32u; w++) t += sm[w][k];
+                if (t != 0.0) atomicAdd(acc_bucket(d, (uint32_t)uniformScene, slot[k], bucket), t);
+            }
+        }
+    } else if (valid) {
+#pragma unroll
+        for (int k = 0; k < K; k++) atomicAdd(acc_bucket(d, sid, slot[k], bucket), v[k]);
+    }
+}
+
 template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, bool valid, const double (&v)[K],
                                                  const int (&slot)[K]) {
@@ -310,6 +351,12 @@ struct Group {
         lane = t % G;
         mask = G == 32u ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(G - 1u)));
     }
+    // The group of this thread serving particle slot `slot` (batch work lists).
+    __device__ __forceinline__ explicit Group(uint32_t slot) {
+        p = slot;
+        lane = threadIdx.x % G;
+        mask = G == 32u ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(G - 1u)));
+    }
     __device__ __forceinline__ float sum(float v) const {
 #pragma unroll
         for (uint32_t o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
@@ -322,6 +369,27 @@ struct Group {
         return v;
     }
 };
+
+// ------------------------------------------------------------ batch work lists
+__device__ __forceinline__ const uint32_t* work_list(const Dev& d, int loop) { return d.WORK + (size_t)loop * d.workStride; }
+__device__ __forceinline__ uint32_t work_total(const Dev& d, int loop) { return __ldg(work_list(d, loop)); }
+// Slot of virtual index vp (< total) of a loop's work list: the listed scene whose
+// prefix is the largest one <= vp, found by binary search.
+__device__ __forceinline__ uint32_t work_slot(const Dev& d, int loop, uint32_t vp, uint32_t& scene) {
+    const uint32_t* w = work_list(d, loop);
+    const uint32_t na = __ldg(w + 1);
+    const uint32_t* pre = w + 2;
+    const uint32_t* beg = w + 2 + d.nscenes;
+    uint32_t lo = 0, hi = na - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (__ldg(pre + mid) <= vp) lo = mid;
+        else hi = mid - 1u;
+    }
+    const uint32_t p = __ldg(beg + lo) + (vp - __ldg(pre + lo));
+    scene = scene_of(d, p);
+    return p;
+}
 
 // Host-side launch helpers.
 inline uint32_t blocks_for(uint32_t n, uint32_t block = kBlock) { return (n + block - 1) / block; }
@@ -343,6 +411,16 @@ extern LaunchProfiler* g_profiler;
 
 // Launch of a neighbour-loop kernel with the tuned lanes per particle; KERNEL(G) names
 // the instantiation (a function-like macro).
+// The same for a batch loop kernel: a fixed grid of d.batchBlocks blocks.
+#define VFD_LAUNCH_LANES_BATCH(name, id, KERNEL)                                                     \
+    do {                                                                                            \
+        switch (d.lanes[id]) {                                                                      \
+            case 4: VFD_LAUNCH(name, s, KERNEL(4)<<<d.batchBlocks, kBlock, 0, s>>>(d)); break;      \
+            case 16: VFD_LAUNCH(name, s, KERNEL(16)<<<d.batchBlocks, kBlock, 0, s>>>(d)); break;    \
+            default: VFD_LAUNCH(name, s, KERNEL(8)<<<d.batchBlocks, kBlock, 0, s>>>(d)); break;     \
+        }                                                                                           \
+    } while (0)
+
 #define VFD_LAUNCH_LANES(name, id, KERNEL)                                                          \
     do {                                                                                            \
         switch (d.lanes[id]) {                                                                      \

@@ -33,6 +33,66 @@ __device__ __forceinline__ void set_condition(const Dev& d, int loop, uint32_t v
     d.status[4 + loop] = value;
 }
 
+// Batches: lists the scenes for which active(s) holds into loop `loop`'s work list
+// (prefix sums of their particle counts by a block-wide scan). One block of 256 threads,
+// called by all of them after the scenes' flags are final.
+template <class F>
+__device__ void build_work_list(const Dev& d, int loop, F active) {
+    __shared__ uint32_t scanP[256], scanA[256];
+    __shared__ uint32_t runP, runA;
+    uint32_t* w = d.WORK + (size_t)loop * d.workStride;
+    uint32_t* pre = w + 2;
+    uint32_t* beg = w + 2 + d.nscenes;
+    if (threadIdx.x == 0) runP = runA = 0u;
+    __syncthreads();
+    for (uint32_t c = 0; c < d.nscenes; c += blockDim.x) {
+        const uint32_t sc = c + threadIdx.x;
+        const bool a = sc < d.nscenes && active(sc);
+        const uint32_t cnt = a ? d.scenes[sc].count : 0u;
+        scanP[threadIdx.x] = cnt;
+        scanA[threadIdx.x] = a ? 1u : 0u;
+        __syncthreads();
+        for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+            const uint32_t tp = threadIdx.x >= off ? scanP[threadIdx.x - off] : 0u;
+            const uint32_t ta = threadIdx.x >= off ? scanA[threadIdx.x - off] : 0u;
+            __syncthreads();
+            scanP[threadIdx.x] += tp;
+            scanA[threadIdx.x] += ta;
+            __syncthreads();
+        }
+        if (a) {
+            const uint32_t idx = runA + scanA[threadIdx.x] - 1u;
+            pre[idx] = runP + scanP[threadIdx.x] - cnt;
+            beg[idx] = d.scenes[sc].begin;
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1u) {
+            runP += scanP[threadIdx.x];
+            runA += scanA[threadIdx.x];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        w[0] = runP;
+        w[1] = runA;
+    }
+}
+
+// Grid-stride walk of a batch loop's work list: base_ is the first virtual index of the
+// block's current chunk of per_ particles (blockDim.x / G of them).
+#define BATCH_LOOP(LOOP, G)                                  \
+    const uint32_t per_ = blockDim.x / (G);                  \
+    const uint32_t total_ = work_total(d, (LOOP));           \
+    for (uint32_t base_ = blockIdx.x * per_; base_ < total_; base_ += gridDim.x * per_)
+
+// Scene of the whole chunk, or -1 when it spans several.
+__device__ __forceinline__ int chunk_scene(const Dev& d, int loop, uint32_t base, uint32_t per, uint32_t total) {
+    uint32_t s0, s1;
+    work_slot(d, loop, base, s0);
+    work_slot(d, loop, min(base + per, total) - 1u, s1);
+    return s0 == s1 ? (int)s0 : -1;
+}
+
 struct Nbr {
     const uint32_t* row;
     const float* gs;
@@ -220,8 +280,62 @@ __global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
     if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
 }
 
+// K5 / K18 of a batch: the scenes still iterating, from the loop's work list.
+template <bool DIV, uint32_t G>
+__global__ void __launch_bounds__(kBlock) k_pressure_accel_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    const int L = DIV ? kLoopDiv : kLoopPres;
+    BATCH_LOOP(L, G) {
+        const uint32_t vp = base_ + threadIdx.x / G;
+        if (vp >= total_) continue;
+        uint32_t sid;
+        const uint32_t p = work_slot(d, L, vp, sid);
+        const Group<G> grp(p);
+        const Nbr nb = neighbors(d, p);
+        const float3 a = pressure_accel<DIV, G>(d, grp, p, d.scenes[sid], nb);
+        if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
+    }
+}
+
 // K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
 // each with ComputeDensityPressureForce (:280-315) and the FP64 residual sum.
+template <bool DIV, uint32_t G>
+__device__ __forceinline__ double jacobi_item(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S) {
+    double res = 0.0;
+    const Nbr nb = neighbors(d, p);
+    const float3 xi = f3(d.X[p]);
+    const float3 ai = f3(d.AP[p]);
+    float f = 0.0f;
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
+        const float3 r = xi - f3(d.X[q]);
+        const float3 aq = f3(d.AP[q]);
+        const float t = dot3(ai - aq, gs * r);
+        if (ok) f += t;
+    });
+    f = grp.sum(f) * S.volume;
+    if (grp.lane == 0) {
+        if (nb.flags & kHasBoundary) f += dot3(ai, f3(d.GB[p]));
+        float r;
+        if (DIV) {
+            f *= S.dt;
+            r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
+            const float k = d.KAPPAV[p] - r * d.ALPHA[p];
+            d.KAPPAV[p] = k;
+            set_kappa(d, p, k);
+        } else {
+            f *= S.dt2;
+            r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
+            const float k = d.KAPPA[p] - r * d.ALPHA[p];
+            d.KAPPA[p] = k;
+            set_kappa(d, p, k);
+        }
+        d.RES[p] = r;
+        res = (double)r;
+    }
+    return res;
+}
+
 template <bool DIV, uint32_t G>
 __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
     VFD_COUNT_LAUNCH(d);
@@ -232,41 +346,32 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
     const SceneDev& S = d.scenes[sid];
     const bool active = inRange && (DIV ? S.div.active : S.pres.active);
     double res = 0.0;
-    if (active) {
-        const Nbr nb = neighbors(d, p);
-        const float3 xi = f3(d.X[p]);
-        const float3 ai = f3(d.AP[p]);
-        float f = 0.0f;
-        for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
-            const float3 r = xi - f3(d.X[q]);
-            const float3 aq = f3(d.AP[q]);
-            const float t = dot3(ai - aq, gs * r);
-            if (ok) f += t;
-        });
-        f = grp.sum(f) * S.volume;
-        if (grp.lane == 0) {
-            if (nb.flags & kHasBoundary) f += dot3(ai, f3(d.GB[p]));
-            float r;
-            if (DIV) {
-                f *= S.dt;
-                r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
-                const float k = d.KAPPAV[p] - r * d.ALPHA[p];
-                d.KAPPAV[p] = k;
-                set_kappa(d, p, k);
-            } else {
-                f *= S.dt2;
-                r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
-                const float k = d.KAPPA[p] - r * d.ALPHA[p];
-                d.KAPPA[p] = k;
-                set_kappa(d, p, k);
-            }
-            d.RES[p] = r;
-            res = (double)r;
-        }
-    }
+    if (active) res = jacobi_item<DIV, G>(d, grp, p, S);
     const double v[1] = {res};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
+}
+
+// The same for a batch (work list of the loop).
+template <bool DIV, uint32_t G>
+__global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    const int L = DIV ? kLoopDiv : kLoopPres;
+    BATCH_LOOP(L, G) {
+        const uint32_t vp = base_ + threadIdx.x / G;
+        const bool in = vp < total_;
+        uint32_t sid = 0;
+        const uint32_t p = in ? work_slot(d, L, vp, sid) : 0u;
+        double res = 0.0;
+        if (in) {
+            const Group<G> grp(p);
+            res = jacobi_item<DIV, G>(d, grp, p, d.scenes[sid]);
+        }
+        const double v[1] = {res};
+        const int slot[1] = {0};
+        scene_accumulate_core<1>(d, chunk_scene(d, L, base_, per_, total_), sid, in && threadIdx.x % G == 0u, v, slot);
+    }
 }
 
 // Loop start: the reference's while condition evaluated with error 0, iteration 0
@@ -290,6 +395,9 @@ __global__ void k_ctrl_jacobi_init(Dev d) {
         if (L.active) atomicOr(&any, 1u);
     }
     __syncthreads();
+    if (d.nscenes > 1)
+        build_work_list(d, DIV ? kLoopDiv : kLoopPres,
+                        [&](uint32_t sc) { return (DIV ? d.scenes[sc].div.active : d.scenes[sc].pres.active) != 0u; });
     if (threadIdx.x == 0) set_condition(d, DIV ? kLoopDiv : kLoopPres, any);
 }
 
@@ -316,6 +424,9 @@ __global__ void k_ctrl_jacobi(Dev d) {
         if (again) atomicOr(&any, 1u);
     }
     __syncthreads();
+    if (d.nscenes > 1)
+        build_work_list(d, DIV ? kLoopDiv : kLoopPres,
+                        [&](uint32_t sc) { return (DIV ? d.scenes[sc].div.active : d.scenes[sc].pres.active) != 0u; });
     if (threadIdx.x == 0) set_condition(d, DIV ? kLoopDiv : kLoopPres, aborted_p(d) ? 0u : any);
 }
 
@@ -672,6 +783,7 @@ __global__ void k_ctrl_cg1(Dev d) {
         if (run) atomicOr(&any, 1u);
     }
     __syncthreads();
+    if (d.nscenes > 1) build_work_list(d, kLoopCG, [&](uint32_t sc) { return d.scenes[sc].cgActive != 0u; });
     if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
 }
 
@@ -699,6 +811,33 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
     scene_accumulate<1, G>(d, sid, valid && grp.lane == 0, v, slot);
 }
 
+// Loop body 1 of a batch.
+template <uint32_t G>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    BATCH_LOOP(kLoopCG, G) {
+        const uint32_t vp = base_ + threadIdx.x / G;
+        const bool in = vp < total_;
+        uint32_t sid = 0;
+        const uint32_t p = in ? work_slot(d, kLoopCG, vp, sid) : 0u;
+        double pap = 0.0;
+        if (in) {
+            const Group<G> grp(p);
+            const float3 pv = f3(d.CP[p]);
+            const float3 ap = visc_matvec<G>(d, grp, p, d.scenes[sid], d.CP, pv);
+            if (grp.lane == 0) {
+                d.CAP[p] = f4(ap, 0.0f);
+                pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
+            }
+        }
+        const double v[1] = {pap};
+        const int slot[1] = {0};
+        scene_accumulate_core<1>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in && threadIdx.x % G == 0u,
+                                 v, slot);
+    }
+}
+
 // alpha = |r . z| / (p . Ap) (:714-720).
 __global__ void k_ctrl_cg_alpha(Dev d) {
     VFD_COUNT_LAUNCH(d);
@@ -710,6 +849,20 @@ __global__ void k_ctrl_cg_alpha(Dev d) {
 }
 
 // Loop body 2: g += alpha p, r -= alpha Ap, |r|^2, z = M^-1 r, r . z (:722-784).
+__device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const SceneDev& S, double& rr, double& rz) {
+    const float alpha = S.cgAlpha;
+    const float3 pv = f3(d.CP[p]);
+    const float4 g4 = d.CG[p];
+    const float3 g = f3(g4) + pv * alpha;
+    const float3 r = f3(d.CR[p]) - f3(d.CAP[p]) * alpha;
+    d.CG[p] = f4(g, g4.w);
+    d.CR[p] = f4(r, 0.0f);
+    const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
+    d.CZ[p] = f4(z, 0.0f);
+    rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+    rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+}
+
 __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -718,22 +871,26 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     const SceneDev& S = d.scenes[sid];
     const bool valid = inRange && S.cgActive;
     double rr = 0.0, rz = 0.0;
-    if (valid) {
-        const float alpha = S.cgAlpha;
-        const float3 pv = f3(d.CP[p]);
-        const float4 g4 = d.CG[p];
-        const float3 g = f3(g4) + pv * alpha;
-        const float3 r = f3(d.CR[p]) - f3(d.CAP[p]) * alpha;
-        d.CG[p] = f4(g, g4.w);
-        d.CR[p] = f4(r, 0.0f);
-        const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
-        d.CZ[p] = f4(z, 0.0f);
-        rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
-        rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
-    }
+    if (valid) cg_update_item(d, p, S, rr, rz);
     const double v[2] = {rr, rz};
     const int slot[2] = {1, 2};
     scene_accumulate<2>(d, sid, valid, v, slot);
+}
+
+__global__ void __launch_bounds__(kBlock) k_cg_update_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    BATCH_LOOP(kLoopCG, 1u) {
+        const uint32_t vp = base_ + threadIdx.x;
+        const bool in = vp < total_;
+        uint32_t sid = 0;
+        const uint32_t p = in ? work_slot(d, kLoopCG, vp, sid) : 0u;
+        double rr = 0.0, rz = 0.0;
+        if (in) cg_update_item(d, p, d.scenes[sid], rr, rz);
+        const double v[2] = {rr, rz};
+        const int slot[2] = {1, 2};
+        scene_accumulate_core<2>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in, v, slot);
+    }
 }
 
 // Loop control: break on |r|^2 < threshold, else beta and the next iteration (:754-805).
@@ -765,6 +922,7 @@ __global__ void k_ctrl_cg(Dev d) {
         if (again) atomicOr(&any, 1u);
     }
     __syncthreads();
+    if (d.nscenes > 1) build_work_list(d, kLoopCG, [&](uint32_t sc) { return d.scenes[sc].cgActive != 0u; });
     if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
 }
 
@@ -777,6 +935,20 @@ __global__ void __launch_bounds__(kBlock) k_cg_p(Dev d) {
     if (!S.cgUpdateP) return;
     const float4 pv = d.CP[p];
     d.CP[p] = f4(f3(pv) * S.cgBeta + f3(d.CZ[p]), pv.w);
+}
+
+// Loop body 3 of a batch: the scenes going on to another iteration.
+__global__ void __launch_bounds__(kBlock) k_cg_p_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    BATCH_LOOP(kLoopCG, 1u) {
+        const uint32_t vp = base_ + threadIdx.x;
+        if (vp >= total_) continue;
+        uint32_t sid;
+        const uint32_t p = work_slot(d, kLoopCG, vp, sid);
+        const float4 pv = d.CP[p];
+        d.CP[p] = f4(f3(pv) * d.scenes[sid].cgBeta + f3(d.CZ[p]), pv.w);
+    }
 }
 
 // K15 ApplyViscosityForceKernel (:844-862) + T1, the CFL maximum of |v + a dt|^2
@@ -912,7 +1084,21 @@ void launch_div_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH_LANES("k_div_init", kTDivInit, K_DIV_INIT);
     VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d));
 }
+#define K_PACCEL_DB(G) k_pressure_accel_b<true, G>
+#define K_PACCEL_PB(G) k_pressure_accel_b<false, G>
+#define K_JACOBI_DB(G) k_jacobi_iter_b<true, G>
+#define K_JACOBI_PB(G) k_jacobi_iter_b<false, G>
+#define K_SPMV_B(G) k_cg_spmv_b<G>
+
+// Batches run the solver-loop kernels over their work lists (the scenes still
+// iterating) with a fixed grid; a single scene keeps one group per particle.
 void launch_div_iter(const Dev& d, cudaStream_t s) {
+    if (d.nscenes > 1) {
+        VFD_LAUNCH_LANES_BATCH("k_pressure_accel", kTPAccel, K_PACCEL_DB);
+        VFD_LAUNCH_LANES_BATCH("k_jacobi_iter", kTJacobi, K_JACOBI_DB);
+        VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
+        return;
+    }
     VFD_LAUNCH_LANES("k_pressure_accel", kTPAccel, K_PACCEL_D);
     VFD_LAUNCH_LANES("k_jacobi_iter", kTJacobi, K_JACOBI_D);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
@@ -932,6 +1118,14 @@ void launch_visc_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_ctrl_cg1", s, k_ctrl_cg1<<<1, 256, 0, s>>>(d));
 }
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
+    if (d.nscenes > 1) {
+        VFD_LAUNCH_LANES_BATCH("k_cg_spmv", kTSpmv, K_SPMV_B);
+        VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
+        VFD_LAUNCH("k_cg_update", s, k_cg_update_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
+        VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
+        VFD_LAUNCH("k_cg_p", s, k_cg_p_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
+        return;
+    }
     VFD_LAUNCH_LANES("k_cg_spmv", kTSpmv, K_SPMV);
     VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     VFD_LAUNCH("k_cg_update", s, k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d));
@@ -948,6 +1142,12 @@ void launch_pres_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_iter(const Dev& d, cudaStream_t s) {
+    if (d.nscenes > 1) {
+        VFD_LAUNCH_LANES_BATCH("k_pressure_accel", kTPAccel, K_PACCEL_PB);
+        VFD_LAUNCH_LANES_BATCH("k_jacobi_iter", kTJacobi, K_JACOBI_PB);
+        VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
+        return;
+    }
     VFD_LAUNCH_LANES("k_pressure_accel", kTPAccel, K_PACCEL_P);
     VFD_LAUNCH_LANES("k_jacobi_iter", kTJacobi, K_JACOBI_P);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
