@@ -439,6 +439,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_density(Dev d, AdjDev a) {
 // where T_ij = cmu (m / rho_j)(g_ij . r) phi(|r|) r, phi = gs / (|r|^2 + eps2) and
 // R(r, g, w) = phi ((r . w) g + (g . r) w) + (g . r)(r . w)(phi' / |r|) r.
 __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const float4* __restrict__ G, float dt) {
+    if (d.scenes[0].cgZeroG) return;  // lambda = 0
     ADJ_GROUP
     const SceneDev& S = d.scenes[0];
     const Spline sp(d.radius);
@@ -716,9 +717,10 @@ __global__ void k_adj_cfl(Dev d, AdjDev a, const float4* V1, const float4* G, fl
     else if (mode == 0) a.VBAR[p] = f4(f3(a.VBAR[p]) + wb, 0.f);
 }
 
+// v1 bar += lambda, unless the adjoint solve's right-hand side was zero (lambda = 0).
 __global__ void k_adj_add_lambda(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
+    if (p >= d.n || d.scenes[0].cgZeroG) return;
     a.VBAR[p] = f4(f3(a.VBAR[p]) + f3(d.CG[p]), 0.f);
 }
 
@@ -730,23 +732,125 @@ __global__ void k_adj_carry(AdjDev a) {
     a.CLAIM[1] = 0u;
 }
 
-// ---------------------------------------------------------------- host side
-#define ADJ_LAUNCH(kernel, grid, ...) kernel<<<(grid), kBlock, 0, st>>>(__VA_ARGS__)
-
-struct StepMeta {
-    SceneDev pre;          // scene state before the step (dt of the divergence and viscosity solves)
+// ---------------------------------------------------------------- tape
+// One recorded step: written by the tape kernels at the tape points of the step
+// (TapePoint), so that one recording graph serves every step: the slot of the current
+// step is steps[*cur], advanced by the step's last tape point.
+struct TapeStep {
+    float4 *Xpre, *V0, *V1, *G, *V2;
+    uint32_t *PID, *NCNT, *NBR;
+    float *RAD, *RAP;
+    float *KD, *RD, *KP, *RP;   // kappa^0..cap, res^0..cap-1 (stride floats each) of each solve
+    uint32_t capD, capP;
+    // written on the device
+    SceneDev pre;               // scene state at the start of the step
+    uint32_t kd, kp, overflow, zeroG, maxNbr, aborted;
     float dto, dtn, maxV2;
-    bool cfl;              // dt_n came from an unclamped CFL maximum above the 0.1 floor
-    bool div, visc, zeroG;
+};
+struct TapeSet {
+    TapeStep* steps;
+    uint32_t* cur;
+    uint32_t count;
 };
 
-struct StepTape {
-    float4 *Xpre = nullptr, *V0 = nullptr, *V1 = nullptr, *G = nullptr, *V2 = nullptr;
-    uint32_t *PID = nullptr, *NCNT = nullptr, *NBR = nullptr;
-    float *RAD = nullptr, *RAP = nullptr;
-    std::vector<float*> KD, RD, KP, RP;  // kappa^0..K, res^0..K-1 of each solve
-    StepMeta meta{};
-};
+__device__ __forceinline__ TapeStep& tape_step(const TapeSet* ts) { return ts->steps[*ts->cur]; }
+
+__global__ void k_tape_begin(Dev d, const TapeSet* ts) {
+    TapeStep& T = tape_step(ts);
+    T.pre = d.scenes[0];
+    T.kd = T.kp = T.overflow = 0u;
+}
+
+__global__ void k_tape_search(Dev d, const TapeSet* ts) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    TapeStep& T = tape_step(ts);
+    T.Xpre[p] = d.X[p];
+    T.PID[p] = d.PID[p];
+    T.NCNT[p] = d.NCNT[p];
+    const uint4* src = reinterpret_cast<const uint4*>(d.NBR + (size_t)p * kRow);
+    uint4* dst = reinterpret_cast<uint4*>(T.NBR + (size_t)p * kRow);
+#pragma unroll
+    for (uint32_t k = 0; k < kRow / 4u; k++) dst[k] = src[k];
+}
+
+// which: 0 V -> V0, 1 V -> V1, 2 CG -> G, 3 V -> V2
+__global__ void k_tape_vec(Dev d, const TapeSet* ts, int which) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    TapeStep& T = tape_step(ts);
+    float4* dst = which == 0 ? T.V0 : which == 1 ? T.V1 : which == 2 ? T.G : T.V2;
+    dst[p] = which == 2 ? d.CG[p] : d.V[p];
+}
+
+// Start of a solve: kappa^0 and rho_adv; after iteration k (the controller has counted
+// it): res^k and kappa^(k+1).
+template <bool DIV>
+__global__ void k_tape_solve(Dev d, const TapeSet* ts, int start) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    TapeStep& T = tape_step(ts);
+    const SceneDev& S = d.scenes[0];
+    const float* kap = DIV ? d.KAPPAV : d.KAPPA;
+    float* K = DIV ? T.KD : T.KP;
+    float* R = DIV ? T.RD : T.RP;
+    const uint32_t cap = DIV ? T.capD : T.capP;
+    if (start) {
+        K[p] = kap[p];
+        (DIV ? T.RAD : T.RAP)[p] = d.RHOADV[p];
+        return;
+    }
+    const uint32_t it = DIV ? S.div.it : S.pres.it;
+    if (it == 0u || it > cap) {
+        if (p == 0) T.overflow = 1u;
+        return;
+    }
+    R[(size_t)(it - 1u) * d.stride + p] = d.RES[p];
+    K[(size_t)it * d.stride + p] = kap[p];
+    if (p == 0) {
+        if (DIV) T.kd = it;
+        else T.kp = it;
+    }
+}
+
+__global__ void k_tape_end(Dev d, TapeSet* ts) {
+    TapeStep& T = tape_step(ts);
+    const SceneDev& S = d.scenes[0];
+    T.dto = T.pre.dt;
+    T.dtn = S.dt;
+    T.maxV2 = S.maxV2;
+    T.zeroG = S.enableVisc && S.cgZeroG ? 1u : 0u;
+    T.maxNbr = S.maxNbr;
+    T.aborted = d.status[1];
+    *ts->cur += 1u;
+}
+
+}  // namespace
+
+namespace host {
+void tape_point(const Dev& d, const void* rec, int point, cudaStream_t st) {
+    TapeSet* ts = const_cast<TapeSet*>(static_cast<const TapeSet*>(rec));
+    const uint32_t g = blocks_for(d.n);
+    switch (point) {
+        case kTapeBegin: k_tape_begin<<<1, 1, 0, st>>>(d, ts); break;
+        case kTapeSearch: k_tape_search<<<g, kBlock, 0, st>>>(d, ts); break;
+        case kTapeBoundary: k_tape_vec<<<g, kBlock, 0, st>>>(d, ts, 0); break;
+        case kTapeDivInit: k_tape_solve<true><<<g, kBlock, 0, st>>>(d, ts, 1); break;
+        case kTapeDivIter: k_tape_solve<true><<<g, kBlock, 0, st>>>(d, ts, 0); break;
+        case kTapeDivFinish: k_tape_vec<<<g, kBlock, 0, st>>>(d, ts, 1); break;
+        case kTapeVisc: k_tape_vec<<<g, kBlock, 0, st>>>(d, ts, 2); break;
+        case kTapeVelocity: k_tape_vec<<<g, kBlock, 0, st>>>(d, ts, 3); break;
+        case kTapePresInit: k_tape_solve<false><<<g, kBlock, 0, st>>>(d, ts, 1); break;
+        case kTapePresIter: k_tape_solve<false><<<g, kBlock, 0, st>>>(d, ts, 0); break;
+        case kTapeEnd: k_tape_end<<<1, 1, 0, st>>>(d, ts); break;
+        default: break;
+    }
+}
+}  // namespace host
+
+namespace {
+
+#define ADJ_LAUNCH(kernel, grid, ...) kernel<<<(grid), kBlock, 0, st>>>(__VA_ARGS__)
 
 struct Checkpoint {
     float4 *XN = nullptr, *V = nullptr, *DV = nullptr;
@@ -763,11 +867,24 @@ struct AdjointState {
     uint32_t steps = 0, every = 0, n = 0, stride = 0;
     uint64_t generation = 0;
     std::vector<Checkpoint> ckpt;  // ckpt[k]: before step k * every; back(): after the last step
-    std::vector<StepTape> tapes;   // one segment
-    std::vector<float*> pool;      // free iterate arrays
+    std::vector<TapeStep> host;    // host copy of one segment's tape slots
+    TapeSet* dset = nullptr;       // device tape set (steps, cur)
+    TapeStep* dsteps = nullptr;
+    uint32_t* dcur = nullptr;
+    bool lastRecorded = false;     // the forward run recorded its last segment
+    cudaGraph_t recGraph[2] = {nullptr, nullptr};
+    cudaGraphExec_t recExec[2] = {nullptr, nullptr};
+    cudaGraph_t cgGraph = nullptr;
+    cudaGraphExec_t cgExec = nullptr;
     std::vector<void*> allocs;
     AdjDev a{};
     ~AdjointState() {
+        for (int k = 0; k < 2; k++) {
+            if (recExec[k]) cudaGraphExecDestroy(recExec[k]);
+            if (recGraph[k]) cudaGraphDestroy(recGraph[k]);
+        }
+        if (cgExec) cudaGraphExecDestroy(cgExec);
+        if (cgGraph) cudaGraphDestroy(cgGraph);
         for (void* p : allocs) cudaFree(p);
     }
 };
@@ -787,20 +904,44 @@ int aalloc(AdjointState* A, T** p, size_t count) {
     return VFD_OK;
 }
 
-int take_array(AdjointState* A, float** out) {
-    if (!A->pool.empty()) {
-        *out = A->pool.back();
-        A->pool.pop_back();
-        return VFD_OK;
+// Tape slots for `every` steps, iterates sized by the scene's iteration caps.
+int alloc_tape(vfd_sim* s, AdjointState* A) {
+    const size_t st = s->stride;
+    const vfd_desc& dd = s->scenes[0].desc;
+    const uint32_t capD = s->anyDiv ? dd.MaxDivergenceSolverIterations : 0u, capP = dd.MaxPressureSolverIterations;
+    const size_t per = st * (5 * sizeof(float4) + (2 + kRow) * sizeof(uint32_t) + 2 * sizeof(float)) +
+                       st * sizeof(float) * (2 * (size_t)capD + 1 + 2 * (size_t)capP + 1);
+    size_t freeB = 0, totalB = 0;
+    CK(cudaMemGetInfo(&freeB, &totalB));
+    if (per * A->every > freeB / 2)
+        return fail(VFD_E_NOMEM, "adjoint: %zu bytes of tape for %u steps exceed half the free device memory; "
+                                 "use a smaller checkpoint_every", per * A->every, A->every);
+    A->host.assign(A->every, TapeStep{});
+    for (auto& T : A->host) {
+        TRY(aalloc(A, &T.Xpre, st));
+        TRY(aalloc(A, &T.V0, st));
+        TRY(aalloc(A, &T.V1, st));
+        TRY(aalloc(A, &T.G, st));
+        TRY(aalloc(A, &T.V2, st));
+        TRY(aalloc(A, &T.PID, st));
+        TRY(aalloc(A, &T.NCNT, st));
+        TRY(aalloc(A, &T.NBR, st * kRow));
+        TRY(aalloc(A, &T.RAD, st));
+        TRY(aalloc(A, &T.RAP, st));
+        TRY(aalloc(A, &T.KD, st * (capD + 1)));
+        TRY(aalloc(A, &T.RD, st * std::max<uint32_t>(1u, capD)));
+        TRY(aalloc(A, &T.KP, st * (capP + 1)));
+        TRY(aalloc(A, &T.RP, st * std::max<uint32_t>(1u, capP)));
+        T.capD = capD;
+        T.capP = capP;
     }
-    return aalloc(A, out, A->stride);
-}
-
-void recycle(AdjointState* A, StepTape& t) {
-    for (auto* v : {&t.KD, &t.RD, &t.KP, &t.RP}) {
-        for (float* f : *v) A->pool.push_back(f);
-        v->clear();
-    }
+    TRY(aalloc(A, &A->dsteps, A->every));
+    TRY(aalloc(A, &A->dcur, 1));
+    TRY(aalloc(A, &A->dset, 1));
+    CK(cudaMemcpy(A->dsteps, A->host.data(), sizeof(TapeStep) * A->every, cudaMemcpyHostToDevice));
+    TapeSet ts{A->dsteps, A->dcur, A->every};
+    CK(cudaMemcpy(A->dset, &ts, sizeof(ts), cudaMemcpyHostToDevice));
+    return VFD_OK;
 }
 
 int save_checkpoint(vfd_sim* s, AdjointState* A, Checkpoint& c) {
@@ -844,197 +985,151 @@ int restore_checkpoint(vfd_sim* s, const Checkpoint& c) {
     return VFD_OK;
 }
 
-int read_scene(vfd_sim* s, SceneDev& S) {
-    CK(cudaMemcpyAsync(&S, s->dScenes, sizeof(SceneDev), cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return VFD_OK;
-}
-
 #define COPY(dst, src, bytes) CK(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st))
 
-// One eagerly launched step (the kernels of launch_eager) that records the tape.
-int record_step(vfd_sim* s, AdjointState* A, StepTape& t) {
-    const size_t n4 = sizeof(float4) * s->stride, n1 = sizeof(float) * s->stride;
+// `count` steps from the current state, recorded into the tape slots 0..count-1, as CUDA
+// graphs (one per parity) unless graphs are off; then the slots' device-written fields
+// are read back and checked.
+int record_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
     cudaStream_t st = s->stream;
-    if (!t.Xpre) {
-        TRY(aalloc(A, &t.Xpre, s->stride));
-        TRY(aalloc(A, &t.V0, s->stride));
-        TRY(aalloc(A, &t.V1, s->stride));
-        TRY(aalloc(A, &t.G, s->stride));
-        TRY(aalloc(A, &t.V2, s->stride));
-        TRY(aalloc(A, &t.PID, s->stride));
-        TRY(aalloc(A, &t.NCNT, s->stride));
-        TRY(aalloc(A, &t.NBR, (size_t)s->stride * kRow));
-        TRY(aalloc(A, &t.RAD, s->stride));
-        TRY(aalloc(A, &t.RAP, s->stride));
+    CK(cudaMemsetAsync(A->dcur, 0, sizeof(uint32_t), st));
+    const bool graphs = s->graphMode && !s->graphFailed;
+    for (uint32_t t = 0; t < count; t++) {
+        if (graphs && !A->recExec[s->cs])
+            TRY(build_graph(s, s->cs, A->dset, &A->recGraph[s->cs], &A->recExec[s->cs]));
+        if (graphs) CK(cudaGraphLaunch(A->recExec[s->cs], st));
+        else TRY(launch_eager(s, A->dset));
+        s->cs = 1 - s->cs;
     }
-    recycle(A, t);
-    TRY(read_scene(s, t.meta.pre));
-    const Dev& d = s->dev[s->cs];
-    uint32_t more = 0;
-    launch_search(d, st);
-    COPY(t.Xpre, d.X, n4);
-    COPY(t.PID, d.PID, sizeof(uint32_t) * s->stride);
-    COPY(t.NCNT, d.NCNT, sizeof(uint32_t) * s->stride);
-    COPY(t.NBR, d.NBR, sizeof(uint32_t) * s->stride * kRow);
-    launch_boundary(d, st);
-    COPY(t.V0, d.V, n4);
-    launch_density(d, st);
-    launch_div_init(d, st);
-    t.meta.div = s->anyDiv;
-    if (s->anyDiv) {
-        float* k0;
-        TRY(take_array(A, &k0));
-        COPY(k0, d.KAPPAV, n1);
-        t.KD.push_back(k0);
-        COPY(t.RAD, d.RHOADV, n1);
-        TRY(read_flag(s, 4, more));
-        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
-            launch_div_iter(d, st);
-            float *r, *k;
-            TRY(take_array(A, &r));
-            TRY(take_array(A, &k));
-            COPY(r, d.RES, n1);
-            COPY(k, d.KAPPAV, n1);
-            t.RD.push_back(r);
-            t.KD.push_back(k);
-            TRY(read_flag(s, 4, more));
-        }
-    }
-    launch_div_finish(d, st);
-    COPY(t.V1, d.V, n4);
-    t.meta.visc = s->anyVisc;
-    if (s->anyVisc) {
-        launch_visc_init(d, st);
-        TRY(read_flag(s, 5, more));
-        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
-            launch_cg_iter(d, st);
-            TRY(read_flag(s, 5, more));
-        }
-        COPY(t.G, d.CG, n4);
-    }
-    launch_visc_finish_dt(d, st);
-    COPY(t.V2, d.V, n4);
-    launch_pres_init(d, st);
-    {
-        float* k0;
-        TRY(take_array(A, &k0));
-        COPY(k0, d.KAPPA, n1);
-        t.KP.push_back(k0);
-        COPY(t.RAP, d.RHOADV, n1);
-    }
-    TRY(read_flag(s, 6, more));
-    for (uint32_t guard = 0; more && guard < 100000u; guard++) {
-        launch_pres_iter(d, st);
-        float *r, *k;
-        TRY(take_array(A, &r));
-        TRY(take_array(A, &k));
-        COPY(r, d.RES, n1);
-        COPY(k, d.KAPPA, n1);
-        t.RP.push_back(r);
-        t.KP.push_back(k);
-        TRY(read_flag(s, 6, more));
-    }
-    launch_pres_finish(d, st);
-    CK(cudaGetLastError());
-    SceneDev post;
-    TRY(read_scene(s, post));
-    CK(cudaMemcpyAsync(s->hStatus, s->dStatus, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    std::vector<TapeStep> dev(count);
+    CK(cudaMemcpyAsync(dev.data(), A->dsteps, sizeof(TapeStep) * count, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (s->hStatus[1]) return fail(VFD_E_STATE, "adjoint: a recomputed step aborted (grid or non-finite position)");
-    if (post.maxNbr >= kMaxNeighbors)
-        return fail(VFD_E_CAPACITY, "adjoint: a particle reached the %u-neighbour cap (neighbour sets must be symmetric)",
-                    kMaxNeighbors);
-    t.meta.dto = t.meta.pre.dt;
-    t.meta.dtn = post.dt;
-    t.meta.maxV2 = post.maxV2;
-    t.meta.zeroG = s->anyVisc && post.cgZeroG;
-    const float raw = 0.4f * (post.diam / sqrtf(post.maxV2));
-    t.meta.cfl = post.maxV2 > 0.1f && raw == post.dt;
-    s->cs = 1 - s->cs;
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), st));
+    for (uint32_t t = 0; t < count; t++) {
+        const TapeStep& T = dev[t];
+        if (T.aborted) return fail(VFD_E_STATE, "adjoint: a recorded step aborted (grid capacity or non-finite position)");
+        if (T.overflow) return fail(VFD_E_STATE, "adjoint: solver iterations exceeded the tape capacity");
+        if (T.maxNbr >= kMaxNeighbors)
+            return fail(VFD_E_CAPACITY, "adjoint: a particle reached the %u-neighbour cap (neighbour sets must be "
+                                        "symmetric)", kMaxNeighbors);
+        A->host[t].pre = T.pre;
+        A->host[t].kd = T.kd;
+        A->host[t].kp = T.kp;
+        A->host[t].zeroG = T.zeroG;
+        A->host[t].dto = T.dto;
+        A->host[t].dtn = T.dtn;
+        A->host[t].maxV2 = T.maxV2;
+    }
     return VFD_OK;
 }
 
-// Backward pass of one recorded step; A->a.XBO / VBO hold the cotangents of its
-// outputs on entry and of its inputs on return.
-int backward_step(vfd_sim* s, AdjointState* A, const StepTape& t) {
+// The adjoint solve A lambda = g_bar: the forward CG (precondition, setup, loop) on the
+// backward's working set, as one graph with a device-side while loop.
+int build_cg_graph(vfd_sim* s, AdjointState* A) {
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(VFD_E_CUDA, "adjoint: cudaGraphConditionalHandleCreate: %s", cudaGetErrorString(e));
+    }
+    Dev d = s->dev[0];
+    d.condHandle[1] = (unsigned long long)h;
+    std::vector<cudaGraphNode_t> leaves;
+    e = add_segment(s->stream, g, leaves, [&](cudaStream_t st) { launch_visc_init(d, st); });
+    if (e == cudaSuccess) e = add_while(s->stream, g, h, leaves, [&](cudaStream_t st) { launch_cg_iter(d, st); });
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(g);
+        return fail(VFD_E_CUDA, "adjoint: CG graph construction failed: %s", cudaGetErrorString(e));
+    }
+    A->cgGraph = g;
+    A->cgExec = exec;
+    return VFD_OK;
+}
+
+// Backward pass of recorded step t (tape slot t); A->a.XBO / VBO hold the cotangents of
+// its outputs on entry and of its inputs on return. No host synchronisation.
+int backward_step(vfd_sim* s, AdjointState* A, uint32_t t) {
     cudaStream_t st = s->stream;
     const Dev& d = s->dev[0];
     AdjDev& a = A->a;
-    const StepMeta& M = t.meta;
+    const TapeStep& T = A->host[t];
     const uint32_t n = s->n;
     const uint32_t g1 = blocks_for(n), gG = blocks_for(n * kAG);
+    const size_t sd = s->stride;
+    auto KD = [&](uint32_t k) { return T.KD + (size_t)k * sd; };
+    auto RD = [&](uint32_t k) { return T.RD + (size_t)k * sd; };
+    auto KP = [&](uint32_t k) { return T.KP + (size_t)k * sd; };
+    auto RP = [&](uint32_t k) { return T.RP + (size_t)k * sd; };
     // the forward arrays of this step
-    CK(cudaMemcpyAsync(s->dScenes, &M.pre, sizeof(SceneDev), cudaMemcpyHostToDevice, st));
-    COPY(d.X, t.Xpre, sizeof(float4) * s->stride);
-    COPY(d.NCNT, t.NCNT, sizeof(uint32_t) * s->stride);
-    COPY(d.NBR, t.NBR, sizeof(uint32_t) * s->stride * kRow);
+    COPY(s->dScenes, &A->dsteps[t].pre, sizeof(SceneDev));
+    COPY(d.X, T.Xpre, sizeof(float4) * sd);
+    COPY(d.NCNT, T.NCNT, sizeof(uint32_t) * sd);
+    COPY(d.NBR, T.NBR, sizeof(uint32_t) * sd * kRow);
     CK(cudaMemsetAsync(s->dStatus, 0, 16 * sizeof(uint32_t), st));
     ADJ_LAUNCH(k_adj_bdata, g1, d, a);
     launch_boundary(d, st);
     launch_density(d, st);
-    ADJ_LAUNCH(k_adj_load, g1, d, a, t.PID);
+    ADJ_LAUNCH(k_adj_load, g1, d, a, T.PID);
 
     // pressure solve, K20 + K21 (v3 and x')
-    const float dtn = M.dtn, dto = M.dto;
-    const uint32_t kp = (uint32_t)t.RP.size();
-    ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, t.KP[kp], 0.0f);
-    ADJ_LAUNCH(k_adj_pres_out, g1, d, a, t.V2, dtn);
-    ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, t.KP[kp], 0.0f);
+    const float dtn = T.dtn, dto = T.dto;
+    const uint32_t kp = T.kp;
+    ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, KP(kp), 0.0f);
+    ADJ_LAUNCH(k_adj_pres_out, g1, d, a, T.V2, dtn);
+    ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, KP(kp), 0.0f);
     for (uint32_t k = kp; k-- > 0;) {
-        ADJ_LAUNCH(k_adj_u<false>, g1, d, a, t.RP[k], t.RAP, 1.0f / (dtn * dtn), 2.0f / dtn);
-        ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, t.KP[k], dtn * dtn);
-        ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, t.KP[k], dtn * dtn);
+        ADJ_LAUNCH(k_adj_u<false>, g1, d, a, RP(k), T.RAP, 1.0f / (dtn * dtn), 2.0f / dtn);
+        ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, KP(k), dtn * dtn);
+        ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, KP(k), dtn * dtn);
     }
-    ADJ_LAUNCH(k_adj_pres_init, g1, d, a, t.RAP, dtn);
-    ADJ_LAUNCH(k_adj_div_b<true>, gG, d, a, t.V2);
+    ADJ_LAUNCH(k_adj_pres_init, g1, d, a, T.RAP, dtn);
+    ADJ_LAUNCH(k_adj_div_b<true>, gG, d, a, T.V2);
 
     // K16 velocity update and the CFL time step
-    const int mode = !M.visc ? 0 : (M.zeroG ? 2 : 1);
-    ADJ_LAUNCH(k_adj_velocity, g1, d, a, t.V1, t.G, dto, dtn, mode);
-    if (M.cfl) {
-        ADJ_LAUNCH(k_adj_cfl_max, g1, d, a, t.V1, t.G, dto, mode);
-        ADJ_LAUNCH(k_adj_cfl, g1, d, a, t.V1, t.G, dto, dtn, M.maxV2, mode);
+    const bool visc = s->anyVisc, div = s->anyDiv;
+    const int mode = !visc ? 0 : (T.zeroG ? 2 : 1);
+    ADJ_LAUNCH(k_adj_velocity, g1, d, a, T.V1, T.G, dto, dtn, mode);
+    const float raw = 0.4f * (T.pre.diam / sqrtf(T.maxV2));
+    if (T.maxV2 > 0.1f && raw == T.dtn) {
+        ADJ_LAUNCH(k_adj_cfl_max, g1, d, a, T.V1, T.G, dto, mode);
+        ADJ_LAUNCH(k_adj_cfl, g1, d, a, T.V1, T.G, dto, dtn, T.maxV2, mode);
     }
 
     // viscosity: A lambda = g_bar with the forward's CG, then the derivative of A g = v1
     if (mode == 1) {
-        COPY(d.V, a.GBAR, sizeof(float4) * s->stride);
-        CK(cudaMemsetAsync(d.DV, 0, sizeof(float4) * s->stride, st));
-        uint32_t more = 0;
-        launch_visc_init(d, st);
-        TRY(read_flag(s, 5, more));
-        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
-            launch_cg_iter(d, st);
-            TRY(read_flag(s, 5, more));
-        }
-        SceneDev sc;
-        TRY(read_scene(s, sc));
-        if (!sc.cgZeroG) {
-            ADJ_LAUNCH(k_adj_add_lambda, g1, d, a);
-            ADJ_LAUNCH(k_adj_visc, gG, d, a, t.G, dto);
-        }
+        COPY(d.V, a.GBAR, sizeof(float4) * sd);
+        CK(cudaMemsetAsync(d.DV, 0, sizeof(float4) * sd, st));
+        if (!A->cgExec) TRY(build_cg_graph(s, A));
+        CK(cudaGraphLaunch(A->cgExec, st));
+        ADJ_LAUNCH(k_adj_add_lambda, g1, d, a);
+        ADJ_LAUNCH(k_adj_visc, gG, d, a, T.G, dto);
     }
 
     // divergence solve, K4-K7
-    if (M.div) {
-        const uint32_t kd = (uint32_t)t.RD.size();
-        ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, t.KD[kd], 0.0f);
+    if (div) {
+        const uint32_t kd = T.kd;
+        ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, KD(kd), 0.0f);
         ADJ_LAUNCH(k_adj_div_out, g1, d, a, dto);
-        ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, t.KD[kd], 0.0f);
+        ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, KD(kd), 0.0f);
         for (uint32_t k = kd; k-- > 0;) {
-            ADJ_LAUNCH(k_adj_u<true>, g1, d, a, t.RD[k], t.RAD, 1.0f / dto, 1.0f / dto);
-            ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, t.KD[k], dto);
-            ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, t.KD[k], dto);
+            ADJ_LAUNCH(k_adj_u<true>, g1, d, a, RD(k), T.RAD, 1.0f / dto, 1.0f / dto);
+            ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, KD(k), dto);
+            ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, KD(k), dto);
         }
-        ADJ_LAUNCH(k_adj_div_init, g1, d, a, t.RAD, dto);
-        ADJ_LAUNCH(k_adj_div_b<false>, gG, d, a, t.V0);
+        ADJ_LAUNCH(k_adj_div_init, g1, d, a, T.RAD, dto);
+        ADJ_LAUNCH(k_adj_div_b<false>, gG, d, a, T.V0);
     }
 
     // density and factor (K2 + K3), then the boundary's velocity reset and original order
     ADJ_LAUNCH(k_adj_gsum, gG, d, a);
     ADJ_LAUNCH(k_adj_density, gG, d, a);
-    ADJ_LAUNCH(k_adj_store, g1, d, a, t.PID);
+    ADJ_LAUNCH(k_adj_store, g1, d, a, T.PID);
     k_adj_carry<<<1, 1, 0, st>>>(a);
     CK(cudaGetLastError());
     return VFD_OK;
@@ -1106,15 +1201,36 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
     adjoint_release(s);
     auto A = std::make_unique<AdjointState>();
     A->steps = steps;
-    A->every = checkpoint_every;
+    A->every = std::min(checkpoint_every, steps);
     A->n = s->n;
     A->stride = s->stride;
-    const uint32_t segs = (steps + checkpoint_every - 1) / checkpoint_every;
+    TRY(alloc_tape(s, A.get()));
+    const uint32_t segs = (steps + A->every - 1) / A->every;
     A->ckpt.resize(segs + 1);
     for (uint32_t k = 0; k < segs; k++) {
         TRY(save_checkpoint(s, A.get(), A->ckpt[k]));
-        const uint32_t cnt = std::min(checkpoint_every, steps - k * checkpoint_every);
-        TRY(run_steps(s, cnt, stats, true));
+        const uint32_t cnt = std::min(A->every, steps - k * A->every);
+        if (k + 1 < segs) {
+            TRY(run_steps(s, cnt, stats, true));
+            continue;
+        }
+        // the last segment is recorded as it runs, so the backward pass starts on it
+        // without a replay; a step the search had to abort (grid growth) falls back to a
+        // plain run and a replay
+        const int rc = record_segment(s, A.get(), cnt);
+        if (rc == VFD_OK) {
+            A->lastRecorded = true;
+            if (stats) {
+                CK(cudaMemcpy(s->hScenes.data(), s->dScenes, sizeof(SceneDev) * s->hScenes.size(),
+                              cudaMemcpyDeviceToHost));
+                fill_stats(s->hScenes[0], stats);
+            }
+        } else if (rc == VFD_E_STATE) {
+            TRY(restore_checkpoint(s, A->ckpt[k]));
+            TRY(run_steps(s, cnt, stats, true));
+        } else {
+            return rc;
+        }
     }
     TRY(save_checkpoint(s, A.get(), A->ckpt[segs]));
     A->generation = s->generation;
@@ -1142,15 +1258,17 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
     CK(cudaMemsetAsync(a.SC, 0, 8 * sizeof(double), st));
     CK(cudaMemsetAsync(a.CLAIM, 0, 2 * sizeof(uint32_t), st));
     const uint32_t segs = (uint32_t)A->ckpt.size() - 1;
-    A->tapes.resize(A->every);
     int rc = VFD_OK;
     for (uint32_t k = segs; k-- > 0 && rc == VFD_OK;) {
-        rc = restore_checkpoint(s, A->ckpt[k]);
         const uint32_t cnt = std::min(A->every, A->steps - k * A->every);
-        for (uint32_t t = 0; t < cnt && rc == VFD_OK; t++) rc = record_step(s, A, A->tapes[t]);
-        for (uint32_t t = cnt; t-- > 0 && rc == VFD_OK;) rc = backward_step(s, A, A->tapes[t]);
+        if (!(k + 1 == segs && A->lastRecorded)) {
+            rc = restore_checkpoint(s, A->ckpt[k]);
+            if (rc == VFD_OK) rc = record_segment(s, A, cnt);
+        }
+        for (uint32_t t = cnt; t-- > 0 && rc == VFD_OK;) rc = backward_step(s, A, t);
     }
-    // leave the simulation where the forward run ended
+    // the tape now holds the first segment; leave the simulation where the forward run ended
+    A->lastRecorded = false;
     const int rc2 = restore_checkpoint(s, A->ckpt[segs]);
     if (rc != VFD_OK) return rc;
     if (rc2 != VFD_OK) return rc2;

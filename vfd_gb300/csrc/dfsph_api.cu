@@ -396,46 +396,7 @@ int upload(vfd_sim* s) {
 }
 
 // ---------------------------------------------------------------- step recording
-template <class F>
-cudaError_t add_while(cudaStream_t cap, cudaGraph_t g, cudaGraphConditionalHandle h, std::vector<cudaGraphNode_t>& leaves,
-                      F body) {
-    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    cudaError_t e = cudaGraphAddNode(&node, g, leaves.data(), nullptr, leaves.size(), &np);
-    if (e != cudaSuccess) return e;
-    cudaGraph_t bodyGraph = np.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(cap, bodyGraph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    body(cap);
-    e = cudaStreamEndCapture(cap, &bodyGraph);
-    if (e != cudaSuccess) return e;
-    leaves.assign(1, node);
-    return cudaSuccess;
-}
-
-template <class F>
-cudaError_t add_segment(cudaStream_t cap, cudaGraph_t g, std::vector<cudaGraphNode_t>& leaves, F seg) {
-    cudaError_t e = cudaStreamBeginCaptureToGraph(cap, g, leaves.empty() ? nullptr : leaves.data(), nullptr,
-                                                  leaves.size(), cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    seg(cap);
-    cudaStreamCaptureStatus status;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t nd = 0;
-    e = cudaStreamGetCaptureInfo(cap, &status, nullptr, nullptr, &deps, nullptr, &nd);
-    if (e != cudaSuccess) return e;
-    std::vector<cudaGraphNode_t> next(deps, deps + nd);
-    cudaGraph_t out = g;
-    e = cudaStreamEndCapture(cap, &out);
-    if (e != cudaSuccess) return e;
-    if (!next.empty()) leaves = next;
-    return cudaSuccess;
-}
-
-int build_graph(vfd_sim* s, int parity) {
+int build_graph(vfd_sim* s, int parity, const void* rec, cudaGraph_t* gOut, cudaGraphExec_t* execOut) {
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle h[3];
@@ -452,27 +413,48 @@ int build_graph(vfd_sim* s, int parity) {
     std::vector<cudaGraphNode_t> leaves;
     const uint32_t passes = s->maxStPasses;
     const bool anyDiv = s->anyDiv, anyVisc = s->anyVisc, anyST = s->anyST;
+    // with a recorder, tape_point() adds the adjoint's tape writes between the stages
+    auto T = [&](int point, cudaStream_t st) {
+        if (rec) tape_point(d, rec, point, st);
+    };
     cudaError_t e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        T(kTapeBegin, st);
         launch_search(d, st);
+        T(kTapeSearch, st);
         launch_boundary(d, st);
+        T(kTapeBoundary, st);
         launch_density(d, st);
         launch_div_init(d, st);
+        T(kTapeDivInit, st);
     });
-    if (e == cudaSuccess && anyDiv) e = add_while(cap, g, h[0], leaves, [&](cudaStream_t st) { launch_div_iter(d, st); });
+    if (e == cudaSuccess && anyDiv) e = add_while(cap, g, h[0], leaves, [&](cudaStream_t st) {
+        launch_div_iter(d, st);
+        T(kTapeDivIter, st);
+    });
     if (e == cudaSuccess)
         e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
             launch_div_finish(d, st);
+            T(kTapeDivFinish, st);
             if (anyST) launch_surface_tension(d, passes, st);
             if (anyVisc) launch_visc_init(d, st);
         });
     if (e == cudaSuccess && anyVisc) e = add_while(cap, g, h[1], leaves, [&](cudaStream_t st) { launch_cg_iter(d, st); });
     if (e == cudaSuccess)
         e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+            T(kTapeVisc, st);
             launch_visc_finish_dt(d, st);
+            T(kTapeVelocity, st);
             launch_pres_init(d, st);
+            T(kTapePresInit, st);
         });
-    if (e == cudaSuccess) e = add_while(cap, g, h[2], leaves, [&](cudaStream_t st) { launch_pres_iter(d, st); });
-    if (e == cudaSuccess) e = add_segment(cap, g, leaves, [&](cudaStream_t st) { launch_pres_finish(d, st); });
+    if (e == cudaSuccess) e = add_while(cap, g, h[2], leaves, [&](cudaStream_t st) {
+        launch_pres_iter(d, st);
+        T(kTapePresIter, st);
+    });
+    if (e == cudaSuccess) e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        launch_pres_finish(d, st);
+        T(kTapeEnd, st);
+    });
     cudaGraphExec_t exec = nullptr;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
     if (e != cudaSuccess) {
@@ -480,10 +462,12 @@ int build_graph(vfd_sim* s, int parity) {
         cudaGraphDestroy(g);
         return fail(VFD_E_CUDA, "step graph construction failed: %s", cudaGetErrorString(e));
     }
-    s->graph[parity] = g;
-    s->exec[parity] = exec;
+    *gOut = g;
+    *execOut = exec;
     return VFD_OK;
 }
+
+int build_graph(vfd_sim* s, int parity) { return build_graph(s, parity, nullptr, &s->graph[parity], &s->exec[parity]); }
 
 int read_flag(vfd_sim* s, int idx, uint32_t& v) {
     CK(cudaMemcpyAsync(s->hStatus + idx, s->dStatus + idx, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
@@ -493,22 +477,31 @@ int read_flag(vfd_sim* s, int idx, uint32_t& v) {
 }
 
 // The reference's host-driven control flow: one flag read per solver iteration.
-int launch_eager(vfd_sim* s) {
+int launch_eager(vfd_sim* s, const void* rec) {
     const Dev& d = s->dev[s->cs];
     cudaStream_t st = s->stream;
+    auto T = [&](int point) {
+        if (rec) tape_point(d, rec, point, st);
+    };
     uint32_t more = 0;
+    T(kTapeBegin);
     launch_search(d, st);
+    T(kTapeSearch);
     launch_boundary(d, st);
+    T(kTapeBoundary);
     launch_density(d, st);
     launch_div_init(d, st);
+    T(kTapeDivInit);
     if (s->anyDiv) {
         TRY(read_flag(s, 4, more));
         for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
             launch_div_iter(d, st);
+            T(kTapeDivIter);
             TRY(read_flag(s, 4, more));
         }
     }
     launch_div_finish(d, st);
+    T(kTapeDivFinish);
     if (s->anyST) launch_surface_tension(d, s->maxStPasses, st);
     if (s->anyVisc) {
         launch_visc_init(d, st);
@@ -518,17 +511,24 @@ int launch_eager(vfd_sim* s) {
             TRY(read_flag(s, 5, more));
         }
     }
+    T(kTapeVisc);
     launch_visc_finish_dt(d, st);
+    T(kTapeVelocity);
     launch_pres_init(d, st);
+    T(kTapePresInit);
     TRY(read_flag(s, 6, more));
     for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
         launch_pres_iter(d, st);
+        T(kTapePresIter);
         TRY(read_flag(s, 6, more));
     }
     launch_pres_finish(d, st);
+    T(kTapeEnd);
     CK(cudaGetLastError());
     return VFD_OK;
 }
+
+int launch_eager(vfd_sim* s) { return launch_eager(s, nullptr); }
 
 int ensure_ready(vfd_sim* s) {
     if (s->scenes.empty()) return fail(VFD_E_STATE, "no scene");

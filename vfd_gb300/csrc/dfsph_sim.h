@@ -214,7 +214,62 @@ int dalloc(vfd_sim* s, T** p, size_t count) {
     return VFD_OK;
 }
 
+// Graph building blocks: a conditional WHILE node whose body `body` captures, and a
+// captured segment appended after the current leaves.
+template <class F>
+cudaError_t add_while(cudaStream_t cap, cudaGraph_t g, cudaGraphConditionalHandle h, std::vector<cudaGraphNode_t>& leaves,
+                      F body) {
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    cudaError_t e = cudaGraphAddNode(&node, g, leaves.data(), nullptr, leaves.size(), &np);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t bodyGraph = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(cap, bodyGraph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    body(cap);
+    e = cudaStreamEndCapture(cap, &bodyGraph);
+    if (e != cudaSuccess) return e;
+    leaves.assign(1, node);
+    return cudaSuccess;
+}
+
+template <class F>
+cudaError_t add_segment(cudaStream_t cap, cudaGraph_t g, std::vector<cudaGraphNode_t>& leaves, F seg) {
+    cudaError_t e = cudaStreamBeginCaptureToGraph(cap, g, leaves.empty() ? nullptr : leaves.data(), nullptr,
+                                                  leaves.size(), cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    seg(cap);
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(cap, &status, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> next(deps, deps + nd);
+    cudaGraph_t out = g;
+    e = cudaStreamEndCapture(cap, &out);
+    if (e != cudaSuccess) return e;
+    if (!next.empty()) leaves = next;
+    return cudaSuccess;
+}
+
+
+// Adjoint tape points of a recorded step (tape_point in dfsph_adjoint.cu).
+enum TapePoint {
+    kTapeBegin = 0, kTapeSearch, kTapeBoundary, kTapeDivInit, kTapeDivIter, kTapeDivFinish, kTapeVisc,
+    kTapeVelocity, kTapePresInit, kTapePresIter, kTapeEnd
+};
+void tape_point(const Dev& d, const void* rec, int point, cudaStream_t st);
+
+// One step as a graph (rec: the adjoint's device tape set, or null) into *gOut / *execOut.
+int build_graph(vfd_sim* s, int parity, const void* rec, cudaGraph_t* gOut, cudaGraphExec_t* execOut);
+// One eagerly launched step (one flag read per solver iteration), optionally recording.
+int launch_eager(vfd_sim* s, const void* rec);
+
 int ensure_ready(vfd_sim* s);
+void fill_stats(const SceneDev& S, vfd_step_stats* st);
 int read_flag(vfd_sim* s, int idx, uint32_t& v);
 int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait);
 int finish_steps(vfd_sim* s, vfd_step_stats* stats, uint32_t& flags);
