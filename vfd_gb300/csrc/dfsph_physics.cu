@@ -107,35 +107,41 @@ __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
 // kappa (or kappa_v) of particle p, mirrored into X[p].w for the neighbours' gathers.
 __device__ __forceinline__ void set_kappa(const Dev& d, uint32_t p, float k) { reinterpret_cast<float*>(d.X)[4 * (size_t)p + 3] = k; }
 
-// Neighbour loop of one group. In a round the group covers 4G consecutive row
-// entries and lane l takes entries l, l + G, l + 2G, l + 3G, so at each of the four
-// steps the group's lanes read consecutive entries -- usually consecutive slots of one
-// cell, which the gathers then fetch in one or two sectors. The first round's index
-// loads do not wait for the count (rows have 72 slots, entries past the count are
-// masked), so the count, the indices and the particle's own fields are fetched
-// together; within a round the four gathers per lane are independent. Masked entries
-// use the particle itself as a stand-in index.
+// Row entries per lane and round of a G-lane neighbour loop.
+constexpr uint32_t unroll_for(uint32_t G) { return G == 4u ? 4u : (G == 8u ? 4u : 4u); }
+
+// Neighbour loop of one group. In a round the group covers U*G consecutive row
+// entries and lane l takes entries l, l + G, ..., l + (U-1)G, so at each step the
+// group's lanes read consecutive entries -- usually consecutive slots of one cell,
+// which the gathers then fetch in one or two sectors. The first round's index loads do
+// not wait for the count (rows have 72 slots, entries past the count are masked), so
+// the count, the indices and the particle's own fields are fetched together; within a
+// round the U gathers per lane are independent. Masked entries use the particle itself
+// as a stand-in index. The row and gradient streams are read once per pass, so they
+// are loaded with the evict-first hint (ld.global.cs) to leave L2 to the gathered
+// fields.
 template <uint32_t G, bool WITH_GS, class F>
 __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb, uint32_t self, F&& f) {
-    static_assert(4u * G <= kRow, "first round must stay inside the row");
-    uint32_t q[4];
-    float g[4];
+    constexpr uint32_t U = unroll_for(G);
+    static_assert(U * G <= kRow, "first round must stay inside the row");
+    uint32_t q[U];
+    float g[U];
 #pragma unroll
-    for (uint32_t u = 0; u < 4u; u++) {
-        q[u] = __ldg(nb.row + grp.lane + u * G);
-        g[u] = WITH_GS ? __ldg(nb.gs + grp.lane + u * G) : 0.0f;
+    for (uint32_t u = 0; u < U; u++) {
+        q[u] = __ldcs(nb.row + grp.lane + u * G);
+        g[u] = WITH_GS ? __ldcs(nb.gs + grp.lane + u * G) : 0.0f;
     }
-    for (uint32_t base = 0; base < nb.count; base += 4u * G) {
+    for (uint32_t base = 0; base < nb.count; base += U * G) {
         if (base > 0) {
 #pragma unroll
-            for (uint32_t u = 0; u < 4u; u++) {
+            for (uint32_t u = 0; u < U; u++) {
                 const uint32_t j = base + grp.lane + u * G;
-                q[u] = j < nb.count ? __ldg(nb.row + j) : self;
-                g[u] = (WITH_GS && j < nb.count) ? __ldg(nb.gs + j) : 0.0f;
+                q[u] = j < nb.count ? __ldcs(nb.row + j) : self;
+                g[u] = (WITH_GS && j < nb.count) ? __ldcs(nb.gs + j) : 0.0f;
             }
         }
 #pragma unroll
-        for (uint32_t u = 0; u < 4u; u++) {
+        for (uint32_t u = 0; u < U; u++) {
             const uint32_t j = base + grp.lane + u * G;
             const bool ok = j < nb.count;
             f(ok ? q[u] : self, g[u], j, ok);
@@ -182,7 +188,7 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
         float w, gs;
         kernel_wg(d, r, w, gs);
         if (!ok) return;
-        gsRow[j] = gs;
+        __stcs(gsRow + j, gs);
         wsum += w;
         const float3 gj = (-V * gs) * r;
         g2 += dot3(gj, gj);
