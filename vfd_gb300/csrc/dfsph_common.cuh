@@ -247,7 +247,7 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
 template <int K>
 __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformScene, uint32_t sid, bool valid,
                                                       const double (&v)[K], const int (&slot)[K]) {
-    __shared__ double sm[kBlock / 32][4];
+    __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bucket = blockIdx.x % kBuckets;
     if (uniformScene >= 0) {
@@ -280,7 +280,7 @@ __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformS
 template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, bool valid, const double (&v)[K],
                                                  const int (&slot)[K]) {
-    __shared__ double sm[kBlock / 32][4];
+    __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
     __shared__ int uniformBlock;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t first = blockIdx.x * (blockDim.x / G);
