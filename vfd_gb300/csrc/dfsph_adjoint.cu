@@ -118,13 +118,15 @@ __device__ __forceinline__ float3 hmul(float gs, float gq, float3 r, float3 w) {
 
 struct Row {
     const uint32_t* nbr;
-    const float* gs;
+    const uint2* ng;
     uint32_t count, flags;
 };
 __device__ __forceinline__ Row row_of(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
-    return Row{d.NBR + (size_t)p * kRow, d.GS + (size_t)p * kRow, w & kCountMask, w};
+    return Row{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w};
 }
+// gradW / r of row entry j (the forward's table value).
+__device__ __forceinline__ float row_gs(const Row& rw, uint32_t j) { return __uint_as_float(__ldg(&rw.ng[j].y)); }
 
 __device__ __forceinline__ float4 bd(const AdjDev& a, const Dev& d, uint32_t k, uint32_t b, uint32_t p) {
     return a.BD[((size_t)k * d.maxBodies + b) * d.stride + p];
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const flo
         xi = f3(d.X[p]);
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
             const uint32_t q = __ldg(rw.nbr + j);
-            const float gs = __ldg(rw.gs + j);
+            const float gs = row_gs(rw, j);
             const float3 r = xi - f3(d.X[q]);
             const float kq = kap[q];
             const float sum = ki + kq;
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a, const flo
         }
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
             const uint32_t q = __ldg(rw.nbr + j);
-            const float gsT = __ldg(rw.gs + j);
+            const float gsT = row_gs(rw, j);
             const float3 r = xi - f3(d.X[q]);
             const float s = sqrtf(dot3(r, r));
             float gs, gq;
@@ -321,7 +323,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const flo
         di = a.DBAR[p];
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
             const uint32_t q = __ldg(rw.nbr + j);
-            const float gsT = __ldg(rw.gs + j);
+            const float gsT = row_gs(rw, j);
             const float3 r = xi - f3(d.X[q]);
             const float s = sqrtf(dot3(r, r));
             float gs, gq;
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsum(Dev d, AdjDev a) {
         const float3 xi = f3(d.X[p]);
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
             const uint32_t q = __ldg(rw.nbr + j);
-            const float3 gj = (V * __ldg(rw.gs + j)) * (xi - f3(d.X[q]));
+            const float3 gj = (V * row_gs(rw, j)) * (xi - f3(d.X[q]));
             g += gj;
             g2 += dot3(gj, gj);
         }
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const floa
         lti = (dt / rhoi) * li;
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
             const uint32_t q = __ldg(rw.nbr + j);
-            const float gsT = __ldg(rw.gs + j);
+            const float gsT = row_gs(rw, j);
             const float3 r = xi - f3(d.X[q]);
             const float s2 = dot3(r, r);
             const float s = sqrtf(s2);

@@ -14,8 +14,9 @@
 //   NBR  u32 [slot][72] neighbour slots, one row per particle in the reference's
 //        z, y, x cell order (at most 70 used), read by groups of G lanes
 //   NCNT u32 [slot] neighbour count | flag bits
-//   GS   f32 [slot][72] gradW / r of each pair, written once per step by the density
-//        pass and streamed by every later neighbour loop instead of a table lookup
+//   NG   (u32, f32) [slot][72] the row again with gradW / r of each pair beside each
+//        index, written once per step by the density pass and streamed (one 8-byte load
+//        per pair) by every later neighbour loop instead of a table lookup
 //   X.w  mirrors kappa_v during the divergence solve and kappa during the pressure
 //        solve, so the pressure-acceleration gather brings it with the position
 // The reference keeps one 120-byte AoS DFSPHParticle per particle
@@ -123,7 +124,7 @@ struct Dev {
     float *RHO, *ALPHA, *RHOADV, *KAPPA, *KAPPAV, *RES;
     float4* XB;
     uint32_t *NBR, *NCNT;
-    float* GS;                 // [slot][72] gradW factor of each neighbour pair (row layout)
+    uint2* NG;                 // [slot][72] (neighbour slot, gradW factor bits) of each pair (row layout)
     // search scratch
     uint32_t *KEY, *KEYS, *TMP, *CELL_START, *CELL_COUNT, *FILL, *SCAN;
     // viscosity CG

@@ -95,13 +95,13 @@ __device__ __forceinline__ int chunk_scene(const Dev& d, int loop, uint32_t base
 
 struct Nbr {
     const uint32_t* row;
-    const float* gs;
+    const uint2* ng;
     uint32_t count, flags;
     __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return __ldg(row + j); }
 };
 __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
-    return Nbr{d.NBR + (size_t)p * kRow, d.GS + (size_t)p * kRow, w & kCountMask, w};
+    return Nbr{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w};
 }
 
 // kappa (or kappa_v) of particle p, mirrored into X[p].w for the neighbours' gathers.
@@ -128,16 +128,28 @@ __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb
     float g[U];
 #pragma unroll
     for (uint32_t u = 0; u < U; u++) {
-        q[u] = __ldcs(nb.row + grp.lane + u * G);
-        g[u] = WITH_GS ? __ldcs(nb.gs + grp.lane + u * G) : 0.0f;
+        if (WITH_GS) {
+            const uint2 e = __ldcs(nb.ng + grp.lane + u * G);
+            q[u] = e.x;
+            g[u] = __uint_as_float(e.y);
+        } else {
+            q[u] = __ldcs(nb.row + grp.lane + u * G);
+            g[u] = 0.0f;
+        }
     }
     for (uint32_t base = 0; base < nb.count; base += U * G) {
         if (base > 0) {
 #pragma unroll
             for (uint32_t u = 0; u < U; u++) {
                 const uint32_t j = base + grp.lane + u * G;
-                q[u] = j < nb.count ? __ldcs(nb.row + j) : self;
-                g[u] = (WITH_GS && j < nb.count) ? __ldcs(nb.gs + j) : 0.0f;
+                if (WITH_GS) {
+                    const uint2 e = j < nb.count ? __ldcs(nb.ng + j) : make_uint2(self, 0u);
+                    q[u] = e.x;
+                    g[u] = __uint_as_float(e.y);
+                } else {
+                    q[u] = j < nb.count ? __ldcs(nb.row + j) : self;
+                    g[u] = 0.0f;
+                }
             }
         }
 #pragma unroll
@@ -182,13 +194,13 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     float wsum = 0.0f, g2 = 0.0f;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     const float V = S.volume;
-    float* gsRow = d.GS + (size_t)p * kRow;
+    uint2* ngRow = d.NG + (size_t)p * kRow;
     for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t j, bool ok) {
         const float3 r = xi - f3(d.X[q]);
         float w, gs;
         kernel_wg(d, r, w, gs);
         if (!ok) return;
-        __stcs(gsRow + j, gs);
+        __stcs(ngRow + j, make_uint2(q, __float_as_uint(gs)));
         wsum += w;
         const float3 gj = (-V * gs) * r;
         g2 += dot3(gj, gj);
