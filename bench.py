@@ -256,6 +256,35 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10):
                            "rel_err_v0": abs(g_v - fd_v) / abs(fd_v), "relative_step": eps}}
 
 
+def precision_form(V, scenes, n_side: int = 40, steps: int = 20):
+    """The 1M configuration's parameters at n_side^3 particles: positions after `steps`
+    steps in FP32 with absolute and with cell-relative positions against the FP64
+    oracle from the same FP32 inputs and volume map (the oracle uses all host threads)."""
+    from oracle import oracle as O
+    s = scenes.viscous_dam_break(n_side=n_side)
+    r = s["desc"]["ParticleRadius"]
+    maps = [O.build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"], r) for b in s["boxes"]]
+    O.set_threads(os.cpu_count() or 1)
+    orc = O.scene_oracle(s, 64, maps=maps)
+    for _ in range(steps):
+        orc.step()
+    xo, _, _ = orc.state()
+    out = {"workload": f"viscous dam break parameters, {len(s['x'])} particles, {steps} steps, FP64 oracle "
+                       f"from the same FP32 inputs"}
+    for name, rel in (("absolute", False), ("cell_relative", True)):
+        sim = V.DFSPHSimulation(V.make_desc(**s["desc"]))
+        sim.SetPositionMode(rel)
+        sim.SetFluidObjects(s["x"], s["v"])
+        for m in maps:
+            sim.AddRigidBody(m)
+        st = sim.Steps(steps)
+        x, _, _ = sim.GetState()
+        e = np.linalg.norm(x.astype(np.float64) - xo, axis=1)
+        out[name] = {"max_position_error_m": float(e.max()), "mean_position_error_m": float(e.mean()),
+                     "mean_density_error_pct": 100.0 * st["PressureSolverError"] / 1000.0}
+    return out
+
+
 def cpu_baseline(n_side: int, steps: int, warmup: int):
     """The oracle (FP32, all host threads) on a c2-parameter sample."""
     from oracle import oracle as O
@@ -425,7 +454,8 @@ def main():
     }
     if not args.no_forms:
         line["forms"] = {"batched": batched_form(V, scenes, args.batch_steps, 3, 16),
-                         "fwd_adjoint": adjoint_form(V, scenes)}
+                         "fwd_adjoint": adjoint_form(V, scenes),
+                         "precision": precision_form(V, scenes)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -47,6 +47,11 @@ enum {
 #define VFD_FLAG_NEIGHBOR_CAP    0x8u  /* some particle reached the 70-neighbour cap     */
 #define VFD_FLAG_NAN             0x10u /* non-finite position or velocity                */
 #define VFD_FLAG_GRID_CAPACITY   0x20u /* search grid larger than the cell table         */
+#define VFD_FLAG_ANCHOR_RANGE    0x40u /* cell-relative positions left their anchor range */
+
+/* Position storage modes (vfd_set_position_mode). */
+#define VFD_POSITIONS_ABSOLUTE       0  /* FP32 absolute coordinates, as the reference stores them */
+#define VFD_POSITIONS_CELL_RELATIVE  1  /* FP32 offsets within anchor cells of edge h             */
 
 /* Maximum neighbours per particle, ParticleSearchKernels.cuh:7 (CUDA_MAX_NEIGHBORS). */
 #define VFD_MAX_NEIGHBORS 70u
@@ -399,6 +404,19 @@ int vfd_adjoint_backward(vfd_sim* sim, const float* x_bar, const float* v_bar, f
                          float* param_bar);
 /* Frees the checkpoints and tapes of the recorded run. */
 int vfd_adjoint_release(vfd_sim* sim);
+
+/*
+ * Position storage. No counterpart in the reference, which stores absolute FP32
+ * coordinates (VFD_POSITIONS_ABSOLUTE, the default). VFD_POSITIONS_CELL_RELATIVE stores
+ * each position as its FP32 offset within an anchor cell (a cube of edge h, the support
+ * radius, at integer coordinates from the cell nearest the centre of the scene's initial
+ * positions, at most 511 cells away); every pair vector x_i - x_j is then formed from
+ * offsets and cell differences, so its rounding error scales with h instead of with the
+ * distance from the origin. Inputs and outputs stay absolute. Changing the mode
+ * restarts the simulation from its fluid objects, like vfd_set_description. A particle
+ * leaving the anchor range fails the step with VFD_E_CAPACITY (VFD_FLAG_ANCHOR_RANGE).
+ */
+int vfd_set_position_mode(vfd_sim* sim, int32_t mode);
 
 /* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
 int vfd_set_device(int32_t device);

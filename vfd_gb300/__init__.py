@@ -32,6 +32,7 @@ EXPORTS = [
     "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version", "vfd_profile_kernels",
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
+    "vfd_set_position_mode",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
@@ -114,6 +115,7 @@ def lib() -> C.CDLL:
                 "vfd_adjoint_forward": [P, C.c_uint32, C.c_uint32, C.POINTER(vfd_step_stats)],
                 "vfd_adjoint_backward": [P, f32p, f32p, f32p, f32p, f32p],
                 "vfd_adjoint_release": [P],
+                "vfd_set_position_mode": [P, C.c_int32],
                 "vfd_last_error": [],
                 "vfd_abi_version": [],
             }
@@ -256,6 +258,11 @@ class DFSPHSimulation:
     def AddRigidBody(self, vmap: VolumeMap, scene: int = 0):
         self._maps.append(vmap)
         _check(lib().vfd_scene_add_rigid_body(self._h, scene, C.byref(vmap.struct)), "vfd_scene_add_rigid_body")
+
+    def SetPositionMode(self, cell_relative: bool):
+        """Absolute FP32 positions (the reference's) or cell-relative ones; restarts the run."""
+        _check(lib().vfd_set_position_mode(self._h, _abi.VFD_POSITIONS_CELL_RELATIVE if cell_relative
+                                           else _abi.VFD_POSITIONS_ABSOLUTE), "vfd_set_position_mode")
 
     def SetGraphMode(self, enabled: bool):
         _check(lib().vfd_set_graph_mode(self._h, int(bool(enabled))), "vfd_set_graph_mode")

@@ -11,6 +11,8 @@ from __future__ import annotations
 import ctypes as C
 
 VFD_OK = 0
+VFD_POSITIONS_ABSOLUTE = 0
+VFD_POSITIONS_CELL_RELATIVE = 1
 VFD_E_ARG = 1
 VFD_E_CUDA = 2
 VFD_E_NONCONVERGED = 3

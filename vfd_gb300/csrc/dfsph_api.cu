@@ -59,6 +59,36 @@ __global__ void k_import3(const uint32_t* pid, const float* in, float4* dst, uin
     const float4 w = dst[p];
     dst[p] = make_float4(in[3 * (size_t)o], in[3 * (size_t)o + 1], in[3 * (size_t)o + 2], w.w);
 }
+// Positions out of / into the cell-relative form (Dev::cellRel): absolute FP32
+// coordinates of slots [begin, begin + count) in original order; `anchors` holds each
+// slot's anchor cell in .w (the positions themselves, or the state set whose frame the
+// values of `src` are in).
+__global__ void k_export_pos(Dev d, const float4* src, const float4* anchors, float* out, uint32_t begin,
+                             uint32_t count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t p = begin + k;
+    const uint32_t o = d.PIDc[p];
+    if (o >= count) return;
+    const float4 v = src[p];
+    const float3 x = abs_pos(d, d.scenes[scene_of(d, p)], make_float4(v.x, v.y, v.z, anchors[p].w));
+    out[3 * (size_t)o] = x.x;
+    out[3 * (size_t)o + 1] = x.y;
+    out[3 * (size_t)o + 2] = x.z;
+}
+__global__ void k_import_pos(Dev d, const float* in, float4* dst, uint32_t begin, uint32_t count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t p = begin + k;
+    const uint32_t o = d.PIDc[p];
+    if (o >= count) return;
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    const float L = d.radius;
+    float3 x = make_float3(in[3 * (size_t)o] - S.org[0], in[3 * (size_t)o + 1] - S.org[1], in[3 * (size_t)o + 2] - S.org[2]);
+    const float fx = floorf(x.x / L), fy = floorf(x.y / L), fz = floorf(x.z / L);
+    const int3 A = make_int3((int)fx, (int)fy, (int)fz);
+    dst[p] = make_float4(x.x - fx * L, x.y - fy * L, x.z - fz * L, anchor_pack(A));
+}
 }  // namespace vfd
 
 using namespace vfd;
@@ -230,6 +260,7 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.ACCB, (size_t)base.nscenes * kAccSlots * kBuckets * 16u));
     TRY(dalloc(s, &base.MAXB, (size_t)base.nscenes * 2u * kBuckets * 32u));
     TRY(dalloc(s, &base.MMB, (size_t)base.nscenes * 6u * kBuckets * 32u));
+    base.cellRel = s->cellRel ? 1u : 0u;
     base.workStride = 2u + 2u * base.nscenes;
     TRY(dalloc(s, &base.WORK, 3 * (size_t)base.workStride));
     {
@@ -366,12 +397,40 @@ int upload(vfd_sim* s) {
     for (uint32_t k = 0; k < s->scenes.size(); k++) {
         const SceneHost& sc = s->scenes[k];
         const uint32_t b = s->sceneBegin[k], cnt = (uint32_t)(sc.x0.size() / 3);
+        SceneDev S = scene_constants(sc.desc, b, cnt, bodyBegin, (uint32_t)sc.bodies.size());
+        // cell-relative positions: anchor cells of edge h counted from the cell nearest the
+        // centre of the initial positions
+        double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        for (uint32_t i = 0; i < cnt; i++)
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::min(lo[k], (double)sc.x0[3 * i + k]);
+                hi[k] = std::max(hi[k], (double)sc.x0[3 * i + k]);
+            }
+        const double L = (double)s->table.radius;
+        for (int k = 0; k < 3; k++) S.org[k] = cnt ? (float)(L * std::nearbyint(0.5 * (lo[k] + hi[k]) / L)) : 0.0f;
         for (uint32_t i = 0; i < cnt; i++) {
-            xn[b + i] = make_float4(sc.x0[3 * i], sc.x0[3 * i + 1], sc.x0[3 * i + 2], 0.0f);
+            if (s->cellRel) {
+                double o[3];
+                int a[3];
+                for (int k = 0; k < 3; k++) {
+                    const double rel = (double)sc.x0[3 * i + k] - (double)S.org[k];
+                    a[k] = (int)std::floor(rel / L);
+                    o[k] = rel - a[k] * L;
+                    if (std::abs(a[k]) > 511) return fail(VFD_E_CAPACITY, "cell-relative positions: a particle lies "
+                                                          "more than 511 cells from its scene's centre");
+                }
+                const uint32_t w = (uint32_t)(a[0] & 1023) | ((uint32_t)(a[1] & 1023) << 10) |
+                                   ((uint32_t)(a[2] & 1023) << 20);
+                float wf;
+                std::memcpy(&wf, &w, sizeof(wf));
+                xn[b + i] = make_float4((float)o[0], (float)o[1], (float)o[2], wf);
+            } else {
+                xn[b + i] = make_float4(sc.x0[3 * i], sc.x0[3 * i + 1], sc.x0[3 * i + 2], 0.0f);
+            }
             if (!sc.v0.empty()) v[b + i] = make_float4(sc.v0[3 * i], sc.v0[3 * i + 1], sc.v0[3 * i + 2], 0.0f);
             pid[b + i] = i;
         }
-        s->hScenes.push_back(scene_constants(sc.desc, b, cnt, bodyBegin, (uint32_t)sc.bodies.size()));
+        s->hScenes.push_back(S);
         bodyBegin += (uint32_t)sc.bodies.size();
         if (sc.desc.EnableSurfaceTensionSolver) s->maxStPasses = std::max(s->maxStPasses, sc.desc.SurfaceTensionSmoothPassCount);
         s->anyDiv |= sc.desc.EnableDivergenceSolverError != 0;
@@ -637,6 +696,9 @@ int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
         CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
         if (!s->hStatus[1]) {
             if (stats) fill_stats(s->hScenes[0], stats);
+            if (flags & 0x40u)
+                return fail(VFD_E_CAPACITY, "cell-relative positions: a particle moved more than 511 cells from "
+                                            "its scene's centre");
             return VFD_OK;
         }
         if (flags & 0x10u) return fail(VFD_E_NAN, "non-finite particle position");
@@ -673,6 +735,28 @@ int gather_vec(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
     if (cnt == 0) return VFD_OK;
     CK(cudaMemcpyAsync(s->dStage, in, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyHostToDevice, s->stream));
     k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, s->dStage, ddst, b, cnt);
+    CK(cudaGetLastError());
+    return VFD_OK;
+}
+
+// Positions (absolute in the caller's frame whatever the storage mode).
+int scatter_pos(vfd_sim* s, uint32_t scene, const float4* dsrc, const float4* anchors, float* out) {
+    if (!s->cellRel) return scatter_vec(s, scene, dsrc, out);
+    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    if (cnt == 0) return VFD_OK;
+    k_export_pos<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs], dsrc, anchors, s->dStage, b, cnt);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->dStage, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return VFD_OK;
+}
+
+int gather_pos(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
+    if (!s->cellRel) return gather_vec(s, scene, in, ddst);
+    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    if (cnt == 0) return VFD_OK;
+    CK(cudaMemcpyAsync(s->dStage, in, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyHostToDevice, s->stream));
+    k_import_pos<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs], s->dStage, ddst, b, cnt);
     CK(cudaGetLastError());
     return VFD_OK;
 }
@@ -945,6 +1029,16 @@ int vfd_reset(vfd_sim* s) {
     return upload(s);
 }
 
+int vfd_set_position_mode(vfd_sim* s, int32_t mode) {
+    TRY(check_sim(s));
+    if (mode != VFD_POSITIONS_ABSOLUTE && mode != VFD_POSITIONS_CELL_RELATIVE)
+        return fail(VFD_E_ARG, "unknown position mode %d", mode);
+    CK(cudaSetDevice(s->device));
+    s->cellRel = mode == VFD_POSITIONS_CELL_RELATIVE;
+    s->releaseBuffers();
+    return VFD_OK;
+}
+
 int vfd_set_graph_mode(vfd_sim* s, int32_t enabled) {
     TRY(check_sim(s));
     s->graphMode = enabled != 0;
@@ -1001,7 +1095,7 @@ int vfd_scene_get_state(vfd_sim* s, uint32_t scene, float* x, float* v, float* a
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     const Dev& d = s->dev[s->cs];
-    if (x) TRY(scatter_vec(s, scene, d.XN, x));
+    if (x) TRY(scatter_pos(s, scene, d.XN, d.XN, x));
     if (v) TRY(scatter_vec(s, scene, d.Vc, v));
     if (a) TRY(scatter_vec(s, scene, d.A, a));
     return VFD_OK;
@@ -1012,7 +1106,7 @@ int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     const Dev& d = s->dev[s->cs];
-    if (x) TRY(gather_vec(s, 0, x, d.XN));
+    if (x) TRY(gather_pos(s, 0, x, d.XN));
     if (v) TRY(gather_vec(s, 0, v, d.Vc));
     CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
@@ -1043,7 +1137,7 @@ int vfd_get_field(vfd_sim* s, int32_t field, uint32_t body, float* out) {
         case VFD_FIELD_BOUNDARY_XJ:
         case VFD_FIELD_BOUNDARY_VOLUME:
             if (body >= s->scenes[0].bodies.size()) return fail(VFD_E_ARG, "body %u out of range", body);
-            if (field == VFD_FIELD_BOUNDARY_XJ) return scatter_vec(s, 0, d.XB + (size_t)body * s->stride, out);
+            if (field == VFD_FIELD_BOUNDARY_XJ) return scatter_pos(s, 0, d.XB + (size_t)body * s->stride, d.Xc, out);
             return scatter_scalar(s, 0, nullptr, out, 3, d.XB + (size_t)body * s->stride);
         default:
             (void)cnt;

@@ -18,6 +18,7 @@
 namespace vfd {
 
 // K1: ComputeVolumeAndBoundaryKernel (DFSPHKernels.cu:69-150).
+template <bool REL>
 __global__ void __launch_bounds__(kBlock) k_boundary(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -29,13 +30,26 @@ __global__ void __launch_bounds__(kBlock) k_boundary(Dev d) {
         return;
     }
     float4 x4 = d.X[p];
+    // x: the particle in its own frame (absolute, or its cell offset when positions are
+    // cell-relative; the boundary samples are stored in that frame); xa: absolute, for
+    // the map lookups
+    // (with cell-relative positions the lookups take the position relative to the map's
+    // corner, (origin - corner) + (anchor cell + offset), the first difference exact)
     float3 x = f3(x4);
+    float3 xa = abs_pos(d, S, x4);
+    float3 cell = make_float3(0.f, 0.f, 0.f);
+    if (REL) {
+        const int3 A = anchor_of(x4.w);
+        cell = make_float3(d.radius * (float)A.x + x.x, d.radius * (float)A.y + x.y, d.radius * (float)A.z + x.z);
+    }
     bool moved = false, stopped = false, any = false;
     for (uint32_t b = 0; b < S.bodyCount; b++) {
         const BodyDev& m = d.bodies[S.bodyBegin + b];
         float3 xb = make_float3(0.f, 0.f, 0.f);
         float vb = 0.0f;
-        const MapSample s = map_lookup(m, x);
+        const MapSample s =
+            REL ? map_lookup_rel(m, make_float3(S.org[0] - m.dmin[0], S.org[1] - m.dmin[1], S.org[2] - m.dmin[2]) + cell)
+                : map_lookup(m, xa);
         const float dist = s.inside ? s.phi0 : FLT_MAX;
         float3 normal = s.grad0;
         if (dist > 0.0f && dist < S.h) {
@@ -57,6 +71,8 @@ __global__ void __launch_bounds__(kBlock) k_boundary(Dev d) {
                 normal = make_float3(normal.x / nl, normal.y / nl, normal.z / nl);
                 const float delta = fminf(S.diam - dist, 0.1f * S.r);
                 x += delta * normal;
+                xa += delta * normal;
+                cell += delta * normal;
                 moved = true;
                 stopped = true;
             }
@@ -69,7 +85,12 @@ __global__ void __launch_bounds__(kBlock) k_boundary(Dev d) {
     d.NCNT[p] = flags | (any ? kHasBoundary : 0u);
 }
 
-void launch_boundary(const Dev& d, cudaStream_t s) { k_boundary<<<blocks_for(d.n), kBlock, 0, s>>>(d); }
+// (one instantiation per position storage mode, so that the absolute one compiles to the
+// same arithmetic as before the cell-relative mode existed)
+void launch_boundary(const Dev& d, cudaStream_t s) {
+    if (d.cellRel) k_boundary<true><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    else k_boundary<false><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+}
 
 // ---------------------------------------------------------------- box map builder
 struct BoxMap {

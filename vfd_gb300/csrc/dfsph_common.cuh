@@ -86,6 +86,7 @@ struct SceneDev {
     int32_t minCell[3], maxCell[3];
     float gridMin[3], gridDelta[3];
     uint32_t dim[3], meta[3];
+    float org[3];              // cell-relative positions: corner of anchor cell (0, 0, 0)
     uint32_t cellBase, cellCount;
     uint32_t flags;            // VFD_FLAG_* of the current step
     uint32_t maxNbr;
@@ -132,6 +133,7 @@ struct Dev {
     // surface tension: (normal, curvature), (smoothed normal, smoothed curvature)
     float4 *STN, *STNS;
     uint16_t* SID;
+    uint32_t cellRel;          // 1: positions are cell-relative (precision mode), see pair_r
     SceneDev* scenes;
     BodyDev* bodies;
     const float *WM, *GM;      // midpoint tables 0.5 (T[i] + T[i+1]), i < 9999
@@ -176,6 +178,43 @@ __device__ __forceinline__ float fast_sqrt(float x) {
     float r;
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+}
+
+// -------------------------------------------------------- cell-relative positions
+// Precision mode (Dev::cellRel): a particle's position is X.xyz = its offset from the
+// corner of its anchor cell, a cube of edge h (the support radius) at integer
+// coordinates A from the scene's origin S.org, with A packed in X.w (10 bits per axis,
+// two's complement, |A| < 512). Pair vectors x_i - x_j = (o_i - o_j) + h (A_i - A_j)
+// are then differences of numbers of size h instead of of absolute coordinates.
+// Quantities of one particle (its boundary samples) live in its own offset frame.
+__device__ __forceinline__ int3 anchor_of(float w) {
+    const uint32_t b = __float_as_uint(w);
+    return make_int3((int)(b << 22) >> 22, (int)((b >> 10) << 22) >> 22, (int)((b >> 20) << 22) >> 22);
+}
+__device__ __forceinline__ float anchor_pack(int3 a) {
+    return __uint_as_float((uint32_t)(a.x & 1023) | ((uint32_t)(a.y & 1023) << 10) | ((uint32_t)(a.z & 1023) << 20));
+}
+// x_a - x_b of two particles of one scene; REL: positions are cell-relative (the
+// neighbour-loop kernels are instantiated for both storage modes).
+template <bool REL>
+__device__ __forceinline__ float3 pair_r(const Dev& d, float4 a, float4 b) {
+    float3 r = make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+    if (REL) {
+        const int3 A = anchor_of(a.w), B = anchor_of(b.w);
+        const float L = d.radius;
+        r.x += L * (float)(A.x - B.x);
+        r.y += L * (float)(A.y - B.y);
+        r.z += L * (float)(A.z - B.z);
+    }
+    return r;
+}
+// Absolute position (FP32) of a particle of scene S.
+__device__ __forceinline__ float3 abs_pos(const Dev& d, const SceneDev& S, float4 x) {
+    if (!d.cellRel) return make_float3(x.x, x.y, x.z);
+    const int3 A = anchor_of(x.w);
+    const float L = d.radius;
+    return make_float3(S.org[0] + (L * (float)A.x + x.x), S.org[1] + (L * (float)A.y + x.y),
+                       S.org[2] + (L * (float)A.z + x.z));
 }
 
 // -------------------------------------------------------- SPH kernel lookups

@@ -116,4 +116,38 @@ __device__ __forceinline__ MapSample map_lookup(const BodyDev& m, float3 p) {
     return s;
 }
 
+// The same lookup for a position given relative to the map's domain corner (p - dmin),
+// so that its precision is that of the offset rather than of the absolute coordinates.
+template <bool GRAD1 = false>
+__device__ __forceinline__ MapSample map_lookup_rel(const BodyDev& m, float3 prel) {
+    MapSample s;
+    s.inside = false;
+    s.phi0 = s.phi1 = 0.0f;
+    s.grad0 = make_float3(0.f, 0.f, 0.f);
+    s.grad1 = make_float3(0.f, 0.f, 0.f);
+    const float x[3] = {prel.x, prel.y, prel.z};
+    uint32_t mi[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (!(0.0f <= x[k] && m.dmax[k] - m.dmin[k] >= x[k])) return s;
+        mi[k] = (uint32_t)(m.csi[k] * x[k]);
+        if (mi[k] >= m.res[k]) mi[k] = m.res[k] - 1u;
+    }
+    const uint32_t i = m.res[1] * m.res[0] * mi[2] + m.res[0] * mi[1] + mi[0];
+    const uint32_t j = __ldg(m.cellMap + i);
+    if (j == UINT_MAX) return s;
+    float c0[3], xi[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        c0[k] = 2.0f / m.cs[k];
+        xi[k] = c0[k] * (x[k] - (float)mi[k] * m.cs[k]) - 1.0f;
+    }
+    const float base = 9.f * (xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2]) - 19.f;
+    NodeLoop<32, GRAD1>::run(m, m.cells + (size_t)j * 32u, xi[0], xi[1], xi[2], base, s);
+    s.grad0 = make_float3(s.grad0.x * c0[0], s.grad0.y * c0[1], s.grad0.z * c0[2]);
+    if (GRAD1) s.grad1 = make_float3(s.grad1.x * c0[0], s.grad1.y * c0[1], s.grad1.z * c0[2]);
+    s.inside = true;
+    return s;
+}
+
 }  // namespace vfd

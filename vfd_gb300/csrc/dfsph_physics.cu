@@ -105,7 +105,10 @@ __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
 }
 
 // kappa (or kappa_v) of particle p, mirrored into X[p].w for the neighbours' gathers.
-__device__ __forceinline__ void set_kappa(const Dev& d, uint32_t p, float k) { reinterpret_cast<float*>(d.X)[4 * (size_t)p + 3] = k; }
+// (Cell-relative positions keep their anchor in X.w; the neighbours then read kappa itself.)
+__device__ __forceinline__ void set_kappa(const Dev& d, uint32_t p, float k) {
+    if (!d.cellRel) reinterpret_cast<float*>(d.X)[4 * (size_t)p + 3] = k;
+}
 
 // Row entries per lane and round of a G-lane neighbour loop.
 constexpr uint32_t unroll_for(uint32_t G) { return G == 4u ? 4u : (G == 8u ? 4u : 4u); }
@@ -184,19 +187,20 @@ __device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, floa
 
 // ---------------------------------------------------------------------------
 // K2 + K3: ComputeDensityKernel (:152-187) and ComputeDFSPHFactorKernel (:189-231).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
-    const float3 xi = f3(d.X[p]);
+    const float4 xi4 = d.X[p];
+    const float3 xi = f3(xi4);
     const Nbr nb = neighbors(d, p);
     float wsum = 0.0f, g2 = 0.0f;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     const float V = S.volume;
     uint2* ngRow = d.NG + (size_t)p * kRow;
     for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t j, bool ok) {
-        const float3 r = xi - f3(d.X[q]);
+        const float3 r = pair_r<REL>(d, xi4, d.X[q]);
         float w, gs;
         kernel_wg(d, r, w, gs);
         if (!ok) return;
@@ -232,12 +236,12 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
 }
 
 // Sum_j (vi - vj) . gradW_ij * V + vi . GB  (K4 :498-522, K17 :253-271); valid on lane 0.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
-                                                     const Nbr& nb, float3 xi, float3 vi) {
+                                                     const Nbr& nb, float4 xi, float3 vi) {
     float s = 0.0f;
     for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
-        const float3 r = xi - f3(d.X[q]);
+        const float3 r = pair_r<REL>(d, xi, d.X[q]);
         const float3 vq = f3(d.V[q]);
         const float t = dot3(vi - vq, gs * r);
         if (ok) s += t;
@@ -248,14 +252,14 @@ __device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G
 }
 
 // K4: ComputeDensityChangeKernel (:483-529).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableDiv) return;
     const Nbr nb = neighbors(d, p);
-    float rhoAdv = velocity_divergence<G>(d, grp, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    float rhoAdv = velocity_divergence<G, REL>(d, grp, p, S, nb, d.X[p], f3(d.V[p]));
     if (grp.lane != 0) return;
     rhoAdv = nb.count < 20u ? 0.0f : fmaxf(rhoAdv, 0.0f);
     d.RHOADV[p] = rhoAdv;
@@ -267,18 +271,18 @@ __global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
 
 // Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481);
 // valid on lane 0.
-template <bool DIV, uint32_t G>
+template <bool DIV, uint32_t G, bool REL>
 __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
                                                  const Nbr& nb) {
     const float* kap = DIV ? d.KAPPAV : d.KAPPA;
     const float ki = kap[p];
-    const float3 xi = f3(d.X[p]);
+    const float4 xi = d.X[p];
     const float V = S.volume;
     float3 a = make_float3(0.f, 0.f, 0.f);
     for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float4 xq = d.X[q];
-        const float sum = ki + xq.w;
-        const float3 r = xi - f3(xq);
+        const float sum = ki + (REL ? kap[q] : xq.w);
+        const float3 r = pair_r<REL>(d, xi, xq);
         if (ok && fabsf(sum) > kEps) a += (sum * (-V * gs)) * r;
     });
     a = grp.sum(a);
@@ -287,19 +291,19 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
 }
 
 // K5 / K18.
-template <bool DIV, uint32_t G>
+template <bool DIV, uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!(DIV ? S.div.active : S.pres.active)) return;
     const Nbr nb = neighbors(d, p);
-    const float3 a = pressure_accel<DIV, G>(d, grp, p, S, nb);
+    const float3 a = pressure_accel<DIV, G, REL>(d, grp, p, S, nb);
     if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
 }
 
 // K5 / K18 of a batch: the scenes still iterating, from the loop's work list.
-template <bool DIV, uint32_t G>
+template <bool DIV, uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_pressure_accel_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted_p(d)) return;
@@ -311,22 +315,22 @@ __global__ void __launch_bounds__(kBlock) k_pressure_accel_b(Dev d) {
         const uint32_t p = work_slot(d, L, vp, sid);
         const Group<G> grp(p);
         const Nbr nb = neighbors(d, p);
-        const float3 a = pressure_accel<DIV, G>(d, grp, p, d.scenes[sid], nb);
+        const float3 a = pressure_accel<DIV, G, REL>(d, grp, p, d.scenes[sid], nb);
         if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
     }
 }
 
 // K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
 // each with ComputeDensityPressureForce (:280-315) and the FP64 residual sum.
-template <bool DIV, uint32_t G>
+template <bool DIV, uint32_t G, bool REL>
 __device__ __forceinline__ double jacobi_item(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S) {
     double res = 0.0;
     const Nbr nb = neighbors(d, p);
-    const float3 xi = f3(d.X[p]);
+    const float4 xi = d.X[p];
     const float3 ai = f3(d.AP[p]);
     float f = 0.0f;
     for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
-        const float3 r = xi - f3(d.X[q]);
+        const float3 r = pair_r<REL>(d, xi, d.X[q]);
         const float3 aq = f3(d.AP[q]);
         const float t = dot3(ai - aq, gs * r);
         if (ok) f += t;
@@ -354,7 +358,7 @@ __device__ __forceinline__ double jacobi_item(const Dev& d, const Group<G>& grp,
     return res;
 }
 
-template <bool DIV, uint32_t G>
+template <bool DIV, uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
@@ -364,14 +368,14 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
     const SceneDev& S = d.scenes[sid];
     const bool active = inRange && (DIV ? S.div.active : S.pres.active);
     double res = 0.0;
-    if (active) res = jacobi_item<DIV, G>(d, grp, p, S);
+    if (active) res = jacobi_item<DIV, G, REL>(d, grp, p, S);
     const double v[1] = {res};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
 }
 
 // The same for a batch (work list of the loop).
-template <bool DIV, uint32_t G>
+template <bool DIV, uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted_p(d)) return;
@@ -384,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
         double res = 0.0;
         if (in) {
             const Group<G> grp(p);
-            res = jacobi_item<DIV, G>(d, grp, p, d.scenes[sid]);
+            res = jacobi_item<DIV, G, REL>(d, grp, p, d.scenes[sid]);
         }
         const double v[1] = {res};
         const int slot[1] = {0};
@@ -449,14 +453,14 @@ __global__ void k_ctrl_jacobi(Dev d) {
 }
 
 // K7 ComputePressureAccelerationAndFactorKernel (:555-602) + K8 ClearAccelerationKernel (:24-37).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_div_finish(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (S.enableDiv) {
         const Nbr nb = neighbors(d, p);
-        const float3 a = pressure_accel<true, G>(d, grp, p, S, nb);
+        const float3 a = pressure_accel<true, G, REL>(d, grp, p, S, nb);
         if (grp.lane == 0) {
             d.AP[p] = f4(a, 0.0f);
             const float4 v = d.V[p];
@@ -471,20 +475,20 @@ __global__ void __launch_bounds__(kBlock) k_div_finish(Dev d) {
 // Surface tension (DFSPHImplementation.cu:810-839).
 // K9: ComputeSurfaceTensionClassificationKernel (DFSPHKernels.cu:881-958); the
 // Monte-Carlo samples are split over the group's lanes.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableST) return;
     const Nbr nb = neighbors(d, p);
-    const float3 xi = f3(d.X[p]);
+    const float4 xi = d.X[p];
     if (nb.count == 0) {
         if (grp.lane == 0) d.STN[p] = make_float4(0.f, 0.f, 0.f, 1.0f / S.h);
         return;
     }
     float3 com = make_float3(0.f, 0.f, 0.f);
-    for (uint32_t j = grp.lane; j < nb.count; j += G) com += f3(d.X[nb[j]]) - xi;
+    for (uint32_t j = grp.lane; j < nb.count; j += G) com += pair_r<REL>(d, d.X[nb[j]], xi);
     com = grp.sum(com);
     com = make_float3(com.x / S.h, com.y / S.h, com.z / S.h);
     const float input = sqrtf(dot3(com, com)) / (float)nb.count;
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
                                                 __ldg(d.halton + (i3 + 2u) % kHaltonCount));
             bool covered = false;
             for (uint32_t j = 0; j < nb.count; j++) {
-                const float3 v = pt - (f3(d.X[nb[j]]) - xi);
+                const float3 v = pt - pair_r<REL>(d, d.X[nb[j]], xi);
                 if (dot3(v, v) <= lim) { covered = true; break; }
             }
             if (!covered) { nsum += pt; count++; }
@@ -524,7 +528,7 @@ __global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
 __device__ __forceinline__ bool nonzero3(float4 a) { return a.x != 0.0f || a.y != 0.0f || a.z != 0.0f; }
 
 // K10: ComputeSurfaceTensionNormalsAndCurvatureKernel (:960-1006).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
@@ -533,12 +537,12 @@ __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
     const float4 ni = d.STN[p];
     if (!nonzero3(ni)) return;
     const Nbr nb = neighbors(d, p);
-    const float3 xi = f3(d.X[p]);
+    const float4 xi = d.X[p];
     float3 nc = make_float3(0.f, 0.f, 0.f);
     float cc = 0.0f, cf = 0.0f;
     for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t, bool ok) {
         const float4 nj = d.STN[q];
-        const float3 dx = f3(d.X[q]) - xi;
+        const float3 dx = pair_r<REL>(d, d.X[q], xi);
         if (ok && nonzero3(nj)) {
             const float num = 1.0f - __fdividef(fast_sqrt(dot3(dx, dx)), S.h);
             nc += f3(nj) * num;
@@ -619,19 +623,20 @@ __device__ __forceinline__ Mat3 inverse3(const Mat3& a) {  // cofactors / determ
 // (:686-756, whose boundary term dots a zero vector: b = v) + the boundary matrix BV of
 // the SpMV's boundary term (:793-839): BV p_i = sum_k c_k (p_i . d_k) gradW_k.
 // CG.w and CP.w hold m / rho (read by the SpMV's neighbours) from here on.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!S.enableVisc) return;
     const Nbr nb = neighbors(d, p);
-    const float3 xi = f3(d.X[p]);
+    const float4 xi4 = d.X[p];
+    const float3 xi = f3(xi4);  // own frame of the boundary samples
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     Mat3 m = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
     for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
-        const float3 r = xi - f3(d.X[q]);
+        const float3 r = pair_r<REL>(d, xi4, d.X[q]);
         const float rho = d.RHO[q];
         if (!ok) return;
         const float3 g = gs * r;
@@ -689,16 +694,16 @@ __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
 }
 
 // ComputeMatrixVecProdFunctionKernel (:758-842): (A x)_i with vec[q].w = m / rho_q; lane 0.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
                                               const float4* vec, float3 vi) {
     const Nbr nb = neighbors(d, p);
-    const float3 xi = f3(d.X[p]);
+    const float4 xi = d.X[p];
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     float3 acc = make_float3(0.f, 0.f, 0.f);
     for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
-        const float3 r = xi - f3(d.X[q]);
+        const float3 r = pair_r<REL>(d, xi, d.X[q]);
         const float4 vq = vec[q];
         const float r2 = dot3(r, r);
         const float3 t = (__fdividef(cmu * vq.w * dot3(vi - f3(vq), r), r2 + eps2) * gs) * r;
@@ -710,7 +715,7 @@ __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp,
 }
 
 // Initial residual r = b - A g and the norms |b|^2, |r|^2 (:627-669).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
@@ -722,7 +727,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
     double bb = 0.0, rr = 0.0;
     if (valid) {
         const float4 g4 = d.CG[p];
-        const float3 ag = visc_matvec<G>(d, grp, p, S, d.CG, f3(g4));
+        const float3 ag = visc_matvec<G, REL>(d, grp, p, S, d.CG, f3(g4));
         if (grp.lane == 0) {
             const float3 b = f3(d.CB[p]);
             const float3 r = b - ag;
@@ -806,7 +811,7 @@ __global__ void k_ctrl_cg1(Dev d) {
 }
 
 // Loop body 1: Ap and p . Ap (:695-720).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
@@ -818,7 +823,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
     double pap = 0.0;
     if (valid) {
         const float3 pv = f3(d.CP[p]);
-        const float3 ap = visc_matvec<G>(d, grp, p, S, d.CP, pv);
+        const float3 ap = visc_matvec<G, REL>(d, grp, p, S, d.CP, pv);
         if (grp.lane == 0) {
             d.CAP[p] = f4(ap, 0.0f);
             pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
@@ -830,7 +835,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
 }
 
 // Loop body 1 of a batch.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted_p(d)) return;
@@ -843,7 +848,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
         if (in) {
             const Group<G> grp(p);
             const float3 pv = f3(d.CP[p]);
-            const float3 ap = visc_matvec<G>(d, grp, p, d.scenes[sid], d.CP, pv);
+            const float3 ap = visc_matvec<G, REL>(d, grp, p, d.scenes[sid], d.CP, pv);
             if (grp.lane == 0) {
                 d.CAP[p] = f4(ap, 0.0f);
                 pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
@@ -1026,13 +1031,13 @@ __global__ void __launch_bounds__(kBlock) k_velocity(Dev d) {
 }
 
 // K17 ComputeDensityAdvectionKernel (:233-278).
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     const Nbr nb = neighbors(d, p);
-    const float delta = velocity_divergence<G>(d, grp, p, S, nb, f3(d.X[p]), f3(d.V[p]));
+    const float delta = velocity_divergence<G, REL>(d, grp, p, S, nb, d.X[p], f3(d.V[p]));
     if (grp.lane != 0) return;
     const float rhoAdv = d.RHO[p] / S.rho0 + S.dt * delta;
     d.RHOADV[p] = rhoAdv;
@@ -1045,20 +1050,33 @@ __global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
 
 // K20 ComputePressureAccelerationAndVelocityKernel (:434-481) + K21 ComputePositionKernel (:54-67);
 // positions go to XN so that the neighbours' positions read here stay unchanged.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_pres_finish(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     const Nbr nb = neighbors(d, p);
-    const float3 a = pressure_accel<false, G>(d, grp, p, S, nb);
+    const float3 a = pressure_accel<false, G, REL>(d, grp, p, S, nb);
     if (grp.lane != 0) return;
     d.AP[p] = f4(a, 0.0f);
     const float3 v = f3(d.V[p]) + S.dt * a;
     d.V[p] = f4(v, 0.0f);
-    const float3 x = f3(d.X[p]) + S.dt * v;
-    d.XN[p] = f4(x, 0.0f);
+    const float4 x4 = d.X[p];
+    float3 x = f3(x4) + S.dt * v;
     if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(d.status, 0x10u);
+    if (d.cellRel) {  // back into [0, h) of a (possibly new) anchor cell
+        const float L = d.radius;
+        int3 A = anchor_of(x4.w);
+        const float fx = floorf(x.x / L), fy = floorf(x.y / L), fz = floorf(x.z / L);
+        if (isfinite(x.x) && isfinite(x.y) && isfinite(x.z)) {
+            A = make_int3(A.x + (int)fx, A.y + (int)fy, A.z + (int)fz);
+            x = make_float3(x.x - fx * L, x.y - fy * L, x.z - fz * L);
+            if (abs(A.x) > 511 || abs(A.y) > 511 || abs(A.z) > 511) atomicOr(d.status, 0x40u);
+        }
+        d.XN[p] = f4(x, anchor_pack(A));
+    } else {
+        d.XN[p] = f4(x, 0.0f);
+    }
 }
 
 // End of step: frame clock and iteration counter (DFSPHImplementation.cu:148-169);
@@ -1082,69 +1100,94 @@ __global__ void k_ctrl_end(Dev d) {
 }
 
 // ---------------------------------------------------------------- launchers
-#define K_DENSITY(G) k_density_factor<G>
-#define K_DIV_INIT(G) k_div_init<G>
-#define K_PACCEL_D(G) k_pressure_accel<true, G>
-#define K_PACCEL_P(G) k_pressure_accel<false, G>
-#define K_JACOBI_D(G) k_jacobi_iter<true, G>
-#define K_JACOBI_P(G) k_jacobi_iter<false, G>
-#define K_DIV_FINISH(G) k_div_finish<G>
-#define K_ST_CLASSIFY(G) k_st_classify<G>
-#define K_ST_SMOOTH(G) k_st_smooth<G>
-#define K_VISC_PRECOND(G) k_visc_precond<G>
-#define K_VISC_SETUP(G) k_visc_setup<G>
-#define K_SPMV(G) k_cg_spmv<G>
-#define K_PRES_INIT(G) k_pres_init<G>
-#define K_PRES_FINISH(G) k_pres_finish<G>
+// The instantiation for the position storage mode (K and its _R variant).
+#define VFD_LAUNCH_MODE(LAUNCHER, name, id, K) \
+    do {                                       \
+        if (d.cellRel) LAUNCHER(name, id, K##_R); \
+        else LAUNCHER(name, id, K);           \
+    } while (0)
+#define K_DENSITY(G) k_density_factor<G, false>
+#define K_DENSITY_R(G) k_density_factor<G, true>
+#define K_DIV_INIT(G) k_div_init<G, false>
+#define K_DIV_INIT_R(G) k_div_init<G, true>
+#define K_PACCEL_D(G) k_pressure_accel<true, G, false>
+#define K_PACCEL_D_R(G) k_pressure_accel<true, G, true>
+#define K_PACCEL_P(G) k_pressure_accel<false, G, false>
+#define K_PACCEL_P_R(G) k_pressure_accel<false, G, true>
+#define K_JACOBI_D(G) k_jacobi_iter<true, G, false>
+#define K_JACOBI_D_R(G) k_jacobi_iter<true, G, true>
+#define K_JACOBI_P(G) k_jacobi_iter<false, G, false>
+#define K_JACOBI_P_R(G) k_jacobi_iter<false, G, true>
+#define K_DIV_FINISH(G) k_div_finish<G, false>
+#define K_DIV_FINISH_R(G) k_div_finish<G, true>
+#define K_ST_CLASSIFY(G) k_st_classify<G, false>
+#define K_ST_CLASSIFY_R(G) k_st_classify<G, true>
+#define K_ST_SMOOTH(G) k_st_smooth<G, false>
+#define K_ST_SMOOTH_R(G) k_st_smooth<G, true>
+#define K_VISC_PRECOND(G) k_visc_precond<G, false>
+#define K_VISC_PRECOND_R(G) k_visc_precond<G, true>
+#define K_VISC_SETUP(G) k_visc_setup<G, false>
+#define K_VISC_SETUP_R(G) k_visc_setup<G, true>
+#define K_SPMV(G) k_cg_spmv<G, false>
+#define K_SPMV_R(G) k_cg_spmv<G, true>
+#define K_PRES_INIT(G) k_pres_init<G, false>
+#define K_PRES_INIT_R(G) k_pres_init<G, true>
+#define K_PRES_FINISH(G) k_pres_finish<G, false>
+#define K_PRES_FINISH_R(G) k_pres_finish<G, true>
 
-void launch_density(const Dev& d, cudaStream_t s) { VFD_LAUNCH_LANES("k_density_factor", kTDensity, K_DENSITY); }
+void launch_density(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY); }
 void launch_div_init(const Dev& d, cudaStream_t s) {
-    VFD_LAUNCH_LANES("k_div_init", kTDivInit, K_DIV_INIT);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_div_init", kTDivInit, K_DIV_INIT);
     VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d));
 }
-#define K_PACCEL_DB(G) k_pressure_accel_b<true, G>
-#define K_PACCEL_PB(G) k_pressure_accel_b<false, G>
-#define K_JACOBI_DB(G) k_jacobi_iter_b<true, G>
-#define K_JACOBI_PB(G) k_jacobi_iter_b<false, G>
-#define K_SPMV_B(G) k_cg_spmv_b<G>
+#define K_PACCEL_DB(G) k_pressure_accel_b<true, G, false>
+#define K_PACCEL_DB_R(G) k_pressure_accel_b<true, G, true>
+#define K_PACCEL_PB(G) k_pressure_accel_b<false, G, false>
+#define K_PACCEL_PB_R(G) k_pressure_accel_b<false, G, true>
+#define K_JACOBI_DB(G) k_jacobi_iter_b<true, G, false>
+#define K_JACOBI_DB_R(G) k_jacobi_iter_b<true, G, true>
+#define K_JACOBI_PB(G) k_jacobi_iter_b<false, G, false>
+#define K_JACOBI_PB_R(G) k_jacobi_iter_b<false, G, true>
+#define K_SPMV_B(G) k_cg_spmv_b<G, false>
+#define K_SPMV_B_R(G) k_cg_spmv_b<G, true>
 
 // Batches run the solver-loop kernels over their work lists (the scenes still
 // iterating) with a fixed grid; a single scene keeps one group per particle.
 void launch_div_iter(const Dev& d, cudaStream_t s) {
     if (d.nscenes > 1) {
-        VFD_LAUNCH_LANES_BATCH("k_pressure_accel", kTPAccel, K_PACCEL_DB);
-        VFD_LAUNCH_LANES_BATCH("k_jacobi_iter", kTJacobi, K_JACOBI_DB);
+        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_pressure_accel", kTPAccel, K_PACCEL_DB);
+        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_DB);
         VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
         return;
     }
-    VFD_LAUNCH_LANES("k_pressure_accel", kTPAccel, K_PACCEL_D);
-    VFD_LAUNCH_LANES("k_jacobi_iter", kTJacobi, K_JACOBI_D);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_D);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_D);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
 }
-void launch_div_finish(const Dev& d, cudaStream_t s) { VFD_LAUNCH_LANES("k_div_finish", kTDivFinish, K_DIV_FINISH); }
+void launch_div_finish(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_div_finish", kTDivFinish, K_DIV_FINISH); }
 void launch_surface_tension(const Dev& d, uint32_t maxPasses, cudaStream_t s) {
-    VFD_LAUNCH_LANES("k_st_classify", kTStClassify, K_ST_CLASSIFY);
-    VFD_LAUNCH_LANES("k_st_smooth", kTStSmooth, K_ST_SMOOTH);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_st_classify", kTStClassify, K_ST_CLASSIFY);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_st_smooth", kTStSmooth, K_ST_SMOOTH);
     for (uint32_t pass = 0; pass < maxPasses; pass++)
         VFD_LAUNCH("k_st_blend", s, k_st_blend<<<blocks_for(d.n), kBlock, 0, s>>>(d, pass));
 }
 void launch_visc_init(const Dev& d, cudaStream_t s) {
-    VFD_LAUNCH_LANES("k_visc_precond", kTViscPrecond, K_VISC_PRECOND);
-    VFD_LAUNCH_LANES("k_visc_setup", kTViscSetup, K_VISC_SETUP);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_visc_precond", kTViscPrecond, K_VISC_PRECOND);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_visc_setup", kTViscSetup, K_VISC_SETUP);
     VFD_LAUNCH("k_ctrl_cg0", s, k_ctrl_cg0<<<1, 256, 0, s>>>(d));
     VFD_LAUNCH("k_cg_p0", s, k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_ctrl_cg1", s, k_ctrl_cg1<<<1, 256, 0, s>>>(d));
 }
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
     if (d.nscenes > 1) {
-        VFD_LAUNCH_LANES_BATCH("k_cg_spmv", kTSpmv, K_SPMV_B);
+        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_cg_spmv", kTSpmv, K_SPMV_B);
         VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
         VFD_LAUNCH("k_cg_update", s, k_cg_update_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
         VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
         VFD_LAUNCH("k_cg_p", s, k_cg_p_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
         return;
     }
-    VFD_LAUNCH_LANES("k_cg_spmv", kTSpmv, K_SPMV);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV);
     VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     VFD_LAUNCH("k_cg_update", s, k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
@@ -1156,22 +1199,22 @@ void launch_visc_finish_dt(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_velocity", s, k_velocity<<<blocks_for(d.n), kBlock, 0, s>>>(d));
 }
 void launch_pres_init(const Dev& d, cudaStream_t s) {
-    VFD_LAUNCH_LANES("k_pres_init", kTPresInit, K_PRES_INIT);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pres_init", kTPresInit, K_PRES_INIT);
     VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_iter(const Dev& d, cudaStream_t s) {
     if (d.nscenes > 1) {
-        VFD_LAUNCH_LANES_BATCH("k_pressure_accel", kTPAccel, K_PACCEL_PB);
-        VFD_LAUNCH_LANES_BATCH("k_jacobi_iter", kTJacobi, K_JACOBI_PB);
+        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_pressure_accel", kTPAccel, K_PACCEL_PB);
+        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_PB);
         VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
         return;
     }
-    VFD_LAUNCH_LANES("k_pressure_accel", kTPAccel, K_PACCEL_P);
-    VFD_LAUNCH_LANES("k_jacobi_iter", kTJacobi, K_JACOBI_P);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_P);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_P);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_finish(const Dev& d, cudaStream_t s) {
-    VFD_LAUNCH_LANES("k_pres_finish", kTPresFinish, K_PRES_FINISH);
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pres_finish", kTPresFinish, K_PRES_FINISH);
     VFD_LAUNCH("k_ctrl_end", s, k_ctrl_end<<<1, 256, 0, s>>>(d));
 }
 

@@ -44,7 +44,8 @@ __global__ void __launch_bounds__(kBlock) k_minmax(Dev d) {
     int c[3] = {INT_MAX, INT_MAX, INT_MAX};
     int cmax[3] = {INT_MIN, INT_MIN, INT_MIN};
     if (valid) {
-        const float4 x = d.XN[i];
+        const float4 x4 = d.XN[i];
+        const float3 x = abs_pos(d, d.scenes[sid], x4);
         const float h = d.scenes[sid].h;
         const bool finite = isfinite(x.x) && isfinite(x.y) && isfinite(x.z);
         if (!finite) {
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(Dev d) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n || aborted(d)) return;
     const SceneDev& S = d.scenes[scene_of(d, i)];
-    const float4 x = d.XN[i];
+    const float3 x = abs_pos(d, S, d.XN[i]);
     const float p[3] = {x.x, x.y, x.z};
     int c[3];
 #pragma unroll
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(Dev d) {
 // hits with a ballot, so the row keeps the reference's order (z, y, x cells, then cell
 // order) and its cap of 70. The squared distance is computed without contraction,
 // x^2 + y^2 + z^2 left to right, as the FP32 oracle does.
-template <uint32_t G>
+template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
@@ -322,7 +323,8 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
     const uint32_t sid = scene_of(d, p);
     const SceneDev& S = d.scenes[sid];
     const float4 xi = d.X[p];
-    const float pos[3] = {xi.x, xi.y, xi.z};
+    const float3 xa = abs_pos(d, S, xi);
+    const float pos[3] = {xa.x, xa.y, xa.z};
     int gc[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) gc[k] = (int)floorf(__fmul_rn(__fsub_rn(pos[k], S.gridMin[k]), S.gridDelta[k]));
@@ -343,8 +345,8 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                     const uint32_t q = base + grp.lane;
                     bool hit = false;
                     if (q < end) {
-                        const float4 xj = d.X[q];
-                        const float ex = __fsub_rn(xj.x, xi.x), ey = __fsub_rn(xj.y, xi.y), ez = __fsub_rn(xj.z, xi.z);
+                        const float3 e = pair_r<REL>(d, d.X[q], xi);
+                        const float ex = e.x, ey = e.y, ez = e.z;
                         const float d2 =
                             __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
                         hit = d2 < h2 && d2 > 0.0f;
@@ -390,8 +392,10 @@ void launch_search(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_scan_down", s, k_scan_down<<<d.scanBlocks, 256, 0, s>>>(d));
     VFD_LAUNCH("k_slots", s, k_slots<<<nb, kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_rank_gather", s, k_rank_gather<<<nb, kBlock, 0, s>>>(d));
-#define K_NEIGHBORS(G) k_neighbors<G>
-    VFD_LAUNCH_LANES("k_neighbors", kTNeighbors, K_NEIGHBORS);
+#define K_NEIGHBORS(G) k_neighbors<G, false>
+#define K_NEIGHBORS_R(G) k_neighbors<G, true>
+    if (d.cellRel) VFD_LAUNCH_LANES("k_neighbors", kTNeighbors, K_NEIGHBORS_R);
+    else VFD_LAUNCH_LANES("k_neighbors", kTNeighbors, K_NEIGHBORS);
 }
 
 uint32_t scan_block_count(uint32_t cellCap) { return (cellCap + kScanItems - 1) / kScanItems; }

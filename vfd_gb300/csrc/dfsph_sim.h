@@ -140,6 +140,7 @@ struct vfd_sim {
     vfd::host::KernelTable table;
     std::vector<float> halton;
     bool graphMode = true;
+    bool cellRel = false;  // VFD_POSITIONS_CELL_RELATIVE
     bool graphFailed = false;
     uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
 
