@@ -18,7 +18,8 @@ cpu_baseline: the CPU restatement of the reference method (oracle, FP32, all
         host threads) on a 64k-particle sample of the same configuration.
 --impl reference: that CPU restatement alone (the reference has no CPU DFSPH and
         its CUDA path needs Windows headers and a missing glm submodule).
-Multi-GPU: replicas only (one independent scene per rank, weak scaling).
+Multi-GPU: replicas of the 1M scene (one per rank, weak scaling); the batched form splits
+its 256 scenes across the ranks by particle count.
 """
 from __future__ import annotations
 
@@ -157,12 +158,18 @@ def c2_config(n_side: int) -> dict:
             "l2": "inputs larger than L2 (state ~0.5 GB for 1M particles)"}
 
 
-def batched_form(V, scenes, steps: int, warmup: int, plain_every: int):
+def batched_form(V, scenes, steps: int, warmup: int, plain_every: int, ws: int = 1, rank: int = 0):
     """The uneven-scene batch (256 scenes, 2k-64k particles each) advanced as one
     simulation, against the plain step run scene by scene on every `plain_every`-th
-    scene. Both in particle-steps/s, timed with CUDA events on the library's stream."""
+    scene. Both in particle-steps/s, timed with CUDA events on the library's stream.
+    With several ranks the scenes are split by particle count (vfd_gb300.partition),
+    each rank advances its share as one batch, and the whole batch's particle-steps are
+    divided by the slowest rank's time."""
     import torch
-    batch = scenes.uneven_batch()
+    from vfd_gb300 import partition
+    full = scenes.uneven_batch()
+    costs = [len(s["x"]) for s in full]
+    idx, batch = partition.local_scenes(full, rank, ws, costs)
     counts = [len(s["x"]) for s in batch]
     maps = [[V.build_box_map(b["min"], b["max"], b["inverted"], b["padding"], b["resolution"],
                              s["desc"]["ParticleRadius"]) for b in s["boxes"]] for s in batch]
@@ -180,9 +187,19 @@ def batched_form(V, scenes, steps: int, warmup: int, plain_every: int):
         return e0.elapsed_time(e1)
 
     sim = V.batch_simulation(batch, maps)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
     ms_b = run(sim, steps)
     errs = [sim.GetDebugInfo(scene=k)["PressureSolverError"] for k in range(len(batch))]
     del sim
+    if ws > 1:
+        t = torch.tensor([ms_b, max(errs)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        parts = partition.assign(costs, ws)
+        return {"workload": f"{len(full)} uneven scenes over {ws} ranks ({sum(costs)} particles)", "steps": steps,
+                "batched": sum(costs) * steps / (float(t[0]) / 1e3), "batched_ms_per_step": float(t[0]) / steps,
+                "rank_imbalance": partition.imbalance(costs, parts), "max_pressure_error": float(t[1])}
     plain_n, plain_ms = 0, 0.0
     for k in range(0, len(batch), plain_every):
         one = V.scene_simulation(batch[k], maps=maps[k])
@@ -453,9 +470,10 @@ def main():
         "mean_density_error_pct": 100.0 * st["PressureSolverError"] / 1000.0,
     }
     if not args.no_forms:
-        line["forms"] = {"batched": batched_form(V, scenes, args.batch_steps, 3, 16),
-                         "fwd_adjoint": adjoint_form(V, scenes),
-                         "precision": precision_form(V, scenes)}
+        line["forms"] = {"batched": batched_form(V, scenes, args.batch_steps, 3, 16, ws, rank)}
+        if ws == 1:
+            line["forms"]["fwd_adjoint"] = adjoint_form(V, scenes)
+            line["forms"]["precision"] = precision_form(V, scenes)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
