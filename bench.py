@@ -249,6 +249,10 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10):
     t0 = time.perf_counter()
     sim.Steps(steps)
     t_fwd = time.perf_counter() - t0
+    restart()  # warm-up of the adjoint (its tape, checkpoints and graphs are allocated once)
+    sim.AdjointForward(steps, every)
+    x, v, _ = sim.GetState()
+    sim.AdjointBackward(np.zeros_like(x), np.zeros_like(v))
     restart()
     t0 = time.perf_counter()
     sim.AdjointForward(steps, every)

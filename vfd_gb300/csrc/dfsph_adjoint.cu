@@ -64,6 +64,8 @@ struct AdjDev {
     float4 *GBAR, *GSUM;      // viscosity-solution cotangent; (sum gradW + GB, S bar)
     float4* BD;               // [3][body][stride]: (n, Vb), (grad pd, pd), (grad Vb, -)
     float *KBAR, *U, *RABAR, *APBAR, *DBAR, *RHOBAR, *ALBAR;
+    float2* KU;               // (kappa^k, U) of the Jacobi iteration being differentiated
+    float4* LAM;              // last adjoint viscosity solution (initial guess of the next solve)
     uint32_t* STOP;           // 1 where the boundary zeroed the velocity
     double* SC;               // [0] dt_o bar, [1] dt_n bar, [2] Viscosity bar, [3] BoundaryViscosity bar
     uint32_t* CLAIM;          // [0] largest recomputed CFL |w|^2 (bits), [1] argmax claimed
@@ -125,8 +127,12 @@ __device__ __forceinline__ Row row_of(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
     return Row{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w};
 }
-// gradW / r of row entry j (the forward's table value).
-__device__ __forceinline__ float row_gs(const Row& rw, uint32_t j) { return __uint_as_float(__ldg(&rw.ng[j].y)); }
+// Row entry j: neighbour slot and its gradW / r (the forward's table value), one load.
+__device__ __forceinline__ uint32_t row_entry(const Row& rw, uint32_t j, float& gs) {
+    const uint2 e = __ldg(rw.ng + j);
+    gs = __uint_as_float(e.y);
+    return e.x;
+}
 
 __device__ __forceinline__ float4 bd(const AdjDev& a, const Dev& d, uint32_t k, uint32_t b, uint32_t p) {
     return a.BD[((size_t)k * d.maxBodies + b) * d.stride + p];
@@ -230,17 +236,29 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const flo
     float3 xi = acc;
     if (live) {
         rw = row_of(d, p);
-        ki = kap[p];
-        ui = HAS_U ? a.U[p] : 0.f;
+        if (HAS_U) {
+            const float2 kui = a.KU[p];
+            ki = kui.x;
+            ui = kui.y;
+        } else {
+            ki = kap[p];
+        }
         xi = f3(d.X[p]);
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            const uint32_t q = __ldg(rw.nbr + j);
-            const float gs = row_gs(rw, j);
+            float gs;
+            const uint32_t q = row_entry(rw, j, gs);
             const float3 r = xi - f3(d.X[q]);
-            const float kq = kap[q];
+            float kq, uq = 0.f;
+            if (HAS_U) {
+                const float2 kuq = a.KU[q];
+                kq = kuq.x;
+                uq = kuq.y;
+            } else {
+                kq = kap[q];
+            }
             const float sum = ki + kq;
             if (fabsf(sum) > kEps) acc += (sum * (-V * gs)) * r;
-            if (HAS_U) ab += ((ui + a.U[q]) * (V * gs)) * r;
+            if (HAS_U) ab += ((ui + uq) * (V * gs)) * r;
         }
     }
     acc = grp.sum(acc);
@@ -248,8 +266,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const flo
     if (!live || grp.lane != 0) return;
     const float3 gb = f3(d.GB[p]);
     if (fabsf(ki) > kEps && (rw.flags & kHasBoundary)) acc += ki * (-gb);
-    a.AK[p] = f4(acc, 0.0f);
-    if (HAS_U) a.ABAR[p] = f4(c * (ab + ui * gb), 0.0f);
+    // .w: U and kappa, for the neighbours' gathers in k_adj_jac_b
+    a.AK[p] = f4(acc, ui);
+    if (HAS_U) a.ABAR[p] = f4(c * (ab + ui * gb), ki);
 }
 
 // KBAR += P^T(ABAR) (masked like P); XBAR += XP(kap, ABAR) + c XD(AK, U), where
@@ -272,23 +291,28 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a, const flo
         xi = f3(d.X[p]);
         abi = f3(a.ABAR[p]);
         if (HAS_U) {
-            ui = a.U[p];
-            aki = f3(a.AK[p]);
+            const float4 ak4 = a.AK[p];
+            ui = ak4.w;
+            aki = f3(ak4);
         }
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            const uint32_t q = __ldg(rw.nbr + j);
-            const float gsT = row_gs(rw, j);
+            float gsT;
+            const uint32_t q = row_entry(rw, j, gsT);
             const float3 r = xi - f3(d.X[q]);
             const float s = sqrtf(dot3(r, r));
             float gs, gq;
             sp.hess(s, gs, gq);
-            const float kq = kap[q];
-            const float3 dab = abi - f3(a.ABAR[q]);
+            const float4 abq = a.ABAR[q];  // (a bar, kappa) of the neighbour
+            const float kq = HAS_U ? abq.w : kap[q];
+            const float3 dab = abi - f3(abq);
             if (fabsf(ki + kq) > kEps) {
                 kb += -V * gsT * dot3(r, dab);
                 xp += (-V * (ki + kq)) * hmul(gs, gq, r, dab);
             }
-            if (HAS_U) xd += (V * (ui + a.U[q])) * hmul(gs, gq, r, aki - f3(a.AK[q]));
+            if (HAS_U) {
+                const float4 akq = a.AK[q];  // (a^k, U) of the neighbour
+                xd += (V * (ui + akq.w)) * hmul(gs, gq, r, aki - f3(akq));
+            }
         }
     }
     kb = grp.sum(kb);
@@ -322,8 +346,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const flo
         wi = f3(w[p]);
         di = a.DBAR[p];
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            const uint32_t q = __ldg(rw.nbr + j);
-            const float gsT = row_gs(rw, j);
+            float gsT;
+            const uint32_t q = row_entry(rw, j, gsT);
             const float3 r = xi - f3(d.X[q]);
             const float s = sqrtf(dot3(r, r));
             float gs, gq;
@@ -368,8 +392,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsum(Dev d, AdjDev a) {
         rw = row_of(d, p);
         const float3 xi = f3(d.X[p]);
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            const uint32_t q = __ldg(rw.nbr + j);
-            const float3 gj = (V * row_gs(rw, j)) * (xi - f3(d.X[q]));
+            float gsT;
+            const uint32_t q = row_entry(rw, j, gsT);
+            const float3 gj = (V * gsT) * (xi - f3(d.X[q]));
             g += gj;
             g2 += dot3(gj, gj);
         }
@@ -461,8 +486,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const floa
         li = f3(d.CG[p]);
         lti = (dt / rhoi) * li;
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            const uint32_t q = __ldg(rw.nbr + j);
-            const float gsT = row_gs(rw, j);
+            float gsT;
+            const uint32_t q = row_entry(rw, j, gsT);
             const float3 r = xi - f3(d.X[q]);
             const float s2 = dot3(r, r);
             const float s = sqrtf(s2);
@@ -598,7 +623,8 @@ __global__ void k_adj_div_out(Dev d, AdjDev a, float dto) {
 // 1 pressure; r = 0 where skipped): U = [r < 0] alpha' k_bar; rho_adv bar += U,
 // alpha' bar += -r k_bar; f = scale * D(P(k)) gives SC[slot] += fdt * U f.
 template <bool DIV>
-__global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, float alphaScale, float fdt) {
+__global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, const float* kap, float alphaScale,
+                        float fdt) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (p < d.n) {
@@ -606,6 +632,7 @@ __global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, 
         const float kb = a.KBAR[p];
         const float u = r < 0.0f ? d.ALPHA[p] * alphaScale * kb : 0.0f;
         a.U[p] = u;
+        a.KU[p] = make_float2(kap[p], u);
         a.RABAR[p] += u;
         a.APBAR[p] += -r * kb;
         if (u != 0.0f) {
@@ -724,6 +751,21 @@ __global__ void k_adj_add_lambda(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n || d.scenes[0].cgZeroG) return;
     a.VBAR[p] = f4(f3(a.VBAR[p]) + f3(d.CG[p]), 0.f);
+}
+
+// Initial guess lambda_0 = lambda of the step after this one (kept in LAM: the forward
+// CG of replayed steps reuses CG): the CG starts from V + DV with V = g_bar, so DV = LAM - V.
+__global__ void k_adj_warm(Dev d, AdjDev a) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    d.DV[p] = f4(f3(a.LAM[p]) - f3(d.V[p]), 0.f);
+}
+
+// Keeps this step's lambda for the next solve.
+__global__ void k_adj_keep(Dev d, AdjDev a) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n || d.scenes[0].cgZeroG) return;
+    a.LAM[p] = d.CG[p];
 }
 
 // dt_o of this step is dt_n of the step before.
@@ -870,23 +912,14 @@ struct AdjointState {
     uint64_t generation = 0;
     std::vector<Checkpoint> ckpt;  // ckpt[k]: before step k * every; back(): after the last step
     std::vector<TapeStep> host;    // host copy of one segment's tape slots
-    TapeSet* dset = nullptr;       // device tape set (steps, cur)
+    TapeSet* dset = nullptr;       // device tape set (steps, cur): the handle's adjTapeSet
     TapeStep* dsteps = nullptr;
     uint32_t* dcur = nullptr;
     bool lastRecorded = false;     // the forward run recorded its last segment
-    cudaGraph_t recGraph[2] = {nullptr, nullptr};
-    cudaGraphExec_t recExec[2] = {nullptr, nullptr};
-    cudaGraph_t cgGraph = nullptr;
-    cudaGraphExec_t cgExec = nullptr;
+    bool warm = false;             // CG holds the last adjoint viscosity solution
     std::vector<void*> allocs;
     AdjDev a{};
     ~AdjointState() {
-        for (int k = 0; k < 2; k++) {
-            if (recExec[k]) cudaGraphExecDestroy(recExec[k]);
-            if (recGraph[k]) cudaGraphDestroy(recGraph[k]);
-        }
-        if (cgExec) cudaGraphExecDestroy(cgExec);
-        if (cgGraph) cudaGraphDestroy(cgGraph);
         for (void* p : allocs) cudaFree(p);
     }
 };
@@ -939,7 +972,12 @@ int alloc_tape(vfd_sim* s, AdjointState* A) {
     }
     TRY(aalloc(A, &A->dsteps, A->every));
     TRY(aalloc(A, &A->dcur, 1));
-    TRY(aalloc(A, &A->dset, 1));
+    if (!s->adjTapeSet) {
+        TapeSet* p = nullptr;
+        TRY(dalloc(s, &p, 1));
+        s->adjTapeSet = p;
+    }
+    A->dset = static_cast<TapeSet*>(s->adjTapeSet);
     CK(cudaMemcpy(A->dsteps, A->host.data(), sizeof(TapeStep) * A->every, cudaMemcpyHostToDevice));
     TapeSet ts{A->dsteps, A->dcur, A->every};
     CK(cudaMemcpy(A->dset, &ts, sizeof(ts), cudaMemcpyHostToDevice));
@@ -994,12 +1032,13 @@ int restore_checkpoint(vfd_sim* s, const Checkpoint& c) {
 // are read back and checked.
 int record_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
     cudaStream_t st = s->stream;
+
     CK(cudaMemsetAsync(A->dcur, 0, sizeof(uint32_t), st));
     const bool graphs = s->graphMode && !s->graphFailed;
     for (uint32_t t = 0; t < count; t++) {
-        if (graphs && !A->recExec[s->cs])
-            TRY(build_graph(s, s->cs, A->dset, &A->recGraph[s->cs], &A->recExec[s->cs]));
-        if (graphs) CK(cudaGraphLaunch(A->recExec[s->cs], st));
+        if (graphs && !s->adjRecExec[s->cs])
+            TRY(build_graph(s, s->cs, A->dset, &s->adjRecGraph[s->cs], &s->adjRecExec[s->cs]));
+        if (graphs) CK(cudaGraphLaunch(s->adjRecExec[s->cs], st));
         else TRY(launch_eager(s, A->dset));
         s->cs = 1 - s->cs;
     }
@@ -1049,8 +1088,8 @@ int build_cg_graph(vfd_sim* s, AdjointState* A) {
         cudaGraphDestroy(g);
         return fail(VFD_E_CUDA, "adjoint: CG graph construction failed: %s", cudaGetErrorString(e));
     }
-    A->cgGraph = g;
-    A->cgExec = exec;
+    s->adjCgGraph = g;
+    s->adjCgExec = exec;
     return VFD_OK;
 }
 
@@ -1086,7 +1125,7 @@ int backward_step(vfd_sim* s, AdjointState* A, uint32_t t) {
     ADJ_LAUNCH(k_adj_pres_out, g1, d, a, T.V2, dtn);
     ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, KP(kp), 0.0f);
     for (uint32_t k = kp; k-- > 0;) {
-        ADJ_LAUNCH(k_adj_u<false>, g1, d, a, RP(k), T.RAP, 1.0f / (dtn * dtn), 2.0f / dtn);
+        ADJ_LAUNCH(k_adj_u<false>, g1, d, a, RP(k), T.RAP, KP(k), 1.0f / (dtn * dtn), 2.0f / dtn);
         ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, KP(k), dtn * dtn);
         ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, KP(k), dtn * dtn);
     }
@@ -1106,10 +1145,24 @@ int backward_step(vfd_sim* s, AdjointState* A, uint32_t t) {
     // viscosity: A lambda = g_bar with the forward's CG, then the derivative of A g = v1
     if (mode == 1) {
         COPY(d.V, a.GBAR, sizeof(float4) * sd);
-        CK(cudaMemsetAsync(d.DV, 0, sizeof(float4) * sd, st));
-        if (!A->cgExec) TRY(build_cg_graph(s, A));
-        CK(cudaGraphLaunch(A->cgExec, st));
+        // initial guess: the previous backward step's lambda (still in CG) when there is one
+        if (A->warm) ADJ_LAUNCH(k_adj_warm, g1, d, a);
+        else CK(cudaMemsetAsync(d.DV, 0, sizeof(float4) * sd, st));
+        if (s->graphMode && !s->graphFailed) {
+            if (!s->adjCgExec) TRY(build_cg_graph(s, A));
+            CK(cudaGraphLaunch(s->adjCgExec, st));
+        } else {  // eager: one flag read per CG iteration
+            uint32_t more = 0;
+            launch_visc_init(d, st);
+            TRY(read_flag(s, 5, more));
+            for (uint32_t guard = 0; more && guard < 100000u; guard++) {
+                launch_cg_iter(d, st);
+                TRY(read_flag(s, 5, more));
+            }
+        }
+        A->warm = true;
         ADJ_LAUNCH(k_adj_add_lambda, g1, d, a);
+        ADJ_LAUNCH(k_adj_keep, g1, d, a);
         ADJ_LAUNCH(k_adj_visc, gG, d, a, T.G, dto);
     }
 
@@ -1120,7 +1173,7 @@ int backward_step(vfd_sim* s, AdjointState* A, uint32_t t) {
         ADJ_LAUNCH(k_adj_div_out, g1, d, a, dto);
         ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, KD(kd), 0.0f);
         for (uint32_t k = kd; k-- > 0;) {
-            ADJ_LAUNCH(k_adj_u<true>, g1, d, a, RD(k), T.RAD, 1.0f / dto, 1.0f / dto);
+            ADJ_LAUNCH(k_adj_u<true>, g1, d, a, RD(k), T.RAD, KD(k), 1.0f / dto, 1.0f / dto);
             ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, KD(k), dto);
             ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, KD(k), dto);
         }
@@ -1156,6 +1209,8 @@ int alloc_cotangents(vfd_sim* s, AdjointState* A) {
     TRY(aalloc(A, &a.BD, 3 * st * std::max<uint32_t>(1u, s->maxBodies)));
     TRY(aalloc(A, &a.KBAR, st));
     TRY(aalloc(A, &a.U, st));
+    TRY(aalloc(A, &a.KU, st));
+    TRY(aalloc(A, &a.LAM, st));
     TRY(aalloc(A, &a.RABAR, st));
     TRY(aalloc(A, &a.APBAR, st));
     TRY(aalloc(A, &a.DBAR, st));
@@ -1201,13 +1256,31 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
     if (steps == 0 || checkpoint_every == 0) return fail(VFD_E_ARG, "adjoint: steps and checkpoint_every must be positive");
     TRY(check_adjoint_scene(s));
     TRY(ensure_ready(s));
-    adjoint_release(s);
-    auto A = std::make_unique<AdjointState>();
+    // the tape, checkpoints and cotangent arrays of the previous run are reused when the
+    // layout matches (same particles, segment length and iteration caps)
+    const uint32_t every = std::min(checkpoint_every, steps);
+    const vfd_desc& dd = s->scenes[0].desc;
+    const uint32_t capD = s->anyDiv ? dd.MaxDivergenceSolverIterations : 0u, capP = dd.MaxPressureSolverIterations;
+    std::unique_ptr<AdjointState> A(s->adjoint);
+    s->adjoint = nullptr;
+    if (A && !(A->n == s->n && A->stride == s->stride && A->every == every && !A->host.empty() &&
+               A->host[0].capD == capD && A->host[0].capP == capP))
+        A.reset();
+    if (!A) {
+        A = std::make_unique<AdjointState>();
+        A->every = every;
+        A->n = s->n;
+        A->stride = s->stride;
+        TRY(alloc_tape(s, A.get()));
+    } else {
+        TapeSet ts{A->dsteps, A->dcur, A->every};
+        A->dset = static_cast<TapeSet*>(s->adjTapeSet);
+        if (!A->dset) TRY(alloc_tape(s, A.get()));  // buffers were reallocated since
+        else CK(cudaMemcpy(A->dset, &ts, sizeof(ts), cudaMemcpyHostToDevice));
+    }
     A->steps = steps;
-    A->every = std::min(checkpoint_every, steps);
-    A->n = s->n;
-    A->stride = s->stride;
-    TRY(alloc_tape(s, A.get()));
+    A->lastRecorded = false;
+    A->warm = false;
     const uint32_t segs = (steps + A->every - 1) / A->every;
     A->ckpt.resize(segs + 1);
     for (uint32_t k = 0; k < segs; k++) {

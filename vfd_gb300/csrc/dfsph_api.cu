@@ -898,7 +898,19 @@ int vfd_set_description(vfd_sim* s, const vfd_desc* desc) {
     if (s->scenes.size() > 1 && desc->ParticleRadius != s->scenes[0].desc.ParticleRadius)
         return fail(VFD_E_ARG, "all scenes of a batch share one ParticleRadius");
     CK(cudaSetDevice(s->device));
+    const vfd_desc old = s->scenes[0].desc;
     s->scenes[0].desc = *desc;
+    // parameters that change neither the table nor the step's graph structure only need
+    // the next step's upload
+    const bool sameShape = desc->ParticleRadius == old.ParticleRadius &&
+                           desc->EnableDivergenceSolverError == old.EnableDivergenceSolverError &&
+                           desc->EnableViscositySolver == old.EnableViscositySolver &&
+                           desc->EnableSurfaceTensionSolver == old.EnableSurfaceTensionSolver &&
+                           desc->SurfaceTensionSmoothPassCount == old.SurfaceTensionSmoothPassCount;
+    if (sameShape && s->allocated) {
+        s->uploaded = false;
+        return VFD_OK;
+    }
     if (desc->ParticleRadius != s->table.radius / 4.0f) s->table.setRadius(4.0f * desc->ParticleRadius);
     s->releaseBuffers();
     return VFD_OK;
@@ -920,9 +932,16 @@ int vfd_scene_set_fluid(vfd_sim* s, uint32_t scene, const float* xyz, const floa
             return fail(VFD_E_NAN, "non-finite input at element %llu", (unsigned long long)i);
     CK(cudaSetDevice(s->device));
     SceneHost& sc = s->scenes[scene];
+    const bool sameCount = sc.x0.size() == 3ull * n;
     sc.x0.assign(xyz, xyz + 3ull * n);
     if (vel) sc.v0.assign(vel, vel + 3ull * n);
     else sc.v0.assign(3ull * n, 0.0f);
+    if (sameCount && s->allocated) {
+        // same layout: the next step uploads the new state into the existing buffers and
+        // keeps the step graphs (the cell table grows if the new state needs it)
+        s->uploaded = false;
+        return VFD_OK;
+    }
     s->releaseBuffers();
     s->cellCap = 0;
     return VFD_OK;

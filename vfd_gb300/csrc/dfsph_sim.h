@@ -171,6 +171,13 @@ struct vfd_sim {
     // counts uploads, so a reset after the recorded run is detected
     vfd::AdjointState* adjoint = nullptr;
     uint64_t generation = 0;
+    // kept across adjoint runs while the buffers live: the device tape set that recording
+    // graphs address, those graphs (one per parity) and the adjoint CG solve's graph
+    void* adjTapeSet = nullptr;
+    cudaGraph_t adjRecGraph[2] = {nullptr, nullptr};
+    cudaGraphExec_t adjRecExec[2] = {nullptr, nullptr};
+    cudaGraph_t adjCgGraph = nullptr;
+    cudaGraphExec_t adjCgExec = nullptr;
 
     ~vfd_sim() { release(); }
 
@@ -180,12 +187,21 @@ struct vfd_sim {
             if (graph[k]) cudaGraphDestroy(graph[k]);
             exec[k] = nullptr;
             graph[k] = nullptr;
+            if (adjRecExec[k]) cudaGraphExecDestroy(adjRecExec[k]);
+            if (adjRecGraph[k]) cudaGraphDestroy(adjRecGraph[k]);
+            adjRecExec[k] = nullptr;
+            adjRecGraph[k] = nullptr;
         }
+        if (adjCgExec) cudaGraphExecDestroy(adjCgExec);
+        if (adjCgGraph) cudaGraphDestroy(adjCgGraph);
+        adjCgExec = nullptr;
+        adjCgGraph = nullptr;
     }
     void releaseBuffers() {
         releaseGraphs();
         for (void* p : allocs) cudaFree(p);
         allocs.clear();
+        adjTapeSet = nullptr;
         if (hStatus) cudaFreeHost(hStatus);
         hStatus = nullptr;
         allocated = false;
