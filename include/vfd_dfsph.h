@@ -236,6 +236,44 @@ int vfd_build_box_map(const float box_min[3], const float box_max[3], int32_t in
                       float* nodes, uint32_t* cells, uint32_t* cell_map, vfd_volume_map* map_out);
 
 /*
+ * Builds the volume map of a closed triangle mesh on the GPU: RigidBody::RigidBody
+ * (Simulation/DFSPH/RigidBody/RigidBody.cu:10-72) with the signed distance of
+ * MeshDistance::SignedDistance (Utility/SDF/MeshDistance.cpp:187-228, angle-weighted
+ * pseudo-normals, MeshDistance.cpp:27-55). `vertices` holds vertex_count xyz triples,
+ * `triangles` triangle_count index triples (counter-clockwise seen from outside, as
+ * the reference's EdgeMesh expects). `transform` is the body's 4x4 placement in
+ * column-major order (glm's layout; RigidBodyDescription::Transform) or NULL for the
+ * identity. Domain = bounds of the placed vertices +- (8h + padding - r); buffers as
+ * for vfd_build_box_map (sized by vfd_box_map_sizes).
+ */
+int vfd_build_mesh_map(const float* vertices, uint32_t vertex_count, const uint32_t* triangles,
+                       uint32_t triangle_count, const float* transform, int32_t inverted, float padding,
+                       const uint32_t resolution[3], float particle_radius, float* nodes, uint32_t* cells,
+                       uint32_t* cell_map, vfd_volume_map* map_out);
+
+/* Lattice packings of ParticleSampler (Utility/Sampler/ParticleSampler.h:7-11). */
+#define VFD_SAMPLE_MIN_DENSITY 0
+#define VFD_SAMPLE_MEDIUM_DENSITY 1
+#define VFD_SAMPLE_MAX_DENSITY 2
+
+/*
+ * Fluid particles filling a mesh volume: FluidObject::FluidObject
+ * (Simulation/DFSPH/FluidObject/FluidObject.cpp:6-25) calling
+ * ParticleSampler::SampleMeshVolume (Utility/Sampler/ParticleSampler.cpp:7-91). The mesh
+ * is placed by `transform` (as in vfd_build_mesh_map), its signed-distance map of
+ * `resolution` cells is built on the GPU (SDF::SDF, Utility/SDF/SDF.cu:16-36), and the
+ * lattice points of the chosen packing with a negative distance are kept, in the
+ * reference's order (z outer, then y, then x). `count` receives the number of samples;
+ * min(count, capacity) xyz triples are written to `positions` unless it is NULL (call
+ * once with NULL to size the buffer). VFD_E_CAPACITY when capacity < count (the first
+ * `capacity` samples are still written) or the lattice exceeds 2^31 points.
+ */
+int vfd_sample_mesh_volume(const float* vertices, uint32_t vertex_count, const uint32_t* triangles,
+                           uint32_t triangle_count, const float* transform, float particle_radius,
+                           const uint32_t resolution[3], int32_t inverted, int32_t sample_mode,
+                           float* positions, uint32_t capacity, uint32_t* count);
+
+/*
  * DFSPHImplementation::Simulate (DFSPHImplementation.cu:33-61) preamble:
  * re-uploads the initial particles, resets dt, frame time and counters.
  */

@@ -40,7 +40,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
+#include <map>
 #include <memory>
+#include <utility>
 #include <vector>
 
 #ifdef _OPENMP
@@ -622,36 +625,29 @@ static void build_cells(MapData& m) {
         for (uint32_t l = 0; l < m.cellCount; l++) m.cellMap.push_back(l);
 }
 
-// RigidBody::RigidBody for a box mesh (RigidBody.cu:10-72).
-static void build_box_map(const float bmin[3], const float bmax[3], bool inverted, float padding,
-                          const uint32_t res[3], float particleRadius, MapData& m) {
-    KernelTable<float> kernel;
-    kernel.setRadius(4.0f * particleRadius);
-    const float supportRadius = 4.0f * particleRadius;
-    const float tolerance = padding - particleRadius;
-    const float sign = inverted ? -1.0f : 1.0f;
+// Grid of a map over [dmin, dmax] (SDF::SDF, SDF.cu:8-14) with `fields` fields.
+static void map_grid(MapData& m, const float dmin[3], const float dmax[3], const uint32_t res[3], uint32_t fields) {
     for (int d = 0; d < 3; d++) {
-        m.dmin[d] = bmin[d] - (8.0f * supportRadius + tolerance);
-        m.dmax[d] = bmax[d] + (8.0f * supportRadius + tolerance);
+        m.dmin[d] = dmin[d];
+        m.dmax[d] = dmax[d];
         m.res[d] = res[d];
-    }
-    for (int d = 0; d < 3; d++) {  // SDF::SDF(domain, resolution), SDF.cu:8-14
         m.cs[d] = (m.dmax[d] - m.dmin[d]) / (float)m.res[d];
         m.csi[d] = 1.0f / m.cs[d];
     }
     box_map_sizes(m.res, m.nodeCount, m.cellCount);
     m.cellMapCount = m.cellCount;
-    m.fieldCount = 2;
+    m.fieldCount = fields;
     build_cells(m);
-    m.nodes.assign((size_t)m.nodeCount * 2u, 0.0f);
-    // field 0: sign * (SignedDistance - tolerance)
-#pragma omp parallel for schedule(static)
-    for (int64_t l = 0; l < (int64_t)m.nodeCount; l++) {
-        const V3<float> x = node_position(m, (uint32_t)l);
-        m.nodes[(size_t)l] = sign * (box_sdf(bmin, bmax, x) - tolerance);
-    }
-    // field 1: 0.8 * Gauss-Legendre(16 points per axis, p = 30) integral over the
-    // support cube (GaussQuadrature.cpp:5621-5656: float weights, float sum).
+    m.nodes.assign((size_t)m.nodeCount * fields, 0.0f);
+}
+
+// Field 1 of a rigid-body map from its field 0 (RigidBody.cu:42-71): 0.8 * Gauss-Legendre
+// (16 points per axis, p = 30) integral over the support cube
+// (GaussQuadrature.cpp:5621-5656: float weights, float sum).
+static void map_volume_field(MapData& m, float particleRadius) {
+    KernelTable<float> kernel;
+    kernel.setRadius(4.0f * particleRadius);
+    const float supportRadius = 4.0f * particleRadius;
     std::vector<double> ga, gw;
     gauss_legendre(16, ga, gw);
     const double c0 = 0.5 * (double)(supportRadius - (-supportRadius));
@@ -686,6 +682,292 @@ static void build_box_map(const float bmin[3], const float bmax[3], bool inverte
         }
         m.nodes[(size_t)m.nodeCount + (size_t)l] = value;
     }
+}
+
+// RigidBody::RigidBody for a box mesh (RigidBody.cu:10-72).
+static void build_box_map(const float bmin[3], const float bmax[3], bool inverted, float padding,
+                          const uint32_t res[3], float particleRadius, MapData& m) {
+    const float supportRadius = 4.0f * particleRadius;
+    const float tolerance = padding - particleRadius;
+    const float sign = inverted ? -1.0f : 1.0f;
+    float dmin[3], dmax[3];
+    for (int d = 0; d < 3; d++) {
+        dmin[d] = bmin[d] - (8.0f * supportRadius + tolerance);
+        dmax[d] = bmax[d] + (8.0f * supportRadius + tolerance);
+    }
+    map_grid(m, dmin, dmax, res, 2);
+    // field 0: sign * (SignedDistance - tolerance)
+#pragma omp parallel for schedule(static)
+    for (int64_t l = 0; l < (int64_t)m.nodeCount; l++) {
+        const V3<float> x = node_position(m, (uint32_t)l);
+        m.nodes[(size_t)l] = sign * (box_sdf(bmin, bmax, x) - tolerance);
+    }
+    map_volume_field(m, particleRadius);
+}
+
+// ---------------------------------------------------------------------------
+// Triangle meshes: MeshDistance (Utility/SDF/MeshDistance.cpp) on an EdgeMesh.
+struct Mesh {
+    std::vector<V3<float>> x;      // placed vertices
+    std::vector<uint32_t> tri;     // 3 per face
+    std::vector<V3<float>> faceN;  // unit face normals
+    std::vector<V3<float>> vertN;  // angle-weighted vertex normals
+    std::vector<int64_t> opp;      // per half-edge (face, k): the face across it, -1 on a border
+    float bmin[3], bmax[3];
+};
+
+// glm::normalize: v * inversesqrt(dot(v, v)).
+static V3<float> glm_normalize(const V3<float>& v) { return v * (1.0f / std::sqrt(dot(v, v))); }
+
+// The placement of RigidBody.cu:19-23 / FluidObject.cpp:10-14 (Transform * vec4(v, 1),
+// glm's column-major product summed in pairs), BoundingBox(vertices)
+// (Core/Structures/BoundingBox.h:16-21), the pre-computed normals of MeshDistance's
+// constructor (MeshDistance.cpp:27-55) and the half-edge pairing of EdgeMesh
+// (Renderer/Mesh/EdgeMesh.cpp:97-130: a half-edge (u, v) pairs with an unpaired (v, u)).
+static bool make_mesh(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nf, const float* T, Mesh& M) {
+    for (size_t i = 0; i < 3 * (size_t)nf; i++)
+        if (tri[i] >= nv) return false;
+    M.x.resize(nv);
+    for (uint32_t i = 0; i < nv; i++) {
+        const float px = v[3 * i], py = v[3 * i + 1], pz = v[3 * i + 2];
+        if (!T) {
+            M.x[i] = V3<float>(px, py, pz);
+            continue;
+        }
+        float r[3];
+        for (int k = 0; k < 3; k++) r[k] = (T[k] * px + T[4 + k] * py) + (T[8 + k] * pz + T[12 + k] * 1.0f);
+        M.x[i] = V3<float>(r[0], r[1], r[2]);
+    }
+    M.tri.assign(tri, tri + 3 * (size_t)nf);
+    for (int d = 0; d < 3; d++) {
+        M.bmin[d] = std::numeric_limits<float>::max();
+        M.bmax[d] = -std::numeric_limits<float>::max();
+    }
+    for (const auto& p : M.x)
+        for (int d = 0; d < 3; d++) {
+            M.bmin[d] = std::min(M.bmin[d], p[d]);
+            M.bmax[d] = std::max(M.bmax[d], p[d]);
+        }
+    M.faceN.assign(nf, V3<float>());
+    M.vertN.assign(nv, V3<float>());
+    for (uint32_t f = 0; f < nf; f++) {
+        const V3<float>& x0 = M.x[tri[3 * f]];
+        const V3<float>& x1 = M.x[tri[3 * f + 1]];
+        const V3<float>& x2 = M.x[tri[3 * f + 2]];
+        const V3<float> n = glm_normalize(cross(x1 - x0, x2 - x0));
+        const V3<float> e1 = glm_normalize(x1 - x0), e2 = glm_normalize(x2 - x1), e3 = glm_normalize(x0 - x2);
+        const float alpha[3] = {std::acos(dot(e1, -e3)), std::acos(dot(e2, -e1)), std::acos(dot(e3, -e2))};
+        for (int k = 0; k < 3; k++) M.vertN[tri[3 * f + k]] += alpha[k] * n;
+        M.faceN[f] = n;
+    }
+    M.opp.assign(3 * (size_t)nf, -1);
+    std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>> open;
+    for (uint32_t f = 0; f < nf; f++)
+        for (uint32_t k = 0; k < 3; k++) {
+            const uint32_t a = tri[3 * f + k], b = tri[3 * f + (k + 1) % 3];
+            auto it = open.find({b, a});
+            if (it != open.end() && !it->second.empty()) {
+                const uint32_t h = it->second.front();
+                it->second.erase(it->second.begin());
+                M.opp[3 * (size_t)f + k] = h / 3;
+                M.opp[h] = f;
+            } else {
+                open[{a, b}].push_back(3 * f + k);
+            }
+        }
+    return true;
+}
+
+// Closest entity classes of MeshDistance (MeshDistance.h): corners A, B, C; edges D (01),
+// E (12), F (20); interior G.
+enum TriEntity { kEntA, kEntB, kEntC, kEntD, kEntE, kEntF, kEntG };
+
+// MeshDistance::PointTriangleDistanceSquared (MeshDistance.cpp:300-607): minimises
+// Q(s, t) = |t0 + s e0 + t e1 - p|^2 over s, t >= 0, s + t <= 1 by the region of the
+// unconstrained minimum (D. Eberly, "Distance Between Point and Triangle in 3D"), in FP32.
+// Returns Q at the minimum (clamped at 0); (s, t) and the entity of the closest point.
+static float point_triangle_d2(const V3<float>& p, const V3<float>& t0, const V3<float>& t1, const V3<float>& t2,
+                               float& s, float& t, int& entity) {
+    const V3<float> diff = t0 - p, e0 = t1 - t0, e1 = t2 - t0;
+    const float a00 = dot(e0, e0), a01 = dot(e0, e1), a11 = dot(e1, e1);
+    const float b0 = dot(diff, e0), b1 = dot(diff, e1), c = dot(diff, diff);
+    const float det = std::fabs(a00 * a11 - a01 * a01);
+    s = a01 * b1 - a11 * b0;
+    t = a01 * b0 - a00 * b1;
+    float d2;
+    auto quad = [&]() { return s * (a00 * s + a01 * t + 2.0f * b0) + t * (a01 * s + a11 * t + 2.0f * b1) + c; };
+    auto cornerA = [&]() { s = 0.0f; t = 0.0f; entity = kEntA; return c; };
+    auto cornerB = [&]() { s = 1.0f; t = 0.0f; entity = kEntB; return a00 + 2.0f * b0 + c; };
+    auto cornerC = [&]() { s = 0.0f; t = 1.0f; entity = kEntC; return a11 + 2.0f * b1 + c; };
+    auto edge01 = [&]() { t = 0.0f; s = -b0 / a00; entity = kEntD; return b0 * s + c; };
+    auto edge20 = [&]() { s = 0.0f; t = -b1 / a11; entity = kEntF; return b1 * t + c; };
+    // t = 0 side: corner A, corner B or the edge between
+    auto side01 = [&]() { return b0 >= 0.0f ? cornerA() : (-b0 >= a00 ? cornerB() : edge01()); };
+    // s = 0 side: corner A, corner C or the edge between
+    auto side20 = [&]() { return b1 >= 0.0f ? cornerA() : (-b1 >= a11 ? cornerC() : edge20()); };
+    if (s + t <= det) {
+        if (s < 0.0f) {
+            if (t < 0.0f) d2 = b0 < 0.0f ? (-b0 >= a00 ? cornerB() : edge01()) : side20();  // region 4
+            else d2 = side20();                                                              // region 3
+        } else if (t < 0.0f) {
+            d2 = side01();  // region 5
+        } else {            // region 0
+            const float inv = 1.0f / det;
+            s *= inv;
+            t *= inv;
+            entity = kEntG;
+            d2 = quad();
+        }
+    } else {
+        const float denom = a00 - 2.0f * a01 + a11;
+        if (s < 0.0f) {  // region 2
+            const float m0 = a01 + b0, m1 = a11 + b1;
+            if (m1 > m0) {
+                const float numer = m1 - m0;
+                if (numer >= denom) d2 = cornerB();
+                else { s = numer / denom; t = 1 - s; entity = kEntE; d2 = quad(); }
+            } else {
+                d2 = m1 <= 0.0f ? cornerC() : (b1 >= 0.0f ? cornerA() : edge20());
+            }
+        } else if (t < 0.0f) {  // region 6
+            const float m0 = a01 + b1, m1 = a00 + b0;
+            if (m1 > m0) {
+                const float numer = m1 - m0;
+                if (numer >= denom) d2 = cornerC();
+                else { t = numer / denom; s = 1 - t; entity = kEntE; d2 = quad(); }
+            } else {
+                d2 = m1 <= 0.0f ? cornerB() : (b0 >= 0.0f ? cornerA() : edge01());
+            }
+        } else {  // region 1
+            const float numer = a11 + b1 - a01 - b0;
+            if (numer <= 0.0f) d2 = cornerC();
+            else if (numer >= denom) d2 = cornerB();
+            else { s = numer / denom; t = 1 - s; entity = kEntE; d2 = quad(); }
+        }
+    }
+    return d2 < 0.0f ? 0.0f : d2;
+}
+
+// MeshDistance::SignedDistance (MeshDistance.cpp:187-228) with the nearest face found by
+// testing every face (the bounding-sphere hierarchy only prunes; ties keep the lowest
+// face index). The sign is that of dot(p - closest point, pseudo-normal of the entity).
+static float mesh_signed_distance(const Mesh& M, const V3<float>& p) {
+    const uint32_t nf = (uint32_t)(M.tri.size() / 3);
+    float best = std::numeric_limits<float>::max();
+    uint32_t face = 0;
+    for (uint32_t f = 0; f < nf; f++) {
+        float s, t;
+        int e;
+        const float d2 = point_triangle_d2(p, M.x[M.tri[3 * f]], M.x[M.tri[3 * f + 1]], M.x[M.tri[3 * f + 2]], s, t, e);
+        if (best > d2) {
+            best = d2;
+            face = f;
+        }
+    }
+    float s, t;
+    int e;
+    const V3<float>& t0 = M.x[M.tri[3 * face]];
+    const float d2 = point_triangle_d2(p, t0, M.x[M.tri[3 * face + 1]], M.x[M.tri[3 * face + 2]], s, t, e);
+    const V3<float> cp = t0 + s * (M.x[M.tri[3 * face + 1]] - t0) + t * (M.x[M.tri[3 * face + 2]] - t0);
+    V3<float> n;
+    if (e <= kEntC) {
+        n = M.vertN[M.tri[3 * face + e]];
+    } else if (e <= kEntF) {
+        const int64_t o = M.opp[3 * (size_t)face + (e - kEntD)];
+        n = o < 0 ? M.faceN[face] : M.faceN[face] + M.faceN[(size_t)o];
+    } else {
+        n = M.faceN[face];
+    }
+    float dist = std::sqrt(d2);
+    if (dot(p - cp, n) < 0.0f) dist *= -1.0f;
+    return dist;
+}
+
+// RigidBody::RigidBody (RigidBody.cu:10-72) for a placed triangle mesh.
+static void build_mesh_map(const Mesh& M, bool inverted, float padding, const uint32_t res[3], float particleRadius,
+                           MapData& m) {
+    const float supportRadius = 4.0f * particleRadius;
+    const float tolerance = padding - particleRadius;
+    const float sign = inverted ? -1.0f : 1.0f;
+    float dmin[3], dmax[3];
+    for (int d = 0; d < 3; d++) {
+        dmax[d] = M.bmax[d] + (8.0f * supportRadius + tolerance);
+        dmin[d] = M.bmin[d] - (8.0f * supportRadius + tolerance);
+    }
+    map_grid(m, dmin, dmax, res, 2);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t l = 0; l < (int64_t)m.nodeCount; l++) {
+        const V3<float> x = node_position(m, (uint32_t)l);
+        m.nodes[(size_t)l] = sign * (mesh_signed_distance(M, x) - tolerance);
+    }
+    map_volume_field(m, particleRadius);
+}
+
+// ParticleSampler::SampleMeshVolume (ParticleSampler.cpp:7-91) with SDF::SDF(mesh, bounds,
+// resolution, inverted) (SDF.cu:16-36) and SDF::GetDistance(x, 0) (SDF.cu:217-225).
+// Returns false when an axis step is lost in the float rounding.
+static bool sample_mesh_volume(const Mesh& M, float radius, const uint32_t res[3], bool inverted, int mode,
+                               std::vector<float>& out) {
+    MapData m;
+    float dmin[3] = {M.bmin[0], M.bmin[1], M.bmin[2]}, dmax[3] = {M.bmax[0], M.bmax[1], M.bmax[2]};
+    {
+        const V3<float> d0(dmax[0] - dmin[0], dmax[1] - dmin[1], dmax[2] - dmin[2]);
+        const float g0 = 0.001f * std::sqrt(dot(d0, d0));
+        for (int d = 0; d < 3; d++) dmax[d] += g0;
+        const V3<float> d1(dmax[0] - dmin[0], dmax[1] - dmin[1], dmax[2] - dmin[2]);
+        const float g1 = 0.001f * std::sqrt(dot(d1, d1));
+        for (int d = 0; d < 3; d++) dmin[d] -= g1;
+    }
+    map_grid(m, dmin, dmax, res, 1);
+    const float factor = inverted ? -1.0f : 1.0f;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t l = 0; l < (int64_t)m.nodeCount; l++)
+        m.nodes[(size_t)l] = factor * mesh_signed_distance(M, node_position(m, (uint32_t)l));
+
+    const float diameter = 2.0f * radius;
+    float shiftX = diameter, shiftY = diameter;
+    if (mode == 1) {
+        shiftY = std::sqrt(3.0f) * radius;
+    } else if (mode == 2) {
+        shiftX = std::sqrt(3.0f) * radius;
+        shiftY = std::sqrt(6.0f) * diameter / 3.0f;
+    }
+    const float step[3] = {shiftX, shiftY, diameter};
+    for (int d = 0; d < 3; d++)
+        if (M.bmin[d] + step[d] == M.bmin[d] || M.bmax[d] + step[d] == M.bmax[d]) return false;
+    out.clear();
+    uint32_t counterY = 0;
+    for (float z = M.bmin[2]; z <= M.bmax[2]; z += diameter) {
+        for (float y = M.bmin[1]; y <= M.bmax[1]; y += shiftY) {
+            uint32_t counterX = 0;
+            for (float x = M.bmin[0]; x <= M.bmax[0]; x += shiftX) {
+                V3<float> q;
+                if (mode == 0) {
+                    q = V3<float>(x + radius, y + radius, z + radius);
+                } else if (mode == 1) {
+                    q = counterY % 2 == 0 ? V3<float>(x, y + radius, z + radius) : V3<float>(x + radius, y + radius, z);
+                } else {
+                    q = V3<float>(x, y + radius, z + radius);
+                    V3<float> shift(0.0f, 0.0f, 0.0f);
+                    if (counterX % 2) shift.z += diameter / (2.0f * (counterY % 2 ? -1 : 1));
+                    if (counterY % 2) {
+                        shift.x += shiftX / 2.0f;
+                        shift.z += diameter / 2.0f;
+                    }
+                    q += shift;
+                }
+                if (map_interpolate_host(m, 0, q) < 0.0f) {
+                    out.push_back(q.x);
+                    out.push_back(q.y);
+                    out.push_back(q.z);
+                }
+                counterX++;
+            }
+            counterY++;
+        }
+        counterY = 0;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1545,6 +1827,62 @@ int orc_build_box_map(const float bmin[3], const float bmax[3], int inverted, fl
     out->node_count = m.nodeCount;
     out->cell_count = m.cellCount;
     out->cell_map_count = m.cellMapCount;
+    return VFD_OK;
+}
+
+static void export_map(const MapData& m, float* nodes, uint32_t* cells, uint32_t* cellMap, vfd_volume_map* out) {
+    std::copy(m.nodes.begin(), m.nodes.end(), nodes);
+    std::copy(m.cells.begin(), m.cells.end(), cells);
+    std::copy(m.cellMap.begin(), m.cellMap.end(), cellMap);
+    out->nodes = nodes;
+    out->cells = cells;
+    out->cell_map = cellMap;
+    for (int d = 0; d < 3; d++) {
+        out->domain_min[d] = m.dmin[d];
+        out->domain_max[d] = m.dmax[d];
+        out->resolution[d] = m.res[d];
+        out->cell_size[d] = m.cs[d];
+        out->cell_size_inverse[d] = m.csi[d];
+    }
+    out->field_count = m.fieldCount;
+    out->node_count = m.nodeCount;
+    out->cell_count = m.cellCount;
+    out->cell_map_count = m.cellMapCount;
+}
+
+// Two-field volume map of a triangle mesh placed by `transform` (column-major 4x4 or null).
+int orc_build_mesh_map(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nf, const float* transform,
+                       int inverted, float padding, const uint32_t res[3], float r, float* nodes, uint32_t* cells,
+                       uint32_t* cellMap, vfd_volume_map* out) {
+    Mesh M;
+    if (nv == 0 || nf == 0 || !make_mesh(v, nv, tri, nf, transform, M)) return VFD_E_ARG;
+    MapData m;
+    build_mesh_map(M, inverted != 0, padding, res, r, m);
+    export_map(m, nodes, cells, cellMap, out);
+    return VFD_OK;
+}
+
+// Signed distance of a placed mesh at n points (MeshDistance::SignedDistance).
+int orc_mesh_signed_distance(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nf, const float* transform,
+                             const float* pts, uint32_t n, float* out) {
+    Mesh M;
+    if (nv == 0 || nf == 0 || !make_mesh(v, nv, tri, nf, transform, M)) return VFD_E_ARG;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++)
+        out[i] = mesh_signed_distance(M, V3<float>(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+    return VFD_OK;
+}
+
+// Samples of a placed mesh's volume; `count` = all samples, min(count, cap) written.
+int orc_sample_mesh_volume(const float* v, uint32_t nv, const uint32_t* tri, uint32_t nf, const float* transform,
+                           float radius, const uint32_t res[3], int inverted, int mode, float* out, uint32_t cap,
+                           uint32_t* count) {
+    Mesh M;
+    if (nv == 0 || nf == 0 || mode < 0 || mode > 2 || !make_mesh(v, nv, tri, nf, transform, M)) return VFD_E_ARG;
+    std::vector<float> pts;
+    if (!sample_mesh_volume(M, radius, res, inverted != 0, mode, pts)) return VFD_E_CAPACITY;
+    *count = (uint32_t)(pts.size() / 3);
+    if (out) std::copy(pts.begin(), pts.begin() + 3 * (size_t)std::min(*count, cap), out);
     return VFD_OK;
 }
 

@@ -65,6 +65,12 @@ def lib():
             L.orc_map_interpolate_d.argtypes = [C.POINTER(_abi.vfd_volume_map), C.c_uint32, f64p, C.c_uint32, f64p,
                                                 f64p]
             L.orc_gauss_legendre.argtypes = [C.c_uint, f64p, f64p]
+            L.orc_build_mesh_map.argtypes = [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_int, C.c_float, u32p,
+                                             C.c_float, f32p, u32p, u32p, C.POINTER(_abi.vfd_volume_map)]
+            L.orc_mesh_signed_distance.argtypes = [f32p, C.c_uint32, u32p, C.c_uint32, f32p, f32p, C.c_uint32,
+                                                   f32p]
+            L.orc_sample_mesh_volume.argtypes = [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_float, u32p, C.c_int,
+                                                 C.c_int, f32p, C.c_uint32, u32p]
             L.orc_map_node_positions.argtypes = [C.POINTER(_abi.vfd_volume_map), f32p]
             L.orc_set_threads.argtypes = [C.c_int]
             L.orc_get_threads.restype = C.c_int
@@ -164,6 +170,62 @@ def build_box_map(bmin, bmax, inverted: bool, padding: float, resolution, partic
                             _ptr(nodes, C.c_float), _ptr(cells, C.c_uint32), _ptr(cell_map, C.c_uint32),
                             C.byref(m))
     return VolumeMap(nodes, cells, cell_map, m)
+
+
+def _mesh(vertices, triangles, transform):
+    v = np.ascontiguousarray(np.asarray(vertices, np.float32).reshape(-1, 3))
+    t = np.ascontiguousarray(np.asarray(triangles, np.uint32).reshape(-1, 3))
+    col = None if transform is None else np.ascontiguousarray(np.asarray(transform, np.float32).reshape(4, 4).T.reshape(16))
+    return v, t, col, (_ptr(col, C.c_float) if col is not None else None)
+
+
+def build_mesh_map(vertices, triangles, transform=None, inverted: bool = False, padding: float = 0.0,
+                   resolution=(20, 20, 20), particle_radius: float = 0.025) -> VolumeMap:
+    """RigidBody::RigidBody (RigidBody.cu:10-72) of a triangle mesh, on the CPU."""
+    res = np.ascontiguousarray(resolution, np.uint32)
+    nn, nc = C.c_uint32(), C.c_uint32()
+    lib().orc_box_map_sizes(_ptr(res, C.c_uint32), C.byref(nn), C.byref(nc))
+    v, t, col, colp = _mesh(vertices, triangles, transform)
+    nodes = np.zeros(2 * nn.value, np.float32)
+    cells = np.zeros(2 * nc.value * 32, np.uint32)
+    cell_map = np.zeros(2 * nc.value, np.uint32)
+    m = _abi.vfd_volume_map()
+    rc = lib().orc_build_mesh_map(_ptr(v, C.c_float), len(v), _ptr(t, C.c_uint32), len(t), colp, int(bool(inverted)),
+                                  C.c_float(padding), _ptr(res, C.c_uint32), C.c_float(particle_radius),
+                                  _ptr(nodes, C.c_float), _ptr(cells, C.c_uint32), _ptr(cell_map, C.c_uint32),
+                                  C.byref(m))
+    if rc != 0:
+        raise ValueError(f"orc_build_mesh_map: {rc}")
+    return VolumeMap(nodes, cells, cell_map, m)
+
+
+def mesh_signed_distance(vertices, triangles, points, transform=None) -> np.ndarray:
+    """MeshDistance::SignedDistance (MeshDistance.cpp:187-228) at points, FP32."""
+    v, t, col, colp = _mesh(vertices, triangles, transform)
+    pts, pp = _f32(points)
+    out = np.zeros(len(pts), np.float32)
+    rc = lib().orc_mesh_signed_distance(_ptr(v, C.c_float), len(v), _ptr(t, C.c_uint32), len(t), colp, pp, len(pts),
+                                        _ptr(out, C.c_float))
+    if rc != 0:
+        raise ValueError(f"orc_mesh_signed_distance: {rc}")
+    return out
+
+
+def sample_mesh_volume(vertices, triangles, particle_radius: float, resolution=(20, 20, 20), inverted: bool = False,
+                       sample_mode: int = 0, transform=None) -> np.ndarray:
+    """ParticleSampler::SampleMeshVolume (ParticleSampler.cpp:7-91), on the CPU."""
+    v, t, col, colp = _mesh(vertices, triangles, transform)
+    res = np.ascontiguousarray(resolution, np.uint32)
+    count = C.c_uint32()
+    args = (_ptr(v, C.c_float), len(v), _ptr(t, C.c_uint32), len(t), colp, C.c_float(particle_radius),
+            _ptr(res, C.c_uint32), int(bool(inverted)), int(sample_mode))
+    rc = lib().orc_sample_mesh_volume(*args, None, 0, C.byref(count))
+    if rc != 0:
+        raise ValueError(f"orc_sample_mesh_volume: {rc}")
+    out = np.zeros((count.value, 3), np.float32)
+    if count.value:
+        lib().orc_sample_mesh_volume(*args, _ptr(out, C.c_float), count.value, C.byref(count))
+    return out
 
 
 def map_interpolate_d(vmap: VolumeMap, field: int, points):

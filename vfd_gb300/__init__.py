@@ -32,7 +32,7 @@ EXPORTS = [
     "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version", "vfd_profile_kernels",
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
-    "vfd_set_position_mode",
+    "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
@@ -116,6 +116,10 @@ def lib() -> C.CDLL:
                 "vfd_adjoint_backward": [P, f32p, f32p, f32p, f32p, f32p],
                 "vfd_adjoint_release": [P],
                 "vfd_set_position_mode": [P, C.c_int32],
+                "vfd_build_mesh_map": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_int32, C.c_float, u32p,
+                                       C.c_float, f32p, u32p, u32p, C.POINTER(vfd_volume_map)],
+                "vfd_sample_mesh_volume": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_float, u32p, C.c_int32,
+                                           C.c_int32, f32p, C.c_uint32, u32p],
                 "vfd_last_error": [],
                 "vfd_abi_version": [],
             }
@@ -191,6 +195,58 @@ def build_box_map(bmin, bmax, inverted: bool, padding: float, resolution, partic
                                    C.c_float(particle_radius), _fptr(nodes), _u32ptr(cells), _u32ptr(cell_map),
                                    C.byref(m)), "vfd_build_box_map")
     return VolumeMap(nodes, cells, cell_map, m)
+
+
+def _mesh_args(vertices, triangles, transform):
+    v = np.ascontiguousarray(np.asarray(vertices, np.float32).reshape(-1, 3))
+    t = np.ascontiguousarray(np.asarray(triangles, np.uint32).reshape(-1, 3))
+    if transform is None:
+        return v, t, None, None
+    m = np.asarray(transform, np.float32).reshape(4, 4)
+    col = np.ascontiguousarray(m.T.reshape(16))  # column-major, as glm stores a mat4
+    return v, t, col, _fptr(col)
+
+
+def build_mesh_map(vertices, triangles, transform=None, inverted: bool = False, padding: float = 0.0,
+                   resolution=(20, 20, 20), particle_radius: float = 0.025) -> VolumeMap:
+    """Volume map of a closed triangle mesh built on the GPU (RigidBody::RigidBody,
+    RigidBody.cu:10-72). `transform` is the body's 4x4 placement matrix (acting on column
+    vectors, translation in the last column) or None."""
+    res = np.ascontiguousarray(resolution, np.uint32)
+    nn, nc = C.c_uint32(), C.c_uint32()
+    _check(lib().vfd_box_map_sizes(_u32ptr(res), C.byref(nn), C.byref(nc)), "vfd_box_map_sizes")
+    v, t, col, colp = _mesh_args(vertices, triangles, transform)
+    nodes = np.zeros(2 * nn.value, np.float32)
+    cells = np.zeros(2 * nc.value * 32, np.uint32)
+    cell_map = np.zeros(2 * nc.value, np.uint32)
+    m = vfd_volume_map()
+    _check(lib().vfd_build_mesh_map(_fptr(v), len(v), _u32ptr(t), len(t), colp, int(bool(inverted)),
+                                    C.c_float(padding), _u32ptr(res), C.c_float(particle_radius), _fptr(nodes),
+                                    _u32ptr(cells), _u32ptr(cell_map), C.byref(m)), "vfd_build_mesh_map")
+    return VolumeMap(nodes, cells, cell_map, m)
+
+
+SAMPLE_MODES = {"min": _abi.VFD_SAMPLE_MIN_DENSITY, "medium": _abi.VFD_SAMPLE_MEDIUM_DENSITY,
+                "max": _abi.VFD_SAMPLE_MAX_DENSITY}
+
+
+def sample_mesh_volume(vertices, triangles, particle_radius: float, resolution=(20, 20, 20), inverted: bool = False,
+                       sample_mode=0, transform=None) -> np.ndarray:
+    """Particles filling a mesh (ParticleSampler::SampleMeshVolume, ParticleSampler.cpp:7-91,
+    on the GPU): an (n, 3) float32 array in the reference's lattice order. `sample_mode` is
+    0/1/2 or "min"/"medium"/"max"."""
+    mode = SAMPLE_MODES[sample_mode] if isinstance(sample_mode, str) else int(sample_mode)
+    res = np.ascontiguousarray(resolution, np.uint32)
+    v, t, col, colp = _mesh_args(vertices, triangles, transform)
+    count = C.c_uint32()
+    args = (_fptr(v), len(v), _u32ptr(t), len(t), colp, C.c_float(particle_radius), _u32ptr(res),
+            int(bool(inverted)), mode)
+    _check(lib().vfd_sample_mesh_volume(*args, None, 0, C.byref(count)), "vfd_sample_mesh_volume")
+    out = np.zeros((count.value, 3), np.float32)
+    if count.value:
+        _check(lib().vfd_sample_mesh_volume(*args, _fptr(out), count.value, C.byref(count)),
+               "vfd_sample_mesh_volume")
+    return out
 
 
 class DFSPHSimulation:

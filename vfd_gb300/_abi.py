@@ -13,6 +13,9 @@ import ctypes as C
 VFD_OK = 0
 VFD_POSITIONS_ABSOLUTE = 0
 VFD_POSITIONS_CELL_RELATIVE = 1
+VFD_SAMPLE_MIN_DENSITY = 0
+VFD_SAMPLE_MEDIUM_DENSITY = 1
+VFD_SAMPLE_MAX_DENSITY = 2
 VFD_E_ARG = 1
 VFD_E_CUDA = 2
 VFD_E_NONCONVERGED = 3

@@ -1007,6 +1007,12 @@ int vfd_box_map_sizes(const uint32_t resolution[3], uint32_t* node_count, uint32
     if (!resolution || !node_count || !cell_count) return fail(VFD_E_ARG, "null argument");
     for (int k = 0; k < 3; k++)
         if (resolution[k] == 0 || resolution[k] > 1024) return fail(VFD_E_ARG, "resolution must be in 1..1024");
+    // the builders index nodes * 32 quadrature lanes and cells * 32 node slots in 32 bits
+    const uint64_t r0 = resolution[0], r1 = resolution[1], r2 = resolution[2];
+    const uint64_t nodes = (r0 + 1) * (r1 + 1) * (r2 + 1) +
+                           2 * (r0 * (r1 + 1) * (r2 + 1) + (r0 + 1) * r1 * (r2 + 1) + (r0 + 1) * (r1 + 1) * r2);
+    if (32 * nodes > 0xffffffffull) return fail(VFD_E_ARG, "resolution too fine (%llu map nodes)",
+                                                (unsigned long long)nodes);
     box_map_sizes(resolution, *node_count, *cell_count);
     return VFD_OK;
 }
@@ -1038,6 +1044,73 @@ int vfd_build_box_map(const float box_min[3], const float box_max[3], int32_t in
     out->node_count = nn;
     out->cell_count = nc;
     out->cell_map_count = nc;
+    return VFD_OK;
+}
+
+// Checks the mesh arguments shared by the mesh entry points and places the mesh.
+static int mesh_arguments(const float* vertices, uint32_t vertexCount, const uint32_t* triangles,
+                          uint32_t triangleCount, const float* transform, MeshHost& mesh) {
+    if (!vertices || !triangles) return fail(VFD_E_ARG, "null mesh");
+    if (vertexCount == 0 || triangleCount == 0) return fail(VFD_E_ARG, "empty mesh");
+    if (prepare_mesh(vertices, vertexCount, triangles, triangleCount, transform, mesh) != 0)
+        return fail(VFD_E_ARG, "triangle index out of range (vertex count %u)", vertexCount);
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(mesh.bmin[k]) || !std::isfinite(mesh.bmax[k])) return fail(VFD_E_ARG, "non-finite vertex");
+    return VFD_OK;
+}
+
+int vfd_build_mesh_map(const float* vertices, uint32_t vertex_count, const uint32_t* triangles,
+                       uint32_t triangle_count, const float* transform, int32_t inverted, float padding,
+                       const uint32_t resolution[3], float particle_radius, float* nodes, uint32_t* cells,
+                       uint32_t* cell_map, vfd_volume_map* out) {
+    if (!resolution || !nodes || !cells || !cell_map || !out) return fail(VFD_E_ARG, "null argument");
+    if (!(particle_radius > 0.0f)) return fail(VFD_E_ARG, "particle radius must be positive");
+    uint32_t nn = 0, nc = 0;
+    TRY(vfd_box_map_sizes(resolution, &nn, &nc));
+    MeshHost mesh;
+    TRY(mesh_arguments(vertices, vertex_count, triangles, triangle_count, transform, mesh));
+    int devCount = 0;
+    if (cudaGetDeviceCount(&devCount) != cudaSuccess || devCount == 0) return fail(VFD_E_NODEVICE, "no CUDA device");
+    CK(cudaSetDevice(g_device));
+    KernelTable t;
+    t.setRadius(4.0f * particle_radius);
+    const int e = build_mesh_map_gpu(mesh, inverted != 0, padding, resolution, particle_radius, t.W.data(), t.wZero,
+                                     t.invStep, nodes, cells, cell_map, out->domain_min, out->domain_max,
+                                     out->cell_size, out->cell_size_inverse);
+    if (e != 0) return fail(VFD_E_CUDA, "mesh volume map build: %s", cudaGetErrorString((cudaError_t)e));
+    out->nodes = nodes;
+    out->cells = cells;
+    out->cell_map = cell_map;
+    for (int k = 0; k < 3; k++) out->resolution[k] = resolution[k];
+    out->field_count = 2;
+    out->node_count = nn;
+    out->cell_count = nc;
+    out->cell_map_count = nc;
+    return VFD_OK;
+}
+
+int vfd_sample_mesh_volume(const float* vertices, uint32_t vertex_count, const uint32_t* triangles,
+                           uint32_t triangle_count, const float* transform, float particle_radius,
+                           const uint32_t resolution[3], int32_t inverted, int32_t sample_mode,
+                           float* positions, uint32_t capacity, uint32_t* count) {
+    if (!resolution || !count) return fail(VFD_E_ARG, "null argument");
+    *count = 0;
+    if (!(particle_radius > 0.0f) || !std::isfinite(particle_radius))
+        return fail(VFD_E_ARG, "particle radius must be positive");
+    if (sample_mode < VFD_SAMPLE_MIN_DENSITY || sample_mode > VFD_SAMPLE_MAX_DENSITY)
+        return fail(VFD_E_ARG, "unknown sample mode %d", sample_mode);
+    uint32_t nn = 0, nc = 0;
+    TRY(vfd_box_map_sizes(resolution, &nn, &nc));
+    MeshHost mesh;
+    TRY(mesh_arguments(vertices, vertex_count, triangles, triangle_count, transform, mesh));
+    int devCount = 0;
+    if (cudaGetDeviceCount(&devCount) != cudaSuccess || devCount == 0) return fail(VFD_E_NODEVICE, "no CUDA device");
+    CK(cudaSetDevice(g_device));
+    const int e = sample_mesh_volume_gpu(mesh, particle_radius, resolution, inverted != 0, sample_mode, positions,
+                                         capacity, count);
+    if (e < 0) return fail(VFD_E_CAPACITY, "sampling lattice too large for the radius");
+    if (e != 0) return fail(VFD_E_CUDA, "mesh volume sampling: %s", cudaGetErrorString((cudaError_t)e));
+    if (positions && *count > capacity) return fail(VFD_E_CAPACITY, "%u samples, capacity %u", *count, capacity);
     return VFD_OK;
 }
 

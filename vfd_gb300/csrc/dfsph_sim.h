@@ -33,6 +33,22 @@ void box_map_sizes(const uint32_t res[3], uint32_t& nodes, uint32_t& cells);
 int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, float padding, const uint32_t res[3],
                       float r, const float* table, float wZero, float invStep, float* nodes, uint32_t* cells,
                       uint32_t* cellMap, float dminOut[3], float dmaxOut[3], float csOut[3], float csiOut[3]);
+
+// A triangle mesh placed in the world, as the distance kernels read it.
+struct MeshHost {
+    std::vector<float4> corners;  // 3 per face: corners A, B, C (w unused)
+    std::vector<float4> normals;  // 7 per face: corner A, B, C; edge AB, BC, CA; face (w unused)
+    float bmin[3], bmax[3];       // bounds of all placed vertices
+};
+// Places the vertices by `transform` (column-major 4x4, null = identity) and computes the
+// pseudo-normals. Returns 0, or -1 when a triangle names a vertex out of range.
+int prepare_mesh(const float* vertices, uint32_t vertexCount, const uint32_t* triangles, uint32_t triangleCount,
+                 const float* transform, MeshHost& out);
+int build_mesh_map_gpu(const MeshHost& mesh, bool inverted, float padding, const uint32_t res[3], float r,
+                       const float* table, float wZero, float invStep, float* nodes, uint32_t* cells,
+                       uint32_t* cellMap, float dminOut[3], float dmaxOut[3], float csOut[3], float csiOut[3]);
+int sample_mesh_volume_gpu(const MeshHost& mesh, float radius, const uint32_t res[3], bool inverted, int mode,
+                           float* out, uint32_t capacity, uint32_t* count);
 }  // namespace vfd
 
 namespace vfd {
