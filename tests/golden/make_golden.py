@@ -10,7 +10,10 @@ fixture that the oracle and the CUDA library are checked against:
   * the 16-point Gauss-Legendre rule the volume map uses (p = 30,
     Core/Math/GaussQuadrature.cpp: GaussianN1, GaussianAbscissae1, GaussianWeights1);
   * the surface-tension classifier constants (DFSPHImplementation.cu:360-365);
-  * the description defaults (DFSPHSimulationDescription.h:11-48).
+  * the description defaults (DFSPHSimulationDescription.h:11-48);
+  * the scene-file layout: the component order of Scene::Save (Scene/Scene.cpp:17-30)
+    and the archive names of the DFSPH description, rigid-body and fluid-object
+    serializers (Scene/Components/*.h), as the scene loader reads them.
 
 Usage: python tests/golden/make_golden.py [VFD_ROOT]
 (default VFD_ROOT: /root/reference). Run only where the reference is present.
@@ -101,10 +104,26 @@ def defaults(root: str) -> dict:
     return out
 
 
+def scene_format(root: str) -> dict:
+    src = os.path.join(root, "VFD", "Source", "Scene")
+    with open(os.path.join(src, "Scene.cpp")) as f:
+        text = f.read()
+    m = re.search(r"entt::snapshot\s*\{[^}]*\}\s*\.entities\(output\)\s*\.component<([^>]*)>", text)
+    order = [t.strip() for t in m.group(1).split(",")]
+
+    def nvps(name: str) -> list[str]:
+        with open(os.path.join(src, "Components", name)) as f:
+            return re.findall(r'make_nvp\("([^"]+)"', f.read())
+
+    return dict(components=order, dfsph_description=nvps("DFSPHSimulationComponent.h"),
+                rigid_body=nvps("RigidBodyComponent.h"), fluid_object=nvps("FluidObjectComponent.h"),
+                transform=nvps("TransformComponent.h"), mesh=nvps("MeshComponent.h"))
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     data = dict(source="VFD (Goubermouche/VFD) source text", halton=halton(root), gauss_legendre=gauss_legendre(root),
-                constants=constants(root), description_defaults=defaults(root))
+                constants=constants(root), description_defaults=defaults(root), scene_format=scene_format(root))
     out = os.path.join(HERE, "reference_tables.json")
     with open(out, "w") as f:
         json.dump(data, f, indent=1)

@@ -62,7 +62,15 @@ f 1 2 6
     p.write_text(text)
     v, t = meshes.load_obj(str(p))
     assert v.shape == (6, 3) and v.dtype == np.float32      # every vertex, as the reference keeps
-    np.testing.assert_array_equal(t, [[0, 1, 2], [0, 2, 3], [1, 0, 4], [1, 3, 2], [3, 2, 4], [0, 4, 3]])
+    # the square's diagonals are equally long: split along 1-3 (tinyobjloader's quad rule)
+    first = [[0, 1, 3], [1, 2, 3], [1, 0, 4], [1, 3, 2], [3, 2, 4], [0, 4, 3]]
+    np.testing.assert_array_equal(t, first + [[0, 1, 5]])  # every shape (TriangleMesh)
+    _, t1 = meshes.load_obj(str(p), first_shape_only=True)  # EdgeMesh(filepath)
+    np.testing.assert_array_equal(t1, first)
+    pq = tmp_path / "polygons.obj"
+    pq.write_text("v 0 0 0\nv 2 0 0\nv 2 1 0\nv 0 1 0\nv 1 2 0\nf 1 2 3 4\nf 1 2 3 5 4\n")
+    _, tq = meshes.load_obj(str(pq))
+    np.testing.assert_array_equal(tq, [[0, 1, 3], [1, 2, 3], [0, 1, 2], [0, 2, 4], [0, 4, 3]])
     v2, t2 = meshes.load_obj(str(p), scale=(2, 1, 1))
     np.testing.assert_array_equal(v2[:, 0], 2 * v[:, 0])
     q = tmp_path / "box.obj"

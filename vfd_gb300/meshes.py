@@ -1,19 +1,39 @@
 """Triangle meshes for rigid bodies and fluid volumes.
 
-`load_obj` reads a Wavefront OBJ the way the reference's EdgeMesh constructor does
-(Renderer/Mesh/EdgeMesh.cpp:61-130 through tinyobjloader): every `v` line becomes a
-vertex, the faces are those of the first shape (the faces before the first `o` or `g`
-line that follows a face), and a face names its corners by their position indices
-(texture and normal indices are ignored). Polygons with more than three corners are
-split into a fan around their first corner. The generators build closed meshes with
-outward, counter-clockwise triangles, the orientation the signed distance expects.
+`load_obj` reads a Wavefront OBJ as the reference's scene meshes are read
+(TriangleMesh::TriangleMesh, Renderer/Mesh/TriangleMesh.cpp:40-120, through the
+vendored tinyobjloader 2.0.0rc, ThirdParty/tinyobjloader): every `v` line is a vertex,
+every face of every shape is kept, and a face names its corners by their position
+indices (texture and normal indices are ignored; negative indices count back from the
+last vertex read). `first_shape_only=True` keeps the faces of the first shape only, as
+EdgeMesh::EdgeMesh(filepath) does (Renderer/Mesh/EdgeMesh.cpp:61-96); a new shape
+starts at an `o` or `g` line that follows a face. Quads are split along their shorter
+diagonal as tinyobjloader does (the (0,1,2),(0,2,3) pair when |v2 - v0| < |v3 - v1| in
+FP32, else (0,1,3),(1,2,3)); larger polygons are split into a fan around their first
+corner (tinyobjloader clips ears there; convex polygons give the same area either way).
+The generators build closed meshes with outward, counter-clockwise triangles, the
+orientation the signed distance expects.
 """
 from __future__ import annotations
 
 import numpy as np
 
 
-def load_obj(path: str, scale=(1.0, 1.0, 1.0)):
+def _split_polygon(idx, verts):
+    if len(idx) == 3:
+        return [idx]
+    if len(idx) == 4:
+        p = [np.asarray(verts[i], np.float32) for i in idx]
+        e02, e13 = p[2] - p[0], p[3] - p[1]
+        sq02 = np.float32(np.float32(e02[0] * e02[0] + e02[1] * e02[1]) + e02[2] * e02[2])
+        sq13 = np.float32(np.float32(e13[0] * e13[0] + e13[1] * e13[1]) + e13[2] * e13[2])
+        if sq02 < sq13:
+            return [[idx[0], idx[1], idx[2]], [idx[0], idx[2], idx[3]]]
+        return [[idx[0], idx[1], idx[3]], [idx[1], idx[2], idx[3]]]
+    return [[idx[0], idx[k], idx[k + 1]] for k in range(1, len(idx) - 1)]
+
+
+def load_obj(path: str, scale=(1.0, 1.0, 1.0), first_shape_only: bool = False):
     """(vertices float32 (n, 3), triangles uint32 (m, 3)) of an OBJ file."""
     verts, tris = [], []
     seen_face = first_done = False
@@ -25,7 +45,7 @@ def load_obj(path: str, scale=(1.0, 1.0, 1.0)):
             tok = line.split()
             key = tok[0]
             if key == "v":
-                verts.append([float(tok[1]), float(tok[2]), float(tok[3])])
+                verts.append([np.float32(tok[1]), np.float32(tok[2]), np.float32(tok[3])])
             elif key == "f":
                 if first_done:
                     continue
@@ -35,15 +55,14 @@ def load_obj(path: str, scale=(1.0, 1.0, 1.0)):
                 for t in tok[1:]:
                     i = int(t.split("/", 1)[0])
                     idx.append(i - 1 if i > 0 else len(verts) + i)
-                for k in range(1, len(idx) - 1):
-                    tris.append([idx[0], idx[k], idx[k + 1]])
+                if min(idx) < 0 or max(idx) >= len(verts):
+                    raise ValueError(f"{path}: face index out of range: {line!r}")
+                tris += _split_polygon(idx, verts)
                 seen_face = True
-            elif key in ("o", "g") and seen_face:
+            elif key in ("o", "g") and seen_face and first_shape_only:
                 first_done = True
     v = np.asarray(verts, np.float32).reshape(-1, 3) * np.asarray(scale, np.float32)
     t = np.asarray(tris, np.int64).reshape(-1, 3)
-    if len(t) and (t.min() < 0 or t.max() >= len(v)):
-        raise ValueError(f"{path}: face index out of range")
     return v.astype(np.float32), t.astype(np.uint32)
 
 
