@@ -292,7 +292,8 @@ int vfd_steps(vfd_sim* sim, uint32_t count, vfd_step_stats* stats);
 int vfd_steps_async(vfd_sim* sim, uint32_t count);
 int vfd_synchronize(vfd_sim* sim, vfd_step_stats* stats);
 
-/* Frame callback for vfd_simulate: x, v, a are n*3 floats in original order. */
+/* Frame callback for vfd_simulate: x, v, a are n*3 floats in original order, valid
+ * until the callback returns (they point into pinned staging memory). */
 typedef void (*vfd_frame_callback)(uint32_t frame_index, uint32_t n, const float* x,
                                    const float* v, const float* a, float max_velocity,
                                    float time_step, void* user);
@@ -300,7 +301,10 @@ typedef void (*vfd_frame_callback)(uint32_t frame_index, uint32_t n, const float
 /*
  * DFSPHImplementation::Simulate (DFSPHImplementation.cu:33-61) with the frame
  * capture of OnUpdate (:148-167): resets, then steps until FrameCount frames
- * were emitted; each frame is handed to `cb` (may be NULL).
+ * were emitted; each frame is handed to `cb` (may be NULL), in order, on the
+ * calling thread. Steps are queued ahead of the host and each frame is copied
+ * to pinned memory on a second stream while the next steps run; the run ends
+ * on the step that completed the last frame. Single-scene simulations only.
  */
 int vfd_simulate(vfd_sim* sim, vfd_frame_callback cb, void* user);
 

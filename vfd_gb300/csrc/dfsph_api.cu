@@ -89,6 +89,55 @@ __global__ void k_import_pos(Dev d, const float* in, float4* dst, uint32_t begin
     const int3 A = make_int3((int)fx, (int)fy, (int)fz);
     dst[p] = make_float4(x.x - fx * L, x.y - fy * L, x.z - fz * L, anchor_pack(A));
 }
+
+// Frame output of vfd_simulate. When a step completes a frame (k_ctrl_end sets frameDue;
+// DFSPHImplementation.cu:148-167 copies the frame there), x, v and a of the particles go
+// to slot (frame - 1) % slots of a device ring, in the original particle order
+// (ConvertParticlesToBuffer); the host copies the slot out asynchronously.
+__global__ void k_frame_snapshot(Dev d, float* ring, uint32_t slots, uint32_t count) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= count || is_aborted(d)) return;
+    const SceneDev& S = d.scenes[0];
+    if (!S.frameDue) return;
+    const uint32_t o = d.PIDc[p];
+    if (o >= count) return;
+    float* slot = ring + (size_t)((S.frameIndex - 1u) % slots) * 9u * count;
+    const float4 x4 = d.XN[p];
+    const float3 x = d.cellRel ? abs_pos(d, S, x4) : make_float3(x4.x, x4.y, x4.z);
+    const float4 v = d.Vc[p], a = d.A[p];
+    float* xs = slot + 3 * (size_t)o;
+    float* vs = slot + 3 * ((size_t)count + o);
+    float* as = slot + 3 * (2 * (size_t)count + o);
+    xs[0] = x.x, xs[1] = x.y, xs[2] = x.z;
+    vs[0] = v.x, vs[1] = v.y, vs[2] = v.z;
+    as[0] = a.x, as[1] = a.y, as[2] = a.z;
+}
+
+struct FrameNote {
+    uint32_t due, index, aborted, flags;
+    float maxV, dt;
+    uint32_t pad[2];
+};
+
+// What the host needs of a step without waiting for the ones after it: whether it made
+// a frame, and the abort and error words. After the last frame the later steps already
+// in the queue are turned into no-ops (abort word 2), so that the run ends on the step
+// that completed the last frame, as the reference's frame loop does
+// (DFSPHImplementation.cu:52-55).
+__global__ void k_frame_note(Dev d, FrameNote* note, uint32_t lastFrame) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const SceneDev& S = d.scenes[0];
+    FrameNote n;
+    n.aborted = d.status[1];
+    n.due = (n.aborted == 0u && S.frameDue) ? 1u : 0u;
+    n.index = S.frameIndex;
+    n.flags = d.status[0];
+    n.maxV = S.maxV2;
+    n.dt = S.dt;
+    n.pad[0] = n.pad[1] = 0u;
+    *note = n;
+    if (n.due && S.frameIndex >= lastFrame) d.status[1] = 2u;
+}
 }  // namespace vfd
 
 using namespace vfd;
@@ -1390,28 +1439,156 @@ int vfd_get_kernel_table(const vfd_sim* s, float* w, float* grad_w, float* radiu
     return VFD_OK;
 }
 
+// Device ring, pinned host ring, step notes and events of one vfd_simulate call.
+struct FramePipe {
+    static constexpr uint32_t kSlots = 4;      // frames in the rings
+    static constexpr uint32_t kLookahead = 3;  // steps in flight ahead of the host (<= kSlots)
+    float* dRing = nullptr;
+    float* hRing = nullptr;
+    FrameNote* dNotes = nullptr;
+    FrameNote* hNotes = nullptr;
+    cudaStream_t copy = nullptr;
+    cudaStream_t main = nullptr;  // the simulation's stream
+    uint32_t* status = nullptr;   // its status words
+    cudaEvent_t stepDone[kLookahead] = {};
+    cudaEvent_t copyDone[kSlots] = {};
+    ~FramePipe() {
+        // nothing of this call may still run when its buffers go; a stop word (2) left by
+        // an early return would turn the simulation's next steps into no-ops
+        if (main) cudaStreamSynchronize(main);
+        if (copy) cudaStreamSynchronize(copy);
+        if (status) {
+            uint32_t w = 0;
+            if (cudaMemcpy(&w, status + 1, sizeof(w), cudaMemcpyDeviceToHost) == cudaSuccess && w == 2u)
+                cudaMemset(status + 1, 0, sizeof(uint32_t));
+        }
+        cudaFree(dRing);
+        cudaFreeHost(hRing);
+        cudaFree(dNotes);
+        cudaFreeHost(hNotes);
+        for (auto& e : stepDone)
+            if (e) cudaEventDestroy(e);
+        for (auto& e : copyDone)
+            if (e) cudaEventDestroy(e);
+        if (copy) cudaStreamDestroy(copy);
+    }
+};
+
+// DFSPHImplementation::Simulate (DFSPHImplementation.cu:33-61): from the initial state,
+// steps until FrameCount frames are complete, handing each frame to `cb`. The steps are
+// queued up to FramePipe::kLookahead ahead of the host; a frame is copied from the device
+// ring to pinned memory on a second stream while the next steps run, and `cb` runs on
+// the calling thread, in frame order, once its copy has landed.
 int vfd_simulate(vfd_sim* s, vfd_frame_callback cb, void* user) {
     TRY(check_sim(s));
+    if (s->scenes.size() != 1) return fail(VFD_E_ARG, "vfd_simulate runs single-scene simulations");
     CK(cudaSetDevice(s->device));
     TRY(upload(s));
     const uint32_t n = (uint32_t)(s->scenes[0].x0.size() / 3);
-    std::vector<float> x(3ull * n), v(3ull * n), a(3ull * n);
     const uint32_t frames = s->scenes[0].desc.FrameCount;
-    uint32_t lastFrame = 0;
-    for (uint64_t guard = 0; guard < 100000000ull; guard++) {
-        vfd_step_stats st;
-        TRY(vfd_step(s, &st));
-        if (st.FrameIndex != lastFrame) {
-            lastFrame = st.FrameIndex;
+    if (frames == 0 || n == 0) return VFD_OK;
+    TRY(ensure_ready(s));
+    constexpr uint32_t R = FramePipe::kSlots, L = FramePipe::kLookahead;
+    FramePipe fp;
+    fp.main = s->stream;
+    fp.status = s->dStatus;
+    const size_t frameFloats = 9 * (size_t)n;
+    CK(cudaMalloc(&fp.dRing, sizeof(float) * frameFloats * R));
+    CK(cudaMallocHost(&fp.hRing, sizeof(float) * frameFloats * R));
+    CK(cudaMalloc(&fp.dNotes, sizeof(FrameNote) * L));
+    CK(cudaMallocHost(&fp.hNotes, sizeof(FrameNote) * L));
+    CK(cudaStreamCreateWithFlags(&fp.copy, cudaStreamNonBlocking));
+    for (auto& e : fp.stepDone) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : fp.copyDone) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
+
+    struct Pending {
+        uint32_t frame;
+        float maxV, dt;
+    };
+    std::vector<Pending> pending;  // frames copied or being copied, in order
+    auto deliver = [&](bool wait, uint32_t upTo) -> int {
+        size_t k = 0;
+        for (; k < pending.size(); k++) {
+            const Pending& f = pending[k];
+            const uint32_t slot = (f.frame - 1u) % R;
+            if (wait || f.frame <= upTo) {
+                CK(cudaEventSynchronize(fp.copyDone[slot]));
+            } else {
+                const cudaError_t q = cudaEventQuery(fp.copyDone[slot]);
+                if (q == cudaErrorNotReady) break;
+                CK(q);
+            }
             if (cb) {
-                TRY(vfd_get_state(s, x.data(), v.data(), a.data()));
-                cb(st.FrameIndex - 1, n, x.data(), v.data(), a.data(), st.MaxVelocityMagnitude, st.TimeStepSize, user);
+                const float* base = fp.hRing + slot * frameFloats;
+                cb(f.frame - 1u, n, base, base + 3 * (size_t)n, base + 6 * (size_t)n, f.maxV, f.dt, user);
             }
         }
-        if (st.FrameIndex >= frames) return VFD_OK;
-        if (n == 0) return VFD_OK;
+        pending.erase(pending.begin(), pending.begin() + k);
+        return VFD_OK;
+    };
+    // the completed-step count decides which state set holds the result (aborted steps
+    // leave it where it was)
+    auto settle = [&](int cs0) -> int {
+        CK(cudaStreamSynchronize(s->stream));
+        CK(cudaMemcpy(s->hStatus, s->dStatus, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        s->cs = (s->hStatus[7] & 1u) ? 1 - cs0 : cs0;
+        CK(cudaMemset(s->dStatus + 7, 0, sizeof(uint32_t)));
+        return VFD_OK;
+    };
+
+    uint64_t launched = 0, processed = 0;
+    int cs0 = s->cs;
+    bool stop = false, searchAbort = false, finished = false;
+    for (uint64_t guard = 0; guard < 100000000ull && !finished; guard++) {
+        while (!stop && launched - processed < L) {
+            for (uint32_t r = 0; r < R; r++) CK(cudaStreamWaitEvent(s->stream, fp.copyDone[r], 0));
+            TRY(launch_one(s));
+            const Dev& d = s->dev[s->cs];
+            const uint32_t k = (uint32_t)(launched % L);
+            k_frame_snapshot<<<blocks_for(n, 256), 256, 0, s->stream>>>(d, fp.dRing, R, n);
+            k_frame_note<<<1, 32, 0, s->stream>>>(d, fp.dNotes + k, frames);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(fp.hNotes + k, fp.dNotes + k, sizeof(FrameNote), cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaEventRecord(fp.stepDone[k], s->stream));
+            launched++;
+        }
+        if (processed < launched) {
+            const uint32_t k = (uint32_t)(processed % L);
+            CK(cudaEventSynchronize(fp.stepDone[k]));
+            const FrameNote note = fp.hNotes[k];
+            processed++;
+            if (note.aborted == 1u && !stop) {
+                searchAbort = true;  // the search aborted: drain, grow the cell table, go on
+                stop = true;
+            } else if (note.due) {
+                const uint32_t slot = (note.index - 1u) % R;
+                TRY(deliver(false, note.index > R ? note.index - R : 0u));  // the host slot is free
+                CK(cudaStreamWaitEvent(fp.copy, fp.stepDone[k], 0));
+                CK(cudaMemcpyAsync(fp.hRing + slot * frameFloats, fp.dRing + slot * frameFloats,
+                                   sizeof(float) * frameFloats, cudaMemcpyDeviceToHost, fp.copy));
+                CK(cudaEventRecord(fp.copyDone[slot], fp.copy));
+                pending.push_back({note.index, note.maxV, note.dt});
+                if (note.index >= frames) stop = true;
+            }
+            TRY(deliver(false, 0u));
+        }
+        if (stop && processed == launched) {
+            TRY(settle(cs0));
+            if (!searchAbort) {
+                finished = true;
+                break;
+            }
+            if (s->hStatus[0] & 0x10u) return fail(VFD_E_NAN, "non-finite particle position");
+            CK(cudaMemset(s->dStatus + 1, 0, sizeof(uint32_t)));
+            TRY(grow_cells(s));
+            cs0 = s->cs;
+            stop = searchAbort = false;
+        }
     }
-    return fail(VFD_E_STATE, "frame clock did not advance");
+    TRY(deliver(true, 0u));
+    if (!finished) return fail(VFD_E_STATE, "frame clock did not advance");
+    return VFD_OK;
 }
 
 int vfd_profile_kernels(vfd_sim* s, uint32_t steps, vfd_kernel_time* out, uint32_t capacity, uint32_t* count) {
