@@ -53,6 +53,10 @@ enum {
 #define VFD_POSITIONS_ABSOLUTE       0  /* FP32 absolute coordinates, as the reference stores them */
 #define VFD_POSITIONS_CELL_RELATIVE  1  /* FP32 offsets within anchor cells of edge h             */
 
+/* SPH kernel evaluation modes (vfd_set_kernel_mode). */
+#define VFD_KERNEL_TABLE     0  /* midpoint of two 10000-entry table values, as the reference */
+#define VFD_KERNEL_ANALYTIC  1  /* the cubic spline evaluated at |r| (smooth in r)            */
+
 /* Maximum neighbours per particle, ParticleSearchKernels.cuh:7 (CUDA_MAX_NEIGHBORS). */
 #define VFD_MAX_NEIGHBORS 70u
 
@@ -459,6 +463,16 @@ int vfd_adjoint_release(vfd_sim* sim);
  * leaving the anchor range fails the step with VFD_E_CAPACITY (VFD_FLAG_ANCHOR_RANGE).
  */
 int vfd_set_position_mode(vfd_sim* sim, int32_t mode);
+
+/*
+ * Kernel evaluation: VFD_KERNEL_TABLE (default) looks W and gradW up in the
+ * precomputed tables as PrecomputedDFSPHCubicKernel does (Kernel/DFSPHKernels.h:43-80);
+ * VFD_KERNEL_ANALYTIC evaluates the same cubic spline (:86-131) at |r|, which makes the
+ * step smooth in the positions, so that finite differences of it match its adjoint.
+ * No counterpart in the reference. Call before the first step; like
+ * vfd_set_position_mode it drops the device state.
+ */
+int vfd_set_kernel_mode(vfd_sim* sim, int32_t mode);
 
 /* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
 int vfd_set_device(int32_t device);

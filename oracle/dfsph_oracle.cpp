@@ -141,6 +141,7 @@ struct KernelTable {
     static const unsigned R = 10000u;
     std::vector<T> W, G;
     T radius = 0, radius2 = 0, invStep = 0, wZero = 0, K = 0, L = 0;
+    bool analytic = false;  // the spline at |r| instead of the table (analytic kernel mode)
 
     T calcW(T r) const {  // :86-104
         T res = 0;
@@ -197,17 +198,29 @@ struct KernelTable {
         return std::min(p, R - 2u);
     }
     T getW(T r) const {  // :43-52
-        if (r <= radius) { const unsigned p = pos(r); return T(0.5) * (W[p] + W[p + 1]); }
+        if (r <= radius) {
+            if (analytic) return calcW(r);
+            const unsigned p = pos(r);
+            return T(0.5) * (W[p] + W[p + 1]);
+        }
         return 0;
     }
     T getW(const V3<T>& r) const {  // :54-65
         const T r2 = dot(r, r);
-        if (r2 <= radius2) { const unsigned p = pos(std::sqrt(r2)); return T(0.5) * (W[p] + W[p + 1]); }
+        if (r2 <= radius2) {
+            if (analytic) return calcW(std::sqrt(r2));
+            const unsigned p = pos(std::sqrt(r2));
+            return T(0.5) * (W[p] + W[p + 1]);
+        }
         return 0;
     }
     V3<T> getGradW(const V3<T>& r) const {  // :67-80
         const T rl = std::sqrt(dot(r, r));
-        if (rl <= radius) { const unsigned p = pos(rl); return (T(0.5) * (G[p] + G[p + 1])) * r; }
+        if (rl <= radius) {
+            if (analytic) return calcGradW(r);
+            const unsigned p = pos(rl);
+            return (T(0.5) * (G[p] + G[p + 1])) * r;
+        }
         return V3<T>();
     }
 };
@@ -1731,6 +1744,14 @@ int orc_add_rigid_body(void* p, const vfd_volume_map* m) {
 }
 
 int orc_reset(void* p) { Handle* h = static_cast<Handle*>(p); ORC_DISPATCH(h, reset()); return VFD_OK; }
+
+// Kernel evaluation: 0 = the reference's tables, 1 = the spline at |r| (analytic mode).
+int orc_set_kernel_mode(void* p, int mode) {
+    Handle* h = static_cast<Handle*>(p);
+    if (h->f) h->f->kernel.analytic = mode != 0;
+    if (h->d) h->d->kernel.analytic = mode != 0;
+    return VFD_OK;
+}
 
 int orc_step(void* p, vfd_step_stats* st) { Handle* h = static_cast<Handle*>(p); return ORC_DISPATCH(h, step(st)); }
 

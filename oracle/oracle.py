@@ -47,6 +47,7 @@ def lib():
             L.orc_set_fluid.argtypes = [P, f32p, f32p, C.c_uint32]
             L.orc_add_rigid_body.argtypes = [P, C.POINTER(_abi.vfd_volume_map)]
             L.orc_reset.argtypes = [P]
+            L.orc_set_kernel_mode.argtypes = [P, C.c_int]
             L.orc_step.argtypes = [P, C.POINTER(_abi.vfd_step_stats)]
             L.orc_find_neighbors.argtypes = [P]
             L.orc_get_neighbors.argtypes = [P, u32p, u32p, u32p, C.c_uint32, u32p, u32p, u32p]
@@ -288,6 +289,10 @@ class OracleSim:
 
     def reset(self):
         lib().orc_reset(self.h)
+
+    def set_kernel_mode(self, analytic: bool):
+        """The spline at |r| (analytic) or the reference's tables."""
+        lib().orc_set_kernel_mode(self.h, int(bool(analytic)))
 
     def step(self) -> dict:
         st = _abi.vfd_step_stats()

@@ -1,6 +1,6 @@
 """The GPU adjoint of the step (vfd_adjoint_forward / vfd_adjoint_backward).
 
-Two checks:
+Three checks:
   * against the FP64 CPU reference gradient (oracle/adjoint_ref.py, itself pinned by
     FP64 central differences) on a block falling onto a floor with viscosity, the
     divergence and pressure solves and the CFL step: the full step;
@@ -9,6 +9,10 @@ Two checks:
     divergence to zero, which puts its residual clamp min(-rho_adv - f, 0) and the
     pressure clamp max(rho_adv - 1, 0) at their kinks, so FP32 differences with a
     usable step straddle kinks there; those cases are left to the FP64 reference.
+  * the same finite differences at 1e-3 with the analytic kernel mode and a fixed time
+    step, where the step is smooth: the reference's kernel tables are piecewise constant
+    in |r| and the adaptive step follows the fastest particle (an argmax), both kinks
+    that finite differences straddle.
 The Jacobi iteration counts are pinned (min = max), as finite differences of a solve
 that stops at a tolerance jump when the count changes.
 """
@@ -41,9 +45,11 @@ def _floor_scene(div: bool, n_side: int = 6, fixed_dt: bool = False):
 
 
 class GpuRun:
-    def __init__(self, sc, steps, every):
+    def __init__(self, sc, steps, every, analytic=False):
         self.sc, self.steps, self.every = sc, steps, every
         self.sim = V.DFSPHSimulation(V.make_desc(**sc["desc"]))
+        if analytic:
+            self.sim.SetKernelMode(True)
         self.sim.SetFluidObjects(sc["x"], sc["v"])
         for m in sc["maps"]:
             self.sim.AddRigidBody(m)
@@ -157,6 +163,47 @@ def test_adjoint_position_finite_difference(smooth):
     # the kernel table is piecewise constant in |r|: finite differences of positions see
     # quantised kernel values, so this check is looser than the FP64 one above
     _check("dL/dx0 . d (finite difference)", float(np.sum(g["x0b"] * d)), fd, 1e-1)
+
+
+# ------------------------------------------------------------ analytic kernel, fixed step
+@pytest.fixture(scope="module")
+def smooth_analytic():
+    sc = _floor_scene(div=False, fixed_dt=True)
+    run = GpuRun(sc, 6, 4, analytic=True)
+    return run, run.gradient()
+
+
+@pytest.mark.parametrize("along_gradient", [True, False])
+def test_analytic_velocity_finite_difference(smooth_analytic, along_gradient):
+    run, g = smooth_analytic
+    # along the gradient the loss changes most, far above FP32 rounding; a random
+    # direction is nearly orthogonal to it, so its difference carries more rounding
+    d = g["v0b"] / np.sqrt(np.mean(g["v0b"] ** 2)) if along_gradient else _direction(run.sc["v"].shape, 3)
+    eps = 2e-3
+    fd = (run.loss(v0=(run.sc["v"] + eps * d).astype(np.float32)) -
+          run.loss(v0=(run.sc["v"] - eps * d).astype(np.float32))) / (2 * eps)
+    _check("dL/dv0 . d (analytic kernel, finite difference)", float(np.sum(g["v0b"] * d)), fd,
+           1e-3 if along_gradient else 3e-3)
+
+
+def test_analytic_viscosity_finite_difference(smooth_analytic):
+    run, g = smooth_analytic
+    nu, nub = run.sc["desc"]["Viscosity"], run.sc["desc"]["BoundaryViscosity"]
+    eps = 1e-2  # six fixed steps: the viscosity moves the loss little, so a wider step
+    fd = (run.loss(nu=nu * (1 + eps), nub=nub * (1 + eps)) - run.loss(nu=nu * (1 - eps), nub=nub * (1 - eps))) / (2 * eps)
+    _check("dL/dlog(viscosity) (analytic kernel, finite difference)", float(g["pb"][0] * nu + g["pb"][1] * nub), fd,
+           1e-3)
+
+
+def test_analytic_position_finite_difference(smooth_analytic):
+    run, g = smooth_analytic
+    d = _direction(run.sc["x"].shape, 4)
+    eps = 1e-4
+    fd = (run.loss(x0=(run.sc["x"] + eps * d).astype(np.float32)) -
+          run.loss(x0=(run.sc["x"] - eps * d).astype(np.float32))) / (2 * eps)
+    # positions also move the boundary samples through the volume map, whose
+    # interpolation is only continuous across map cells
+    _check("dL/dx0 . d (analytic kernel, finite difference)", float(np.sum(g["x0b"] * d)), fd, 5e-3)
 
 
 # ------------------------------------------------------------ wrapper and errors

@@ -32,7 +32,7 @@ EXPORTS = [
     "vfd_scene_get_stats", "vfd_set_device", "vfd_last_error", "vfd_abi_version", "vfd_profile_kernels",
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
-    "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume",
+    "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
@@ -116,6 +116,7 @@ def lib() -> C.CDLL:
                 "vfd_adjoint_backward": [P, f32p, f32p, f32p, f32p, f32p],
                 "vfd_adjoint_release": [P],
                 "vfd_set_position_mode": [P, C.c_int32],
+                "vfd_set_kernel_mode": [P, C.c_int32],
                 "vfd_build_mesh_map": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_int32, C.c_float, u32p,
                                        C.c_float, f32p, u32p, u32p, C.POINTER(vfd_volume_map)],
                 "vfd_sample_mesh_volume": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_float, u32p, C.c_int32,
@@ -319,6 +320,11 @@ class DFSPHSimulation:
         """Absolute FP32 positions (the reference's) or cell-relative ones; restarts the run."""
         _check(lib().vfd_set_position_mode(self._h, _abi.VFD_POSITIONS_CELL_RELATIVE if cell_relative
                                            else _abi.VFD_POSITIONS_ABSOLUTE), "vfd_set_position_mode")
+
+    def SetKernelMode(self, analytic: bool):
+        """VFD_KERNEL_ANALYTIC (the spline at |r|, smooth in r) or the reference's tables."""
+        mode = _abi.VFD_KERNEL_ANALYTIC if analytic else _abi.VFD_KERNEL_TABLE
+        _check(lib().vfd_set_kernel_mode(self._h, mode), "vfd_set_kernel_mode")
 
     def SetGraphMode(self, enabled: bool):
         _check(lib().vfd_set_graph_mode(self._h, int(bool(enabled))), "vfd_set_graph_mode")

@@ -13,6 +13,8 @@ import ctypes as C
 VFD_OK = 0
 VFD_POSITIONS_ABSOLUTE = 0
 VFD_POSITIONS_CELL_RELATIVE = 1
+VFD_KERNEL_TABLE = 0
+VFD_KERNEL_ANALYTIC = 1
 VFD_SAMPLE_MIN_DENSITY = 0
 VFD_SAMPLE_MEDIUM_DENSITY = 1
 VFD_SAMPLE_MAX_DENSITY = 2

@@ -310,6 +310,9 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.MAXB, (size_t)base.nscenes * 2u * kBuckets * 32u));
     TRY(dalloc(s, &base.MMB, (size_t)base.nscenes * 6u * kBuckets * 32u));
     base.cellRel = s->cellRel ? 1u : 0u;
+    base.analytic = s->analyticKernel ? 1u : 0u;
+    base.splK = s->table.K;
+    base.splL = s->table.L;
     base.workStride = 2u + 2u * base.nscenes;
     TRY(dalloc(s, &base.WORK, 3 * (size_t)base.workStride));
     {
@@ -1176,6 +1179,15 @@ int vfd_set_position_mode(vfd_sim* s, int32_t mode) {
         return fail(VFD_E_ARG, "unknown position mode %d", mode);
     CK(cudaSetDevice(s->device));
     s->cellRel = mode == VFD_POSITIONS_CELL_RELATIVE;
+    s->releaseBuffers();
+    return VFD_OK;
+}
+
+int vfd_set_kernel_mode(vfd_sim* s, int32_t mode) {
+    TRY(check_sim(s));
+    if (mode != VFD_KERNEL_TABLE && mode != VFD_KERNEL_ANALYTIC) return fail(VFD_E_ARG, "unknown kernel mode %d", mode);
+    CK(cudaSetDevice(s->device));
+    s->analyticKernel = mode == VFD_KERNEL_ANALYTIC;
     s->releaseBuffers();
     return VFD_OK;
 }

@@ -134,6 +134,8 @@ struct Dev {
     float4 *STN, *STNS;
     uint16_t* SID;
     uint32_t cellRel;          // 1: positions are cell-relative (precision mode), see pair_r
+    uint32_t analytic;         // 1: W and gradW from the spline itself instead of the tables
+    float splK, splL;          // 8 / (pi h^3), 48 / (pi h^3)
     SceneDev* scenes;
     BodyDev* bodies;
     const float *WM, *GM;      // midpoint tables 0.5 (T[i] + T[i+1]), i < 9999
@@ -224,14 +226,35 @@ __device__ __forceinline__ uint32_t table_pos(const Dev& d, float rl) {
     const uint32_t p = __float2uint_rz(rl * d.invStep);
     return min(p, kTableRes - 2u);
 }
+// The cubic spline the tables sample (CalculateW / CalculateGradientW,
+// Kernel/DFSPHKernels.h:86-131), evaluated at |r| itself: the analytic kernel mode, in
+// which W and gradW are smooth in r (the tables are piecewise constant in |r|).
+__device__ __forceinline__ float spline_w(const Dev& d, float rl) {
+    const float q = rl / d.radius;
+    if (q > 1.0f) return 0.0f;
+    if (q <= 0.5f) {
+        const float q2 = q * q, q3 = q2 * q;
+        return d.splK * (6.0f * q3 - 6.0f * q2 + 1.0f);
+    }
+    const float f = 1.0f - q;
+    return d.splK * (2.0f * (f * f * f));
+}
+__device__ __forceinline__ float spline_gs(const Dev& d, float rl) {  // gradW = gs * r
+    const float q = rl / d.radius;
+    if (!(rl > 1.0e-5f) || q > 1.0f) return 0.0f;
+    const float gq = 1.0f / (rl * d.radius);
+    if (q <= 0.5f) return ((d.splL * q) * (3.0f * q - 2.0f)) * gq;
+    const float f = 1.0f - q;
+    return (d.splL * (-f * f)) * gq;
+}
 __device__ __forceinline__ float kernel_w(const Dev& d, float3 r) {
     const float r2 = dot3(r, r);
-    if (r2 <= d.radius2) return __ldg(d.WM + table_pos(d, fast_sqrt(r2)));
+    if (r2 <= d.radius2) return d.analytic ? spline_w(d, fast_sqrt(r2)) : __ldg(d.WM + table_pos(d, fast_sqrt(r2)));
     return 0.0f;
 }
 __device__ __forceinline__ float3 kernel_grad(const Dev& d, float3 r) {
     const float rl = fast_sqrt(dot3(r, r));
-    if (rl <= d.radius) return __ldg(d.GM + table_pos(d, rl)) * r;
+    if (rl <= d.radius) return (d.analytic ? spline_gs(d, rl) : __ldg(d.GM + table_pos(d, rl))) * r;
     return make_float3(0.f, 0.f, 0.f);
 }
 

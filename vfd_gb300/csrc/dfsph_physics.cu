@@ -167,7 +167,8 @@ __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb
 // gradW factor of one pair: GetGradientW(r) = gs * r (Kernel/DFSPHKernels.h:67-80).
 __device__ __forceinline__ float grad_factor(const Dev& d, float3 r) {
     const float rl = fast_sqrt(dot3(r, r));
-    return rl <= d.radius ? __ldg(d.GM + table_pos(d, rl)) : 0.0f;
+    if (!(rl <= d.radius)) return 0.0f;
+    return d.analytic ? spline_gs(d, rl) : __ldg(d.GM + table_pos(d, rl));
 }
 
 // W and gradW of one pair from one table position (GetW / GetGradientW keep their own
@@ -175,6 +176,11 @@ __device__ __forceinline__ float grad_factor(const Dev& d, float3 r) {
 __device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, float& gs) {
     const float r2 = dot3(r, r);
     const float rl = fast_sqrt(r2);
+    if (d.analytic) {
+        w = r2 <= d.radius2 ? spline_w(d, rl) : 0.0f;
+        gs = rl <= d.radius ? spline_gs(d, rl) : 0.0f;
+        return;
+    }
     const uint32_t pos = table_pos(d, rl);
     w = r2 <= d.radius2 ? __ldg(d.WM + pos) : 0.0f;
     gs = rl <= d.radius ? __ldg(d.GM + pos) : 0.0f;

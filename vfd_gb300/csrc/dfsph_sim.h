@@ -157,6 +157,7 @@ struct vfd_sim {
     std::vector<float> halton;
     bool graphMode = true;
     bool cellRel = false;  // VFD_POSITIONS_CELL_RELATIVE
+    bool analyticKernel = false;  // VFD_KERNEL_ANALYTIC
     bool graphFailed = false;
     uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
 
