@@ -474,6 +474,17 @@ int vfd_set_position_mode(vfd_sim* sim, int32_t mode);
  */
 int vfd_set_kernel_mode(vfd_sim* sim, int32_t mode);
 
+/*
+ * Appends `count` particles (xyz, and velocities or NULL for zero) to the running state
+ * of a single-scene simulation: an inflow emitter's call. The particles already there
+ * keep their state and their indices; the new ones take the next original indices
+ * (n, n + 1, ...) and start with zero acceleration and solver warm starts. The device
+ * layout grows by a quarter when it is full (the state is kept); the step graphs are
+ * rebuilt at the next step. vfd_reset / vfd_simulate go back to the initial particles.
+ * No counterpart in the reference, which has no emitter.
+ */
+int vfd_emit(vfd_sim* sim, const float* xyz, const float* vel, uint32_t count);
+
 /* Device the library runs on (default 0, SystemInfo::InitDevice, Debug/SystemInfo.cpp:34-35). */
 int vfd_set_device(int32_t device);
 

@@ -1613,8 +1613,28 @@ struct Sim {
         reset();
     }
 
+    // Appends particles to the running state (the GPU library's vfd_emit; the reference
+    // has no emitter): zero accelerations and warm starts, original indices n, n+1, ...
+    void emit(const float* x, const float* v, uint32_t k) {
+        for (uint32_t i = 0; i < k; i++) {
+            Particle<T> q{};
+            q.x = V3<T>((T)x[3 * i], (T)x[3 * i + 1], (T)x[3 * i + 2]);
+            if (v) q.v = V3<T>((T)v[3 * i], (T)v[3 * i + 1], (T)v[3 * i + 2]);
+            p.push_back(q);
+        }
+        resize_state((uint32_t)p.size());
+    }
+    void resize_state(uint32_t n) {
+        info.n = n;
+        for (auto* a : {&cgR, &cgP, &cgZ, &cgTmp, &cgB, &cgG}) a->resize(n, V3<T>());
+        cgMinv.resize(n, M3<T>());
+        for (auto& b : bxj) b.resize(n, V3<T>());
+        for (auto& b : bvol) b.resize(n, 0);
+    }
+
     void reset() {  // Simulate preamble, :33-51
         p = init;
+        if (info.n != (uint32_t)init.size()) resize_state((uint32_t)init.size());
         set_dt((T)desc.TimeStepSize);
         update_samples();
         dbg = vfd_step_stats{};
@@ -1744,6 +1764,13 @@ int orc_add_rigid_body(void* p, const vfd_volume_map* m) {
 }
 
 int orc_reset(void* p) { Handle* h = static_cast<Handle*>(p); ORC_DISPATCH(h, reset()); return VFD_OK; }
+
+int orc_emit(void* p, const float* x, const float* v, uint32_t n) {
+    Handle* h = static_cast<Handle*>(p);
+    if (h->f) h->f->emit(x, v, n);
+    if (h->d) h->d->emit(x, v, n);
+    return VFD_OK;
+}
 
 // Kernel evaluation: 0 = the reference's tables, 1 = the spline at |r| (analytic mode).
 int orc_set_kernel_mode(void* p, int mode) {

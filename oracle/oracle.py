@@ -48,6 +48,7 @@ def lib():
             L.orc_add_rigid_body.argtypes = [P, C.POINTER(_abi.vfd_volume_map)]
             L.orc_reset.argtypes = [P]
             L.orc_set_kernel_mode.argtypes = [P, C.c_int]
+            L.orc_emit.argtypes = [P, f32p, f32p, C.c_uint32]
             L.orc_step.argtypes = [P, C.POINTER(_abi.vfd_step_stats)]
             L.orc_find_neighbors.argtypes = [P]
             L.orc_get_neighbors.argtypes = [P, u32p, u32p, u32p, C.c_uint32, u32p, u32p, u32p]
@@ -258,7 +259,7 @@ class OracleSim:
         self.h = lib().orc_create(C.byref(desc), precision)
         if not self.h:
             raise ValueError("orc_create failed")
-        self.n = 0
+        self.n = self.n0 = 0
         self._maps = []
 
     def close(self):
@@ -278,7 +279,7 @@ class OracleSim:
             va, vp = _f32(v)
         else:
             vp = None
-        self.n = len(xa)
+        self.n = self.n0 = len(xa)
         lib().orc_set_fluid(self.h, xp, vp, self.n)
 
     def add_rigid_body(self, vmap: VolumeMap):
@@ -289,6 +290,14 @@ class OracleSim:
 
     def reset(self):
         lib().orc_reset(self.h)
+        self.n = self.n0
+
+    def emit(self, x, v=None):
+        """Appends particles to the running state (as vfd_emit)."""
+        xa, xp = _f32(x)
+        va, vp = _f32(v) if v is not None else (None, None)
+        lib().orc_emit(self.h, xp, vp, len(xa))
+        self.n += len(xa)
 
     def set_kernel_mode(self, analytic: bool):
         """The spline at |r| (analytic) or the reference's tables."""

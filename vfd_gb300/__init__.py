@@ -33,6 +33,7 @@ EXPORTS = [
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
+    "vfd_emit",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
@@ -117,6 +118,7 @@ def lib() -> C.CDLL:
                 "vfd_adjoint_release": [P],
                 "vfd_set_position_mode": [P, C.c_int32],
                 "vfd_set_kernel_mode": [P, C.c_int32],
+                "vfd_emit": [P, f32p, f32p, C.c_uint32],
                 "vfd_build_mesh_map": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_int32, C.c_float, u32p,
                                        C.c_float, f32p, u32p, u32p, C.POINTER(vfd_volume_map)],
                 "vfd_sample_mesh_volume": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_float, u32p, C.c_int32,
@@ -321,6 +323,12 @@ class DFSPHSimulation:
         _check(lib().vfd_set_position_mode(self._h, _abi.VFD_POSITIONS_CELL_RELATIVE if cell_relative
                                            else _abi.VFD_POSITIONS_ABSOLUTE), "vfd_set_position_mode")
 
+    def Emit(self, positions, velocities=None):
+        """Appends particles to the running state (vfd_emit)."""
+        x, xp = _f32(positions)
+        v, vp = _f32(velocities) if velocities is not None else (None, None)
+        _check(lib().vfd_emit(self._h, xp, vp, len(x)), "vfd_emit")
+
     def SetKernelMode(self, analytic: bool):
         """VFD_KERNEL_ANALYTIC (the spline at |r|, smooth in r) or the reference's tables."""
         mode = _abi.VFD_KERNEL_ANALYTIC if analytic else _abi.VFD_KERNEL_TABLE
@@ -407,8 +415,14 @@ class DFSPHSimulation:
                "vfd_get_kernel_table")
         return dict(W=w, GradW=g, radius=r.value, w_zero=wz.value)
 
+    def _n(self, scene: int = 0) -> int:
+        # a single scene can grow (Emit) and shrink back (Reset, Simulate): ask the library
+        if len(self._counts) == 1:
+            return self.GetParticleCount()
+        return self._counts[scene]
+
     def GetState(self, scene: int = 0):
-        n = self._counts[scene]
+        n = self._n(scene)
         x = np.zeros((n, 3), np.float32)
         v = np.zeros((n, 3), np.float32)
         a = np.zeros((n, 3), np.float32)
@@ -417,21 +431,27 @@ class DFSPHSimulation:
 
     def GetStateInto(self, x=None, v=None, a=None, scene: int = 0):
         """GetState into caller arrays (float32, C-contiguous, (n, 3)), e.g. pinned host memory."""
+        n = self._n(scene)
         for arr in (x, v, a):
-            if arr is not None and (arr.dtype != np.float32 or not arr.flags.c_contiguous):
-                raise ValueError("arrays must be C-contiguous float32")
+            if arr is not None and (arr.dtype != np.float32 or not arr.flags.c_contiguous or arr.size != 3 * n):
+                raise ValueError(f"arrays must be C-contiguous float32 of shape ({n}, 3)")
         _check(lib().vfd_scene_get_state(self._h, scene, _fptr(x), _fptr(v), _fptr(a)), "vfd_scene_get_state")
 
     def SetState(self, x=None, v=None):
         xp = vp = None
+        n = self._n(0)
         if x is not None:
             xa, xp = _f32(np.asarray(x).reshape(-1, 3))
+            if len(xa) != n:
+                raise ValueError(f"SetState: {len(xa)} positions for {n} particles")
         if v is not None:
             va, vp = _f32(np.asarray(v).reshape(-1, 3))
+            if len(va) != n:
+                raise ValueError(f"SetState: {len(va)} velocities for {n} particles")
         _check(lib().vfd_set_state(self._h, xp, vp), "vfd_set_state")
 
     def GetField(self, field: int, body: int = 0) -> np.ndarray:
-        n = self._counts[0]
+        n = self._n(0)
         shape = (n, 3) if field in _abi.VECTOR_FIELDS else (n,)
         out = np.zeros(shape, np.float32)
         _check(lib().vfd_get_field(self._h, field, body, _fptr(out)), "vfd_get_field")
@@ -498,7 +518,7 @@ class DFSPHSimulation:
         _check(lib().vfd_find_neighbors(self._h), "vfd_find_neighbors")
 
     def GetNeighbors(self) -> dict:
-        n = self._counts[0]
+        n = self._n(0)
         counts = np.zeros(n, np.uint32)
         offsets = np.zeros(n, np.uint32)
         sort_idx = np.zeros(n, np.uint32)

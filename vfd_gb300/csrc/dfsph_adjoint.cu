@@ -1194,6 +1194,7 @@ int check_adjoint_scene(vfd_sim* s) {
     if (s->scenes.size() != 1) return fail(VFD_E_ARG, "adjoint: one scene per simulation");
     if (s->scenes[0].desc.EnableSurfaceTensionSolver) return fail(VFD_E_ARG, "adjoint: surface tension is not differentiated");
     if (s->cellRel) return fail(VFD_E_ARG, "adjoint: positions must be absolute (VFD_POSITIONS_ABSOLUTE)");
+    if (s->scenes[0].emitted) return fail(VFD_E_ARG, "adjoint: emitted particles are not differentiated");
     return VFD_OK;
 }
 

@@ -138,6 +138,36 @@ __global__ void k_frame_note(Dev d, FrameNote* note, uint32_t lastFrame) {
     *note = n;
     if (n.due && S.frameIndex >= lastFrame) d.status[1] = 2u;
 }
+
+// Appends particles [n0, n0 + count) to the current state set (vfd_emit): positions
+// converted to the storage mode (cell-relative: anchor cell of edge h around the scene
+// origin, as upload does), zero warm starts, original indices n0 + k. The next step's
+// search sorts them in with the others.
+__global__ void k_emit(Dev d, const float* xyz, const float* vel, uint32_t n0, uint32_t count, uint32_t* status) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t p = n0 + k;
+    const SceneDev& S = d.scenes[0];
+    float3 x = make_float3(xyz[3 * (size_t)k], xyz[3 * (size_t)k + 1], xyz[3 * (size_t)k + 2]);
+    float w = 0.0f;
+    if (d.cellRel) {
+        const float L = d.radius;
+        x = make_float3(x.x - S.org[0], x.y - S.org[1], x.z - S.org[2]);
+        const float fx = floorf(x.x / L), fy = floorf(x.y / L), fz = floorf(x.z / L);
+        const int3 A = make_int3((int)fx, (int)fy, (int)fz);
+        if (abs(A.x) > 511 || abs(A.y) > 511 || abs(A.z) > 511) atomicOr(status, 0x40u);
+        x = make_float3(x.x - fx * L, x.y - fy * L, x.z - fz * L);
+        w = anchor_pack(A);
+    }
+    d.XN[p] = make_float4(x.x, x.y, x.z, w);
+    d.Vc[p] = vel ? make_float4(vel[3 * (size_t)k], vel[3 * (size_t)k + 1], vel[3 * (size_t)k + 2], 0.0f)
+                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d.DVc[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d.DKc[p] = 0.0f;
+    d.PIDc[p] = p;
+    d.A[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (k == 0) d.scenes[0].count = n0 + count;
+}
 }  // namespace vfd
 
 using namespace vfd;
@@ -240,11 +270,11 @@ int allocate(vfd_sim* s) {
     s->sceneBegin.clear();
     for (const auto& sc : s->scenes) {
         s->sceneBegin.push_back(n);
-        n += (uint32_t)(sc.x0.size() / 3);
+        n += sc.count();
         maxBodies = std::max<uint32_t>(maxBodies, (uint32_t)sc.bodies.size());
     }
     s->n = n;
-    s->stride = std::max<uint32_t>(32u, (n + 31u) & ~31u);
+    s->stride = std::max<uint32_t>(32u, (std::max(n, s->reserve) + 31u) & ~31u);
     s->maxBodies = maxBodies;
     if (s->cellCap == 0) s->cellCap = estimate_cells(s);
     const size_t st = s->stride;
@@ -353,7 +383,7 @@ int allocate(vfd_sim* s) {
     std::vector<uint16_t> sid(st, 0);
     std::vector<BodyDev> bodies;
     for (uint32_t k = 0; k < s->scenes.size(); k++) {
-        const uint32_t cnt = (uint32_t)(s->scenes[k].x0.size() / 3);
+        const uint32_t cnt = s->scenes[k].count();
         for (uint32_t i = 0; i < cnt; i++) sid[s->sceneBegin[k] + i] = (uint16_t)k;
         for (const auto& b : s->scenes[k].bodies) bodies.push_back(b.dev);
     }
@@ -438,7 +468,14 @@ SceneDev scene_constants(const vfd_desc& d, uint32_t begin, uint32_t count, uint
 // Simulate() preamble (DFSPHImplementation.cu:33-51): initial particles to the device,
 // dt and counters reset.
 int upload(vfd_sim* s) {
-    if (!s->allocated) TRY(allocate(s));
+    // the initial particles only: appended ones go, and the layout shrinks back with them
+    uint32_t initial = 0, emitted = 0;
+    for (auto& sc : s->scenes) {
+        emitted += sc.emitted;
+        sc.emitted = 0;
+        initial += (uint32_t)(sc.x0.size() / 3);
+    }
+    if (!s->allocated || s->n != initial) TRY(allocate(s));
     const size_t st = s->stride;
     std::vector<float4> xn(st, make_float4(0, 0, 0, 0)), v(st, make_float4(0, 0, 0, 0));
     std::vector<uint32_t> pid(st, 0);
@@ -763,7 +800,7 @@ int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
 int check_sim(const vfd_sim* s) { return s ? VFD_OK : fail(VFD_E_ARG, "null handle"); }
 
 int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out) {
-    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     k_export3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, dsrc, s->dStage, b, cnt);
     CK(cudaGetLastError());
@@ -773,7 +810,7 @@ int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out) {
 }
 
 int scatter_scalar(vfd_sim* s, uint32_t scene, const float* dsrc, float* out, int comp = -1, const float4* d4 = nullptr) {
-    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     k_export1<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, dsrc, d4, comp, s->dStage, b, cnt);
     CK(cudaGetLastError());
@@ -783,7 +820,7 @@ int scatter_scalar(vfd_sim* s, uint32_t scene, const float* dsrc, float* out, in
 }
 
 int gather_vec(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
-    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     CK(cudaMemcpyAsync(s->dStage, in, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyHostToDevice, s->stream));
     k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, s->dStage, ddst, b, cnt);
@@ -794,7 +831,7 @@ int gather_vec(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
 // Positions (absolute in the caller's frame whatever the storage mode).
 int scatter_pos(vfd_sim* s, uint32_t scene, const float4* dsrc, const float4* anchors, float* out) {
     if (!s->cellRel) return scatter_vec(s, scene, dsrc, out);
-    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     k_export_pos<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs], dsrc, anchors, s->dStage, b, cnt);
     CK(cudaGetLastError());
@@ -805,7 +842,7 @@ int scatter_pos(vfd_sim* s, uint32_t scene, const float4* dsrc, const float4* an
 
 int gather_pos(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
     if (!s->cellRel) return gather_vec(s, scene, in, ddst);
-    const uint32_t b = s->sceneBegin[scene], cnt = (uint32_t)(s->scenes[scene].x0.size() / 3);
+    const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     CK(cudaMemcpyAsync(s->dStage, in, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyHostToDevice, s->stream));
     k_import_pos<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs], s->dStage, ddst, b, cnt);
@@ -1183,6 +1220,80 @@ int vfd_set_position_mode(vfd_sim* s, int32_t mode) {
     return VFD_OK;
 }
 
+int vfd_emit(vfd_sim* s, const float* xyz, const float* vel, uint32_t count) {
+    TRY(check_sim(s));
+    if (s->scenes.size() != 1) return fail(VFD_E_ARG, "vfd_emit adds to single-scene simulations");
+    if (count == 0) return VFD_OK;
+    if (!xyz) return fail(VFD_E_ARG, "null positions");
+    for (size_t i = 0; i < 3 * (size_t)count; i++)
+        if (!std::isfinite(xyz[i]) || (vel && !std::isfinite(vel[i]))) return fail(VFD_E_NAN, "non-finite input");
+    if ((uint64_t)s->n + count > 0x7fffffffull) return fail(VFD_E_CAPACITY, "particle count limit");
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    vfd::adjoint_release(s);
+    CK(cudaStreamSynchronize(s->stream));
+    const uint32_t n0 = s->n, n1 = n0 + count;
+    if (n1 > s->stride) {
+        // grow with headroom for later emissions, keeping the carried state (as grow_cells)
+        const size_t st = s->stride;
+        const Dev& d = s->dev[s->cs];
+        std::vector<float4> xn(st), v(st), dv(st), acc(st);
+        std::vector<float> dk(st);
+        std::vector<uint32_t> pid(st);
+        CK(cudaMemcpy(xn.data(), d.XN, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(v.data(), d.Vc, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(dv.data(), d.DVc, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(dk.data(), d.DKc, sizeof(float) * st, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(pid.data(), d.PIDc, sizeof(uint32_t) * st, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(acc.data(), d.A, sizeof(float4) * st, cudaMemcpyDeviceToHost));
+        std::vector<SceneDev> sc(s->hScenes.size());
+        CK(cudaMemcpy(sc.data(), s->dScenes, sizeof(SceneDev) * sc.size(), cudaMemcpyDeviceToHost));
+        s->reserve = std::max<uint32_t>(n1, (uint32_t)std::min<uint64_t>(0x7fffffffull, (uint64_t)n1 + n1 / 4));
+        s->scenes[0].emitted += count;  // allocate() sizes the layout for n1
+        TRY(allocate(s));
+        s->allocated = true;
+        const Dev& e = s->dev[0];
+        s->cs = 0;
+        CK(cudaMemcpy(e.XN, xn.data(), sizeof(float4) * n0, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e.Vc, v.data(), sizeof(float4) * n0, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e.DVc, dv.data(), sizeof(float4) * n0, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e.DKc, dk.data(), sizeof(float) * n0, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e.PIDc, pid.data(), sizeof(uint32_t) * n0, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e.A, acc.data(), sizeof(float4) * n0, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->dScenes, sc.data(), sizeof(SceneDev) * sc.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemset(s->dStatus, 0, 16 * sizeof(uint32_t)));
+        TRY(reset_buckets(s, e));
+        s->hScenes = sc;
+        s->uploaded = true;
+    } else {
+        // same layout, more particles: the step graphs carry n, so they are rebuilt
+        s->releaseGraphs();
+        s->scenes[0].emitted += count;
+        s->n = n1;
+        for (int k = 0; k < 2; k++) s->dev[k].n = n1;
+    }
+    // the new particles through the staging buffer (3 floats each), in chunks of its size
+    for (uint32_t done = 0; done < count;) {
+        const uint32_t chunk = std::min<uint32_t>(count - done, s->stride / 2u);
+        CK(cudaMemcpyAsync(s->dStage, xyz + 3 * (size_t)done, sizeof(float) * 3 * chunk, cudaMemcpyHostToDevice,
+                           s->stream));
+        if (vel)
+            CK(cudaMemcpyAsync(s->dStage + 3 * (size_t)chunk, vel + 3 * (size_t)done, sizeof(float) * 3 * chunk,
+                               cudaMemcpyHostToDevice, s->stream));
+        k_emit<<<blocks_for(chunk, 256), 256, 0, s->stream>>>(s->dev[s->cs], s->dStage,
+                                                              vel ? s->dStage + 3 * (size_t)chunk : nullptr,
+                                                              n0 + done, chunk, s->dStatus);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s->stream));
+        done += chunk;
+    }
+    uint32_t flags = 0;
+    CK(cudaMemcpy(&flags, s->dStatus, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (flags & 0x40u) return fail(VFD_E_CAPACITY, "cell-relative positions: an emitted particle lies more than 511 "
+                                                   "cells from the scene's centre");
+    return VFD_OK;
+}
+
 int vfd_set_kernel_mode(vfd_sim* s, int32_t mode) {
     TRY(check_sim(s));
     if (mode != VFD_KERNEL_TABLE && mode != VFD_KERNEL_ANALYTIC) return fail(VFD_E_ARG, "unknown kernel mode %d", mode);
@@ -1272,7 +1383,7 @@ int vfd_get_field(vfd_sim* s, int32_t field, uint32_t body, float* out) {
     TRY(ensure_ready(s));
     CK(cudaStreamSynchronize(s->stream));
     const Dev& d = s->dev[s->cs];
-    const uint32_t cnt = (uint32_t)(s->scenes[0].x0.size() / 3);
+    const uint32_t cnt = s->scenes[0].count();
     switch (field) {
         case VFD_FIELD_DENSITY: return scatter_scalar(s, 0, d.RHO, out);
         case VFD_FIELD_FACTOR: return scatter_scalar(s, 0, d.ALPHA, out);
@@ -1330,7 +1441,7 @@ int vfd_get_neighbors(vfd_sim* s, uint32_t* counts, uint32_t* offsets, uint32_t*
     TRY(ensure_ready(s));
     CK(cudaStreamSynchronize(s->stream));
     const Dev& d = s->dev[s->cs];
-    const uint32_t cnt = (uint32_t)(s->scenes[0].x0.size() / 3);
+    const uint32_t cnt = s->scenes[0].count();
     std::vector<uint32_t> pid(cnt), ncnt(cnt), keys(cnt);
     CK(cudaMemcpy(pid.data(), d.PIDc, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(ncnt.data(), d.NCNT, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
@@ -1366,7 +1477,7 @@ int vfd_get_info(const vfd_sim* s, vfd_info* info) {
     TRY(check_sim(s));
     if (!info) return fail(VFD_E_ARG, "null output");
     const vfd_desc& d = s->scenes[0].desc;
-    SceneDev S = scene_constants(d, 0, (uint32_t)(s->scenes[0].x0.size() / 3), 0, (uint32_t)s->scenes[0].bodies.size());
+    SceneDev S = scene_constants(d, 0, s->scenes[0].count(), 0, (uint32_t)s->scenes[0].bodies.size());
     std::memset(info, 0, sizeof(*info));
     info->ParticleCount = S.count;
     info->RigidBodyCount = S.bodyCount;
@@ -1406,7 +1517,7 @@ int vfd_get_info(const vfd_sim* s, vfd_info* info) {
 int vfd_get_particle_count(const vfd_sim* s, uint32_t* n) {
     TRY(check_sim(s));
     if (!n) return fail(VFD_E_ARG, "null output");
-    *n = (uint32_t)(s->scenes[0].x0.size() / 3);
+    *n = s->scenes[0].count();
     return VFD_OK;
 }
 
@@ -1496,7 +1607,7 @@ int vfd_simulate(vfd_sim* s, vfd_frame_callback cb, void* user) {
     if (s->scenes.size() != 1) return fail(VFD_E_ARG, "vfd_simulate runs single-scene simulations");
     CK(cudaSetDevice(s->device));
     TRY(upload(s));
-    const uint32_t n = (uint32_t)(s->scenes[0].x0.size() / 3);
+    const uint32_t n = s->scenes[0].count();
     const uint32_t frames = s->scenes[0].desc.FrameCount;
     if (frames == 0 || n == 0) return VFD_OK;
     TRY(ensure_ready(s));

@@ -281,22 +281,30 @@ __device__ __forceinline__ int32_t* mm_bucket(const Dev& d, uint32_t s, int k, u
     return d.MMB + ((size_t)(s * 6u + (uint32_t)k) * kBuckets + b) * 32u;
 }
 // Controller side: sum (and zero) one accumulator's buckets.
+// (all bucket loads are issued before the first add, so the fold costs one L2 round trip
+// rather than kBuckets of them; the sum runs in bucket order as before)
 __device__ __forceinline__ double fold_acc(const Dev& d, uint32_t s, int slot) {
+    double* q = acc_bucket(d, s, slot, 0);
+    double v[kBuckets];
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) v[b] = __ldcg(q + (size_t)b * 16u);
     double t = 0.0;
-    for (uint32_t b = 0; b < kBuckets; b++) {
-        double* q = acc_bucket(d, s, slot, b);
-        t += *q;
-        *q = 0.0;
-    }
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) t += v[b];
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) q[(size_t)b * 16u] = 0.0;
     return t;
 }
 __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
+    uint32_t* q = max_bucket(d, s, k, 0);
+    uint32_t v[kBuckets];
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) v[b] = __ldcg(q + (size_t)b * 32u);
     uint32_t t = 0u;
-    for (uint32_t b = 0; b < kBuckets; b++) {
-        uint32_t* q = max_bucket(d, s, k, b);
-        t = max(t, *q);
-        *q = 0u;
-    }
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) t = max(t, v[b]);
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) q[(size_t)b * 32u] = 0u;
     return t;
 }
 

@@ -139,6 +139,8 @@ struct SceneHost {
     vfd_desc desc{};
     std::vector<float> x0, v0;
     std::vector<BodyHost> bodies;
+    uint32_t emitted = 0;  // particles appended by vfd_emit since the last upload
+    uint32_t count() const { return (uint32_t)(x0.size() / 3) + emitted; }
 };
 
 }  // namespace host
@@ -164,6 +166,7 @@ struct vfd_sim {
     // layout
     bool allocated = false, uploaded = false;
     uint32_t n = 0, stride = 0, cellCap = 0, maxBodies = 0;
+    uint32_t reserve = 0;  // particle capacity to allocate for (vfd_emit grows it)
     std::vector<uint32_t> sceneBegin;
     std::vector<void*> allocs;
     vfd::Dev dev[2]{};

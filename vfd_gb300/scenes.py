@@ -216,6 +216,27 @@ def viscous_drop_c4(r: float = 0.0025, radius: float = 0.1, seed: int | None = N
     return dict(name=f"viscous_drop_{len(x)}", x=x, v=v.astype(np.float32), desc=desc, boxes=[floor])
 
 
+def jet_coiling_c5(pool=(400, 50, 400), r: float = 0.0015, seed: int | None = None,
+                   map_resolution=(40, 24, 40)) -> dict:
+    """Config 5: a viscous jet (inflow disk of radius 0.02 m at 1 m/s, downwards, 0.5 m
+    above the floor) onto a resting pool. The inflow alone adds ~140 particles per layer
+    (about 5e4 per second of flow), far from 8M, so a pool of pool[0] x pool[1] x pool[2]
+    particles (400 x 50 x 400 = 8M at spacing 2r = 3 mm: 1.2 x 0.15 x 1.2 m) rests on
+    the floor of a closed box and the jet falls 0.35 m onto it. Kinematic viscosity 0.2
+    (200 Pa s), surface tension 0.07, 2000 steps. Returns the scene and the emitter's
+    parameters (center, direction, radius, speed)."""
+    rng = SplitMix64(config_seed(5) if seed is None else seed)
+    g = wall_gap(r)
+    x = lattice_block(pool, r, (g, g, g), 0.05, rng)
+    edge = [c * 2.0 * r + 2.0 * g for c in pool]
+    box = (edge[0], 0.8, edge[2])
+    desc = dict(ParticleRadius=r, Viscosity=0.2, BoundaryViscosity=0.2, MaxViscositySolverError=0.01,
+                EnableViscositySolver=1, EnableSurfaceTensionSolver=1, SurfaceTension=0.07, **SOLVER)
+    inflow = dict(center=(0.5 * box[0], 0.5, 0.5 * box[2]), direction=(0.0, -1.0, 0.0), radius=0.02, speed=1.0)
+    return dict(name=f"jet_coiling_{len(x)}", x=x, v=np.zeros_like(x), desc=desc,
+                boxes=[container((0.0, 0.0, 0.0), box, r, map_resolution)], inflow=inflow)
+
+
 def small_dam_break(n_side: int = 12, r: float = 0.025, viscosity: float = 0.0, surface_tension: float = 0.0,
                     seed: int = 7, box_scale=(2.0, 1.5, 1.0), map_resolution=(24, 18, 12)) -> dict:
     """A small dam break for parity tests (all features switchable)."""
