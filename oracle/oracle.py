@@ -26,7 +26,9 @@ def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (seconds)."""
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
             os.path.getmtime(os.path.join(HERE, "dfsph_oracle.cpp")),
-            os.path.getmtime(os.path.join(HERE, "..", "include", "vfd_dfsph.h"))):
+            os.path.getmtime(os.path.join(HERE, "sph_oracle.cpp")),
+            os.path.getmtime(os.path.join(HERE, "..", "include", "vfd_dfsph.h")),
+            os.path.getmtime(os.path.join(HERE, "..", "include", "vfd_sph.h"))):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -362,3 +364,61 @@ def scene_oracle(scene: dict, precision: int = 64, desc_overrides: dict | None =
     for m in maps:
         sim.add_rigid_body(m)
     return sim
+
+
+class SphOracle:
+    """CPU oracle of the legacy SPH pipeline (sph_oracle.cpp), FP32 in the reference's order."""
+
+    def __init__(self, desc, positions):
+        L = lib()
+        if not getattr(L, "_sph_bound", False):
+            from vfd_gb300.sph import vfd_sph_desc, vfd_sph_params
+            f32p, u32p = C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+            L.orc_sph_create.restype = C.c_void_p
+            L.orc_sph_create.argtypes = [C.POINTER(vfd_sph_desc), f32p, C.c_uint32]
+            L.orc_sph_destroy.argtypes = [C.c_void_p]
+            L.orc_sph_steps.argtypes = [C.c_void_p, C.c_uint32]
+            L.orc_sph_set_velocities.argtypes = [C.c_void_p, f32p]
+            L.orc_sph_get_state.argtypes = [C.c_void_p, f32p, f32p, f32p, f32p]
+            L.orc_sph_get_sort.argtypes = [C.c_void_p, u32p, u32p]
+            L.orc_sph_params.argtypes = [C.c_void_p, C.POINTER(vfd_sph_params)]
+            L._sph_bound = True
+        self.desc = desc
+        x, xp = _f32(np.asarray(positions).reshape(-1, 3))
+        self.n = len(x)
+        self.h = L.orc_sph_create(C.byref(desc), xp, self.n)
+        if not self.h:
+            raise ValueError("orc_sph_create: invalid description")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_sph_destroy(self.h)
+            self.h = None
+
+    def steps(self, count: int):
+        lib().orc_sph_steps(self.h, int(count))
+
+    def set_velocities(self, v):
+        va, vp = _f32(np.asarray(v).reshape(-1, 3))
+        lib().orc_sph_set_velocities(self.h, vp)
+
+    def state(self):
+        x = np.zeros((self.n, 3), np.float32)
+        v = np.zeros((self.n, 3), np.float32)
+        rho = np.zeros(self.n, np.float32)
+        p = np.zeros(self.n, np.float32)
+        lib().orc_sph_get_state(self.h, _ptr(x, C.c_float), _ptr(v, C.c_float), _ptr(rho, C.c_float),
+                                _ptr(p, C.c_float))
+        return x, v, rho, p
+
+    def sort(self):
+        k = np.zeros(self.n, np.uint32)
+        i = np.zeros(self.n, np.uint32)
+        lib().orc_sph_get_sort(self.h, _ptr(k, C.c_uint32), _ptr(i, C.c_uint32))
+        return k, i
+
+    def params(self) -> dict:
+        from vfd_gb300.sph import vfd_sph_params
+        p = vfd_sph_params()
+        lib().orc_sph_params(self.h, C.byref(p))
+        return {k: (list(getattr(p, k)) if k == "GridSize" else getattr(p, k)) for k, _ in vfd_sph_params._fields_}

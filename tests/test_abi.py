@@ -1,5 +1,5 @@
 """The C-ABI library without a GPU: it builds, loads, exports every entry point
-declared in include/vfd_dfsph.h, its structs have the layout the Python mirror
+declared in include/vfd_dfsph.h and include/vfd_sph.h, its structs have the layout the Python mirror
 assumes, and calls that need a device fail with a status code (no hang, no exit).
 """
 import ctypes as C
@@ -11,15 +11,15 @@ import numpy as np
 import pytest
 
 import vfd_gb300
-from vfd_gb300 import _abi
+from vfd_gb300 import _abi, sph
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "vfd_dfsph.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("vfd_dfsph.h", "vfd_sph.h")]
 
 
 def header_functions():
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(vfd_\w+)\s*\(", text, re.M)))
+    text = "".join(open(h).read() for h in HEADERS)
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(vfd_\w+)\s*\(", text, re.M)))
 
 
 def test_python_mirror_lists_every_header_function():
@@ -39,7 +39,7 @@ def test_library_has_no_host_only_fallback(built_library):
 
 
 def _c_layout(struct_name, fields):
-    src = "#include <stdio.h>\n#include <stddef.h>\n#include \"vfd_dfsph.h\"\nint main(void){\n"
+    src = "#include <stdio.h>\n#include <stddef.h>\n#include \"vfd_sph.h\"\nint main(void){\n"
     src += f'printf("%zu\\n", sizeof({struct_name}));\n'
     for f in fields:
         src += f'printf("%zu\\n", offsetof({struct_name}, {f}));\n'
@@ -47,7 +47,8 @@ def _c_layout(struct_name, fields):
     return src
 
 
-@pytest.mark.parametrize("cls", [_abi.vfd_desc, _abi.vfd_volume_map, _abi.vfd_step_stats, _abi.vfd_info])
+@pytest.mark.parametrize("cls", [_abi.vfd_desc, _abi.vfd_volume_map, _abi.vfd_step_stats, _abi.vfd_info,
+                                 sph.vfd_sph_desc, sph.vfd_sph_params])
 def test_struct_layout_matches_header(tmp_path, cls):
     names = [n for n, _ in cls._fields_]
     src = tmp_path / "layout.c"

@@ -34,6 +34,10 @@ EXPORTS = [
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
     "vfd_emit",
+    # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
+    "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
+    "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
+    "vfd_sph_get_sort",
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
