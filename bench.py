@@ -365,6 +365,31 @@ def jet_form(V, scenes, steps: int = 8, warmup: int = 2):
     return out
 
 
+def legacy_sph_form(steps: int = 100, warmup: int = 5):
+    """The reference's legacy SPH pipeline (vfd_sph_*): a 100^3 block (1M particles,
+    r = 4 mm, h = 1 cm) falling in a 1.6 x 1.2 x 1.6 m world box, `steps` steps with the
+    state on the device, host clock around synchronous calls; and the FP32 oracle (one
+    thread) on a 20^3 block for 10 steps as its CPU sample."""
+    from oracle import oracle as O
+    from vfd_gb300 import scenes, sph
+    d = sph.make_sph_desc(WorldMin=(-0.8, -0.6, -0.8), WorldMax=(0.8, 0.6, 0.8))
+    x = scenes.lattice_block((100, 100, 100), 0.004, (-0.4, -0.5, -0.4), 0.05, scenes.SplitMix64(7))
+    sim = sph.SPHSimulation(d, x)
+    sim.Steps(warmup)
+    t0 = time.perf_counter()
+    sim.Steps(steps)
+    el = time.perf_counter() - t0
+    sim.close()
+    xs = scenes.lattice_block((20, 20, 20), 0.004, (-0.05, -0.5, -0.05), 0.05, scenes.SplitMix64(7))
+    o = O.SphOracle(d, xs)
+    t1 = time.perf_counter()
+    o.steps(10)
+    cpu = len(xs) * 10 / (time.perf_counter() - t1)
+    return {"workload": f"legacy SPH, {len(x)} particles (100^3 block, r = 4 mm, h = 1 cm), {steps} steps",
+            "particle_steps_per_s": len(x) * steps / el, "ms_per_step": 1e3 * el / steps,
+            "cpu_oracle_particle_steps_per_s": cpu, "cpu_sample": "FP32 oracle, one thread, 8000 particles, 10 steps"}
+
+
 def precision_form(V, scenes, n_side: int = 40, steps: int = 20):
     """The 1M configuration's parameters at n_side^3 particles: positions after `steps`
     steps in FP32 with absolute and with cell-relative positions against the FP64
@@ -569,6 +594,7 @@ def main():
             line["forms"]["precision"] = precision_form(V, scenes)
             if not args.no_jet:
                 line["forms"]["jet_c5"] = jet_form(V, scenes)
+            line["forms"]["legacy_sph"] = legacy_sph_form()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
