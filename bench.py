@@ -261,6 +261,18 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
     xb = (2.0 / n) * (x.astype(np.float64) - target)
     x0b, v0b, pb = sim.AdjointBackward(xb.astype(np.float32), np.zeros_like(v))
     t_adj = time.perf_counter() - t0
+    # the same run with every step recorded in the forward pass (no segment replays):
+    # what 280 GB of HBM allows at this size
+    restart()
+    sim.AdjointForward(steps, steps)
+    sim.AdjointBackward(np.zeros_like(x), np.zeros_like(v))
+    restart()
+    t0 = time.perf_counter()
+    sim.AdjointForward(steps, steps)
+    x2, v2, _ = sim.GetState()
+    sim.AdjointBackward(((2.0 / n) * (x2.astype(np.float64) - target)).astype(np.float32), np.zeros_like(v2))
+    t_all = time.perf_counter() - t0
+
     # Gradient check by central differences on the smooth variant of the same scene.
     # The method has kinks a finite difference straddles: the adaptive time step follows
     # the fastest particle (an argmax), the divergence solve clamps its residual at zero,
@@ -306,6 +318,7 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
                         f"checkpoint every {every}",
             "forward": n * steps / t_fwd, "fwd_adjoint": n * steps / t_adj, "adjoint_over_forward": t_adj / t_fwd,
             "forward_s": t_fwd, "fwd_adjoint_s": t_adj,
+            "every_step_recorded": {"fwd_adjoint_s": t_all, "adjoint_over_forward": t_all / t_fwd},
             "grad_check": {"variant": "same scene, fixed dt 1 ms, divergence solve off, pressure iterations "
                                       "pinned to 3, analytic kernel" if analytic_check else
                                       "same scene, fixed dt 1 ms, divergence solve off, pressure iterations "
