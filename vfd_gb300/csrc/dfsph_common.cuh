@@ -360,12 +360,14 @@ __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, boo
     if (threadIdx.x == 0) uniformBlock = (first < d.n) && (scene_of(d, first) == scene_of(d, last)) ? 1 : 0;
     __syncthreads();
     if (uniformBlock) {
+        // only the first lane of each G-lane group contributes, so the rounds below G
+        // would add zeros: the tree starts at offset 16 and stops at G (same sums)
         double s[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
             s[k] = valid ? v[k] : 0.0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+            for (int o = 16; o >= (int)G; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
         }
         if (lane == 0)
 #pragma unroll
