@@ -314,8 +314,9 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
 // per particle pass G (a block then covers blockDim.x / G particles); all threads of
 // the block must call this.
 // Core of scene_accumulate: `uniformScene` is the scene of every particle the block
-// serves, or -1 when they belong to several scenes.
-template <int K>
+// serves, or -1 when they belong to several scenes; G as for scene_accumulate (only the
+// first lane of each G-lane group contributes).
+template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformScene, uint32_t sid, bool valid,
                                                       const double (&v)[K], const int (&slot)[K]) {
     __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
@@ -327,7 +328,7 @@ __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformS
         for (int k = 0; k < K; k++) {
             s[k] = valid ? v[k] : 0.0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+            for (int o = 16; o >= (int)G; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
         }
         __syncthreads();
         if (lane == 0)

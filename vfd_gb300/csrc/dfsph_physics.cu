@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
         }
         const double v[1] = {res};
         const int slot[1] = {0};
-        scene_accumulate_core<1>(d, chunk_scene(d, L, base_, per_, total_), sid, in && threadIdx.x % G == 0u, v, slot);
+        scene_accumulate_core<1, G>(d, chunk_scene(d, L, base_, per_, total_), sid, in && threadIdx.x % G == 0u, v, slot);
     }
 }
 
@@ -862,7 +862,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
         }
         const double v[1] = {pap};
         const int slot[1] = {0};
-        scene_accumulate_core<1>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in && threadIdx.x % G == 0u,
+        scene_accumulate_core<1, G>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in && threadIdx.x % G == 0u,
                                  v, slot);
     }
 }
