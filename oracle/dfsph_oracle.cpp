@@ -31,7 +31,7 @@
 //   * solver error reductions: FP64 sum, error = -rho0 * sum(res) / N (the
 //     reference folds with thrust::minus, DFSPHImplementation.cu:483-489,
 //     whose result depends on the reduction tree);
-//   * viscosity CG dot products in FP64.
+//   * viscosity CG dot products summed in FP64 over particles (each particle's term in T).
 #include "../include/vfd_dfsph.h"
 
 #include <algorithm>
@@ -1388,9 +1388,11 @@ struct Sim {
         return rhs[i] - (info.dt / p[i].rho) * acc;
     }
 
+    // CG dot product: each particle's term in T (FP32 for the mirror: x + y then z), the
+    // sum over particles in FP64.
     static double dotv(const std::vector<V3<T>>& a, const std::vector<V3<T>>& b, uint32_t n) {
         double s = 0;
-        for (uint32_t i = 0; i < n; i++) s += (double)a[i].x * b[i].x + (double)a[i].y * b[i].y + (double)a[i].z * b[i].z;
+        for (uint32_t i = 0; i < n; i++) s += (double)(a[i].x * b[i].x + a[i].y * b[i].y + a[i].z * b[i].z);
         return s;
     }
 

@@ -164,6 +164,14 @@ __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb
     }
 }
 
+// One particle's term of a CG dot product: the FP32 dot of its two vectors (no
+// contraction, x + y then z, as the FP32 oracle forms it), widened for the FP64 sum
+// over particles. FP64 arithmetic runs at a small fraction of the FP32 rate on this
+// GPU, so the per-particle terms stay FP32, as every per-particle sum of the reference.
+__device__ __forceinline__ double dot_term(float3 a, float3 b) {
+    return (double)__fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+
 // gradW factor of one pair: GetGradientW(r) = gs * r (Kernel/DFSPHKernels.h:67-80).
 __device__ __forceinline__ float grad_factor(const Dev& d, float3 r) {
     const float rl = fast_sqrt(dot3(r, r));
@@ -738,8 +746,8 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
             const float3 b = f3(d.CB[p]);
             const float3 r = b - ag;
             d.CR[p] = f4(r, 0.0f);
-            bb = (double)b.x * b.x + (double)b.y * b.y + (double)b.z * b.z;
-            rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+            bb = dot_term(b, b);
+            rr = dot_term(r, r);
         }
     }
     const double v[2] = {bb, rr};
@@ -790,7 +798,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
         const float3 r = f3(d.CR[p]);
         const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
         d.CP[p] = f4(z, d.CG[p].w);
-        rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+        rz = dot_term(r, z);
     }
     const double v[1] = {rz};
     const int slot[1] = {0};
@@ -832,7 +840,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
         const float3 ap = visc_matvec<G, REL>(d, grp, p, S, d.CP, pv);
         if (grp.lane == 0) {
             d.CAP[p] = f4(ap, 0.0f);
-            pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
+            pap = dot_term(pv, ap);
         }
     }
     const double v[1] = {pap};
@@ -857,7 +865,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
             const float3 ap = visc_matvec<G, REL>(d, grp, p, d.scenes[sid], d.CP, pv);
             if (grp.lane == 0) {
                 d.CAP[p] = f4(ap, 0.0f);
-                pap = (double)pv.x * ap.x + (double)pv.y * ap.y + (double)pv.z * ap.z;
+                pap = dot_term(pv, ap);
             }
         }
         const double v[1] = {pap};
@@ -888,8 +896,8 @@ __device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const S
     d.CR[p] = f4(r, 0.0f);
     const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
     d.CZ[p] = f4(z, 0.0f);
-    rr = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
-    rz = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+    rr = dot_term(r, r);
+    rz = dot_term(r, z);
 }
 
 __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
