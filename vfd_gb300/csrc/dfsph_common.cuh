@@ -308,28 +308,47 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
     return t;
 }
 
-// Adds `v` into scene `sid`'s FP64 accumulators `slot` (bucket blockIdx % 32). A block
-// whose particles lie in one scene reduces in shared memory and issues one atomic per
+// Warp sum of the FP32 values v over the lanes that are multiples of `step` (the others
+// hold zeros), as an unevaluated pair hi + lo of FP32 numbers: each level adds the
+// partners' high parts with Knuth's error-free TwoSum and carries the rounding error
+// and the partners' low parts in lo, so the pair keeps ~44 significant bits (relative
+// error ~1e-13 for a warp's 32 terms). Widened to FP64 at the end: FP64 arithmetic runs
+// at a small fraction of the FP32 rate on this GPU, and a DADD per lane and level cost
+// more than the rest of a reduction kernel's arithmetic.
+__device__ __forceinline__ double warp_sum_pair(float v, int step) {
+    float hi = v, lo = 0.0f;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        if (o < step) break;
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float sum = __fadd_rn(hi, h2);
+        const float bb = __fsub_rn(sum, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(h2, bb));
+        lo = __fadd_rn(__fadd_rn(lo, l2), err);
+        hi = sum;
+    }
+    return (double)hi + (double)lo;
+}
+
+// Adds the FP32 terms `v` into scene `sid`'s FP64 accumulators `slot` (bucket
+// blockIdx % 32). A block whose particles lie in one scene sums each warp as an FP32
+// pair (warp_sum_pair), the warps in FP64 in shared memory, and issues one atomic per
 // accumulator; otherwise each valid thread adds its own value. Kernels running G lanes
-// per particle pass G (a block then covers blockDim.x / G particles); all threads of
-// the block must call this.
+// per particle pass G (a block then covers blockDim.x / G particles; only the first
+// lane of each group contributes); all threads of the block must call this.
 // Core of scene_accumulate: `uniformScene` is the scene of every particle the block
-// serves, or -1 when they belong to several scenes; G as for scene_accumulate (only the
-// first lane of each G-lane group contributes).
+// serves, or -1 when they belong to several scenes.
 template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformScene, uint32_t sid, bool valid,
-                                                      const double (&v)[K], const int (&slot)[K]) {
+                                                      const float (&v)[K], const int (&slot)[K]) {
     __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bucket = blockIdx.x % kBuckets;
     if (uniformScene >= 0) {
         double s[K];
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            s[k] = valid ? v[k] : 0.0;
-#pragma unroll
-            for (int o = 16; o >= (int)G; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
-        }
+        for (int k = 0; k < K; k++) s[k] = warp_sum_pair(valid ? v[k] : 0.0f, (int)G);
         __syncthreads();
         if (lane == 0)
 #pragma unroll
@@ -345,12 +364,12 @@ __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformS
         }
     } else if (valid) {
 #pragma unroll
-        for (int k = 0; k < K; k++) atomicAdd(acc_bucket(d, sid, slot[k], bucket), v[k]);
+        for (int k = 0; k < K; k++) atomicAdd(acc_bucket(d, sid, slot[k], bucket), (double)v[k]);
     }
 }
 
 template <int K, uint32_t G = 1>
-__device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, bool valid, const double (&v)[K],
+__device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, bool valid, const float (&v)[K],
                                                  const int (&slot)[K]) {
     __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
     __shared__ int uniformBlock;
@@ -361,15 +380,9 @@ __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, boo
     if (threadIdx.x == 0) uniformBlock = (first < d.n) && (scene_of(d, first) == scene_of(d, last)) ? 1 : 0;
     __syncthreads();
     if (uniformBlock) {
-        // only the first lane of each G-lane group contributes, so the rounds below G
-        // would add zeros: the tree starts at offset 16 and stops at G (same sums)
         double s[K];
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            s[k] = valid ? v[k] : 0.0;
-#pragma unroll
-            for (int o = 16; o >= (int)G; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
-        }
+        for (int k = 0; k < K; k++) s[k] = warp_sum_pair(valid ? v[k] : 0.0f, (int)G);
         if (lane == 0)
 #pragma unroll
             for (int k = 0; k < K; k++) sm[warp][k] = s[k];
@@ -385,7 +398,7 @@ __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, boo
         }
     } else if (valid) {
 #pragma unroll
-        for (int k = 0; k < K; k++) atomicAdd(acc_bucket(d, sid, slot[k], bucket), v[k]);
+        for (int k = 0; k < K; k++) atomicAdd(acc_bucket(d, sid, slot[k], bucket), (double)v[k]);
     }
 }
 

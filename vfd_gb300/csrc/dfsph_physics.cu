@@ -165,11 +165,12 @@ __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb
 }
 
 // One particle's term of a CG dot product: the FP32 dot of its two vectors (no
-// contraction, x + y then z, as the FP32 oracle forms it), widened for the FP64 sum
-// over particles. FP64 arithmetic runs at a small fraction of the FP32 rate on this
-// GPU, so the per-particle terms stay FP32, as every per-particle sum of the reference.
-__device__ __forceinline__ double dot_term(float3 a, float3 b) {
-    return (double)__fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+// contraction, x + y then z, as the FP32 oracle forms it); the sum over particles is
+// FP64-accurate (scene_accumulate). FP64 arithmetic runs at a small fraction of the
+// FP32 rate on this GPU, so the per-particle terms stay FP32, as every per-particle sum
+// of the reference does.
+__device__ __forceinline__ float dot_term(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
 }
 
 // gradW factor of one pair: GetGradientW(r) = gs * r (Kernel/DFSPHKernels.h:67-80).
@@ -335,10 +336,10 @@ __global__ void __launch_bounds__(kBlock) k_pressure_accel_b(Dev d) {
 }
 
 // K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
-// each with ComputeDensityPressureForce (:280-315) and the FP64 residual sum.
+// each with ComputeDensityPressureForce (:280-315) and the FP64-accurate residual sum.
 template <bool DIV, uint32_t G, bool REL>
-__device__ __forceinline__ double jacobi_item(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S) {
-    double res = 0.0;
+__device__ __forceinline__ float jacobi_item(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S) {
+    float res = 0.0f;
     const Nbr nb = neighbors(d, p);
     const float4 xi = d.X[p];
     const float3 ai = f3(d.AP[p]);
@@ -367,7 +368,7 @@ __device__ __forceinline__ double jacobi_item(const Dev& d, const Group<G>& grp,
             set_kappa(d, p, k);
         }
         d.RES[p] = r;
-        res = (double)r;
+        res = r;
     }
     return res;
 }
@@ -381,9 +382,9 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
     const bool active = inRange && (DIV ? S.div.active : S.pres.active);
-    double res = 0.0;
+    float res = 0.0f;
     if (active) res = jacobi_item<DIV, G, REL>(d, grp, p, S);
-    const double v[1] = {res};
+    const float v[1] = {res};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
 }
@@ -399,12 +400,12 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
         const bool in = vp < total_;
         uint32_t sid = 0;
         const uint32_t p = in ? work_slot(d, L, vp, sid) : 0u;
-        double res = 0.0;
+        float res = 0.0f;
         if (in) {
             const Group<G> grp(p);
             res = jacobi_item<DIV, G, REL>(d, grp, p, d.scenes[sid]);
         }
-        const double v[1] = {res};
+        const float v[1] = {res};
         const int slot[1] = {0};
         scene_accumulate_core<1, G>(d, chunk_scene(d, L, base_, per_, total_), sid, in && threadIdx.x % G == 0u, v, slot);
     }
@@ -738,7 +739,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
     const bool valid = inRange && S.enableVisc;
-    double bb = 0.0, rr = 0.0;
+    float bb = 0.0f, rr = 0.0f;
     if (valid) {
         const float4 g4 = d.CG[p];
         const float3 ag = visc_matvec<G, REL>(d, grp, p, S, d.CG, f3(g4));
@@ -750,7 +751,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
             rr = dot_term(r, r);
         }
     }
-    const double v[2] = {bb, rr};
+    const float v[2] = {bb, rr};
     const int slot[2] = {0, 1};
     scene_accumulate<2, G>(d, sid, valid && grp.lane == 0, v, slot);
 }
@@ -793,14 +794,14 @@ __global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
     const bool valid = inRange && S.enableVisc && !S.cgDone;
-    double rz = 0.0;
+    float rz = 0.0f;
     if (valid) {
         const float3 r = f3(d.CR[p]);
         const float3 z = mul(load_mat(d.MINV, d.stride, p), r);
         d.CP[p] = f4(z, d.CG[p].w);
         rz = dot_term(r, z);
     }
-    const double v[1] = {rz};
+    const float v[1] = {rz};
     const int slot[1] = {0};
     scene_accumulate<1>(d, sid, valid, v, slot);
 }
@@ -834,7 +835,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
     const bool valid = inRange && S.cgActive;
-    double pap = 0.0;
+    float pap = 0.0f;
     if (valid) {
         const float3 pv = f3(d.CP[p]);
         const float3 ap = visc_matvec<G, REL>(d, grp, p, S, d.CP, pv);
@@ -843,7 +844,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
             pap = dot_term(pv, ap);
         }
     }
-    const double v[1] = {pap};
+    const float v[1] = {pap};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, valid && grp.lane == 0, v, slot);
 }
@@ -858,7 +859,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
         const bool in = vp < total_;
         uint32_t sid = 0;
         const uint32_t p = in ? work_slot(d, kLoopCG, vp, sid) : 0u;
-        double pap = 0.0;
+        float pap = 0.0f;
         if (in) {
             const Group<G> grp(p);
             const float3 pv = f3(d.CP[p]);
@@ -868,7 +869,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
                 pap = dot_term(pv, ap);
             }
         }
-        const double v[1] = {pap};
+        const float v[1] = {pap};
         const int slot[1] = {0};
         scene_accumulate_core<1, G>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in && threadIdx.x % G == 0u,
                                  v, slot);
@@ -886,7 +887,7 @@ __global__ void k_ctrl_cg_alpha(Dev d) {
 }
 
 // Loop body 2: g += alpha p, r -= alpha Ap, |r|^2, z = M^-1 r, r . z (:722-784).
-__device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const SceneDev& S, double& rr, double& rz) {
+__device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const SceneDev& S, float& rr, float& rz) {
     const float alpha = S.cgAlpha;
     const float3 pv = f3(d.CP[p]);
     const float4 g4 = d.CG[p];
@@ -907,9 +908,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
     const bool valid = inRange && S.cgActive;
-    double rr = 0.0, rz = 0.0;
+    float rr = 0.0f, rz = 0.0f;
     if (valid) cg_update_item(d, p, S, rr, rz);
-    const double v[2] = {rr, rz};
+    const float v[2] = {rr, rz};
     const int slot[2] = {1, 2};
     scene_accumulate<2>(d, sid, valid, v, slot);
 }
@@ -922,9 +923,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_b(Dev d) {
         const bool in = vp < total_;
         uint32_t sid = 0;
         const uint32_t p = in ? work_slot(d, kLoopCG, vp, sid) : 0u;
-        double rr = 0.0, rz = 0.0;
+        float rr = 0.0f, rz = 0.0f;
         if (in) cg_update_item(d, p, d.scenes[sid], rr, rz);
-        const double v[2] = {rr, rz};
+        const float v[2] = {rr, rz};
         const int slot[2] = {1, 2};
         scene_accumulate_core<2>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in, v, slot);
     }
