@@ -153,10 +153,11 @@ __device__ float3 jgb_t(const Dev& d, const AdjDev& a, const Spline& sp, uint32_
     return out;
 }
 
-// Adds v into dst (one atomic per block); every thread of the block must call it.
-__device__ void block_add(double* dst, double v) {
+// Adds the FP32 terms v of the block into dst (one atomic per block): each warp sums as
+// an FP32 pair (warp_sum_pair), the warps in FP64; every thread of the block must call it.
+__device__ void block_add(double* dst, float term) {
     __shared__ double part[32];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const double v = warp_sum_pair(term, 1);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __syncthreads();
     if (lane == 0) part[warp] = v;
@@ -362,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const flo
     vb = grp.sum(vb);
     xd = grp.sum(xd);
     if (DT) dv = grp.sum(dv);
-    double acc = 0.0;
+    float acc = 0.0f;
     if (live && grp.lane == 0) {
         if (rw.flags & kHasBoundary) {
             const float3 gb = f3(d.GB[p]);
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const flo
         }
         a.VBAR[p] = f4(f3(a.VBAR[p]) + vb, 0.0f);
         a.XBAR[p] = f4(f3(a.XBAR[p]) + xd, 0.0f);
-        if (DT) acc = (double)a.RABAR[p] * (double)dv;
+        if (DT) acc = a.RABAR[p] * dv;
     }
     if (DT) block_add(a.SC + 1, acc);
 }
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const floa
     q1 = grp.sum(q1);
     qf = grp.sum(qf);
     racc = grp.sum(racc);
-    double s0 = 0.0, s2v = 0.0, s3v = 0.0;
+    float s0 = 0.0f, s2v = 0.0f, s3v = 0.0f;
     if (live && grp.lane == 0) {
         float3 b1 = make_float3(0.f, 0.f, 0.f);  // B g per unit dynamic boundary viscosity
         if (S.dynBVisc != 0.0f && (rw.flags & kHasBoundary)) {
@@ -556,9 +557,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const floa
         racc += -dot3(lti, Q) / rhoi;
         a.XBAR[p] = f4(f3(a.XBAR[p]) + xacc, 0.0f);
         a.RHOBAR[p] += racc;
-        s0 = dot3d(li, Q) / (double)rhoi;
-        s2v = (double)S.rho0 * dot3d(lti, q1);
-        s3v = (double)S.rho0 * dot3d(lti, b1);
+        s0 = dot3(li, Q) / rhoi;
+        s2v = S.rho0 * dot3(lti, q1);
+        s3v = S.rho0 * dot3(lti, b1);
     }
     block_add(a.SC + 0, s0);
     block_add(a.SC + 2, s2v);
@@ -588,13 +589,13 @@ __global__ void k_adj_store(Dev d, AdjDev a, const uint32_t* pid) {
 // x' = x + dt_n v3, v3 = v2 + dt_n a_p (K20 + K21): v3 bar, dt_n bar; ABAR = dt_n v3 bar.
 __global__ void k_adj_pres_out(Dev d, AdjDev a, const float4* V2, float dtn) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
+    float acc = 0.0f;
     if (p < d.n) {
         const float3 ap = f3(a.AK[p]);
         const float3 v3 = f3(V2[p]) + dtn * ap;
         const float3 xb = f3(a.XBAR[p]);
         const float3 vb = f3(a.VBAR[p]) + dtn * xb;
-        acc = dot3d(v3, xb) + dot3d(ap, vb);
+        acc = dot3(v3, xb) + dot3(ap, vb);
         a.VBAR[p] = f4(vb, 0.f);
         a.ABAR[p] = f4(dtn * vb, 0.f);
         a.KBAR[p] = 0.f;
@@ -607,10 +608,10 @@ __global__ void k_adj_pres_out(Dev d, AdjDev a, const float4* V2, float dtn) {
 // v1 = v0 + dt_o a_d (K7): dt_o bar; ABAR = dt_o v1 bar.
 __global__ void k_adj_div_out(Dev d, AdjDev a, float dto) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
+    float acc = 0.0f;
     if (p < d.n) {
         const float3 vb = f3(a.VBAR[p]);
-        acc = dot3d(f3(a.AK[p]), vb);
+        acc = dot3(f3(a.AK[p]), vb);
         a.ABAR[p] = f4(dto * vb, 0.f);
         a.KBAR[p] = 0.f;
         a.RABAR[p] = 0.f;
@@ -626,7 +627,7 @@ template <bool DIV>
 __global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, const float* kap, float alphaScale,
                         float fdt) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
+    float acc = 0.0f;
     if (p < d.n) {
         const float r = res[p];
         const float kb = a.KBAR[p];
@@ -637,7 +638,7 @@ __global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, 
         a.APBAR[p] += -r * kb;
         if (u != 0.0f) {
             const float f = (DIV ? 0.0f : 1.0f) - rhoadv[p] - r;
-            acc = (double)fdt * (double)u * (double)f;
+            acc = fdt * u * f;
         }
     }
     block_add(a.SC + (DIV ? 0 : 1), acc);
@@ -647,7 +648,7 @@ __global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, 
 // alpha'' = alpha / dt_n^2.
 __global__ void k_adj_pres_init(Dev d, AdjDev a, const float* rhoadv, float dtn) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
+    float acc = 0.0f;
     if (p < d.n) {
         const SceneDev& S = d.scenes[0];
         const float ra = rhoadv[p];
@@ -660,7 +661,7 @@ __global__ void k_adj_pres_init(Dev d, AdjDev a, const float* rhoadv, float dtn)
         a.RHOBAR[p] += rab / S.rho0;
         a.DBAR[p] = dtn * rab;
         a.ALBAR[p] += apb / (dtn * dtn);
-        acc = -2.0 * (double)apb * (double)al / ((double)dtn * dtn * dtn);
+        acc = -2.0f * apb * al / (dtn * dtn * dtn);
     }
     block_add(a.SC + 1, acc);
 }
@@ -669,7 +670,7 @@ __global__ void k_adj_pres_init(Dev d, AdjDev a, const float* rhoadv, float dtn)
 // alpha' = alpha / dt_o.
 __global__ void k_adj_div_init(Dev d, AdjDev a, const float* rhoadv, float dto) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
+    float acc = 0.0f;
     if (p < d.n) {
         const float ra = rhoadv[p];
         const float al = d.ALPHA[p];
@@ -679,7 +680,7 @@ __global__ void k_adj_div_init(Dev d, AdjDev a, const float* rhoadv, float dto) 
         const bool counted = (d.NCNT[p] & kCountMask) >= 20u;
         a.DBAR[p] = (counted && ra > 0.0f) ? rab : 0.0f;
         a.ALBAR[p] += apb / dto;
-        acc = -(double)apb * (double)al / ((double)dto * dto);
+        acc = -apb * al / (dto * dto);
     }
     block_add(a.SC + 0, acc);
 }
@@ -688,20 +689,20 @@ __global__ void k_adj_div_init(Dev d, AdjDev a, const float* rhoadv, float dto) 
 // right-hand side was zero). mode: 0 no viscosity, 1 viscosity, 2 viscosity with g = 0.
 __global__ void k_adj_velocity(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, float dtn, int mode) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    double sn = 0.0, so = 0.0;
+    float sn = 0.0f, so = 0.0f;
     if (p < d.n) {
         const SceneDev& S = d.scenes[0];
         const float3 grav = make_float3(S.g[0], S.g[1], S.g[2]);
         const float3 vb = f3(a.VBAR[p]);
         if (mode == 0) {
-            sn = dot3d(vb, grav);
+            sn = dot3(vb, grav);
             a.GBAR[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         } else {
             const float3 v1 = f3(V1[p]);
             const float3 g = mode == 1 ? f3(G[p]) : make_float3(0.f, 0.f, 0.f);
             const float3 dg = g - v1;
-            sn = dot3d(vb, grav + (1.0f / dto) * dg);
-            so = -(double)(dtn / (dto * dto)) * dot3d(vb, dg);
+            sn = dot3(vb, grav + (1.0f / dto) * dg);
+            so = -(dtn / (dto * dto)) * dot3(vb, dg);
             a.GBAR[p] = mode == 1 ? f4((dtn / dto) * vb, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
             a.VBAR[p] = f4((1.0f - dtn / dto) * vb, 0.f);
         }
