@@ -157,10 +157,10 @@ __device__ float3 jgb_t(const Dev& d, const AdjDev& a, const Spline& sp, uint32_
 // an FP32 pair (warp_sum_pair), the warps in FP64; every thread of the block must call it.
 __device__ void block_add(double* dst, float term) {
     __shared__ double part[32];
-    const double v = warp_sum_pair(term, 1);
+    const float2 v = warp_sum_pair(term, 1);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __syncthreads();
-    if (lane == 0) part[warp] = v;
+    if (lane == 0) part[warp] = pair_value(v);
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;

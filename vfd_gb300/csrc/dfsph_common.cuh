@@ -312,10 +312,11 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
 // hold zeros), as an unevaluated pair hi + lo of FP32 numbers: each level adds the
 // partners' high parts with Knuth's error-free TwoSum and carries the rounding error
 // and the partners' low parts in lo, so the pair keeps ~44 significant bits (relative
-// error ~1e-13 for a warp's 32 terms). Widened to FP64 at the end: FP64 arithmetic runs
-// at a small fraction of the FP32 rate on this GPU, and a DADD per lane and level cost
-// more than the rest of a reduction kernel's arithmetic.
-__device__ __forceinline__ double warp_sum_pair(float v, int step) {
+// error ~1e-13 for a warp's 32 terms), widened to FP64 by the lane that stores it
+// (pair_value): FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU,
+// and a DADD per lane and level cost more than the rest of a reduction kernel's
+// arithmetic.
+__device__ __forceinline__ float2 warp_sum_pair(float v, int step) {
     float hi = v, lo = 0.0f;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
@@ -328,8 +329,11 @@ __device__ __forceinline__ double warp_sum_pair(float v, int step) {
         lo = __fadd_rn(__fadd_rn(lo, l2), err);
         hi = sum;
     }
-    return (double)hi + (double)lo;
+    return make_float2(hi, lo);
 }
+// The FP64 value of a pair (taken by the one lane that stores it, so that no other lane
+// does FP64 work).
+__device__ __forceinline__ double pair_value(float2 p) { return (double)p.x + (double)p.y; }
 
 // Adds the FP32 terms `v` into scene `sid`'s FP64 accumulators `slot` (bucket
 // blockIdx % 32). A block whose particles lie in one scene sums each warp as an FP32
@@ -346,13 +350,13 @@ __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformS
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bucket = blockIdx.x % kBuckets;
     if (uniformScene >= 0) {
-        double s[K];
+        float2 s[K];
 #pragma unroll
         for (int k = 0; k < K; k++) s[k] = warp_sum_pair(valid ? v[k] : 0.0f, (int)G);
         __syncthreads();
         if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < K; k++) sm[warp][k] = s[k];
+            for (int k = 0; k < K; k++) sm[warp][k] = pair_value(s[k]);
         __syncthreads();
         if (threadIdx.x == 0) {
 #pragma unroll
@@ -380,12 +384,12 @@ __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, boo
     if (threadIdx.x == 0) uniformBlock = (first < d.n) && (scene_of(d, first) == scene_of(d, last)) ? 1 : 0;
     __syncthreads();
     if (uniformBlock) {
-        double s[K];
+        float2 s[K];
 #pragma unroll
         for (int k = 0; k < K; k++) s[k] = warp_sum_pair(valid ? v[k] : 0.0f, (int)G);
         if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < K; k++) sm[warp][k] = s[k];
+            for (int k = 0; k < K; k++) sm[warp][k] = pair_value(s[k]);
         __syncthreads();
         if (threadIdx.x == 0) {
             const uint32_t sc = scene_of(d, first);
