@@ -725,7 +725,7 @@ void fill_stats(const SceneDev& S, vfd_step_stats* st) {
     st->ViscositySolverIterationCount = S.enableVisc ? S.cgIt : 0u;
     st->DivergenceSolverError = S.enableDiv ? S.div.err : 0.0f;
     st->PressureSolverError = S.pres.err;
-    st->ViscositySolverError = S.enableVisc ? S.cgErr : 0.0f;
+    st->ViscositySolverError = (S.enableVisc && S.cgRhs > 0.0) ? (float)std::sqrt(S.cgRR / S.cgRhs) : 0.0f;
     st->FrameTime = S.frameTime;
     st->FrameIndex = S.frameIndex;
     st->TimeStepSize = S.dt;

@@ -93,7 +93,6 @@ struct SceneDev {
     LoopState div, pres;
     // viscosity CG
     uint32_t cgIt, cgActive, cgDone, cgZeroG, cgUpdateP;
-    float cgErr;
     double cgRhs, cgThr, cgAbsNew, cgRR;
     float cgAlpha, cgBeta;
 };
@@ -294,6 +293,19 @@ __device__ __forceinline__ double fold_acc(const Dev& d, uint32_t s, int slot) {
 #pragma unroll
     for (uint32_t b = 0; b < kBuckets; b++) q[(size_t)b * 16u] = 0.0;
     return t;
+}
+// The same fold by a whole warp (one scene's controller): lane b loads and zeroes bucket
+// b, and an xor butterfly adds them, five dependent FP64 adds instead of 32 (a dependent
+// FP64 add takes ~64 cycles on this GPU, an FP32 one 4). Every lane ends with the same
+// sum: partners add the same two numbers, and IEEE addition is commutative.
+__device__ __forceinline__ double fold_acc_warp(const Dev& d, uint32_t s, int slot, uint32_t lane) {
+    static_assert(kBuckets == 32u, "one bucket per lane");
+    double* q = acc_bucket(d, s, slot, lane);
+    double v = __ldcg(q);
+    *q = 0.0;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
     uint32_t* q = max_bucket(d, s, k, 0);

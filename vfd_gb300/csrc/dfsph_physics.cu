@@ -439,26 +439,46 @@ __global__ void k_ctrl_jacobi_init(Dev d) {
 }
 
 // After an iteration: error = -rho0 * sum(res) / N (order-independent form of the
-// reference's thrust::minus fold, DFSPHImplementation.cu:483-491, :554-563).
+// reference's thrust::minus fold, DFSPHImplementation.cu:483-491, :554-563). Returns
+// whether the scene runs another iteration.
+template <bool DIV>
+__device__ __forceinline__ bool jacobi_control(SceneDev& S, double sum) {
+    LoopState& L = DIV ? S.div : S.pres;
+    const double err = -(double)S.rho0 * sum / (double)S.count;
+    L.err = (float)err;
+    L.it++;
+    const uint32_t mn = DIV ? S.minIterD : S.minIterP, mx = DIV ? S.maxIterD : S.maxIterP;
+    const float eta = DIV ? S.dtInv * S.maxErrD * 0.0001f * S.rho0 : S.maxErrP * 0.0001f * S.rho0;
+    const bool again = (err > (double)eta || L.it < mn) && L.it < mx;
+    if (!again && L.it >= mx && err > (double)eta) S.flags |= DIV ? 0x2u : 0x1u;
+    L.active = again ? 1u : 0u;
+    return again;
+}
+
+// The loop controllers run as one block. With one scene its first warp folds the
+// buckets together (fold_acc_warp) and lane 0 takes the decisions; a batch gives each
+// scene a thread.
 template <bool DIV>
 __global__ void k_ctrl_jacobi(Dev d) {
     VFD_COUNT_LAUNCH(d);
+    if (d.nscenes == 1) {
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        const bool act = (DIV ? S.div.active : S.pres.active) != 0u;
+        const double sum = act ? fold_acc_warp(d, 0, 0, threadIdx.x) : 0.0;
+        if (threadIdx.x == 0) {
+            const bool again = act && jacobi_control<DIV>(S, sum);
+            set_condition(d, DIV ? kLoopDiv : kLoopPres, (again && !aborted_p(d)) ? 1u : 0u);
+        }
+        return;
+    }
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
-        LoopState& L = DIV ? S.div : S.pres;
-        if (!L.active) continue;
-        const double err = -(double)S.rho0 * fold_acc(d, s, 0) / (double)S.count;
-        L.err = (float)err;
-        L.it++;
-        const uint32_t mn = DIV ? S.minIterD : S.minIterP, mx = DIV ? S.maxIterD : S.maxIterP;
-        const float eta = DIV ? S.dtInv * S.maxErrD * 0.0001f * S.rho0 : S.maxErrP * 0.0001f * S.rho0;
-        const bool again = (err > (double)eta || L.it < mn) && L.it < mx;
-        if (!again && L.it >= mx && err > (double)eta) S.flags |= DIV ? 0x2u : 0x1u;
-        L.active = again ? 1u : 0u;
-        if (again) atomicOr(&any, 1u);
+        if (!(DIV ? S.div.active : S.pres.active)) continue;
+        if (jacobi_control<DIV>(S, fold_acc(d, s, 0))) atomicOr(&any, 1u);
     }
     __syncthreads();
     if (d.nscenes > 1)
@@ -756,33 +776,50 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
     scene_accumulate<2, G>(d, sid, valid && grp.lane == 0, v, slot);
 }
 
-// Early outs of SolveViscosity (:646-675).
+// Early outs of SolveViscosity (:646-675). The solver error sqrt(|r|^2 / |b|^2) is
+// formed on the host from cgRR and cgRhs when the statistics are read, so that no
+// controller spends an FP64 division and square root on it per iteration.
+__device__ __forceinline__ void cg_start(const Dev& d, SceneDev& S, bool on, double rhs, double rr) {
+    S.cgIt = 0;
+    S.cgActive = 0;
+    S.cgUpdateP = 0;
+    S.cgZeroG = 0;
+    S.cgDone = 1;
+    S.cgRhs = 0.0;
+    S.cgRR = 0.0;
+    if (!on || aborted_p(d)) return;
+    S.cgRhs = rhs;
+    S.cgRR = rr;
+    if (rhs == 0.0) {
+        S.cgZeroG = 1;
+        return;
+    }
+    const double e = (double)S.maxErrV;
+    S.cgThr = fmax(e * e * 0.0001 * rhs, (double)FLT_MIN);
+    if (rr < S.cgThr) return;
+    S.cgDone = 0;
+}
+
 __global__ void k_ctrl_cg0(Dev d) {
     VFD_COUNT_LAUNCH(d);
+    if (d.nscenes == 1) {
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        const bool on = S.enableVisc != 0;
+        double rhs = 0.0, rr = 0.0;
+        if (on) {
+            rhs = fold_acc_warp(d, 0, 0, threadIdx.x);
+            rr = fold_acc_warp(d, 0, 1, threadIdx.x);
+        }
+        if (threadIdx.x == 0) cg_start(d, S, on, rhs, rr);
+        return;
+    }
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
-        S.cgIt = 0;
-        S.cgActive = 0;
-        S.cgUpdateP = 0;
-        S.cgZeroG = 0;
-        S.cgDone = 1;
-        S.cgErr = 0.0f;
-        if (!S.enableVisc) continue;
-        const double rhs = fold_acc(d, s, 0), rr = fold_acc(d, s, 1);
-        if (aborted_p(d)) continue;
-        S.cgRhs = rhs;
-        S.cgRR = rr;
-        if (rhs == 0.0) {
-            S.cgZeroG = 1;
-            continue;
-        }
-        const double e = (double)S.maxErrV;
-        S.cgThr = fmax(e * e * 0.0001 * rhs, (double)FLT_MIN);
-        if (rr < S.cgThr) {
-            S.cgErr = (float)sqrt(rr / rhs);
-            continue;
-        }
-        S.cgDone = 0;
+        const bool on = S.enableVisc != 0;
+        const double rhs = on ? fold_acc(d, s, 0) : 0.0;
+        const double rr = on ? fold_acc(d, s, 1) : 0.0;
+        cg_start(d, S, on, rhs, rr);
     }
 }
 
@@ -806,19 +843,30 @@ __global__ void __launch_bounds__(kBlock) k_cg_p0(Dev d) {
     scene_accumulate<1>(d, sid, valid, v, slot);
 }
 
+__device__ __forceinline__ bool cg_first(const Dev& d, SceneDev& S, double rz) {
+    S.cgAbsNew = fabs(rz);
+    const bool run = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
+    S.cgActive = run ? 1u : 0u;
+    return run;
+}
+
 __global__ void k_ctrl_cg1(Dev d) {
     VFD_COUNT_LAUNCH(d);
+    if (d.nscenes == 1) {
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        const bool on = S.enableVisc && !S.cgDone;
+        const double rz = on ? fold_acc_warp(d, 0, 0, threadIdx.x) : 0.0;
+        if (threadIdx.x == 0) set_condition(d, kLoopCG, (on && cg_first(d, S, rz)) ? 1u : 0u);
+        return;
+    }
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
         if (!S.enableVisc || S.cgDone) continue;
-        S.cgAbsNew = fabs(fold_acc(d, s, 0));
-        S.cgErr = (float)sqrt(S.cgRR / S.cgRhs);
-        const bool run = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
-        S.cgActive = run ? 1u : 0u;
-        if (run) atomicOr(&any, 1u);
+        if (cg_first(d, S, fold_acc(d, s, 0))) atomicOr(&any, 1u);
     }
     __syncthreads();
     if (d.nscenes > 1) build_work_list(d, kLoopCG, [&](uint32_t sc) { return d.scenes[sc].cgActive != 0u; });
@@ -879,6 +927,14 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
 // alpha = |r . z| / (p . Ap) (:714-720).
 __global__ void k_ctrl_cg_alpha(Dev d) {
     VFD_COUNT_LAUNCH(d);
+    if (d.nscenes == 1) {
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        if (!S.cgActive) return;
+        const double pap = fold_acc_warp(d, 0, 0, threadIdx.x);
+        if (threadIdx.x == 0) S.cgAlpha = (float)(S.cgAbsNew / pap);
+        return;
+    }
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
         if (!S.cgActive) continue;
@@ -932,8 +988,41 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_b(Dev d) {
 }
 
 // Loop control: break on |r|^2 < threshold, else beta and the next iteration (:754-805).
+__device__ __forceinline__ bool cg_control(const Dev& d, SceneDev& S, double rr, double rz) {
+    S.cgRR = rr;
+    if (rr < S.cgThr) {
+        S.cgActive = 0;
+        S.cgDone = 1;
+        return false;
+    }
+    const double absOld = S.cgAbsNew;
+    S.cgAbsNew = fabs(rz);
+    S.cgBeta = (float)(S.cgAbsNew / absOld);
+    S.cgIt++;
+    S.cgUpdateP = 1;
+    const bool again = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
+    if (!again) S.flags |= 0x4u;
+    S.cgActive = again ? 1u : 0u;
+    return again;
+}
+
 __global__ void k_ctrl_cg(Dev d) {
     VFD_COUNT_LAUNCH(d);
+    if (d.nscenes == 1) {
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        const bool act = S.cgActive != 0u;
+        double rr = 0.0, rz = 0.0;
+        if (act) {
+            rr = fold_acc_warp(d, 0, 1, threadIdx.x);
+            rz = fold_acc_warp(d, 0, 2, threadIdx.x);
+        }
+        if (threadIdx.x == 0) {
+            S.cgUpdateP = 0;
+            set_condition(d, kLoopCG, (act && cg_control(d, S, rr, rz)) ? 1u : 0u);
+        }
+        return;
+    }
     __shared__ uint32_t any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
@@ -942,22 +1031,7 @@ __global__ void k_ctrl_cg(Dev d) {
         S.cgUpdateP = 0;
         if (!S.cgActive) continue;
         const double rr = fold_acc(d, s, 1), rz = fold_acc(d, s, 2);
-        S.cgRR = rr;
-        S.cgErr = (float)sqrt(rr / S.cgRhs);
-        if (rr < S.cgThr) {
-            S.cgActive = 0;
-            S.cgDone = 1;
-            continue;
-        }
-        const double absOld = S.cgAbsNew;
-        S.cgAbsNew = fabs(rz);
-        S.cgBeta = (float)(S.cgAbsNew / absOld);
-        S.cgIt++;
-        S.cgUpdateP = 1;
-        const bool again = S.cgIt >= S.minIterV && S.cgIt < S.maxIterV && !aborted_p(d);
-        if (!again) S.flags |= 0x4u;
-        S.cgActive = again ? 1u : 0u;
-        if (again) atomicOr(&any, 1u);
+        if (cg_control(d, S, rr, rz)) atomicOr(&any, 1u);
     }
     __syncthreads();
     if (d.nscenes > 1) build_work_list(d, kLoopCG, [&](uint32_t sc) { return d.scenes[sc].cgActive != 0u; });
