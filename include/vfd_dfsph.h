@@ -359,6 +359,9 @@ int vfd_get_kernel_table(const vfd_sim* sim, float* w, float* grad_w, float* rad
  * host with one flag read per solver iteration (the reference's control flow).
  */
 int vfd_set_graph_mode(vfd_sim* sim, int32_t enabled);
+/* Whether graphs are requested, and whether the steps so far ran from them (0 when the
+ * step graph could not be built and the same kernels were launched from the host). */
+int vfd_get_graph_mode(const vfd_sim* sim, int32_t* requested, int32_t* active);
 
 /* Batched scenes: independent scenes advanced together, one launch per stage.
  * vfd_create_batch takes one description per scene (same ParticleRadius for all);

@@ -33,7 +33,7 @@ EXPORTS = [
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
-    "vfd_emit",
+    "vfd_emit", "vfd_get_graph_mode",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -123,6 +123,7 @@ def lib() -> C.CDLL:
                 "vfd_set_position_mode": [P, C.c_int32],
                 "vfd_set_kernel_mode": [P, C.c_int32],
                 "vfd_emit": [P, f32p, f32p, C.c_uint32],
+                "vfd_get_graph_mode": [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
                 "vfd_build_mesh_map": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_int32, C.c_float, u32p,
                                        C.c_float, f32p, u32p, u32p, C.POINTER(vfd_volume_map)],
                 "vfd_sample_mesh_volume": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_float, u32p, C.c_int32,
@@ -340,6 +341,12 @@ class DFSPHSimulation:
 
     def SetGraphMode(self, enabled: bool):
         _check(lib().vfd_set_graph_mode(self._h, int(bool(enabled))), "vfd_set_graph_mode")
+
+    def GetGraphMode(self) -> tuple[bool, bool]:
+        """(graphs requested, steps so far ran from graphs)."""
+        req, act = C.c_int32(), C.c_int32()
+        _check(lib().vfd_get_graph_mode(self._h, C.byref(req), C.byref(act)), "vfd_get_graph_mode")
+        return bool(req.value), bool(act.value)
 
     # stepping
     def Reset(self):

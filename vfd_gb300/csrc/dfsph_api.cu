@@ -547,16 +547,21 @@ int upload(vfd_sim* s) {
 int build_graph(vfd_sim* s, int parity, const void* rec, cudaGraph_t* gOut, cudaGraphExec_t* execOut) {
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h[3];
+    // One conditional handle per while node the graph has (divergence, CG, pressure): a
+    // handle that no node uses makes cudaGraphInstantiate fail with "invalid argument".
+    Dev d = s->dev[parity];
+    const bool used[3] = {s->anyDiv, s->anyVisc, true};
+    cudaGraphConditionalHandle h[3] = {};
     for (int k = 0; k < 3; k++) {
+        d.condHandle[k] = 0ull;
+        if (!used[k]) continue;
         cudaError_t e = cudaGraphConditionalHandleCreate(&h[k], g, 0, 0);
         if (e != cudaSuccess) {
             cudaGraphDestroy(g);
             return fail(VFD_E_CUDA, "cudaGraphConditionalHandleCreate: %s", cudaGetErrorString(e));
         }
+        d.condHandle[k] = (unsigned long long)h[k];
     }
-    Dev d = s->dev[parity];
-    for (int k = 0; k < 3; k++) d.condHandle[k] = (unsigned long long)h[k];
     cudaStream_t cap = s->stream;
     std::vector<cudaGraphNode_t> leaves;
     const uint32_t passes = s->maxStPasses;
@@ -1307,6 +1312,13 @@ int vfd_set_graph_mode(vfd_sim* s, int32_t enabled) {
     TRY(check_sim(s));
     s->graphMode = enabled != 0;
     s->graphFailed = false;
+    return VFD_OK;
+}
+
+int vfd_get_graph_mode(const vfd_sim* s, int32_t* requested, int32_t* active) {
+    TRY(check_sim(s));
+    if (requested) *requested = s->graphMode ? 1 : 0;
+    if (active) *active = (s->graphMode && !s->graphFailed) ? 1 : 0;
     return VFD_OK;
 }
 
