@@ -476,7 +476,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-side", type=int, default=100)
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="end-to-end steps (default: --steps, the same steps)")
+    ap.add_argument("--lanes", default="", help="lanes per particle instead of autotuning: N, or one per tuned "
+                    "kernel (comma-separated); profilers use it, as they distort the autotuner's timings")
     ap.add_argument("--cpu-steps", type=int, default=150)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched-scene measurement")
@@ -506,7 +508,13 @@ def main():
     n = len(s["x"])
     sim = V.scene_simulation(s)
     sim.Steps(1)
-    lanes = sim.Autotune(2)  # per-kernel lanes per particle, state restored
+    if args.lanes:  # fixed lanes per particle (one value, or one per tuned kernel)
+        vals = [int(x) for x in args.lanes.split(",")]
+        vals = vals * len(V.TUNED_KERNELS) if len(vals) == 1 else vals
+        sim.SetLanes(vals)
+        lanes = dict(zip(V.TUNED_KERNELS, vals))
+    else:
+        lanes = sim.Autotune(2)  # per-kernel lanes per particle, state restored
     sim.SetGraphMode(not args.eager)
     sim.Steps(args.warmup)
     stream = torch.cuda.ExternalStream(sim.GetStream())
@@ -542,7 +550,11 @@ def main():
     ms_max = float(t.item())
     value = n * ws * args.steps / (ms_max / 1e3)
 
-    # end to end through the C-ABI with pinned host buffers
+    # end to end through the C-ABI with pinned host buffers, over the same simulated steps
+    # as the timed region: the scene restarts and advances to where that region began
+    e2e_steps = args.e2e_steps or args.steps
+    sim.SetFluidObjects(s["x"], s["v"])
+    sim.Steps(1 + args.warmup)
     pin = lambda: torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
     xh, vh, ah = pin(), pin(), pin()
     sim.GetStateInto(xh, vh, ah)
@@ -550,7 +562,7 @@ def main():
     if ws > 1:
         dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         sim.SetState(xh, vh)
         sim.OnUpdate()
         sim.GetStateInto(xh, vh, ah)
@@ -558,7 +570,7 @@ def main():
     t = torch.tensor([el], dtype=torch.float64, device="cuda")
     if ws > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e = {"value": n * ws * args.e2e_steps / float(t.item()), "unit": UNIT, "h2d_bytes_per_step": 24 * n,
+    e2e = {"value": n * ws * e2e_steps / float(t.item()), "unit": UNIT, "steps": e2e_steps, "h2d_bytes_per_step": 24 * n,
            "d2h_bytes_per_step": 36 * n}
 
     # per-kernel event timing of eager launches -> dominant kernel and roofline
