@@ -158,6 +158,12 @@ int vfd_find_neighbors_noalloc(const float* xyz, uint32_t n, float particle_radi
     d.MAXB = (uint32_t*)(b + Layout::MAXB);
     d.ACCB = (double*)(b + Layout::ACCB);
     for (int k = 0; k < 16; k++) d.lanes[k] = 8;
+    {  // the neighbour search strides a fixed grid over the cells
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        d.batchBlocks = (uint32_t)(sms > 0 ? sms : 1) * (2048u / kBlock);
+    }
 
     // the search radius and squared radius exactly as SetDescription derives them
     SceneDev scene;

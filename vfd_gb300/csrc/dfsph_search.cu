@@ -310,73 +310,92 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(Dev d) {
 }
 
 // N6-N8: ComputeCountsKernel + NeighborhoodQueryWithCountsKernel (ParticleSearchKernels.cu:93-193)
-// in one pass. G lanes test consecutive candidates of a cell together and compact the
-// hits with a ballot, so the row keeps the reference's order (z, y, x cells, then cell
-// order) and its cap of 70. The squared distance is computed without contraction,
-// x^2 + y^2 + z^2 left to right, as the FP32 oracle does.
-template <uint32_t G, bool REL>
+// in one pass, one warp per cell. The particles of a cell share their 27 candidate cells,
+// so the warp walks that candidate set once, 32 candidates per round (lane j < 27 holds
+// cell j's range, a prefix over the lanes flattens them), and tests each candidate
+// against every particle of the cell, whose positions sit in shared memory. A ballot per
+// particle appends its hits in candidate order, so each row keeps the reference's order
+// (z, y, x cells, then cell order) and its cap of 70. The squared distance is computed
+// without contraction, x^2 + y^2 + z^2 left to right, as the FP32 oracle does. The
+// cell's grid coordinates come from its first particle by the same formula a
+// per-particle search would use on each of them (they agree: it is how they were binned).
+template <bool REL>
 __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
     VFD_COUNT_LAUNCH(d);
-    const Group<G> grp;
-    const uint32_t p = grp.p;
-    if (p >= d.n || aborted(d)) return;
-    const uint32_t sid = scene_of(d, p);
-    const SceneDev& S = d.scenes[sid];
-    const float4 xi = d.X[p];
-    const float3 xa = abs_pos(d, S, xi);
-    const float pos[3] = {xa.x, xa.y, xa.z};
-    int gc[3];
+    if (aborted(d)) return;
+    __shared__ float4 sx[kBlock / 32u][32];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t below = (1u << lane) - 1u;
+    const uint32_t total = d.status[2];
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < total; c += warps) {
+        const uint32_t cnt = d.CELL_COUNT[c];
+        if (cnt == 0u) continue;
+        const uint32_t start = d.CELL_START[c];
+        const uint32_t sid = scene_of(d, start);
+        const SceneDev& S = d.scenes[sid];
+        const float3 xa = abs_pos(d, S, d.X[start]);
+        const float pos[3] = {xa.x, xa.y, xa.z};
+        int gc[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) gc[k] = (int)floorf(__fmul_rn(__fsub_rn(pos[k], S.gridMin[k]), S.gridDelta[k]));
-    const float h2 = S.h2;
-    const uint32_t shift = (threadIdx.x & 31u) & ~(G - 1u);
-    const uint32_t below = (1u << grp.lane) - 1u;
-    uint32_t count = 0;
-    uint32_t* row = d.NBR + (size_t)p * kRow;
-    for (int dz = -1; dz < 2; dz++) {
-        for (int dy = -1; dy < 2; dy++) {
-            for (int dx = -1; dx < 2; dx++) {
-                const int fx = gc[0] + dx, fy = gc[1] + dy, fz = gc[2] + dz;
-                if (fx < 0 || fy < 0 || fz < 0 || fx >= (int)S.dim[0] || fy >= (int)S.dim[1] || fz >= (int)S.dim[2])
-                    continue;
-                const uint32_t c = S.cellBase + cell_key(S, fx, fy, fz);
-                const uint32_t start = d.CELL_START[c], end = start + d.CELL_COUNT[c];
-                for (uint32_t base = start; base < end; base += G) {
-                    const uint32_t q = base + grp.lane;
-                    bool hit = false;
-                    if (q < end) {
-                        const float3 e = pair_r<REL>(d, d.X[q], xi);
-                        const float ex = e.x, ey = e.y, ez = e.z;
-                        const float d2 =
-                            __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
-                        hit = d2 < h2 && d2 > 0.0f;
-                    }
-                    const uint32_t bits = (__ballot_sync(grp.mask, hit) >> shift) & (G == 32u ? 0xffffffffu : ((1u << G) - 1u));
-                    const uint32_t at = count + __popc(bits & below);
-                    if (hit && at < kMaxNeighbors) row[at] = q;
-                    count += __popc(bits);
-                    if (count >= kMaxNeighbors) {
-                        count = kMaxNeighbors;
-                        goto done;
-                    }
-                }
+        for (int k = 0; k < 3; k++) gc[k] = (int)floorf(__fmul_rn(__fsub_rn(pos[k], S.gridMin[k]), S.gridDelta[k]));
+        // lane j < 27: candidate cell j (dz, dy, dx = j / 9, j / 3 % 3, j % 3, each minus 1)
+        uint32_t cs = 0u, cc = 0u;
+        if (lane < 27u) {
+            const int fx = gc[0] + (int)(lane % 3u) - 1, fy = gc[1] + (int)(lane / 3u % 3u) - 1,
+                      fz = gc[2] + (int)(lane / 9u) - 1;
+            if (fx >= 0 && fy >= 0 && fz >= 0 && fx < (int)S.dim[0] && fy < (int)S.dim[1] && fz < (int)S.dim[2]) {
+                const uint32_t key = S.cellBase + cell_key(S, fx, fy, fz);
+                cs = d.CELL_START[key];
+                cc = d.CELL_COUNT[key];
             }
         }
-    }
-done:
-    if (grp.lane == 0) {
-        d.NCNT[p] = count;
-        if (count == kMaxNeighbors) atomicOr(&d.scenes[sid].flags, 0x8u);
-    }
-    // one max per warp (per scene) into the bucket
-    const uint32_t active = __activemask();
-    const uint32_t leader = __ffs(active) - 1u;
-    const uint32_t s0 = __shfl_sync(active, sid, leader);
-    if (__all_sync(active, sid == s0)) {
-        const uint32_t m = __reduce_max_sync(active, count);
-        if ((threadIdx.x & 31u) == leader) atomicMax(max_bucket(d, s0, 1, blockIdx.x % kBuckets), m);
-    } else if (grp.lane == 0) {
-        atomicMax(max_bucket(d, sid, 1, blockIdx.x % kBuckets), count);
+        uint32_t incl = cc;
+#pragma unroll
+        for (uint32_t o = 1; o < 32u; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const uint32_t ncand = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t excl = incl - cc;
+        const float h2 = S.h2;
+        uint32_t mx = 0u;
+        for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
+            const uint32_t kk = min(32u, cnt - k0);
+            __syncwarp();
+            if (lane < kk) sx[w][lane] = d.X[start + k0 + lane];
+            __syncwarp();
+            uint32_t count = 0u;  // neighbours so far of particle start + k0 + lane
+            for (uint32_t base = 0; base < ncand; base += 32u) {
+                const uint32_t i = base + lane;
+                // candidate i lies in the last cell j whose flattened start is <= i
+                uint32_t j = 0u;
+#pragma unroll
+                for (uint32_t step = 16u; step > 0u; step >>= 1) {
+                    const uint32_t e = __shfl_sync(0xffffffffu, excl, min(j + step, 26u));
+                    if (j + step <= 26u && e <= i) j += step;
+                }
+                const uint32_t q = __shfl_sync(0xffffffffu, cs, j) + (i - __shfl_sync(0xffffffffu, excl, j));
+                const bool valid = i < ncand;
+                const float4 xq = valid ? d.X[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+                for (uint32_t k = 0; k < kk; k++) {
+                    const float3 e = pair_r<REL>(d, xq, sx[w][k]);
+                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(e.x, e.x), __fmul_rn(e.y, e.y)), __fmul_rn(e.z, e.z));
+                    const bool hit = valid && d2 < h2 && d2 > 0.0f;
+                    const uint32_t bits = __ballot_sync(0xffffffffu, hit);
+                    const uint32_t ck = __shfl_sync(0xffffffffu, count, k);
+                    const uint32_t at = ck + __popc(bits & below);
+                    if (hit && at < kMaxNeighbors) d.NBR[(size_t)(start + k0 + k) * kRow + at] = q;
+                    if (lane == k) count = min(kMaxNeighbors, ck + __popc(bits));
+                }
+            }
+            if (lane < kk) {
+                d.NCNT[start + k0 + lane] = count;
+                if (count == kMaxNeighbors) atomicOr(&d.scenes[sid].flags, 0x8u);
+            }
+            mx = max(mx, __reduce_max_sync(0xffffffffu, lane < kk ? count : 0u));
+        }
+        if (lane == 0) atomicMax(max_bucket(d, sid, 1, blockIdx.x % kBuckets), mx);
     }
 }
 
@@ -392,10 +411,9 @@ void launch_search(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_scan_down", s, k_scan_down<<<d.scanBlocks, 256, 0, s>>>(d));
     VFD_LAUNCH("k_slots", s, k_slots<<<nb, kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_rank_gather", s, k_rank_gather<<<nb, kBlock, 0, s>>>(d));
-#define K_NEIGHBORS(G) k_neighbors<G, false>
-#define K_NEIGHBORS_R(G) k_neighbors<G, true>
-    if (d.cellRel) VFD_LAUNCH_LANES("k_neighbors", kTNeighbors, K_NEIGHBORS_R);
-    else VFD_LAUNCH_LANES("k_neighbors", kTNeighbors, K_NEIGHBORS);
+    // a warp per cell, a fixed grid striding over the cells the device counted
+    if (d.cellRel) VFD_LAUNCH("k_neighbors", s, k_neighbors<true><<<d.batchBlocks, kBlock, 0, s>>>(d));
+    else VFD_LAUNCH("k_neighbors", s, k_neighbors<false><<<d.batchBlocks, kBlock, 0, s>>>(d));
 }
 
 uint32_t scan_block_count(uint32_t cellCap) { return (cellCap + kScanItems - 1) / kScanItems; }
