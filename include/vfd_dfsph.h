@@ -393,8 +393,8 @@ int vfd_profile_kernels(vfd_sim* sim, uint32_t steps, vfd_kernel_time* out, uint
  * density+factor, density change, pressure acceleration, Jacobi iteration,
  * divergence finish, surface classification, surface smoothing, viscosity
  * preconditioner, viscosity setup, CG matrix-vector product, density advection,
- * pressure finish, neighbour search (no counterpart in the reference, which
- * launches every kernel with 256 threads, one per particle).
+ * pressure finish (no counterpart in the reference, which launches every kernel
+ * with 256 threads, one per particle). The neighbour search runs a warp per cell.
  */
 int vfd_set_lanes(vfd_sim* sim, const uint8_t* lanes, uint32_t count);
 int vfd_get_lanes(const vfd_sim* sim, uint8_t* lanes, uint32_t count);

@@ -41,7 +41,7 @@ EXPORTS = [
 ]
 
 TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
-                 "st_smooth", "visc_precond", "visc_setup", "cg_spmv", "pres_init", "pres_finish", "neighbors"]
+                 "st_smooth", "visc_precond", "visc_setup", "cg_spmv", "pres_init", "pres_finish"]
 
 
 class vfd_kernel_time(C.Structure):

@@ -1792,8 +1792,7 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
     if (s->n == 0 || steps == 0) return VFD_OK;
     static const char* names[kTunedCount] = {"k_density_factor", "k_div_init", "k_pressure_accel", "k_jacobi_iter",
                                              "k_div_finish", "k_st_classify", "k_st_smooth", "k_visc_precond",
-                                             "k_visc_setup", "k_cg_spmv", "k_pres_init", "k_pres_finish",
-                                             "k_neighbors"};
+                                             "k_visc_setup", "k_cg_spmv", "k_pres_init", "k_pres_finish"};
     const uint8_t cand[3] = {4, 8, 16};
     // snapshot of everything a step carries: positions, the current state set, scenes
     const size_t st = s->stride;

@@ -46,7 +46,7 @@ constexpr uint32_t kHasBoundaryVisc = 1u << 9;
 // Neighbour-loop kernels whose lanes per particle (4, 8 or 16) the autotuner picks.
 enum TunedKernel {
     kTDensity = 0, kTDivInit, kTPAccel, kTJacobi, kTDivFinish, kTStClassify, kTStSmooth, kTViscPrecond,
-    kTViscSetup, kTSpmv, kTPresInit, kTPresFinish, kTNeighbors, kTunedCount
+    kTViscSetup, kTSpmv, kTPresInit, kTPresFinish, kTunedCount
 };
 
 // Per-scene solver loop state (one Jacobi or CG loop).
