@@ -60,6 +60,25 @@ def test_search_bit_exact(factory):
     assert_neighbors_equal(g, o)
 
 
+@pytest.mark.parametrize("n,side", [(3000, 2.5), (600, 1.2)])
+def test_search_bit_exact_dense_cells(n, side):
+    # cells of 100+ particles (the warp-per-cell search then takes a cell's particles
+    # 32 at a time) and particles past the 70-neighbour cap, beside a normal block
+    s = scenes.small_dam_break(n_side=8)
+    h = 4 * s["desc"]["ParticleRadius"]
+    rng = np.random.default_rng(n)
+    blob = (np.float32([0.6, 0.3, 0.3]) + side * h * rng.random((n, 3))).astype(np.float32)
+    x = np.concatenate([s["x"], blob]).astype(np.float32)
+    s = dict(s, x=x, v=np.zeros_like(x))
+    g = V.scene_simulation(s)
+    o = O.scene_oracle(s, 32, maps=[])
+    g.FindNeighbors()
+    o.find_neighbors()
+    a = g.GetNeighbors()
+    assert a["counts"].max() == 70 and a["counts"].min() < 70
+    assert_neighbors_equal(g, o)
+
+
 def test_search_bit_exact_after_steps():
     s = scenes.small_dam_break(n_side=14)
     g = V.scene_simulation(s)
