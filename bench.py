@@ -593,6 +593,11 @@ def main():
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": kms / cnt,
                 "share_of_step": kms / tot}
+        if traffic:
+            # the DRAM rate the measured traffic implies: ncu's bytes per launch (cold
+            # cache, scaled from the 512k capture) over this run's launch time
+            roof["traffic_gbs"] = traffic / (kms / cnt / 1e3) / 1e9
+            roof["traffic_frac"] = roof["traffic_gbs"] / peak
     # the whole step: algorithmic bytes of every launch over the summed kernel time
     step_bytes = sum(ALGO_BYTES.get(k, 0) * n * c for k, (c, _) in prof.items())
     step_achieved = step_bytes / (tot / 1e3) / 1e9
