@@ -154,17 +154,19 @@ __device__ float3 jgb_t(const Dev& d, const AdjDev& a, const Spline& sp, uint32_
 }
 
 // Adds the FP32 terms v of the block into dst (one atomic per block): each warp sums as
-// an FP32 pair (warp_sum_pair), the warps in FP64; every thread of the block must call it.
+// an FP32 pair (warp_sum_pair), the warps' pairs likewise, widened to FP64 once; every
+// thread of the block must call it.
 __device__ void block_add(double* dst, float term) {
-    __shared__ double part[32];
+    __shared__ float2 part[32];
     const float2 v = warp_sum_pair(term, 1);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __syncthreads();
-    if (lane == 0) part[warp] = pair_value(v);
+    if (lane == 0) part[warp] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (uint32_t w = 0; w < (blockDim.x + 31u) / 32u; w++) t += part[w];
+        float hi = 0.0f, lo = 0.0f;
+        for (uint32_t w = 0; w < (blockDim.x + 31u) / 32u; w++) pair_add(hi, lo, part[w].x, part[w].y);
+        const double t = pair_value(make_float2(hi, lo));
         if (t != 0.0) atomicAdd(dst, t);
     }
 }

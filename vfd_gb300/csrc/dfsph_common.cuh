@@ -324,10 +324,17 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
 // hold zeros), as an unevaluated pair hi + lo of FP32 numbers: each level adds the
 // partners' high parts with Knuth's error-free TwoSum and carries the rounding error
 // and the partners' low parts in lo, so the pair keeps ~44 significant bits (relative
-// error ~1e-13 for a warp's 32 terms), widened to FP64 by the lane that stores it
-// (pair_value): FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU,
-// and a DADD per lane and level cost more than the rest of a reduction kernel's
-// arithmetic.
+// error ~1e-13 for a warp's 32 terms). FP64 arithmetic runs at a small fraction of the
+// FP32 rate on this GPU (a dependent add takes ~64 cycles, and a warp instruction holds
+// the FP64 pipe whatever its active lanes), so a block combines its warps' pairs the
+// same way (pair_add) and widens the result to FP64 once (pair_value).
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
+    const float sum = __fadd_rn(hi, h2);
+    const float bb = __fsub_rn(sum, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(h2, bb));
+    lo = __fadd_rn(__fadd_rn(lo, l2), err);
+    hi = sum;
+}
 __device__ __forceinline__ float2 warp_sum_pair(float v, int step) {
     float hi = v, lo = 0.0f;
 #pragma unroll
@@ -335,22 +342,16 @@ __device__ __forceinline__ float2 warp_sum_pair(float v, int step) {
         if (o < step) break;
         const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
         const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
-        const float sum = __fadd_rn(hi, h2);
-        const float bb = __fsub_rn(sum, hi);
-        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(h2, bb));
-        lo = __fadd_rn(__fadd_rn(lo, l2), err);
-        hi = sum;
+        pair_add(hi, lo, h2, l2);
     }
     return make_float2(hi, lo);
 }
-// The FP64 value of a pair (taken by the one lane that stores it, so that no other lane
-// does FP64 work).
 __device__ __forceinline__ double pair_value(float2 p) { return (double)p.x + (double)p.y; }
 
 // Adds the FP32 terms `v` into scene `sid`'s FP64 accumulators `slot` (bucket
 // blockIdx % 32). A block whose particles lie in one scene sums each warp as an FP32
-// pair (warp_sum_pair), the warps in FP64 in shared memory, and issues one atomic per
-// accumulator; otherwise each valid thread adds its own value. Kernels running G lanes
+// pair (warp_sum_pair), the warps' pairs likewise in shared memory, and issues one FP64
+// atomic per accumulator; otherwise each valid thread adds its own value. Kernels running G lanes
 // per particle pass G (a block then covers blockDim.x / G particles; only the first
 // lane of each group contributes); all threads of the block must call this.
 // Core of scene_accumulate: `uniformScene` is the scene of every particle the block
@@ -358,7 +359,7 @@ __device__ __forceinline__ double pair_value(float2 p) { return (double)p.x + (d
 template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformScene, uint32_t sid, bool valid,
                                                       const float (&v)[K], const int (&slot)[K]) {
-    __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
+    __shared__ float2 sm[32][4];  // one row per warp of a block of up to 1024 threads
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bucket = blockIdx.x % kBuckets;
     if (uniformScene >= 0) {
@@ -368,13 +369,14 @@ __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformS
         __syncthreads();
         if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < K; k++) sm[warp][k] = pair_value(s[k]);
+            for (int k = 0; k < K; k++) sm[warp][k] = s[k];
         __syncthreads();
         if (threadIdx.x == 0) {
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                double t = 0.0;
-                for (uint32_t w = 0; w < blockDim.x / 32u; w++) t += sm[w][k];
+                float hi = 0.0f, lo = 0.0f;
+                for (uint32_t w = 0; w < blockDim.x / 32u; w++) pair_add(hi, lo, sm[w][k].x, sm[w][k].y);
+                const double t = pair_value(make_float2(hi, lo));
                 if (t != 0.0) atomicAdd(acc_bucket(d, (uint32_t)uniformScene, slot[k], bucket), t);
             }
         }
@@ -387,7 +389,7 @@ __device__ __forceinline__ void scene_accumulate_core(const Dev& d, int uniformS
 template <int K, uint32_t G = 1>
 __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, bool valid, const float (&v)[K],
                                                  const int (&slot)[K]) {
-    __shared__ double sm[32][4];  // one row per warp of a block of up to 1024 threads
+    __shared__ float2 sm[32][4];  // one row per warp of a block of up to 1024 threads
     __shared__ int uniformBlock;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t first = blockIdx.x * (blockDim.x / G);
@@ -401,14 +403,15 @@ __device__ __forceinline__ void scene_accumulate(const Dev& d, uint32_t sid, boo
         for (int k = 0; k < K; k++) s[k] = warp_sum_pair(valid ? v[k] : 0.0f, (int)G);
         if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < K; k++) sm[warp][k] = pair_value(s[k]);
+            for (int k = 0; k < K; k++) sm[warp][k] = s[k];
         __syncthreads();
         if (threadIdx.x == 0) {
             const uint32_t sc = scene_of(d, first);
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                double t = 0.0;
-                for (uint32_t w = 0; w < blockDim.x / 32u; w++) t += sm[w][k];
+                float hi = 0.0f, lo = 0.0f;
+                for (uint32_t w = 0; w < blockDim.x / 32u; w++) pair_add(hi, lo, sm[w][k].x, sm[w][k].y);
+                const double t = pair_value(make_float2(hi, lo));
                 if (t != 0.0) atomicAdd(acc_bucket(d, sc, slot[k], bucket), t);
             }
         }
