@@ -390,7 +390,8 @@ int vfd_profile_kernels(vfd_sim* sim, uint32_t steps, vfd_kernel_time* out, uint
 
 /*
  * Lanes per particle (4, 8 or 16) of the neighbour-loop kernels, in the order
- * density+factor, density change, pressure acceleration, Jacobi iteration,
+ * density+factor (with the density change when the divergence solve runs), pressure
+ * acceleration, Jacobi iteration,
  * divergence finish, surface classification, surface smoothing, viscosity
  * preconditioner, viscosity setup, CG matrix-vector product, density advection,
  * pressure finish (no counterpart in the reference, which launches every kernel

@@ -40,7 +40,7 @@ EXPORTS = [
     "vfd_sph_get_sort",
 ]
 
-TUNED_KERNELS = ["density_factor", "div_init", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
+TUNED_KERNELS = ["density_factor", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
                  "st_smooth", "visc_precond", "visc_setup", "cg_spmv", "pres_init", "pres_finish"]
 
 

@@ -576,8 +576,7 @@ int build_graph(vfd_sim* s, int parity, const void* rec, cudaGraph_t* gOut, cuda
         T(kTapeSearch, st);
         launch_boundary(d, st);
         T(kTapeBoundary, st);
-        launch_density(d, st);
-        launch_div_init(d, st);
+        launch_density_div_init(d, st);
         T(kTapeDivInit, st);
     });
     if (e == cudaSuccess && anyDiv) e = add_while(cap, g, h[0], leaves, [&](cudaStream_t st) {
@@ -642,8 +641,7 @@ int launch_eager(vfd_sim* s, const void* rec) {
     T(kTapeSearch);
     launch_boundary(d, st);
     T(kTapeBoundary);
-    launch_density(d, st);
-    launch_div_init(d, st);
+    launch_density_div_init(d, st);
     T(kTapeDivInit);
     if (s->anyDiv) {
         TRY(read_flag(s, 4, more));
@@ -1790,7 +1788,7 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     if (s->n == 0 || steps == 0) return VFD_OK;
-    static const char* names[kTunedCount] = {"k_density_factor", "k_div_init", "k_pressure_accel", "k_jacobi_iter",
+    static const char* names[kTunedCount] = {"k_density_factor", "k_pressure_accel", "k_jacobi_iter",
                                              "k_div_finish", "k_st_classify", "k_st_smooth", "k_visc_precond",
                                              "k_visc_setup", "k_cg_spmv", "k_pres_init", "k_pres_finish"};
     const uint8_t cand[3] = {4, 8, 16};

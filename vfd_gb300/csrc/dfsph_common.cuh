@@ -45,7 +45,7 @@ constexpr uint32_t kHasBoundaryVisc = 1u << 9;
 
 // Neighbour-loop kernels whose lanes per particle (4, 8 or 16) the autotuner picks.
 enum TunedKernel {
-    kTDensity = 0, kTDivInit, kTPAccel, kTJacobi, kTDivFinish, kTStClassify, kTStSmooth, kTViscPrecond,
+    kTDensity = 0, kTPAccel, kTJacobi, kTDivFinish, kTStClassify, kTStSmooth, kTViscPrecond,
     kTViscSetup, kTSpmv, kTPresInit, kTPresFinish, kTunedCount
 };
 

@@ -202,7 +202,11 @@ __device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, floa
 
 // ---------------------------------------------------------------------------
 // K2 + K3: ComputeDensityKernel (:152-187) and ComputeDFSPHFactorKernel (:189-231).
-template <uint32_t G, bool REL>
+// With DIV, also K4 (ComputeDensityChangeKernel, :483-529) for the scenes that run the
+// divergence solve: it walks the same pairs and needs only the particle's own factor
+// and boundary gradient and each pair's gradW, so it rides along (the terms and order of
+// velocity_divergence, which K17 uses).
+template <uint32_t G, bool REL, bool DIV = false>
 __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
@@ -210,24 +214,29 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     const float4 xi4 = d.X[p];
     const float3 xi = f3(xi4);
     const Nbr nb = neighbors(d, p);
-    float wsum = 0.0f, g2 = 0.0f;
+    float wsum = 0.0f, g2 = 0.0f, sdiv = 0.0f;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     const float V = S.volume;
+    const bool div = DIV && S.enableDiv;
+    const float3 vi = div ? f3(d.V[p]) : make_float3(0.f, 0.f, 0.f);
     uint2* ngRow = d.NG + (size_t)p * kRow;
     for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t j, bool ok) {
         const float3 r = pair_r<REL>(d, xi4, d.X[q]);
         float w, gs;
         kernel_wg(d, r, w, gs);
+        const float3 vq = div ? f3(d.V[q]) : make_float3(0.f, 0.f, 0.f);
         if (!ok) return;
         __stcs(ngRow + j, make_uint2(q, __float_as_uint(gs)));
         wsum += w;
         const float3 gj = (-V * gs) * r;
         g2 += dot3(gj, gj);
         gi -= gj;
+        if (div) sdiv += dot3(vi - vq, gs * r);
     });
     wsum = grp.sum(wsum);
     g2 = grp.sum(g2);
     gi = grp.sum(gi);
+    if (DIV) sdiv = grp.sum(sdiv);
     if (grp.lane != 0) return;
     float rhoB = 0.0f;
     float3 gb = make_float3(0.f, 0.f, 0.f);
@@ -246,8 +255,21 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     gi += gb;
     d.RHO[p] = (V * d.wZero + V * wsum + rhoB) * S.rho0;
     g2 += dot3(gi, gi);
-    d.ALPHA[p] = g2 > kEps ? 1.0f / g2 : 0.0f;
+    const float alpha = g2 > kEps ? 1.0f / g2 : 0.0f;
     d.GB[p] = f4(gb, 0.0f);
+    if (!div) {
+        d.ALPHA[p] = alpha;
+        return;
+    }
+    // K4 (:498-528)
+    float rhoAdv = sdiv * V;
+    if (nb.flags & kHasBoundary) rhoAdv += dot3(vi, gb);
+    rhoAdv = nb.count < 20u ? 0.0f : fmaxf(rhoAdv, 0.0f);
+    d.RHOADV[p] = rhoAdv;
+    const float alphaDt = alpha * S.dtInv;
+    d.ALPHA[p] = alphaDt;
+    d.KAPPAV[p] = rhoAdv * alphaDt;
+    set_kappa(d, p, rhoAdv * alphaDt);
 }
 
 // Sum_j (vi - vj) . gradW_ij * V + vi . GB  (K4 :498-522, K17 :253-271); valid on lane 0.
@@ -264,24 +286,6 @@ __device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G
     s = grp.sum(s) * S.volume;
     if (nb.flags & kHasBoundary) s += dot3(vi, f3(d.GB[p]));
     return s;
-}
-
-// K4: ComputeDensityChangeKernel (:483-529).
-template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_div_init(Dev d) {
-    VFD_COUNT_LAUNCH(d);
-    GROUP_PROLOGUE(G)
-    const SceneDev& S = d.scenes[scene_of(d, p)];
-    if (!S.enableDiv) return;
-    const Nbr nb = neighbors(d, p);
-    float rhoAdv = velocity_divergence<G, REL>(d, grp, p, S, nb, d.X[p], f3(d.V[p]));
-    if (grp.lane != 0) return;
-    rhoAdv = nb.count < 20u ? 0.0f : fmaxf(rhoAdv, 0.0f);
-    d.RHOADV[p] = rhoAdv;
-    const float alpha = d.ALPHA[p] * S.dtInv;
-    d.ALPHA[p] = alpha;
-    d.KAPPAV[p] = rhoAdv * alpha;
-    set_kappa(d, p, rhoAdv * alpha);
 }
 
 // Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481);
@@ -1197,8 +1201,8 @@ __global__ void k_ctrl_end(Dev d) {
     } while (0)
 #define K_DENSITY(G) k_density_factor<G, false>
 #define K_DENSITY_R(G) k_density_factor<G, true>
-#define K_DIV_INIT(G) k_div_init<G, false>
-#define K_DIV_INIT_R(G) k_div_init<G, true>
+#define K_DENSITY_DIV(G) k_density_factor<G, false, true>
+#define K_DENSITY_DIV_R(G) k_density_factor<G, true, true>
 #define K_PACCEL_D(G) k_pressure_accel<true, G, false>
 #define K_PACCEL_D_R(G) k_pressure_accel<true, G, true>
 #define K_PACCEL_P(G) k_pressure_accel<false, G, false>
@@ -1225,8 +1229,9 @@ __global__ void k_ctrl_end(Dev d) {
 #define K_PRES_FINISH_R(G) k_pres_finish<G, true>
 
 void launch_density(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY); }
-void launch_div_init(const Dev& d, cudaStream_t s) {
-    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_div_init", kTDivInit, K_DIV_INIT);
+// K2 + K3 + K4 in one pass, then the divergence loop's start.
+void launch_density_div_init(const Dev& d, cudaStream_t s) {
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY_DIV);
     VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d));
 }
 #define K_PACCEL_DB(G) k_pressure_accel_b<true, G, false>

@@ -19,7 +19,7 @@ void launch_search(const Dev& d, cudaStream_t s);
 uint32_t scan_block_count(uint32_t cellCap);
 void launch_boundary(const Dev& d, cudaStream_t s);
 void launch_density(const Dev& d, cudaStream_t s);
-void launch_div_init(const Dev& d, cudaStream_t s);
+void launch_density_div_init(const Dev& d, cudaStream_t s);
 void launch_div_iter(const Dev& d, cudaStream_t s);
 void launch_div_finish(const Dev& d, cudaStream_t s);
 void launch_surface_tension(const Dev& d, uint32_t maxPasses, cudaStream_t s);
