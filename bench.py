@@ -50,7 +50,7 @@ ALGO_BYTES = {
     "k_cg_p": 12 * 2 + 12,                  # p, z -> p
     "k_pressure_accel": 12 + 4 + 12,        # x, kappa -> a_p
     "k_jacobi_iter": 12 + 12 + 4 + 4 + 4 + 4,  # x, a_p, rho_adv, alpha, kappa -> kappa, res
-    "k_density_factor": 12 + 4 + 4,         # x -> rho, alpha
+    "k_density_factor": 12 + 12 + 4 * 4,    # x, v -> rho, alpha, rho_adv, kappa_v (K2-K4: divergence solve on)
     "k_neighbors": 12 + 4,                  # x -> count (list excluded)
     "k_visc_precond": 12 + 4 + 12 + 12 + 36 + 12 + 12,
     "k_visc_setup": 12 + 4 + 12 + 12 + 12,
@@ -58,7 +58,6 @@ ALGO_BYTES = {
     "k_boundary": 12 + 16,
     "k_pres_finish": 12 + 4 + 12 + 12 + 12,
     "k_pres_init": 12 + 12 + 4 + 4 + 4 + 4 + 4,
-    "k_div_init": 12 + 12 + 4 + 4 + 4 + 4,
     "k_div_finish": 12 + 4 + 12 + 4 + 12 + 12,
     "k_rank_gather": 4 + 4 + 12 + 12 + 12 + 4 + 4 + 4 + 4 + 12 + 12 + 12 + 4 + 4,
     "k_minmax": 12,
