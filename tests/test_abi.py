@@ -107,3 +107,17 @@ def test_no_device_is_reported(built_library):
     with pytest.raises(vfd_gb300.VFDError) as e:
         vfd_gb300.DFSPHSimulation()
     assert e.value.code == _abi.VFD_E_NODEVICE
+
+
+def test_tuned_kernel_lists_agree():
+    # vfd_set_lanes / vfd_autotune index lanes by the device's TunedKernel enum; the Python
+    # names, the autotuner's kernel names and the header's documented order must follow it
+    src = os.path.join(ROOT, "vfd_gb300", "csrc")
+    enum = re.search(r"enum TunedKernel \{(.*?)\};", open(os.path.join(src, "dfsph_common.cuh")).read(), re.S).group(1)
+    members = [m.strip().split("=")[0].strip() for m in enum.split(",") if m.strip()]
+    assert members[-1] == "kTunedCount"
+    assert len(members) - 1 == len(vfd_gb300.TUNED_KERNELS)
+    api = open(os.path.join(src, "dfsph_api.cu")).read()
+    names = re.search(r"names\[kTunedCount\] = \{(.*?)\};", api, re.S).group(1)
+    names = re.findall(r'"(k_\w+)"', names)
+    assert names == ["k_" + k for k in vfd_gb300.TUNED_KERNELS]
