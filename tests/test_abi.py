@@ -92,6 +92,10 @@ def test_argument_errors_are_status_codes(built_library):
     L = vfd_gb300.lib()
     assert L.vfd_create(None, None) == _abi.VFD_E_ARG
     assert L.vfd_step(None, None) == _abi.VFD_E_ARG
+    req, act = C.c_int32(7), C.c_int32(7)
+    assert L.vfd_get_graph_mode(None, C.byref(req), C.byref(act)) == _abi.VFD_E_ARG
+    assert (req.value, act.value) == (7, 7)
+    assert L.vfd_set_lanes(None, None, 0) == _abi.VFD_E_ARG
     assert L.vfd_destroy(None) == 0
     bad = _abi.make_desc(ParticleRadius=-1.0)
     h = C.c_void_p()
