@@ -110,8 +110,8 @@ __device__ __forceinline__ void set_kappa(const Dev& d, uint32_t p, float k) {
     if (!d.cellRel) reinterpret_cast<float*>(d.X)[4 * (size_t)p + 3] = k;
 }
 
-// Row entries per lane and round of a G-lane neighbour loop.
-constexpr uint32_t unroll_for(uint32_t G) { return G == 4u ? 4u : (G == 8u ? 4u : 4u); }
+// Row entries per lane and round of a neighbour loop (other depths measured slower).
+constexpr uint32_t kUnroll = 4u;
 
 // Neighbour loop of one group. In a round the group covers U*G consecutive row
 // entries and lane l takes entries l, l + G, ..., l + (U-1)G, so at each step the
@@ -125,7 +125,7 @@ constexpr uint32_t unroll_for(uint32_t G) { return G == 4u ? 4u : (G == 8u ? 4u 
 // fields.
 template <uint32_t G, bool WITH_GS, class F>
 __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb, uint32_t self, F&& f) {
-    constexpr uint32_t U = unroll_for(G);
+    constexpr uint32_t U = kUnroll;
     static_assert(U * G <= kRow, "first round must stay inside the row");
     uint32_t q[U];
     float g[U];
