@@ -412,8 +412,9 @@ void launch_search(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_slots", s, k_slots<<<nb, kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_rank_gather", s, k_rank_gather<<<nb, kBlock, 0, s>>>(d));
     // a warp per cell, a fixed grid striding over the cells the device counted
-    if (d.cellRel) VFD_LAUNCH("k_neighbors", s, k_neighbors<true><<<d.batchBlocks, kBlock, 0, s>>>(d));
-    else VFD_LAUNCH("k_neighbors", s, k_neighbors<false><<<d.batchBlocks, kBlock, 0, s>>>(d));
+    const uint32_t nbrBlocks = 4u * d.batchBlocks;
+    if (d.cellRel) VFD_LAUNCH("k_neighbors", s, k_neighbors<true><<<nbrBlocks, kBlock, 0, s>>>(d));
+    else VFD_LAUNCH("k_neighbors", s, k_neighbors<false><<<nbrBlocks, kBlock, 0, s>>>(d));
 }
 
 uint32_t scan_block_count(uint32_t cellCap) { return (cellCap + kScanItems - 1) / kScanItems; }
