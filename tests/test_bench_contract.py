@@ -1,0 +1,52 @@
+"""bench.py's static parts, without a GPU: every kernel its roofline table names is a
+kernel the library launches (by the name the per-kernel profiler reports), the default
+run is the configuration's 500 steps with at least 3 warm-up steps, and the profiles'
+per-particle traffic covers kernels of that table."""
+import ast
+import json
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _bench_tree():
+    return ast.parse(open(os.path.join(ROOT, "bench.py")).read())
+
+
+def _algo_bytes_keys():
+    for node in ast.walk(_bench_tree()):
+        if isinstance(node, ast.Assign) and any(getattr(t, "id", "") == "ALGO_BYTES" for t in node.targets):
+            return [k.value for k in node.value.keys]
+    raise AssertionError("ALGO_BYTES not found")
+
+
+def _launched_names():
+    names = set()
+    src = os.path.join(ROOT, "vfd_gb300", "csrc")
+    for f in os.listdir(src):
+        if f.endswith((".cu", ".cuh")):
+            text = open(os.path.join(src, f)).read()
+            names.update(re.findall(r'VFD_LAUNCH(?:_MODE)?\((?:[A-Z_]+,\s*)?"(k_\w+)"', text))
+    return names
+
+
+def test_roofline_table_names_launched_kernels():
+    launched = _launched_names()
+    assert "k_cg_spmv" in launched and "k_neighbors" in launched
+    stale = sorted(set(_algo_bytes_keys()) - launched)
+    assert not stale, stale
+
+
+def test_default_run_is_the_configuration():
+    src = open(os.path.join(ROOT, "bench.py")).read()
+    steps = int(re.search(r'"--steps", type=int, default=(\d+)', src).group(1))
+    warm = int(re.search(r'"--warmup", type=int, default=(\d+)', src).group(1))
+    assert steps == 500 and warm >= 3
+
+
+def test_traffic_figures_cover_table_kernels():
+    traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+    keys = set(_algo_bytes_keys())
+    for k, v in traffic.items():
+        assert k in keys and v["bytes_per_particle"] > 0, k

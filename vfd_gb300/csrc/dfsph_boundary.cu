@@ -84,8 +84,8 @@ __global__ void __launch_bounds__(kBlock) k_boundary(Dev d) {
 // (one instantiation per position storage mode, so that the absolute one compiles to the
 // same arithmetic as before the cell-relative mode existed)
 void launch_boundary(const Dev& d, cudaStream_t s) {
-    if (d.cellRel) k_boundary<true><<<blocks_for(d.n), kBlock, 0, s>>>(d);
-    else k_boundary<false><<<blocks_for(d.n), kBlock, 0, s>>>(d);
+    if (d.cellRel) VFD_LAUNCH("k_boundary", s, k_boundary<true><<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    else VFD_LAUNCH("k_boundary", s, k_boundary<false><<<blocks_for(d.n), kBlock, 0, s>>>(d));
 }
 
 }  // namespace vfd
