@@ -35,3 +35,16 @@ def test_recording_and_adjoint_graphs_build():
     x, v, _ = sim.GetState()
     sim.AdjointBackward(np.ones_like(x) * 1e-3, np.zeros_like(v))
     assert sim.GetGraphMode() == (True, True)
+
+
+def test_kernel_profile_covers_the_step():
+    # vfd_profile_kernels times every kernel of the step with CUDA events: the once-per-step
+    # kernels appear once per step, the solver loops once per iteration
+    s = scenes.small_dam_break(n_side=12)
+    sim = V.scene_simulation(s)
+    sim.Steps(2)
+    prof = sim.ProfileKernels(3)
+    for k in ("k_neighbors", "k_boundary", "k_density_factor", "k_pres_init", "k_ctrl_end"):
+        assert k in prof and prof[k][0] == 3 and prof[k][1] > 0.0, (k, prof.get(k))
+    assert prof["k_jacobi_iter"][0] == prof["k_pressure_accel"][0] >= 3
+    assert sim.GetGraphMode() == (True, True)  # profiling runs eagerly but leaves graphs on
