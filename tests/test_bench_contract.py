@@ -50,3 +50,17 @@ def test_traffic_figures_cover_table_kernels():
     keys = set(_algo_bytes_keys())
     for k, v in traffic.items():
         assert k in keys and v["bytes_per_particle"] > 0, k
+
+
+def test_every_step_kernel_counts_its_launch():
+    # gpu_launches is counted on the device: every kernel of the step increments the
+    # launch counter (VFD_COUNT_LAUNCH) as its first statement
+    src = os.path.join(ROOT, "vfd_gb300", "csrc")
+    missing = []
+    for f in ("dfsph_physics.cu", "dfsph_search.cu", "dfsph_boundary.cu"):
+        text = open(os.path.join(src, f)).read()
+        for m in re.finditer(r"__global__ void (?:__launch_bounds__\(\w+\) )?(k_\w+)\(Dev d\) \{", text):
+            body = text[m.end():m.end() + 200]
+            if "VFD_COUNT_LAUNCH(d)" not in body.split(";")[0] + ";":
+                missing.append(m.group(1))
+    assert not missing, missing
