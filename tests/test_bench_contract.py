@@ -64,3 +64,13 @@ def test_every_step_kernel_counts_its_launch():
             if "VFD_COUNT_LAUNCH(d)" not in body.split(";")[0] + ";":
                 missing.append(m.group(1))
     assert not missing, missing
+
+
+def test_device_code_has_no_trap_or_assert():
+    # failures are reported through status words; no kernel traps or asserts on the device
+    src = os.path.join(ROOT, "vfd_gb300", "csrc")
+    for f in os.listdir(src):
+        if f.endswith((".cu", ".cuh")):
+            text = open(os.path.join(src, f)).read()
+            assert "__trap" not in text, f
+            assert not re.search(r"(?<!static_)\bassert\s*\(", text), f
