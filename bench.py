@@ -154,7 +154,7 @@ def c2_config(n_side: int) -> dict:
             "dynamic_viscosity_pa_s": 50.0, "cg_relative_tolerance": 1e-4, "surface_tension": 0.05,
             "pressure_error_bound": "0.1% of rho0 (MaxPressureSolverError=10)", "min_solver_iterations": 2,
             "boundary": "volume map (GPU-built, 40x30x20 cells)", "parallelism": "replicas",
-            "l2": "inputs larger than L2 (state ~0.5 GB for 1M particles)"}
+            "l2": "inputs larger than L2 (device state ~1.3 GB for 1M particles, L2 129 MB)"}
 
 
 def batched_form(V, scenes, steps: int, warmup: int, plain_every: int, ws: int = 1, rank: int = 0):
