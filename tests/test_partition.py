@@ -25,6 +25,18 @@ def test_largest_scenes_go_to_different_ranks():
     assert {0, 1} != set(parts[0]) and {0, 1} != set(parts[1])
 
 
+def test_edge_cases():
+    # more ranks than scenes: some ranks get none; no scenes: every rank gets none
+    parts = partition.assign([5, 3], 4)
+    assert sorted(i for p in parts for i in p) == [0, 1] and sum(1 for p in parts if not p) == 2
+    assert partition.assign([], 3) == [[], [], []]
+    assert partition.imbalance([], [[], []]) == 1.0
+    # equal costs split evenly, ties broken by index
+    assert partition.assign([1] * 6, 3) == [[0, 3], [1, 4], [2, 5]]
+    with pytest.raises(ValueError):
+        partition.assign([1, 2], 0)
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
