@@ -1,8 +1,9 @@
 """Benchmark of the DFSPH step: particle-steps/s on the 1M-particle viscous dam break.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+python bench.py --profile-case N_SIDE [--lanes L]   (a short run for ncu to capture)
 
-Workload (BASELINE config 2): 100^3 jittered lattice (r = 0.005, a 1 m block) in
+Workload (the 1M-particle high-viscosity dam break): 100^3 jittered lattice (r = 0.005, a 1 m block) in
 a 2 x 1.5 x 1 m box (volume-map boundary), dynamic viscosity 50 Pa s with the
 implicit CG solve (relative tolerance 1e-4), surface tension 0.05, CFL time
 steps, pressure solve to <= 0.1 % mean density error. Synthetic seeded data.
@@ -82,6 +83,26 @@ def dist_info():
     return ws, rank, local
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -146,7 +167,7 @@ class ClockSampler:
                 "samples": len(rows), "reasons": reasons}
 
 
-def c2_config(n_side: int) -> dict:
+def dam_break_config(n_side: int) -> dict:
     edge = n_side * 0.01
     return {"workload": f"viscous dam break, {n_side ** 3} particles ({n_side}^3 lattice, r=0.005)",
             "particles": n_side ** 3, "box_m": [round(2 * edge + 0.02, 4), round(1.5 * edge + 0.02, 4),
@@ -223,7 +244,7 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
     Loss = mean |x_T - y|^2, y a jittered copy of the drop moved by (0.05, -0.2, 0);
     its gradient is checked against central differences (relative step 1e-3) in the
     viscosity and along one random initial-velocity direction."""
-    s = scenes.viscous_drop_c4()
+    s = scenes.viscous_drop_33k()
     n = len(s["x"])
     rng = np.random.default_rng(scenes.config_seed(4))
     target = s["x"].astype(np.float64) + np.array([0.05, -0.2, 0.0]) + 0.25 * s["desc"]["ParticleRadius"] * \
@@ -329,7 +350,7 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
 
 
 def jet_form(V, scenes, steps: int = 8, warmup: int = 2):
-    """Config 5: the viscous jet onto an 8M-particle pool, the inflow emitter adding a disk
+    """The jet-coiling scene: the viscous jet onto an 8M-particle pool, the inflow emitter adding a disk
     layer each time the flow has covered one spacing, run with FP32 absolute and with
     cell-relative positions. Reports particle-steps/s (host clock around synchronous
     steps, emission included), the mean density error of every step, the solver
@@ -342,7 +363,7 @@ def jet_form(V, scenes, steps: int = 8, warmup: int = 2):
     out = {}
     peak, _ = measured_peaks()
     for mode in ("absolute", "cell_relative"):
-        s = scenes.jet_coiling_c5()
+        s = scenes.jet_coiling_8m()
         r = s["desc"]["ParticleRadius"]
         sigma = 0.07 * (r / 0.025) ** 3
         s["desc"]["SurfaceTension"] = sigma
@@ -432,7 +453,7 @@ def precision_form(V, scenes, n_side: int = 40, steps: int = 20):
 
 
 def cpu_baseline(n_side: int, steps: int, warmup: int):
-    """The oracle (FP32, all host threads) on a c2-parameter sample."""
+    """The oracle (FP32, all host threads) on a sample with the 1M dam break's parameters."""
     from oracle import oracle as O
     from vfd_gb300 import scenes
     threads = os.cpu_count() or 1
@@ -459,13 +480,53 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(c2_config(100), sample=f"{n} particles ({n_side}^3) with the same parameters"),
+        "config": dict(dam_break_config(100), sample=f"{n} particles ({n_side}^3) with the same parameters"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"c2 parameters at {n} particles, {args.steps} steps after {args.warmup}"},
+                         "sample": f"1M dam-break parameters at {n} particles, {args.steps} steps after {args.warmup}",
+                         "cpu_model": cpu_model(), "nproc": os.cpu_count()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement of the reference's DFSPH step (no CPU DFSPH exists in the reference)",
     }
     print(json.dumps(line), flush=True)
+
+
+def summary(line: dict) -> dict:
+    """The forms' headline figures in a few keys at the end of the line, so that a
+    reader of a truncated log still sees them."""
+    f = line.get("forms", {})
+    adj = f.get("fwd_adjoint", {})
+    gc = adj.get("grad_check", {})
+    out = {"value": line.get("value"), "e2e": (line.get("e2e") or {}).get("value"),
+           "mean_density_error_pct": line.get("mean_density_error_pct"),
+           "roofline_frac": (line.get("roofline") or {}).get("frac"),
+           "roofline_kernel": (line.get("roofline") or {}).get("kernel"),
+           "step_roofline_frac": (line.get("step_roofline") or {}).get("frac"),
+           "batched_over_plain": f.get("batched", {}).get("batched_over_plain"),
+           "adjoint_over_forward": adj.get("adjoint_over_forward"),
+           "grad_rel_err_mu": gc.get("rel_err_mu"), "grad_rel_err_v0": gc.get("rel_err_v0"),
+           "cpu_baseline": (line.get("cpu_baseline") or {}).get("value")}
+    return {k: (round(v, 6) if isinstance(v, float) else v) for k, v in out.items()}
+
+
+def profile_case(args):
+    """The viscous dam break at args.profile_case^3 particles (the 1M configuration's
+    parameters), --graph-steps graph steps (lanes per particle from --lanes, else
+    autotuned), then --eager-steps steps with every kernel launched from the host."""
+    import vfd_gb300 as V
+    from vfd_gb300 import scenes
+    V.lib().vfd_set_device(0)
+    s = scenes.viscous_dam_break(n_side=args.profile_case)
+    sim = V.scene_simulation(s)
+    sim.Steps(2)
+    if args.lanes:
+        vals = [int(x) for x in args.lanes.split(",")]
+        sim.SetLanes(vals * len(V.TUNED_KERNELS) if len(vals) == 1 else vals)
+    else:
+        log("lanes", sim.Autotune(1))
+    sim.Steps(args.graph_steps)
+    sim.SetGraphMode(False)
+    st = sim.Steps(args.eager_steps)
+    log("particles", len(s["x"]), "stats", st)
 
 
 def main():
@@ -481,15 +542,23 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=150)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched-scene measurement")
-    ap.add_argument("--no-jet", action="store_true", help="skip the 8M-particle jet (config 5) form")
+    ap.add_argument("--no-jet", action="store_true", help="skip the 8M-particle jet-coiling form")
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--eager", action="store_true",
                     help="launch the timed steps kernel by kernel instead of as CUDA graphs (same kernels, same "
                          "results); profilers cannot see the kernels inside graphs with conditional nodes")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="N_SIDE",
+                    help="profiling run instead of the benchmark: the viscous dam break at N_SIDE^3 particles, "
+                         "--graph-steps steps as CUDA graphs, then --eager-steps steps with every kernel launched "
+                         "from the host (what a profiler filtering by kernel name captures)")
+    ap.add_argument("--graph-steps", type=int, default=4)
+    ap.add_argument("--eager-steps", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return profile_case(args)
 
     import torch
     import torch.distributed as dist
@@ -608,7 +677,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (f64 reductions)", "data": "synthetic (seeded jittered lattice)",
-        "config": dict(c2_config(args.n_side), launch="eager" if args.eager else "cuda graph per step"),
+        "config": dict(dam_break_config(args.n_side), launch="eager" if args.eager else "cuda graph per step"),
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
         "roofline": roof, "step_roofline": step_roof, "kernel_shares": shares, "lanes_per_particle": lanes,
         "solver": {k: st[k] for k in ("DivergenceSolverIterationCount", "PressureSolverIterationCount",
@@ -622,13 +691,15 @@ def main():
             line["forms"]["fwd_adjoint"] = adjoint_form(V, scenes)
             line["forms"]["precision"] = precision_form(V, scenes)
             if not args.no_jet:
-                line["forms"]["jet_c5"] = jet_form(V, scenes)
+                line["forms"]["jet_8m"] = jet_form(V, scenes)
             line["forms"]["legacy_sph"] = legacy_sph_form()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"oracle FP32 on c2 parameters at {nc} particles (40^3), "
-                                          f"{args.cpu_steps} steps after 2 ({el:.1f} s)"}
+                                "sample": f"oracle FP32 on the 1M dam-break parameters at {nc} particles (40^3), "
+                                          f"{args.cpu_steps} steps after 2 ({el:.1f} s)",
+                                "cpu_model": cpu_model(), "nproc": os.cpu_count()}
+    line["summary"] = summary(line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

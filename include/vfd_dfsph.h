@@ -48,6 +48,7 @@ enum {
 #define VFD_FLAG_NAN             0x10u /* non-finite position or velocity                */
 #define VFD_FLAG_GRID_CAPACITY   0x20u /* search grid larger than the cell table         */
 #define VFD_FLAG_ANCHOR_RANGE    0x40u /* cell-relative positions left their anchor range */
+#define VFD_FLAG_BOUNDS          0x80u /* bounds-checked build only: a device index check failed */
 
 /* Position storage modes (vfd_set_position_mode). */
 #define VFD_POSITIONS_ABSOLUTE       0  /* FP32 absolute coordinates, as the reference stores them */
@@ -319,8 +320,26 @@ int vfd_simulate(vfd_sim* sim, vfd_frame_callback cb, void* user);
  */
 int vfd_get_state(vfd_sim* sim, float* x, float* v, float* a);
 
-/* Overwrites positions and velocities (original order; vel may be NULL) of the running state. */
+/* Overwrites positions and velocities (original order; vel may be NULL) of the running state;
+ * VFD_E_NAN for non-finite input. */
 int vfd_set_state(vfd_sim* sim, const float* x, const float* v);
+
+/*
+ * Checkpoint and resume of the carried state. The reference keeps no checkpoints
+ * (its only state between steps is the DFSPHParticle array and DFSPHSimulationInfo:
+ * x, v, the viscosity warm start Delta v (DFSPHKernels.cu:755,861), the temporal
+ * curvature delta kappa (:1034) and dt, DFSPHImplementation.cu:395-428). vfd_checkpoint
+ * writes those, the last accelerations and each scene's solver clock (dt, frame time
+ * and index, iteration count, surface-tension sample count) into `buffer` as an opaque
+ * image of vfd_checkpoint_size bytes. vfd_restore makes a simulation with the same
+ * scenes, particle counts, position mode and kernel mode continue from such an image:
+ * its next steps repeat the checkpointed run's bit for bit. The description's
+ * constants stay those of the restoring simulation. VFD_E_STATE when the image does
+ * not match the simulation, VFD_E_CAPACITY when the buffer is too small.
+ */
+int vfd_checkpoint_size(vfd_sim* sim, uint64_t* bytes);
+int vfd_checkpoint(vfd_sim* sim, void* buffer, uint64_t bytes);
+int vfd_restore(vfd_sim* sim, const void* buffer, uint64_t bytes);
 
 /* One per-particle field (VFD_FIELD_*) of the last step, original order. */
 int vfd_get_field(vfd_sim* sim, int32_t field, uint32_t body, float* out);
@@ -426,9 +445,10 @@ int vfd_get_launch_count(vfd_sim* sim, uint64_t* launches, int32_t reset);
  * index). Intermediate data lives in a fixed ~10 MB __device__ array that every GPU
  * loading the library keeps until exit; limits: n <= 16384 and a search grid of at most
  * 262144 cells, else VFD_E_CAPACITY. The first call on a device looks the array up
- * (cudaGetSymbolAddress) and should come before any stream capture. All calls share the
- * array: calls that overlap on the GPU race and must be serialised by the caller. Runs on
- * `stream` (a cudaStream_t, NULL = default) and waits for it. Errors: return code only.
+ * (cudaGetSymbolAddress, once per CUDA context) and should come before any stream
+ * capture. All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. Runs on `stream` (a cudaStream_t, NULL = default) and waits
+ * for it before returning the status. Errors: return code only.
  */
 int vfd_find_neighbors_noalloc(const float* xyz, uint32_t n, float particle_radius, uint32_t* counts,
                                uint32_t* neighbors, uint32_t* sort_indices, void* stream);

@@ -1634,6 +1634,21 @@ struct Sim {
         for (auto& b : bvol) b.resize(n, 0);
     }
 
+    // The state one step carries to the next (DFSPHParticle x, v, VelocityDifference,
+    // DeltaFinalCurvature; DFSPHSimulationInfo dt and the surface-tension sample count
+    // derived from it), taken from another run: the next step() then starts where that
+    // run stands. Arrays in original order; dv and dk may be null (zero).
+    void set_carried(const float* x, const float* v, const float* dv, const float* dk, double dt) {
+        for (uint32_t i = 0; i < info.n; i++) {
+            p[i].x = V3<T>((T)x[3 * i], (T)x[3 * i + 1], (T)x[3 * i + 2]);
+            p[i].v = V3<T>((T)v[3 * i], (T)v[3 * i + 1], (T)v[3 * i + 2]);
+            p[i].dv = dv ? V3<T>((T)dv[3 * i], (T)dv[3 * i + 1], (T)dv[3 * i + 2]) : V3<T>();
+            p[i].dCurv = dk ? (T)dk[i] : T(0);
+        }
+        set_dt((T)(float)dt);
+        update_samples();
+    }
+
     void reset() {  // Simulate preamble, :33-51
         p = init;
         if (info.n != (uint32_t)init.size()) resize_state((uint32_t)init.size());
@@ -1779,6 +1794,13 @@ int orc_set_kernel_mode(void* p, int mode) {
     Handle* h = static_cast<Handle*>(p);
     if (h->f) h->f->kernel.analytic = mode != 0;
     if (h->d) h->d->kernel.analytic = mode != 0;
+    return VFD_OK;
+}
+
+int orc_set_carried(void* p, const float* x, const float* v, const float* dv, const float* dk, double dt) {
+    Handle* h = static_cast<Handle*>(p);
+    if (!x || !v) return VFD_E_ARG;
+    ORC_DISPATCH(h, set_carried(x, v, dv, dk, dt));
     return VFD_OK;
 }
 

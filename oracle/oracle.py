@@ -52,6 +52,7 @@ def lib():
             L.orc_set_kernel_mode.argtypes = [P, C.c_int]
             L.orc_emit.argtypes = [P, f32p, f32p, C.c_uint32]
             L.orc_step.argtypes = [P, C.POINTER(_abi.vfd_step_stats)]
+            L.orc_set_carried.argtypes = [P, f32p, f32p, f32p, f32p, C.c_double]
             L.orc_find_neighbors.argtypes = [P]
             L.orc_get_neighbors.argtypes = [P, u32p, u32p, u32p, C.c_uint32, u32p, u32p, u32p]
             L.orc_get_state.argtypes = [P, f64p, f64p, f64p]
@@ -304,6 +305,17 @@ class OracleSim:
     def set_kernel_mode(self, analytic: bool):
         """The spline at |r| (analytic) or the reference's tables."""
         lib().orc_set_kernel_mode(self.h, int(bool(analytic)))
+
+    def set_carried(self, x, v, dv=None, dk=None, dt: float = 0.0):
+        """Makes the next step start from another run's carried state: positions,
+        velocities, viscosity warm start dv, temporal curvature dk and time step dt."""
+        xa, xp = _f32(x)
+        va, vp = _f32(v)
+        dva, dvp = _f32(dv) if dv is not None else (None, None)
+        dka, dkp = _f32(np.asarray(dk).reshape(-1)) if dk is not None else (None, None)
+        rc = lib().orc_set_carried(self.h, xp, vp, dvp, dkp, float(dt))
+        if rc != 0:
+            raise ValueError(f"orc_set_carried -> {rc}")
 
     def step(self) -> dict:
         st = _abi.vfd_step_stats()

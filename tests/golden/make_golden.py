@@ -15,8 +15,8 @@ fixture that the oracle and the CUDA library are checked against:
     and the archive names of the DFSPH description, rigid-body and fluid-object
     serializers (Scene/Components/*.h), as the scene loader reads them.
 
-Usage: python tests/golden/make_golden.py [VFD_ROOT]
-(default VFD_ROOT: /root/reference). Run only where the reference is present.
+Usage: python tests/golden/make_golden.py VFD_ROOT
+(the root of a VFD checkout). Run only where the reference is present.
 """
 from __future__ import annotations
 
@@ -121,7 +121,9 @@ def scene_format(root: str) -> dict:
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py VFD_ROOT")
+    root = sys.argv[1]
     data = dict(source="VFD (Goubermouche/VFD) source text", halton=halton(root), gauss_legendre=gauss_legendre(root),
                 constants=constants(root), description_defaults=defaults(root), scene_format=scene_format(root))
     out = os.path.join(HERE, "reference_tables.json")

@@ -27,7 +27,7 @@ def _launched_names():
     for f in os.listdir(src):
         if f.endswith((".cu", ".cuh")):
             text = open(os.path.join(src, f)).read()
-            names.update(re.findall(r'VFD_LAUNCH(?:_MODE)?\((?:[A-Z_]+,\s*)?"(k_\w+)"', text))
+            names.update(re.findall(r'(?:VFD|SEARCH)_LAUNCH(?:_MODE)?\((?:[A-Z_]+,\s*)?"(k_\w+)"', text))
     return names
 
 

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("div,visc", [(1, 1), (0, 1), (1, 0), (0, 0)])
 def test_step_graph_builds_for_every_solver_set(div, visc):
-    s = scenes.viscous_drop_c4(r=0.006)
+    s = scenes.viscous_drop_33k(r=0.006)
     over = dict(EnableDivergenceSolverError=div, EnableViscositySolver=visc)
     g = V.scene_simulation(s, desc_overrides=over)
     g.Steps(3)
@@ -29,7 +29,7 @@ def test_step_graph_builds_for_every_solver_set(div, visc):
 def test_recording_and_adjoint_graphs_build():
     # the adjoint's recording steps and its CG solve are graphs too (divergence solve off,
     # as in the smooth variant that the gradient checks use)
-    s = scenes.viscous_drop_c4(r=0.006)
+    s = scenes.viscous_drop_33k(r=0.006)
     sim = V.scene_simulation(s, desc_overrides=dict(EnableDivergenceSolverError=0))
     sim.AdjointForward(6, 3)
     x, v, _ = sim.GetState()

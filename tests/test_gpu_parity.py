@@ -48,7 +48,7 @@ def assert_neighbors_equal(g, o):
 
 @pytest.mark.parametrize("factory", [
     lambda: scenes.small_dam_break(n_side=12),
-    lambda: scenes.dam_break_c1(),
+    lambda: scenes.dam_break_8k(),
     lambda: scenes.viscous_dam_break(n_side=40),
 ])
 def test_search_bit_exact(factory):
@@ -145,7 +145,7 @@ def test_steps_track_fp32_oracle():
 
 
 def test_twenty_steps_track_fp64_oracle():
-    s = scenes.dam_break_c1(n_side=12, box_scale=(2, 1, 1))
+    s = scenes.dam_break_8k(n_side=12, box_scale=(2, 1, 1))
     g, o = pair(s, 64)
     h = 4 * s["desc"]["ParticleRadius"]
     for _ in range(20):

@@ -1,4 +1,4 @@
-"""Config 5's surface tension on the CPU oracle (the reference's model, restated): at
+"""The jet-coiling scene's surface tension on the CPU oracle (the reference's model, restated): at
 sigma = 0.07 and r = 1.5 mm the free surface of a resting pool is driven to tens of m/s
 within a few steps and the CFL step falls to its minimum; sigma * (r / 25 mm)^3 keeps it
 at rest. The jet form of the benchmark therefore runs the scaled coefficient."""
@@ -9,7 +9,7 @@ from vfd_gb300 import scenes
 
 
 def _run(sigma, steps=4):
-    s = scenes.jet_coiling_c5(pool=(24, 6, 24))
+    s = scenes.jet_coiling_8m(pool=(24, 6, 24))
     s["desc"]["SurfaceTension"] = sigma
     o = O.scene_oracle(s, 32)
     for _ in range(steps):

@@ -134,7 +134,7 @@ def test_neighbor_sets_match_brute_force(n_side):
 
 def test_sort_permutation_rules():
     """Cell keys ascend along the sort; equal keys keep ascending particle index."""
-    s = scenes.dam_break_c1()
+    s = scenes.dam_break_8k()
     sim = O.OracleSim(_abi.make_desc(**s["desc"]), 32)
     sim.set_fluid(s["x"], s["v"])
     sim.find_neighbors()
@@ -173,7 +173,7 @@ def test_fp32_mirror_tracks_fp64_oracle():
 def test_dam_break_stays_bounded():
     """Physics sanity of the restatement: particles stay in the box, density error
     at pressure-solve exit within the 0.1 % bound, no solver hits its cap."""
-    s = scenes.dam_break_c1(n_side=10, box_scale=(2, 1, 1))
+    s = scenes.dam_break_8k(n_side=10, box_scale=(2, 1, 1))
     sim = O.scene_oracle(s, 64)
     for _ in range(30):
         st = sim.step()

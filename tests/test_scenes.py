@@ -15,7 +15,7 @@ def _spacing_ok(x, r, jitter_frac):
 
 
 def test_config1_dam_break():
-    s = scenes.dam_break_c1()
+    s = scenes.dam_break_8k()
     assert len(s["x"]) == 8000 and s["desc"]["ParticleRadius"] == 0.025
     assert s["desc"].get("EnableViscositySolver", 0) == 0 and s["desc"].get("EnableSurfaceTensionSolver", 0) == 0
     _spacing_ok(s["x"], 0.025, 0.05)
@@ -43,10 +43,10 @@ def test_config3_uneven_batch():
 
 
 def test_config4_viscous_drop():
-    s = scenes.viscous_drop_c4()
+    s = scenes.viscous_drop_33k()
     x, v = s["x"].astype(np.float64), s["v"].astype(np.float64)
     assert 30000 < len(x) < 36000 and s["desc"]["Viscosity"] * 1000.0 == 10.0
     c = x.mean(axis=0)
     assert np.linalg.norm(x - c, axis=1).max() <= 0.1 + 0.01  # a sphere of radius 0.1 m
     assert abs(np.linalg.norm(v, axis=1).max() - 0.5) < 1e-6  # Fourier modes scaled to 0.5 m/s
-    assert np.array_equal(scenes.viscous_drop_c4()["v"], s["v"])
+    assert np.array_equal(scenes.viscous_drop_33k()["v"], s["v"])

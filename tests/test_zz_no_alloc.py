@@ -50,7 +50,7 @@ def check_equal(x, r):
 
 
 def test_noalloc_search_matches_regular_search_twice():
-    a = scenes.dam_break_c1()                      # 8000 particles, r = 0.025
+    a = scenes.dam_break_8k()                      # 8000 particles, r = 0.025
     b = scenes.small_dam_break(n_side=14, seed=3)  # 2744 particles, other positions
     check_equal(a["x"], a["desc"]["ParticleRadius"])
     check_equal(b["x"], b["desc"]["ParticleRadius"])
@@ -60,3 +60,18 @@ def test_noalloc_search_rejects_too_many_particles():
     x = scenes.lattice_block((26, 26, 26), 0.01, (0, 0, 0), 0.05, scenes.SplitMix64(1))  # 17576 > 16384
     rc, _, _, _ = noalloc_search(x, 0.01)
     assert rc == _abi.VFD_E_CAPACITY
+
+
+def test_noalloc_search_device_side_rejections_leave_it_usable():
+    """Rejections found on the device come back as status codes, and a call after
+    them (the abort flags and buckets live in the shared array) is still exact."""
+    r = 0.01
+    far = np.float32([[0.0, 0.0, 0.0], [1000.0, 0.0, 0.0]])  # a grid of ~1.6M cells > 262144
+    rc, _, _, _ = noalloc_search(far, r)
+    assert rc == _abi.VFD_E_CAPACITY
+    x = scenes.lattice_block((6, 6, 6), r, (0, 0, 0), 0.05, scenes.SplitMix64(2))
+    bad = x.copy()
+    bad[17, 2] = np.nan
+    rc, _, _, _ = noalloc_search(bad, r)
+    assert rc == _abi.VFD_E_NAN
+    check_equal(x, r)

@@ -18,7 +18,9 @@ from . import _abi
 from ._abi import make_desc, vfd_desc, vfd_info, vfd_step_stats, vfd_volume_map  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libvfd_dfsph.so")
+# VFD_LIBRARY selects another build of the library (the bounds-checked variant,
+# libvfd_dfsph_checked.so); the default is the in-tree release build.
+LIB_PATH = os.environ.get("VFD_LIBRARY") or os.path.join(HERE, "libvfd_dfsph.so")
 
 # Every entry point declared in include/vfd_dfsph.h.
 EXPORTS = [
@@ -33,7 +35,7 @@ EXPORTS = [
     "vfd_get_stream", "vfd_get_launch_count", "vfd_set_lanes", "vfd_get_lanes", "vfd_autotune",
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
-    "vfd_emit", "vfd_get_graph_mode",
+    "vfd_emit", "vfd_get_graph_mode", "vfd_checkpoint_size", "vfd_checkpoint", "vfd_restore",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -124,6 +126,9 @@ def lib() -> C.CDLL:
                 "vfd_set_kernel_mode": [P, C.c_int32],
                 "vfd_emit": [P, f32p, f32p, C.c_uint32],
                 "vfd_get_graph_mode": [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+                "vfd_checkpoint_size": [P, C.POINTER(C.c_uint64)],
+                "vfd_checkpoint": [P, C.c_void_p, C.c_uint64],
+                "vfd_restore": [P, C.c_void_p, C.c_uint64],
                 "vfd_build_mesh_map": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_int32, C.c_float, u32p,
                                        C.c_float, f32p, u32p, u32p, C.POINTER(vfd_volume_map)],
                 "vfd_sample_mesh_volume": [f32p, C.c_uint32, u32p, C.c_uint32, f32p, C.c_float, u32p, C.c_int32,
@@ -460,6 +465,22 @@ class DFSPHSimulation:
             if len(va) != n:
                 raise ValueError(f"SetState: {len(va)} velocities for {n} particles")
         _check(lib().vfd_set_state(self._h, xp, vp), "vfd_set_state")
+
+    def Checkpoint(self) -> bytes:
+        """The carried state (positions, velocities, viscosity warm start, temporal
+        curvature, accelerations, original indices) and the solver clock (dt, frame
+        time, iteration) as an opaque image for Restore."""
+        size = C.c_uint64(0)
+        _check(lib().vfd_checkpoint_size(self._h, C.byref(size)), "vfd_checkpoint_size")
+        buf = C.create_string_buffer(size.value)
+        _check(lib().vfd_checkpoint(self._h, buf, size.value), "vfd_checkpoint")
+        return buf.raw
+
+    def Restore(self, image: bytes):
+        """Continues from a Checkpoint image of a simulation with the same scenes,
+        particle counts and modes; the next steps repeat the checkpointed run's."""
+        buf = C.create_string_buffer(bytes(image), len(image))
+        _check(lib().vfd_restore(self._h, buf, len(image)), "vfd_restore")
 
     def GetField(self, field: int, body: int = 0) -> np.ndarray:
         n = self._n(0)

@@ -43,6 +43,16 @@ FLAG_GRID_CAPACITY = 0x20
 
 MAX_NEIGHBORS = 70
 
+# Bits of vfd_step_stats.Flags.
+VFD_FLAG_PRESSURE_CAP = 0x1
+VFD_FLAG_DIVERGENCE_CAP = 0x2
+VFD_FLAG_VISCOSITY_CAP = 0x4
+VFD_FLAG_NEIGHBOR_CAP = 0x8
+VFD_FLAG_NAN = 0x10
+VFD_FLAG_GRID_CAPACITY = 0x20
+VFD_FLAG_ANCHOR_RANGE = 0x40
+VFD_FLAG_BOUNDS = 0x80
+
 FIELD_DENSITY = 0
 FIELD_FACTOR = 1
 FIELD_DENSITY_ADVECTION = 2

@@ -18,6 +18,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvfd_dfsph.so")
+# The bounds-checked variant (-DVFD_BOUNDS_CHECK): device index checks that record a
+# failure in the status word instead of faulting; a debugging build, never the default.
+BUILD_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(HERE, "libvfd_dfsph_checked.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -49,16 +53,19 @@ def _stale(target: str, inputs: list[str]) -> bool:
     return any(os.path.getmtime(p) > t for p in inputs)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
-    """Compile (if needed) and return the library path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None,
+          bounds_check: bool = False) -> str:
+    """Compile (if needed) and return the library path (the bounds-checked variant
+    with bounds_check=True)."""
+    build_dir, lib_path = (BUILD_CHECKED, LIB_CHECKED) if bounds_check else (BUILD, LIB)
+    os.makedirs(build_dir, exist_ok=True)
     cc = nvcc()
-    flags = ARCH + NVCC_FLAGS + (extra_flags or [])
+    flags = ARCH + NVCC_FLAGS + (extra_flags or []) + (["-DVFD_BOUNDS_CHECK"] if bounds_check else [])
     deps = _deps()
     jobs = []
     objs = []
     for src in sources():
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + deps):
             jobs.append([cc, *flags, "-c", src, "-o", obj])
@@ -74,12 +81,12 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
+    if force or jobs or _stale(lib_path, objs):
+        tmp = lib_path + ".tmp"
         run([cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, bounds_check="--bounds-check" in sys.argv))

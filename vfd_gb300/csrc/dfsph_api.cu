@@ -12,12 +12,15 @@
 #include <climits>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/vfd_dfsph.h"
 #include "dfsph_common.cuh"
@@ -628,6 +631,15 @@ int read_flag(vfd_sim* s, int idx, uint32_t& v) {
     return VFD_OK;
 }
 
+// NVTX range of one phase of the step on the host timeline (a profiler shows the phases
+// of eager steps; a graph step is one range around its launch).
+struct PhaseRange {
+    explicit PhaseRange(const char* name) { nvtxRangePushA(name); }
+    ~PhaseRange() { nvtxRangePop(); }
+    PhaseRange(const PhaseRange&) = delete;
+    PhaseRange& operator=(const PhaseRange&) = delete;
+};
+
 // The reference's host-driven control flow: one flag read per solver iteration.
 int launch_eager(vfd_sim* s, const void* rec) {
     const Dev& d = s->dev[s->cs];
@@ -636,14 +648,25 @@ int launch_eager(vfd_sim* s, const void* rec) {
         if (rec) tape_point(d, rec, point, st);
     };
     uint32_t more = 0;
+    PhaseRange step("vfd_step (eager)");
     T(kTapeBegin);
-    launch_search(d, st);
+    {
+        PhaseRange r("neighbour search");
+        launch_search(d, st);
+    }
     T(kTapeSearch);
-    launch_boundary(d, st);
+    {
+        PhaseRange r("boundary");
+        launch_boundary(d, st);
+    }
     T(kTapeBoundary);
-    launch_density_div_init(d, st);
+    {
+        PhaseRange r("density and factor");
+        launch_density_div_init(d, st);
+    }
     T(kTapeDivInit);
     if (s->anyDiv) {
+        PhaseRange r("divergence solve");
         TRY(read_flag(s, 4, more));
         for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
             launch_div_iter(d, st);
@@ -653,8 +676,12 @@ int launch_eager(vfd_sim* s, const void* rec) {
     }
     launch_div_finish(d, st);
     T(kTapeDivFinish);
-    if (s->anyST) launch_surface_tension(d, s->maxStPasses, st);
+    if (s->anyST) {
+        PhaseRange r("surface tension");
+        launch_surface_tension(d, s->maxStPasses, st);
+    }
     if (s->anyVisc) {
+        PhaseRange r("viscosity solve");
         launch_visc_init(d, st);
         TRY(read_flag(s, 5, more));
         for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
@@ -663,17 +690,26 @@ int launch_eager(vfd_sim* s, const void* rec) {
         }
     }
     T(kTapeVisc);
-    launch_visc_finish_dt(d, st);
-    T(kTapeVelocity);
-    launch_pres_init(d, st);
-    T(kTapePresInit);
-    TRY(read_flag(s, 6, more));
-    for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
-        launch_pres_iter(d, st);
-        T(kTapePresIter);
-        TRY(read_flag(s, 6, more));
+    {
+        PhaseRange r("time step");
+        launch_visc_finish_dt(d, st);
     }
-    launch_pres_finish(d, st);
+    T(kTapeVelocity);
+    {
+        PhaseRange r("pressure solve");
+        launch_pres_init(d, st);
+        T(kTapePresInit);
+        TRY(read_flag(s, 6, more));
+        for (uint32_t guard = 0; more && guard < 1000000u; guard++) {
+            launch_pres_iter(d, st);
+            T(kTapePresIter);
+            TRY(read_flag(s, 6, more));
+        }
+    }
+    {
+        PhaseRange r("integration");
+        launch_pres_finish(d, st);
+    }
     T(kTapeEnd);
     CK(cudaGetLastError());
     return VFD_OK;
@@ -698,6 +734,7 @@ int launch_one(vfd_sim* s) {
             }
         }
         if (!s->graphFailed) {
+            PhaseRange r("vfd_step (graph)");
             CK(cudaGraphLaunch(s->exec[s->cs], s->stream));
             s->cs = 1 - s->cs;
             return VFD_OK;
@@ -788,6 +825,8 @@ int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
         CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
         if (!s->hStatus[1]) {
             if (stats) fill_stats(s->hScenes[0], stats);
+            if (flags & 0x80u)
+                return fail(VFD_E_STATE, "device bounds check failed (first index %u)", s->hStatus[9] - 1u);
             if (flags & 0x40u)
                 return fail(VFD_E_CAPACITY, "cell-relative positions: a particle moved more than 511 cells from "
                                             "its scene's centre");
@@ -1379,10 +1418,129 @@ int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
     TRY(check_sim(s));
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
+    const size_t cnt3 = 3 * (size_t)s->scenes[0].count();
+    for (size_t i = 0; i < cnt3; i++)
+        if ((x && !std::isfinite(x[i])) || (v && !std::isfinite(v[i])))
+            return fail(VFD_E_NAN, "non-finite input at element %zu", i);
     const Dev& d = s->dev[s->cs];
     if (x) TRY(gather_pos(s, 0, x, d.XN));
     if (v) TRY(gather_vec(s, 0, v, d.Vc));
     CK(cudaStreamSynchronize(s->stream));
+    return VFD_OK;
+}
+
+// ---------------------------------------------------------------- checkpoints
+// Image layout: header, then per scene its SceneDev (the solver clock, dt and frame
+// state; constants are taken from the restoring simulation), then per scene the raw
+// slot ranges of the carried state: XN, Vc, DVc, A (float4), DKc (float), PIDc (u32).
+namespace {
+constexpr uint32_t kCkptMagic = 0x4B444656u;  // "VFDK"
+constexpr uint32_t kCkptVersion = 1u;
+struct CkptHeader {
+    uint32_t magic, version, scenes, flags;  // flags: bit 0 cell-relative, bit 1 analytic kernel
+    uint32_t stride, pad[3];
+};
+constexpr size_t kCkptPerParticle = 4 * sizeof(float4) + sizeof(float) + sizeof(uint32_t);
+uint64_t checkpoint_bytes(const vfd_sim* s) {
+    uint64_t b = sizeof(CkptHeader) + (sizeof(uint32_t) + sizeof(SceneDev)) * (uint64_t)s->scenes.size();
+    for (const auto& sc : s->scenes) b += kCkptPerParticle * (uint64_t)sc.count();
+    return b;
+}
+}  // namespace
+
+int vfd_checkpoint_size(vfd_sim* s, uint64_t* bytes) {
+    TRY(check_sim(s));
+    if (!bytes) return fail(VFD_E_ARG, "null output");
+    TRY(ensure_ready(s));
+    *bytes = checkpoint_bytes(s);
+    return VFD_OK;
+}
+
+int vfd_checkpoint(vfd_sim* s, void* buffer, uint64_t bytes) {
+    TRY(check_sim(s));
+    if (!buffer) return fail(VFD_E_ARG, "null buffer");
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    if (bytes < checkpoint_bytes(s)) return fail(VFD_E_CAPACITY, "checkpoint buffer too small");
+    CK(cudaStreamSynchronize(s->stream));
+    unsigned char* out = static_cast<unsigned char*>(buffer);
+    CkptHeader h{kCkptMagic, kCkptVersion, (uint32_t)s->scenes.size(),
+                 (s->cellRel ? 1u : 0u) | (s->analyticKernel ? 2u : 0u), s->stride, {0u, 0u, 0u}};
+    std::memcpy(out, &h, sizeof(h));
+    out += sizeof(h);
+    std::vector<SceneDev> sc(s->hScenes.size());
+    CK(cudaMemcpy(sc.data(), s->dScenes, sizeof(SceneDev) * sc.size(), cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < s->scenes.size(); k++) {
+        const uint32_t cnt = s->scenes[k].count();
+        std::memcpy(out, &cnt, sizeof(cnt));
+        std::memcpy(out + sizeof(cnt), &sc[k], sizeof(SceneDev));
+        out += sizeof(cnt) + sizeof(SceneDev);
+    }
+    const Dev& d = s->dev[s->cs];
+    for (uint32_t k = 0; k < s->scenes.size(); k++) {
+        const size_t b = s->sceneBegin[k], cnt = s->scenes[k].count();
+        const void* src4[4] = {d.XN + b, d.Vc + b, d.DVc + b, d.A + b};
+        for (const void* p : src4) {
+            CK(cudaMemcpy(out, p, sizeof(float4) * cnt, cudaMemcpyDeviceToHost));
+            out += sizeof(float4) * cnt;
+        }
+        CK(cudaMemcpy(out, d.DKc + b, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+        out += sizeof(float) * cnt;
+        CK(cudaMemcpy(out, d.PIDc + b, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost));
+        out += sizeof(uint32_t) * cnt;
+    }
+    return VFD_OK;
+}
+
+int vfd_restore(vfd_sim* s, const void* buffer, uint64_t bytes) {
+    TRY(check_sim(s));
+    if (!buffer) return fail(VFD_E_ARG, "null buffer");
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    const unsigned char* in = static_cast<const unsigned char*>(buffer);
+    if (bytes < sizeof(CkptHeader)) return fail(VFD_E_ARG, "checkpoint image too short");
+    CkptHeader h;
+    std::memcpy(&h, in, sizeof(h));
+    in += sizeof(h);
+    if (h.magic != kCkptMagic || h.version != kCkptVersion) return fail(VFD_E_ARG, "not a checkpoint image");
+    if (h.scenes != s->scenes.size()) return fail(VFD_E_STATE, "checkpoint has %u scenes, simulation %zu",
+                                                  h.scenes, s->scenes.size());
+    const uint32_t modes = (s->cellRel ? 1u : 0u) | (s->analyticKernel ? 2u : 0u);
+    if (h.flags != modes) return fail(VFD_E_STATE, "checkpoint was taken in another position or kernel mode");
+    if (bytes < checkpoint_bytes(s)) return fail(VFD_E_ARG, "checkpoint image too short");
+    std::vector<SceneDev> cur(s->hScenes.size());
+    CK(cudaMemcpy(cur.data(), s->dScenes, sizeof(SceneDev) * cur.size(), cudaMemcpyDeviceToHost));
+    const size_t dyn = offsetof(SceneDev, dt);
+    for (uint32_t k = 0; k < h.scenes; k++) {
+        uint32_t cnt;
+        std::memcpy(&cnt, in, sizeof(cnt));
+        if (cnt != s->scenes[k].count())
+            return fail(VFD_E_STATE, "scene %u: checkpoint has %u particles, simulation %u", k, cnt,
+                        s->scenes[k].count());
+        SceneDev saved;
+        std::memcpy(&saved, in + sizeof(cnt), sizeof(SceneDev));
+        // the solver clock and state of the checkpoint, the constants of this simulation
+        std::memcpy(reinterpret_cast<unsigned char*>(&cur[k]) + dyn, reinterpret_cast<unsigned char*>(&saved) + dyn,
+                    sizeof(SceneDev) - dyn);
+        in += sizeof(cnt) + sizeof(SceneDev);
+    }
+    const Dev& d = s->dev[s->cs];
+    for (uint32_t k = 0; k < h.scenes; k++) {
+        const size_t b = s->sceneBegin[k], cnt = s->scenes[k].count();
+        void* dst4[4] = {d.XN + b, d.Vc + b, d.DVc + b, d.A + b};
+        for (void* p : dst4) {
+            CK(cudaMemcpy(p, in, sizeof(float4) * cnt, cudaMemcpyHostToDevice));
+            in += sizeof(float4) * cnt;
+        }
+        CK(cudaMemcpy(d.DKc + b, in, sizeof(float) * cnt, cudaMemcpyHostToDevice));
+        in += sizeof(float) * cnt;
+        CK(cudaMemcpy(d.PIDc + b, in, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice));
+        in += sizeof(uint32_t) * cnt;
+    }
+    CK(cudaMemcpy(s->dScenes, cur.data(), sizeof(SceneDev) * cur.size(), cudaMemcpyHostToDevice));
+    s->hScenes = cur;
+    s->generation++;  // a recorded adjoint run no longer matches the state
+    CK(cudaDeviceSynchronize());
     return VFD_OK;
 }
 

@@ -442,6 +442,25 @@ __device__ __forceinline__ void scene_max_float(const Dev& d, uint32_t sid, bool
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd((d).status + 8, 1u); \
     } while (0)
 
+// Bounds-checked build (-DVFD_BOUNDS_CHECK, vfd_gb300.build.build(bounds_check=True)):
+// device index checks that record a failure in the status word (VFD_FLAG_BOUNDS in
+// status[0]; status[9] keeps the first offending index + 1) and substitute index 0, so
+// the kernel neither faults nor traps and the host reports the failure after the step.
+// The default build compiles the checks out.
+__device__ __forceinline__ uint32_t checked_index(uint32_t* status, uint32_t idx, uint32_t limit) {
+#ifdef VFD_BOUNDS_CHECK
+    if (idx >= limit) {
+        atomicOr(status, 0x80u);
+        atomicCAS(status + 9, 0u, idx + 1u);
+        return 0u;
+    }
+#else
+    (void)status;
+    (void)limit;
+#endif
+    return idx;
+}
+
 // The abort flag is raised only by the search kernels; later kernels read it through
 // the read-only path (one L2 request per SM instead of one per thread).
 __device__ __forceinline__ bool is_aborted(const Dev& d) { return __ldg(d.status + 1) != 0u; }

@@ -15,7 +15,12 @@
 // other host threads) race on the array and must be serialised by the caller.
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current; make that first call before any
-// stream capture. No cudaMalloc, cudaFree or allocating library call is made.
+// stream capture. The address is remembered per CUDA context (by the context's unique
+// id), so a device reset or a second context on the same device gets its own look-up
+// instead of a stale address. Each call waits for its stream before it returns the
+// status. No cudaMalloc, cudaFree or allocating library call is made, and the launches
+// bypass the per-kernel profiler (which would create CUDA events).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -26,7 +31,7 @@
 #include "dfsph_common.cuh"
 
 namespace vfd {
-void launch_search(const Dev& d, cudaStream_t s);
+void launch_search(const Dev& d, cudaStream_t s, bool profiled);
 uint32_t scan_block_count(uint32_t cellCap);
 }  // namespace vfd
 
@@ -64,8 +69,39 @@ struct Layout {
 // The scratch itself (about 10 MB).
 static __device__ __align__(256) unsigned char g_noallocScratch[Layout::TOTAL];
 
+// The array's device address per CUDA context, keyed by the context's unique id
+// (cuCtxGetId; ids are never reused within a process).
+struct AddrEntry {
+    unsigned long long ctx;
+    void* addr;
+};
 std::mutex g_noallocMutex;
-void* g_noallocAddr[64] = {};
+AddrEntry g_noallocAddr[64] = {};
+uint32_t g_noallocUsed = 0;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context (the runtime's primary context once the
+// device is in use), through the driver entry points the runtime hands out.
+int current_context_id(unsigned long long& id) {
+    static CtxGetCurrentFn getCurrent = nullptr;
+    static CtxGetIdFn getId = nullptr;
+    if (!getCurrent || !getId) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess)
+            return VFD_E_CUDA;
+        getCurrent = (CtxGetCurrentFn)f1;
+        getId = (CtxGetIdFn)f2;
+    }
+    CUcontext ctx = nullptr;
+    if (getCurrent(&ctx) != CUDA_SUCCESS || !ctx) return VFD_E_CUDA;
+    return getId(ctx, &id) == CUDA_SUCCESS ? VFD_OK : VFD_E_CUDA;
+}
 
 // Clears the per-call state: one scene, status words, reduction buckets.
 __global__ void k_noalloc_reset(Dev d, SceneDev scene) {
@@ -113,17 +149,23 @@ int vfd_find_neighbors_noalloc(const float* xyz, uint32_t n, float particle_radi
     if (n > kNoAllocMaxParticles)
         return na_fail(VFD_E_CAPACITY, "vfd_find_neighbors_noalloc handles at most 16384 particles per call");
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return na_fail(VFD_E_CUDA, "no current device");
+    if (cudaGetDevice(&dev) != cudaSuccess) return na_fail(VFD_E_CUDA, "no current device");
+    if (cudaSetDevice(dev) != cudaSuccess) return na_fail(VFD_E_CUDA, "no context");  // binds the primary context
+    unsigned long long ctx = 0;
+    if (current_context_id(ctx) != VFD_OK) return na_fail(VFD_E_CUDA, "no current context");
     void* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_noallocMutex);
-        if (!g_noallocAddr[dev]) {
+        for (uint32_t k = 0; k < g_noallocUsed; k++)
+            if (g_noallocAddr[k].ctx == ctx) base = g_noallocAddr[k].addr;
+        if (!base) {  // set-up, once per context, with this device current
             void* p = nullptr;
             const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
-            if (e != cudaSuccess) return na_fail(VFD_E_CUDA, cudaGetErrorString(e));
-            g_noallocAddr[dev] = p;
+            if (e != cudaSuccess || !p) return na_fail(VFD_E_CUDA, cudaGetErrorString(e));
+            const uint32_t slot = g_noallocUsed < 64u ? g_noallocUsed++ : (uint32_t)(ctx % 64u);
+            g_noallocAddr[slot] = AddrEntry{ctx, p};
+            base = p;
         }
-        base = g_noallocAddr[dev];
     }
     unsigned char* b = static_cast<unsigned char*>(base);
     Dev d;
@@ -176,7 +218,7 @@ int vfd_find_neighbors_noalloc(const float* xyz, uint32_t n, float particle_radi
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     k_noalloc_reset<<<1, 256, 0, s>>>(d, scene);
     k_noalloc_load<<<blocks_for(n, 256), 256, 0, s>>>(d, xyz);
-    launch_search(d, s);
+    launch_search(d, s, false);
     k_noalloc_export<<<blocks_for(n, 256), 256, 0, s>>>(d, counts, neighbors, sort_indices);
     cudaError_t e = cudaGetLastError();
     uint32_t status[2] = {0u, 0u};

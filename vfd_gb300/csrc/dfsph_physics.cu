@@ -97,11 +97,22 @@ struct Nbr {
     const uint32_t* row;
     const uint2* ng;
     uint32_t count, flags;
-    __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return __ldg(row + j); }
+#ifdef VFD_BOUNDS_CHECK
+    uint32_t n;
+    uint32_t* status;
+    __device__ __forceinline__ uint32_t check(uint32_t q) const { return checked_index(status, q, n); }
+#else
+    __device__ __forceinline__ uint32_t check(uint32_t q) const { return q; }
+#endif
+    __device__ __forceinline__ uint32_t operator[](uint32_t j) const { return check(__ldg(row + j)); }
 };
 __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
+#ifdef VFD_BOUNDS_CHECK
+    return Nbr{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w, d.n, d.status};
+#else
     return Nbr{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w};
+#endif
 }
 
 // kappa (or kappa_v) of particle p, mirrored into X[p].w for the neighbours' gathers.
@@ -159,7 +170,7 @@ __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb
         for (uint32_t u = 0; u < U; u++) {
             const uint32_t j = base + grp.lane + u * G;
             const bool ok = j < nb.count;
-            f(ok ? q[u] : self, g[u], j, ok);
+            f(ok ? nb.check(q[u]) : self, g[u], j, ok);
         }
     }
 }

@@ -8,8 +8,8 @@
 //     by original index (the reference's atomicAdd rank allows any order);
 //   * the carried state is gathered into cell order (coalesced float4 rows for
 //     every later kernel) instead of being read through an index;
-//   * neighbour lists are ELL columns (slot-major per rank), capped at 70 in the
-//     reference's z, y, x cell order; one pass, no count/scan/query split.
+//   * neighbour lists are rows of kRow slots per particle (row-major), capped at 70
+//     in the reference's z, y, x cell order; one pass, no count/scan/query split.
 #include "dfsph_common.cuh"
 
 namespace vfd {
@@ -375,8 +375,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                     const uint32_t e = __shfl_sync(0xffffffffu, excl, min(j + step, 26u));
                     if (j + step <= 26u && e <= i) j += step;
                 }
-                const uint32_t q = __shfl_sync(0xffffffffu, cs, j) + (i - __shfl_sync(0xffffffffu, excl, j));
                 const bool valid = i < ncand;
+                const uint32_t q = checked_index(d.status, __shfl_sync(0xffffffffu, cs, j) +
+                                                 (i - __shfl_sync(0xffffffffu, excl, j)), valid ? d.n : 0xFFFFFFFFu);
                 const float4 xq = valid ? d.X[q] : make_float4(0.f, 0.f, 0.f, 0.f);
                 for (uint32_t k = 0; k < kk; k++) {
                     const float3 e = pair_r<REL>(d, xq, sx[w][k]);
@@ -400,22 +401,30 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
 }
 
 // ---------------------------------------------------------------- launchers
-void launch_search(const Dev& d, cudaStream_t s) {
+// `profiled` = false launches without the per-kernel profiler hook (the allocation-free
+// search must not create CUDA events, whatever another thread is profiling).
+#define SEARCH_LAUNCH(name, ...)                 \
+    do {                                         \
+        if (profiled) VFD_LAUNCH(name, s, __VA_ARGS__); \
+        else { __VA_ARGS__; }                    \
+    } while (0)
+void launch_search(const Dev& d, cudaStream_t s, bool profiled) {
     const uint32_t nb = blocks_for(d.n);
-    VFD_LAUNCH("k_minmax", s, k_minmax<<<nb, kBlock, 0, s>>>(d));
-    VFD_LAUNCH("k_grid", s, k_grid<<<1, 256, 0, s>>>(d));
-    VFD_LAUNCH("k_clear_cells", s, k_clear_cells<<<1216, 256, 0, s>>>(d));
-    VFD_LAUNCH("k_keys", s, k_keys<<<nb, kBlock, 0, s>>>(d));
-    VFD_LAUNCH("k_scan_reduce", s, k_scan_reduce<<<d.scanBlocks, 256, 0, s>>>(d));
-    VFD_LAUNCH("k_scan_top", s, k_scan_top<<<1, 1024, 0, s>>>(d));
-    VFD_LAUNCH("k_scan_down", s, k_scan_down<<<d.scanBlocks, 256, 0, s>>>(d));
-    VFD_LAUNCH("k_slots", s, k_slots<<<nb, kBlock, 0, s>>>(d));
-    VFD_LAUNCH("k_rank_gather", s, k_rank_gather<<<nb, kBlock, 0, s>>>(d));
+    SEARCH_LAUNCH("k_minmax", k_minmax<<<nb, kBlock, 0, s>>>(d));
+    SEARCH_LAUNCH("k_grid", k_grid<<<1, 256, 0, s>>>(d));
+    SEARCH_LAUNCH("k_clear_cells", k_clear_cells<<<1216, 256, 0, s>>>(d));
+    SEARCH_LAUNCH("k_keys", k_keys<<<nb, kBlock, 0, s>>>(d));
+    SEARCH_LAUNCH("k_scan_reduce", k_scan_reduce<<<d.scanBlocks, 256, 0, s>>>(d));
+    SEARCH_LAUNCH("k_scan_top", k_scan_top<<<1, 1024, 0, s>>>(d));
+    SEARCH_LAUNCH("k_scan_down", k_scan_down<<<d.scanBlocks, 256, 0, s>>>(d));
+    SEARCH_LAUNCH("k_slots", k_slots<<<nb, kBlock, 0, s>>>(d));
+    SEARCH_LAUNCH("k_rank_gather", k_rank_gather<<<nb, kBlock, 0, s>>>(d));
     // a warp per cell, a fixed grid striding over the cells the device counted
     const uint32_t nbrBlocks = 4u * d.batchBlocks;
-    if (d.cellRel) VFD_LAUNCH("k_neighbors", s, k_neighbors<true><<<nbrBlocks, kBlock, 0, s>>>(d));
-    else VFD_LAUNCH("k_neighbors", s, k_neighbors<false><<<nbrBlocks, kBlock, 0, s>>>(d));
+    if (d.cellRel) SEARCH_LAUNCH("k_neighbors", k_neighbors<true><<<nbrBlocks, kBlock, 0, s>>>(d));
+    else SEARCH_LAUNCH("k_neighbors", k_neighbors<false><<<nbrBlocks, kBlock, 0, s>>>(d));
 }
+#undef SEARCH_LAUNCH
 
 uint32_t scan_block_count(uint32_t cellCap) { return (cellCap + kScanItems - 1) / kScanItems; }
 

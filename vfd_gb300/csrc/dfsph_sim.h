@@ -15,7 +15,7 @@
 #include "dfsph_common.cuh"
 
 namespace vfd {
-void launch_search(const Dev& d, cudaStream_t s);
+void launch_search(const Dev& d, cudaStream_t s, bool profiled = true);
 uint32_t scan_block_count(uint32_t cellCap);
 void launch_boundary(const Dev& d, cudaStream_t s);
 void launch_density(const Dev& d, cudaStream_t s);

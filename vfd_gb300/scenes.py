@@ -114,9 +114,9 @@ SOLVER = dict(MinPressureSolverIterations=2, MinDivergenceSolverIterations=2,
               MaxPressureSolverError=10.0, MaxDivergenceSolverError=10.0)
 
 
-def dam_break_c1(n_side: int = 20, box_scale=(1.0, 1.0, 1.0), seed: int | None = None,
+def dam_break_8k(n_side: int = 20, box_scale=(1.0, 1.0, 1.0), seed: int | None = None,
                  map_resolution=(20, 20, 20)) -> dict:
-    """Config 1: n_side^3 block (20^3), r = 0.025, jitter +-0.05 r, in the corner
+    """The 8,000-particle dam break: n_side^3 block (20^3), r = 0.025, jitter +-0.05 r, in the corner
     of a closed box. A 20^3 block at spacing 2r is 1 m wide, so the box edge is
     the block edge plus the wall gaps (1.1 m); box_scale = (2, 1, 1) is the
     dam-break variant c1b. No viscosity, no surface tension."""
@@ -134,7 +134,7 @@ def dam_break_c1(n_side: int = 20, box_scale=(1.0, 1.0, 1.0), seed: int | None =
 
 def viscous_dam_break(n_side: int = 100, r: float = 0.005, seed: int | None = None,
                       map_resolution=None) -> dict:
-    """Config 2: n_side^3 jittered lattice (100^3 = 1M at r = 0.005, a 1 m block)
+    """The 1M-particle high-viscosity dam break: n_side^3 jittered lattice (100^3 = 1M at r = 0.005, a 1 m block)
     in a box of 2 x 1.5 x 1 block edges; dynamic viscosity 50 Pa s
     (Viscosity = 0.05), boundary viscosity 0.05, CG tolerance 1e-4 relative
     (MaxViscositySolverError = 0.01), surface tension 0.05, CSD 10000."""
@@ -177,7 +177,7 @@ def block_dam_break(n_target: int, r: float, viscosity: float, rng: SplitMix64) 
 
 def uneven_batch(count: int = 256, r: float = 0.005, n_min: int = 2000, n_max: int = 64000,
                  seed: int | None = None) -> list[dict]:
-    """Config 3: `count` independent scenes, particle counts log-uniform in
+    """The uneven batch: `count` independent scenes, particle counts log-uniform in
     [n_min, n_max], even = dam break, odd = falling drop, dynamic viscosity
     log-uniform in [0.01, 100] Pa s (Viscosity = mu / 1000)."""
     rng = SplitMix64(config_seed(3) if seed is None else seed)
@@ -192,8 +192,8 @@ def uneven_batch(count: int = 256, r: float = 0.005, n_min: int = 2000, n_max: i
     return scenes
 
 
-def viscous_drop_c4(r: float = 0.0025, radius: float = 0.1, seed: int | None = None) -> dict:
-    """Config 4: sphere of radius 0.1 m at spacing 2r (r = 0.0025 gives ~33k
+def viscous_drop_33k(r: float = 0.0025, radius: float = 0.1, seed: int | None = None) -> dict:
+    """The differentiable viscous drop: sphere of radius 0.1 m at spacing 2r (r = 0.0025 gives ~33k
     particles), 0.3 m above a floor, velocity = 8 seeded Fourier modes scaled to
     max 0.5 m/s, dynamic viscosity 10 Pa s (Viscosity = 0.01)."""
     rng = SplitMix64(config_seed(4) if seed is None else seed)
@@ -216,9 +216,9 @@ def viscous_drop_c4(r: float = 0.0025, radius: float = 0.1, seed: int | None = N
     return dict(name=f"viscous_drop_{len(x)}", x=x, v=v.astype(np.float32), desc=desc, boxes=[floor])
 
 
-def jet_coiling_c5(pool=(400, 50, 400), r: float = 0.0015, seed: int | None = None,
+def jet_coiling_8m(pool=(400, 50, 400), r: float = 0.0015, seed: int | None = None,
                    map_resolution=(40, 24, 40)) -> dict:
-    """Config 5: a viscous jet (inflow disk of radius 0.02 m at 1 m/s, downwards, 0.5 m
+    """The 8M-particle jet-coiling scene: a viscous jet (inflow disk of radius 0.02 m at 1 m/s, downwards, 0.5 m
     above the floor) onto a resting pool. The inflow alone adds ~140 particles per layer
     (about 5e4 per second of flow), far from 8M, so a pool of pool[0] x pool[1] x pool[2]
     particles (400 x 50 x 400 = 8M at spacing 2r = 3 mm: 1.2 x 0.15 x 1.2 m) rests on
