@@ -582,7 +582,7 @@ def main():
         sim.SetLanes(vals)
         lanes = dict(zip(V.TUNED_KERNELS, vals))
     else:
-        lanes = sim.Autotune(2)  # per-kernel lanes per particle, state restored
+        lanes = sim.Autotune(2)  # per-kernel lanes per particle and tile sizes, state restored
     sim.SetGraphMode(not args.eager)
     sim.Steps(args.warmup)
     stream = torch.cuda.ExternalStream(sim.GetStream())
@@ -680,6 +680,7 @@ def main():
         "config": dict(dam_break_config(args.n_side), launch="eager" if args.eager else "cuda graph per step"),
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
         "roofline": roof, "step_roofline": step_roof, "kernel_shares": shares, "lanes_per_particle": lanes,
+        "tile_log2_cells": sim.GetTiles(),
         "solver": {k: st[k] for k in ("DivergenceSolverIterationCount", "PressureSolverIterationCount",
                                       "ViscositySolverIterationCount", "PressureSolverError", "TimeStepSize",
                                       "MaxNeighborCount", "Flags")},

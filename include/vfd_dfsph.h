@@ -420,9 +420,21 @@ int vfd_set_lanes(vfd_sim* sim, const uint8_t* lanes, uint32_t count);
 int vfd_get_lanes(const vfd_sim* sim, uint8_t* lanes, uint32_t count);
 
 /*
+ * Cell tiles of the solver-loop kernels (pressure acceleration, Jacobi update, CG
+ * matrix-vector product), in the order of vfd_set_lanes (the other entries are
+ * ignored): log2 of the cells per tile, 3 = a 2x2x2 block of cells, 4 = 4x2x2. A block
+ * stages the tile's halo of cells in shared memory and walks its particles' neighbours
+ * there. No counterpart in the reference, which reads every neighbour through an index
+ * from global memory (DFSPHKernels.cu:317-432, :758-842). vfd_autotune picks them with
+ * the lanes.
+ */
+int vfd_set_tiles(vfd_sim* sim, const uint8_t* tiles, uint32_t count);
+int vfd_get_tiles(const vfd_sim* sim, uint8_t* tiles, uint32_t count);
+
+/*
  * Autotuner: runs `steps` steps from a snapshot of the current state once per
- * lane count, times every neighbour-loop kernel with CUDA events, keeps the
- * fastest lane count per kernel and restores the state exactly (positions,
+ * lane count and tile size, times every neighbour-loop kernel with CUDA events, keeps the
+ * fastest lane count (and tile size, vfd_set_tiles) per kernel and restores the state exactly (positions,
  * velocities, accelerations and all carried solver state; the simulation does not
  * advance). Per-step diagnostics (vfd_get_field, vfd_get_neighbors) reflect the
  * last tuning step until the next step. lanes_out (may be NULL) receives the choice.

@@ -28,6 +28,7 @@ def _launched_names():
         if f.endswith((".cu", ".cuh")):
             text = open(os.path.join(src, f)).read()
             names.update(re.findall(r'(?:VFD|SEARCH)_LAUNCH(?:_MODE)?\((?:[A-Z_]+,\s*)?"(k_\w+)"', text))
+            names.update(re.findall(r'VFD_TILE_DISPATCH\("(k_\w+)"', text))
     return names
 
 

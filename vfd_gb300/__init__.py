@@ -36,6 +36,7 @@ EXPORTS = [
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
     "vfd_emit", "vfd_get_graph_mode", "vfd_checkpoint_size", "vfd_checkpoint", "vfd_restore",
+    "vfd_set_tiles", "vfd_get_tiles",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -44,6 +45,8 @@ EXPORTS = [
 
 TUNED_KERNELS = ["density_factor", "pressure_accel", "jacobi_iter", "div_finish", "st_classify",
                  "st_smooth", "visc_precond", "visc_setup", "cg_spmv", "pres_init", "pres_finish"]
+# the solver-loop passes that run on cell tiles (vfd_set_tiles)
+TILE_KERNELS = ["pressure_accel", "jacobi_iter", "cg_spmv"]
 
 
 class vfd_kernel_time(C.Structure):
@@ -116,6 +119,8 @@ def lib() -> C.CDLL:
                 "vfd_get_launch_count": [P, C.POINTER(C.c_uint64), C.c_int32],
                 "vfd_set_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_get_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
+                "vfd_set_tiles": [P, C.POINTER(C.c_uint8), C.c_uint32],
+                "vfd_get_tiles": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_autotune": [P, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_find_neighbors_noalloc": [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p],
@@ -535,6 +540,18 @@ class DFSPHSimulation:
         arr = (C.c_uint8 * 16)()
         _check(lib().vfd_get_lanes(self._h, arr, 16), "vfd_get_lanes")
         return list(arr)[:len(TUNED_KERNELS)]
+
+    def SetTiles(self, tiles):
+        """log2 of the cells per tile of the cell-tile kernels, in TUNED_KERNELS order
+        (3 = 2x2x2, 4 = 4x2x2; entries of other kernels are ignored)."""
+        arr = (C.c_uint8 * len(tiles))(*tiles)
+        _check(lib().vfd_set_tiles(self._h, arr, len(tiles)), "vfd_set_tiles")
+
+    def GetTiles(self) -> dict:
+        """Tile sizes (log2 of the cells) of the three cell-tile kernels."""
+        arr = (C.c_uint8 * 16)()
+        _check(lib().vfd_get_tiles(self._h, arr, 16), "vfd_get_tiles")
+        return {k: arr[i] for i, k in enumerate(TUNED_KERNELS) if k in TILE_KERNELS}
 
     def GetStream(self) -> int:
         p = C.c_void_p()

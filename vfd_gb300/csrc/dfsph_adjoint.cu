@@ -120,19 +120,15 @@ __device__ __forceinline__ float3 hmul(float gs, float gq, float3 r, float3 w) {
 
 struct Row {
     const uint32_t* nbr;
-    const uint2* ng;
     uint32_t count, flags;
 };
 __device__ __forceinline__ Row row_of(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
-    return Row{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w};
+    return Row{d.NBR + (size_t)p * kRow, w & kCountMask, w};
 }
-// Row entry j: neighbour slot and its gradW / r (the forward's table value), one load.
-__device__ __forceinline__ uint32_t row_entry(const Row& rw, uint32_t j, float& gs) {
-    const uint2 e = __ldg(rw.ng + j);
-    gs = __uint_as_float(e.y);
-    return e.x;
-}
+// Row entry j: the neighbour slot; its gradW / r (the forward's table value) is
+// grad_factor of the same pair vector, computed by the caller.
+__device__ __forceinline__ uint32_t row_entry(const Row& rw, uint32_t j) { return __ldg(rw.nbr + j); }
 
 __device__ __forceinline__ float4 bd(const AdjDev& a, const Dev& d, uint32_t k, uint32_t b, uint32_t p) {
     return a.BD[((size_t)k * d.maxBodies + b) * d.stride + p];
@@ -248,9 +244,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const flo
         }
         xi = f3(d.X[p]);
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            float gs;
-            const uint32_t q = row_entry(rw, j, gs);
+            const uint32_t q = row_entry(rw, j);
             const float3 r = xi - f3(d.X[q]);
+            const float gs = grad_factor(d, r);
             float kq, uq = 0.f;
             if (HAS_U) {
                 const float2 kuq = a.KU[q];
@@ -299,9 +295,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a, const flo
             aki = f3(ak4);
         }
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            float gsT;
-            const uint32_t q = row_entry(rw, j, gsT);
+            const uint32_t q = row_entry(rw, j);
             const float3 r = xi - f3(d.X[q]);
+            const float gsT = grad_factor(d, r);
             const float s = sqrtf(dot3(r, r));
             float gs, gq;
             sp.hess(s, gs, gq);
@@ -349,9 +345,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const flo
         wi = f3(w[p]);
         di = a.DBAR[p];
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            float gsT;
-            const uint32_t q = row_entry(rw, j, gsT);
+            const uint32_t q = row_entry(rw, j);
             const float3 r = xi - f3(d.X[q]);
+            const float gsT = grad_factor(d, r);
             const float s = sqrtf(dot3(r, r));
             float gs, gq;
             sp.hess(s, gs, gq);
@@ -395,9 +391,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_gsum(Dev d, AdjDev a) {
         rw = row_of(d, p);
         const float3 xi = f3(d.X[p]);
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            float gsT;
-            const uint32_t q = row_entry(rw, j, gsT);
-            const float3 gj = (V * gsT) * (xi - f3(d.X[q]));
+            const uint32_t q = row_entry(rw, j);
+            const float3 rq = xi - f3(d.X[q]);
+            const float gsT = grad_factor(d, rq);
+            const float3 gj = (V * gsT) * rq;
             g += gj;
             g2 += dot3(gj, gj);
         }
@@ -489,9 +486,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const floa
         li = f3(d.CG[p]);
         lti = (dt / rhoi) * li;
         for (uint32_t j = grp.lane; j < rw.count; j += kAG) {
-            float gsT;
-            const uint32_t q = row_entry(rw, j, gsT);
+            const uint32_t q = row_entry(rw, j);
             const float3 r = xi - f3(d.X[q]);
+            const float gsT = grad_factor(d, r);
             const float s2 = dot3(r, r);
             const float s = sqrtf(s2);
             float gs, gq;

@@ -313,7 +313,7 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.RES, st));
     TRY(dalloc(s, &base.XB, st * std::max<uint32_t>(1u, maxBodies)));
     TRY(dalloc(s, &base.NBR, st * kRow));
-    TRY(dalloc(s, &base.NG, st * kRow));
+    TRY(dalloc(s, &base.MASK, st * kMaskWords));
     TRY(dalloc(s, &base.NCNT, st));
     TRY(dalloc(s, &base.KEY, st));
     TRY(dalloc(s, &base.KEYS, st));
@@ -353,6 +353,8 @@ int allocate(vfd_sim* s) {
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
         base.batchBlocks = (uint32_t)std::max(1, sms) * (2048u / kBlock);
     }
+    std::memcpy(base.tiles, s->tiles, sizeof(base.tiles));
+    CK(prepare_tile_kernels());
     TRY(dalloc(s, &s->dWM, kTableRes));
     TRY(dalloc(s, &s->dGM, kTableRes));
     TRY(dalloc(s, &s->dHalton, kHaltonCount));
@@ -395,7 +397,7 @@ int allocate(vfd_sim* s) {
         CK(cudaMemcpy(s->dBodies, bodies.data(), sizeof(BodyDev) * bodies.size(), cudaMemcpyHostToDevice));
     CK(cudaMemset(base.NCNT, 0, sizeof(uint32_t) * st));
     CK(cudaMemset(base.NBR, 0, sizeof(uint32_t) * st * kRow));
-    CK(cudaMemset(base.NG, 0, sizeof(uint2) * st * kRow));
+    CK(cudaMemset(base.MASK, 0, sizeof(unsigned long long) * st * kMaskWords));
     CK(cudaMemset(base.A, 0, sizeof(float4) * st));
     CK(cudaMemset(base.AP, 0, sizeof(float4) * st));
     CK(cudaMemset(base.STN, 0, sizeof(float4) * st));
@@ -1507,6 +1509,15 @@ int vfd_restore(vfd_sim* s, const void* buffer, uint64_t bytes) {
                                                   h.scenes, s->scenes.size());
     const uint32_t modes = (s->cellRel ? 1u : 0u) | (s->analyticKernel ? 2u : 0u);
     if (h.flags != modes) return fail(VFD_E_STATE, "checkpoint was taken in another position or kernel mode");
+    if (bytes < sizeof(CkptHeader) + (sizeof(uint32_t) + sizeof(SceneDev)) * (uint64_t)h.scenes)
+        return fail(VFD_E_ARG, "checkpoint image too short");
+    for (uint32_t k = 0; k < h.scenes; k++) {  // particle counts first: a different scene is a state mismatch
+        uint32_t cnt;
+        std::memcpy(&cnt, in + k * (sizeof(uint32_t) + sizeof(SceneDev)), sizeof(cnt));
+        if (cnt != s->scenes[k].count())
+            return fail(VFD_E_STATE, "scene %u: checkpoint has %u particles, simulation %u", k, cnt,
+                        s->scenes[k].count());
+    }
     if (bytes < checkpoint_bytes(s)) return fail(VFD_E_ARG, "checkpoint image too short");
     std::vector<SceneDev> cur(s->hScenes.size());
     CK(cudaMemcpy(cur.data(), s->dScenes, sizeof(SceneDev) * cur.size(), cudaMemcpyDeviceToHost));
@@ -1941,6 +1952,24 @@ int vfd_get_lanes(const vfd_sim* s, uint8_t* lanes, uint32_t count) {
     return VFD_OK;
 }
 
+int vfd_set_tiles(vfd_sim* s, const uint8_t* tiles, uint32_t count) {
+    TRY(check_sim(s));
+    if (!tiles || count == 0 || count > kTunedCount) return fail(VFD_E_ARG, "tiles: 1..%d values", (int)kTunedCount);
+    for (uint32_t k = 0; k < count; k++)
+        if (tiles[k] != 3 && tiles[k] != 4) return fail(VFD_E_ARG, "tile size must be 3 (2x2x2) or 4 (4x2x2)");
+    std::memcpy(s->tiles, tiles, count);
+    for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+    s->releaseGraphs();
+    return VFD_OK;
+}
+
+int vfd_get_tiles(const vfd_sim* s, uint8_t* tiles, uint32_t count) {
+    TRY(check_sim(s));
+    if (!tiles) return fail(VFD_E_ARG, "null output");
+    std::memcpy(tiles, s->tiles, std::min<uint32_t>(count, 16));
+    return VFD_OK;
+}
+
 int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count) {
     TRY(check_sim(s));
     CK(cudaSetDevice(s->device));
@@ -1992,11 +2021,17 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
         release();
         return fail(VFD_E_CUDA, "autotune snapshot: %s", cudaGetErrorString(e));
     }
-    double times[kTunedCount][3] = {};
+    // every lane count with every tile size of the cell-tile kernels (the others ignore it)
+    const uint8_t tileCand[2] = {3, 4};
+    double times[kTunedCount][3][2] = {};
     int rc = VFD_OK;
-    for (int c = 0; c < 3 && rc == VFD_OK; c++) {
+    for (int ct = 0; ct < 6 && rc == VFD_OK; ct++) {
+        const int c = ct % 3, tl = ct / 3;
         for (int k = 0; k < 2; k++)
-            for (int t = 0; t < kTunedCount; t++) s->dev[k].lanes[t] = cand[c];
+            for (int t = 0; t < kTunedCount; t++) {
+                s->dev[k].lanes[t] = cand[c];
+                s->dev[k].tiles[t] = tileCand[tl];
+            }
         EventProfiler prof;
         g_profiler = &prof;
         for (uint32_t k = 0; k < steps && rc == VFD_OK; k++) {
@@ -2012,7 +2047,7 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
             float ms = 0.0f;
             if (rc == VFD_OK && cudaEventElapsedTime(&ms, rec.a, rec.b) == cudaSuccess)
                 for (int t = 0; t < kTunedCount; t++)
-                    if (rec.name == names[t]) times[t][c] += ms;
+                    if (rec.name == names[t]) times[t][c][tl] += ms;
         }
         s->cs = cs0;
         e = copy_all(false);
@@ -2020,16 +2055,33 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
     }
     release();
     if (rc != VFD_OK) {
-        for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+        for (int k = 0; k < 2; k++) {
+            std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+            std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+        }
         return rc;
     }
     for (int t = 0; t < kTunedCount; t++) {
-        int best = 1;
+        int best = 1, bestTile = 0;
+        double bt = times[t][1][0] + times[t][1][1];  // lanes alone: both tile runs summed
+        const bool tiled = t == kTPAccel || t == kTJacobi || t == kTSpmv;
+        if (tiled) bt = times[t][1][0];
         for (int c = 0; c < 3; c++)
-            if (times[t][c] > 0.0 && times[t][c] < times[t][best]) best = c;
+            for (int tl = 0; tl < (tiled ? 2 : 1); tl++) {
+                const double v = tiled ? times[t][c][tl] : times[t][c][0] + times[t][c][1];
+                if (v > 0.0 && v < bt) {
+                    bt = v;
+                    best = c;
+                    bestTile = tl;
+                }
+            }
         s->lanes[t] = cand[best];
+        s->tiles[t] = tileCand[bestTile];
     }
-    for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+    for (int k = 0; k < 2; k++) {
+        std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
+        std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+    }
     s->releaseGraphs();
     if (lanes_out) std::memcpy(lanes_out, s->lanes, std::min<uint32_t>(count, 16));
     return VFD_OK;

@@ -14,9 +14,10 @@
 //   NBR  u32 [slot][72] neighbour slots, one row per particle in the reference's
 //        z, y, x cell order (at most 70 used), read by groups of G lanes
 //   NCNT u32 [slot] neighbour count | flag bits
-//   NG   (u32, f32) [slot][72] the row again with gradW / r of each pair beside each
-//        index, written once per step by the density pass and streamed (one 8-byte load
-//        per pair) by every later neighbour loop instead of a table lookup
+//   MASK u64 [slot][10] the same neighbour set as bit masks over the particle's 27-cell
+//        candidate set: word w = 3 (dz + 1) + (dy + 1) covers the x-run of cells
+//        (x-1, x, x+1) at (y+dy, z+dz), bit b = the run's b-th candidate in cell order;
+//        read by the cell-tile kernels of the solver loops (word 9 unused, 16-B rows)
 //   X.w  mirrors kappa_v during the divergence solve and kappa during the pressure
 //        solve, so the pressure-acceleration gather brings it with the position
 // The reference keeps one 120-byte AoS DFSPHParticle per particle
@@ -42,6 +43,9 @@ constexpr float kEps = 1.0e-5f;              // Core/Math/Math.h:6
 constexpr uint32_t kCountMask = 0xFFu;
 constexpr uint32_t kHasBoundary = 1u << 8;   // some body gave this particle Vb > 0
 constexpr uint32_t kHasBoundaryVisc = 1u << 9;
+constexpr uint32_t kRowPath = 1u << 10;      // an x-run of the cell's candidates exceeds 64: no masks
+constexpr uint32_t kMaskWords = 10u;         // MASK row: 9 x-runs + 1 pad word (80 B, 16-B aligned)
+constexpr uint32_t kRunMax = 64u;            // candidates one mask word covers
 
 // Neighbour-loop kernels whose lanes per particle (4, 8 or 16) the autotuner picks.
 enum TunedKernel {
@@ -124,7 +128,7 @@ struct Dev {
     float *RHO, *ALPHA, *RHOADV, *KAPPA, *KAPPAV, *RES;
     float4* XB;
     uint32_t *NBR, *NCNT;
-    uint2* NG;                 // [slot][72] (neighbour slot, gradW factor bits) of each pair (row layout)
+    unsigned long long* MASK;  // [slot][kMaskWords] neighbour masks per x-run (null: not kept)
     // search scratch
     uint32_t *KEY, *KEYS, *TMP, *CELL_START, *CELL_COUNT, *FILL, *SCAN;
     // viscosity CG
@@ -154,6 +158,10 @@ struct Dev {
     // kernels of a batch walk this list with a fixed grid of batchBlocks blocks.
     uint32_t* WORK;
     uint32_t workStride, batchBlocks;
+    // Cell tiles of the solver-loop kernels (pressure acceleration, Jacobi update, CG
+    // product), per TunedKernel: 2^tiles[k] consecutive Morton cells (3: a 2x2x2 block,
+    // 4: 4x2x2).
+    uint8_t tiles[16];
 };
 
 // ---------------------------------------------------------------- float3 math
@@ -256,6 +264,38 @@ __device__ __forceinline__ float3 kernel_grad(const Dev& d, float3 r) {
     if (rl <= d.radius) return (d.analytic ? spline_gs(d, rl) : __ldg(d.GM + table_pos(d, rl))) * r;
     return make_float3(0.f, 0.f, 0.f);
 }
+
+// gradW factor of one pair: GetGradientW(r) = gs * r (Kernel/DFSPHKernels.h:67-80),
+// from the pair's squared distance r2.
+__device__ __forceinline__ float grad_factor_r2(const Dev& d, float r2) {
+    const float rl = fast_sqrt(r2);
+    if (!(rl <= d.radius)) return 0.0f;
+    return d.analytic ? spline_gs(d, rl) : __ldg(d.GM + table_pos(d, rl));
+}
+__device__ __forceinline__ float grad_factor(const Dev& d, float3 r) { return grad_factor_r2(d, dot3(r, r)); }
+
+// ------------------------------------------------------------ Morton cell keys
+__device__ __forceinline__ uint32_t part1by2(uint32_t x) {  // ParticleSearchKernels.cu:9-17
+    x &= 0x000003ffu;
+    x = (x ^ (x << 16)) & 0xff0000ffu;
+    x = (x ^ (x << 8)) & 0x0300f00fu;
+    x = (x ^ (x << 4)) & 0x030c30c3u;
+    x = (x ^ (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// ToCellIndexMortonMetaGrid, ParticleSearchKernels.cu:24-38: 8^3-cell meta blocks in
+// row-major order, Morton order (x lowest bit) inside each.
+__device__ __forceinline__ uint32_t cell_key(const SceneDev& s, int cx, int cy, int cz) {
+    const uint32_t mx = (uint32_t)cx >> 3, my = (uint32_t)cy >> 3, mz = (uint32_t)cz >> 3;
+    const uint32_t meta = mz * s.meta[1] * s.meta[0] + my * s.meta[0] + mx;
+    return meta * 512u + ((part1by2((uint32_t)cz & 7u) << 2) + (part1by2((uint32_t)cy & 7u) << 1) +
+                          part1by2((uint32_t)cx & 7u));
+}
+
+// Inverse of the Morton interleave inside a meta block: bits 0, 3, 6 of m -> bits 0, 1, 2
+// (x of m, y of m >> 1, z of m >> 2).
+__device__ __forceinline__ uint32_t compact3(uint32_t m) { return (m & 1u) | ((m >> 2) & 2u) | ((m >> 4) & 4u); }
 
 // Orthogonal vectors of a unit vector (Core/Math/Math.h:19-33).
 __device__ __forceinline__ void orthogonal_vectors(float3 vec, float3& x, float3& y) {
@@ -494,6 +534,18 @@ struct Group {
         return v;
     }
 };
+
+// Sum over the G lanes of a group (mask: the group's lanes of the warp).
+template <uint32_t G>
+__device__ __forceinline__ float group_sum(uint32_t mask, float v) {
+#pragma unroll
+    for (uint32_t o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    return v;
+}
+template <uint32_t G>
+__device__ __forceinline__ float3 group_sum(uint32_t mask, float3 v) {
+    return make_float3(group_sum<G>(mask, v.x), group_sum<G>(mask, v.y), group_sum<G>(mask, v.z));
+}
 
 // ------------------------------------------------------------ batch work lists
 __device__ __forceinline__ const uint32_t* work_list(const Dev& d, int loop) { return d.WORK + (size_t)loop * d.workStride; }

@@ -16,23 +16,6 @@ namespace vfd {
 
 constexpr uint32_t kScanItems = 1024u;  // cells per scan block (256 threads x 4)
 
-__device__ __forceinline__ uint32_t part1by2(uint32_t x) {  // ParticleSearchKernels.cu:9-17
-    x &= 0x000003ffu;
-    x = (x ^ (x << 16)) & 0xff0000ffu;
-    x = (x ^ (x << 8)) & 0x0300f00fu;
-    x = (x ^ (x << 4)) & 0x030c30c3u;
-    x = (x ^ (x << 2)) & 0x09249249u;
-    return x;
-}
-
-// ToCellIndexMortonMetaGrid, ParticleSearchKernels.cu:24-38.
-__device__ __forceinline__ uint32_t cell_key(const SceneDev& s, int cx, int cy, int cz) {
-    const uint32_t mx = (uint32_t)cx >> 3, my = (uint32_t)cy >> 3, mz = (uint32_t)cz >> 3;
-    const uint32_t meta = mz * s.meta[1] * s.meta[0] + my * s.meta[0] + mx;
-    return meta * 512u + ((part1by2((uint32_t)cz & 7u) << 2) + (part1by2((uint32_t)cy & 7u) << 1) +
-                          part1by2((uint32_t)cx & 7u));
-}
-
 __device__ __forceinline__ bool aborted(const Dev& d) { return is_aborted(d); }
 
 // N1: ComputeMinMaxKernel (ParticleSearchKernels.cu:40-62) on the current positions.
@@ -319,11 +302,16 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(Dev d) {
 // without contraction, x^2 + y^2 + z^2 left to right, as the FP32 oracle does. The
 // cell's grid coordinates come from its first particle by the same formula a
 // per-particle search would use on each of them (they agree: it is how they were binned).
+// The same hits also go into the particles' MASK rows (when kept): the candidates of
+// cells 3w, 3w + 1, 3w + 2 (an x-run) are bits 0.. of word w, collected with shared-memory
+// atomics and written out as the chunk's consecutive rows. A cell with an x-run of more
+// than 64 candidates gets no masks; its particles are flagged kRowPath.
 template <bool REL>
 __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted(d)) return;
     __shared__ float4 sx[kBlock / 32u][32];
+    __shared__ unsigned long long smask[kBlock / 32u][32u * kMaskWords];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t below = (1u << lane) - 1u;
     const uint32_t total = d.status[2];
@@ -359,11 +347,19 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
         const uint32_t ncand = __shfl_sync(0xffffffffu, incl, 31);
         const uint32_t excl = incl - cc;
         const float h2 = S.h2;
+        // x-run w (lanes 3w, 3w + 1, 3w + 2): its candidate total decides whether masks fit
+        const uint32_t runEnd = __shfl_sync(0xffffffffu, incl, min(3u * lane + 2u, 31u));
+        const uint32_t runBeg = __shfl_sync(0xffffffffu, excl, min(3u * lane, 31u));
+        const bool masks = d.MASK != nullptr &&
+                           !__any_sync(0xffffffffu, lane < 9u && runEnd - runBeg > kRunMax);
+        const uint32_t rowFlag = (d.MASK != nullptr && !masks) ? kRowPath : 0u;
         uint32_t mx = 0u;
         for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
             const uint32_t kk = min(32u, cnt - k0);
             __syncwarp();
             if (lane < kk) sx[w][lane] = d.X[start + k0 + lane];
+            if (masks)
+                for (uint32_t t = lane; t < kk * kMaskWords; t += 32u) smask[w][t] = 0ull;
             __syncwarp();
             uint32_t count = 0u;  // neighbours so far of particle start + k0 + lane
             for (uint32_t base = 0; base < ncand; base += 32u) {
@@ -378,6 +374,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                 const bool valid = i < ncand;
                 const uint32_t q = checked_index(d.status, __shfl_sync(0xffffffffu, cs, j) +
                                                  (i - __shfl_sync(0xffffffffu, excl, j)), valid ? d.n : 0xFFFFFFFFu);
+                // mask word and bit of this candidate: its x-run and place in the run
+                const uint32_t run = j / 3u;
+                const uint32_t bit = i - __shfl_sync(0xffffffffu, excl, 3u * run);
                 const float4 xq = valid ? d.X[q] : make_float4(0.f, 0.f, 0.f, 0.f);
                 for (uint32_t k = 0; k < kk; k++) {
                     const float3 e = pair_r<REL>(d, xq, sx[w][k]);
@@ -386,12 +385,20 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                     const uint32_t bits = __ballot_sync(0xffffffffu, hit);
                     const uint32_t ck = __shfl_sync(0xffffffffu, count, k);
                     const uint32_t at = ck + __popc(bits & below);
-                    if (hit && at < kMaxNeighbors) d.NBR[(size_t)(start + k0 + k) * kRow + at] = q;
+                    if (hit && at < kMaxNeighbors) {
+                        d.NBR[(size_t)(start + k0 + k) * kRow + at] = q;
+                        if (masks) atomicOr(&smask[w][k * kMaskWords + run], 1ull << bit);
+                    }
                     if (lane == k) count = min(kMaxNeighbors, ck + __popc(bits));
                 }
             }
+            __syncwarp();
+            if (masks) {  // the chunk's rows are consecutive slots: one coalesced copy
+                unsigned long long* out = d.MASK + (size_t)(start + k0) * kMaskWords;
+                for (uint32_t t = lane; t < kk * kMaskWords; t += 32u) out[t] = smask[w][t];
+            }
             if (lane < kk) {
-                d.NCNT[start + k0 + lane] = count;
+                d.NCNT[start + k0 + lane] = count | rowFlag;
                 if (count == kMaxNeighbors) atomicOr(&d.scenes[sid].flags, 0x8u);
             }
             mx = max(mx, __reduce_max_sync(0xffffffffu, lane < kk ? count : 0u));

@@ -29,6 +29,8 @@ void launch_visc_finish_dt(const Dev& d, cudaStream_t s);
 void launch_pres_init(const Dev& d, cudaStream_t s);
 void launch_pres_iter(const Dev& d, cudaStream_t s);
 void launch_pres_finish(const Dev& d, cudaStream_t s);
+// Occupancy and shared-memory limits of the cell-tile kernels (once, before any capture).
+cudaError_t prepare_tile_kernels();
 void box_map_sizes(const uint32_t res[3], uint32_t& nodes, uint32_t& cells);
 int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, float padding, const uint32_t res[3],
                       float r, const float* table, float wZero, float invStep, float* nodes, uint32_t* cells,
@@ -162,6 +164,8 @@ struct vfd_sim {
     bool analyticKernel = false;  // VFD_KERNEL_ANALYTIC
     bool graphFailed = false;
     uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+    // cell tiles of the solver-loop kernels per TunedKernel: log2 of the cells in a tile
+    uint8_t tiles[16] = {3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3};
 
     // layout
     bool allocated = false, uploaded = false;
