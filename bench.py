@@ -525,8 +525,71 @@ def profile_case(args):
         log("lanes", sim.Autotune(1))
     sim.Steps(args.graph_steps)
     sim.SetGraphMode(False)
+    import torch
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()  # `ncu --profile-from-start off` records the eager steps only
     st = sim.Steps(args.eager_steps)
-    log("particles", len(s["x"]), "stats", st)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    log("particles", len(s["x"]), "stats", st, "tiles", sim.GetTiles())
+
+
+def free_port() -> int:
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        return so.getsockname()[1]
+
+
+def relaunch(n: int) -> int:
+    """`bench.py --gpus N` outside torchrun: start N ranks on this node (one per GPU) with
+    torch.distributed.run and the same arguments; rank 0 prints the line."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.abspath(__file__)] + sys.argv[1:]
+    log("launching", n, "ranks:", " ".join(cmd))
+    return subprocess.run(cmd).returncode
+
+
+def dry_run(args):
+    """The replica path of the benchmark on the CPU: a gloo process group, every rank
+    advancing its own seeded scene (a 10^3 dam break, the FP32 oracle on one thread),
+    barriers around the timed steps, the slowest rank's time, and rank 0's JSON line
+    with n_gpus = world size. Tests the multi-rank launcher and reduction only."""
+    import torch
+    import torch.distributed as dist
+    from oracle import oracle as O
+    from vfd_gb300 import scenes
+    ws, rank, _ = dist_info()
+    if ws > 1:
+        dist.init_process_group("gloo")
+    O.set_threads(1)
+    s = scenes.small_dam_break(n_side=10, seed=scenes.config_seed(2) + rank)
+    sim = O.scene_oracle(s, 32)
+    for _ in range(args.warmup):
+        sim.step()
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = sim.step()
+    el = time.perf_counter() - t0
+    if ws > 1:
+        dist.barrier()
+    t = torch.tensor([el], dtype=torch.float64)
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = len(s["x"])
+    value = n * ws * args.steps / float(t.item())
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": 1e3 * float(t.item()) / args.steps,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic", "dry_run": True,
+                          "config": {"workload": f"dry run: {n}-particle dam break per rank on the CPU oracle",
+                                     "parallelism": f"replicas x{ws}"},
+                          "mean_density_error_pct": 100.0 * st["PressureSolverError"] / 1000.0}), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
 
 
 def main():
@@ -553,12 +616,20 @@ def main():
                          "from the host (what a profiler filtering by kernel name captures)")
     ap.add_argument("--graph-steps", type=int, default=4)
     ap.add_argument("--eager-steps", type=int, default=2)
+    ap.add_argument("--dry-run", action="store_true",
+                    help="exercise the multi-rank path on the CPU: gloo process group, each rank steps a small "
+                         "scene with the FP32 oracle instead of the GPU, same barriers, max-over-ranks timing "
+                         "and JSON line (for testing the launcher without GPUs; the numbers are not a benchmark)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return relaunch(args.gpus)
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_case:
         return profile_case(args)
+    if args.dry_run:
+        return dry_run(args)
 
     import torch
     import torch.distributed as dist

@@ -1078,6 +1078,7 @@ int build_cg_graph(vfd_sim* s, AdjointState* A) {
     }
     Dev d = s->dev[0];
     d.condHandle[1] = (unsigned long long)h;
+    d.rowLoops = 1u;  // the recorded rows; the cell tables are not the recorded step's
     std::vector<cudaGraphNode_t> leaves;
     e = add_segment(s->stream, g, leaves, [&](cudaStream_t st) { launch_visc_init(d, st); });
     if (e == cudaSuccess) e = add_while(s->stream, g, h, leaves, [&](cudaStream_t st) { launch_cg_iter(d, st); });
@@ -1153,10 +1154,12 @@ int backward_step(vfd_sim* s, AdjointState* A, uint32_t t) {
             CK(cudaGraphLaunch(s->adjCgExec, st));
         } else {  // eager: one flag read per CG iteration
             uint32_t more = 0;
-            launch_visc_init(d, st);
+            Dev dr = d;
+            dr.rowLoops = 1u;  // the recorded rows; the cell tables are not the recorded step's
+            launch_visc_init(dr, st);
             TRY(read_flag(s, 5, more));
             for (uint32_t guard = 0; more && guard < 100000u; guard++) {
-                launch_cg_iter(d, st);
+                launch_cg_iter(dr, st);
                 TRY(read_flag(s, 5, more));
             }
         }

@@ -162,6 +162,9 @@ struct Dev {
     // product), per TunedKernel: 2^tiles[k] consecutive Morton cells (3: a 2x2x2 block,
     // 4: 4x2x2).
     uint8_t tiles[16];
+    // 1: the CG product walks the neighbour rows instead of cell tiles (the adjoint's CG
+    // runs on recorded rows of a past step, whose cell tables are no longer current)
+    uint32_t rowLoops;
 };
 
 // ---------------------------------------------------------------- float3 math

@@ -902,6 +902,32 @@ __global__ void k_ctrl_cg1(Dev d) {
     if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
 }
 
+// Loop body 1 from the neighbour rows (Dev::rowLoops): Ap and p . Ap. The adjoint's CG
+// runs the forward CG on a recorded step, whose rows are restored but whose cell tables
+// (and thus tiles and masks) belong to another step.
+template <uint32_t G, bool REL>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv_rows(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    const Group<G> grp;
+    const uint32_t p = grp.p;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool valid = inRange && S.cgActive;
+    float pap = 0.0f;
+    if (valid) {
+        const float3 pv = f3(d.CP[p]);
+        const float3 ap = visc_matvec<G, REL>(d, grp, p, S, d.CP, pv);
+        if (grp.lane == 0) {
+            d.CAP[p] = f4(ap, 0.0f);
+            pap = dot_term(pv, ap);
+        }
+    }
+    const float v[1] = {pap};
+    const int slot[1] = {0};
+    scene_accumulate<1, G>(d, sid, valid && grp.lane == 0, v, slot);
+}
+
 // alpha = |r . z| / (p . Ap) (:714-720).
 __global__ void k_ctrl_cg_alpha(Dev d) {
     VFD_COUNT_LAUNCH(d);
@@ -1212,8 +1238,8 @@ template <void (*K)(Dev), size_t SMEM>
 cudaError_t prepare_tile() {
     int& r = tile_resident<K, SMEM>();
     if (r > 0) return cudaSuccess;
-    cudaError_t e = cudaSuccess;
-    if (SMEM > 48u * 1024u) e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    // the limit covers dynamic + static shared memory; raise it to what this kernel asks
+    cudaError_t e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
     int n = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, K, kTileBlock, SMEM);
     r = n > 0 ? n : 1;
@@ -1312,8 +1338,11 @@ void launch_visc_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_cg_p0", s, k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_ctrl_cg1", s, k_ctrl_cg1<<<1, 256, 0, s>>>(d));
 }
+#define K_SPMV_ROWS(G) k_cg_spmv_rows<G, false>
+#define K_SPMV_ROWS_R(G) k_cg_spmv_rows<G, true>
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
-    VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
+    if (d.rowLoops) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV_ROWS);
+    else VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
     VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     if (d.nscenes > 1) {
         VFD_LAUNCH("k_cg_update", s, k_cg_update_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
