@@ -129,6 +129,34 @@ def test_adjoint_matches_fp64_reference(full):
     _check("dL/dBoundaryViscosity", gpu["pb"][1], ref["pb"][1], 2e-2)
 
 
+# ------------------------------------------------------------ FP64 reference, full step, like for like
+@pytest.fixture(scope="module")
+def full_analytic():
+    """The full step (divergence and pressure solves, viscosity CG, adaptive CFL step,
+    volume-map boundary) with the GPU in analytic kernel mode, the kernel the FP64
+    reference evaluates: the two differ by FP32 against FP64 arithmetic only."""
+    sc = _floor_scene(div=True)
+    steps = 6
+    gpu = GpuRun(sc, steps, 4, analytic=True).gradient()
+    roll = R.Rollout(sc["desc"], sc["maps"])
+    x, v = roll.forward(sc["x"].astype(np.float64), sc["v"].astype(np.float64), steps)
+    x0b, v0b, pb = roll.backward(2.0 / len(x) * (x - sc["target"]), np.zeros_like(v))
+    return sc, gpu, dict(x=x, x0b=x0b, v0b=v0b, pb=pb)
+
+
+def test_adjoint_matches_fp64_reference_analytic_kernel(full_analytic):
+    """Gradients of the full method within 1e-3 of the FP64 reference (relative L2 for the
+    initial positions and velocities, relative for both viscosities)."""
+    _, gpu, ref = full_analytic
+    assert np.abs(gpu["x"] - ref["x"]).max() < 1e-5
+    for key in ("v0b", "x0b"):
+        rel = np.linalg.norm(gpu[key] - ref[key]) / np.linalg.norm(ref[key])
+        print(f"{key}: relative L2 difference {rel:.2e}")
+        assert rel < 1e-3, (key, rel)
+    _check("dL/dViscosity (analytic kernel)", gpu["pb"][0], ref["pb"][0], 1e-3)
+    _check("dL/dBoundaryViscosity (analytic kernel)", gpu["pb"][1], ref["pb"][1], 1e-3)
+
+
 # ------------------------------------------------------------ finite differences, smooth step
 @pytest.fixture(scope="module")
 def smooth():

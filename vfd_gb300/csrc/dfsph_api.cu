@@ -313,7 +313,7 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.RES, st));
     TRY(dalloc(s, &base.XB, st * std::max<uint32_t>(1u, maxBodies)));
     TRY(dalloc(s, &base.NBR, st * kRow));
-    TRY(dalloc(s, &base.MASK, st * kMaskWords));
+    TRY(dalloc(s, &base.NBRC, st * kRow));
     TRY(dalloc(s, &base.NCNT, st));
     TRY(dalloc(s, &base.KEY, st));
     TRY(dalloc(s, &base.KEYS, st));
@@ -397,7 +397,7 @@ int allocate(vfd_sim* s) {
         CK(cudaMemcpy(s->dBodies, bodies.data(), sizeof(BodyDev) * bodies.size(), cudaMemcpyHostToDevice));
     CK(cudaMemset(base.NCNT, 0, sizeof(uint32_t) * st));
     CK(cudaMemset(base.NBR, 0, sizeof(uint32_t) * st * kRow));
-    CK(cudaMemset(base.MASK, 0, sizeof(unsigned long long) * st * kMaskWords));
+    CK(cudaMemset(base.NBRC, 0, sizeof(uint16_t) * st * kRow));
     CK(cudaMemset(base.A, 0, sizeof(float4) * st));
     CK(cudaMemset(base.AP, 0, sizeof(float4) * st));
     CK(cudaMemset(base.STN, 0, sizeof(float4) * st));

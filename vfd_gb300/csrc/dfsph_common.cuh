@@ -14,10 +14,10 @@
 //   NBR  u32 [slot][72] neighbour slots, one row per particle in the reference's
 //        z, y, x cell order (at most 70 used), read by groups of G lanes
 //   NCNT u32 [slot] neighbour count | flag bits
-//   MASK u64 [slot][10] the same neighbour set as bit masks over the particle's 27-cell
-//        candidate set: word w = 3 (dz + 1) + (dy + 1) covers the x-run of cells
-//        (x-1, x, x+1) at (y+dy, z+dz), bit b = the run's b-th candidate in cell order;
-//        read by the cell-tile kernels of the solver loops (word 9 unused, 16-B rows)
+//   NBRC u16 [slot][72] the same row as stencil positions: entry (w << 6) | b is the b-th
+//        candidate, in cell order, of x-run w = 3 (dz + 1) + (dy + 1) of the 27-cell
+//        stencil (cells x-1, x, x+1 at y+dy, z+dz); read by the cell-tile kernels of the
+//        solver loops, which stage each run contiguously in shared memory
 //   X.w  mirrors kappa_v during the divergence solve and kappa during the pressure
 //        solve, so the pressure-acceleration gather brings it with the position
 // The reference keeps one 120-byte AoS DFSPHParticle per particle
@@ -43,9 +43,8 @@ constexpr float kEps = 1.0e-5f;              // Core/Math/Math.h:6
 constexpr uint32_t kCountMask = 0xFFu;
 constexpr uint32_t kHasBoundary = 1u << 8;   // some body gave this particle Vb > 0
 constexpr uint32_t kHasBoundaryVisc = 1u << 9;
-constexpr uint32_t kRowPath = 1u << 10;      // an x-run of the cell's candidates exceeds 64: no masks
-constexpr uint32_t kMaskWords = 10u;         // MASK row: 9 x-runs + 1 pad word (80 B, 16-B aligned)
-constexpr uint32_t kRunMax = 64u;            // candidates one mask word covers
+constexpr uint32_t kRowPath = 1u << 10;      // an x-run of the cell's candidates exceeds 64: no NBRC row
+constexpr uint32_t kRunMax = 64u;            // candidates of one x-run an NBRC entry can address
 
 // Neighbour-loop kernels whose lanes per particle (4, 8 or 16) the autotuner picks.
 enum TunedKernel {
@@ -128,7 +127,7 @@ struct Dev {
     float *RHO, *ALPHA, *RHOADV, *KAPPA, *KAPPAV, *RES;
     float4* XB;
     uint32_t *NBR, *NCNT;
-    unsigned long long* MASK;  // [slot][kMaskWords] neighbour masks per x-run (null: not kept)
+    uint16_t* NBRC;            // [slot][kRow] stencil-position rows (null: not kept)
     // search scratch
     uint32_t *KEY, *KEYS, *TMP, *CELL_START, *CELL_COUNT, *FILL, *SCAN;
     // viscosity CG

@@ -302,16 +302,15 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(Dev d) {
 // without contraction, x^2 + y^2 + z^2 left to right, as the FP32 oracle does. The
 // cell's grid coordinates come from its first particle by the same formula a
 // per-particle search would use on each of them (they agree: it is how they were binned).
-// The same hits also go into the particles' MASK rows (when kept): the candidates of
-// cells 3w, 3w + 1, 3w + 2 (an x-run) are bits 0.. of word w, collected with shared-memory
-// atomics and written out as the chunk's consecutive rows. A cell with an x-run of more
-// than 64 candidates gets no masks; its particles are flagged kRowPath.
+// Each hit also goes into the particle's NBRC row (when kept) as its stencil position: the
+// candidates of cells 3w, 3w + 1, 3w + 2 (an x-run) are positions 0.. of run w, and the entry
+// is (w << 6) | position. A cell with an x-run of more than 64 candidates gets no NBRC rows;
+// its particles are flagged kRowPath.
 template <bool REL>
 __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted(d)) return;
     __shared__ float4 sx[kBlock / 32u][32];
-    __shared__ unsigned long long smask[kBlock / 32u][32u * kMaskWords];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t below = (1u << lane) - 1u;
     const uint32_t total = d.status[2];
@@ -350,16 +349,14 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
         // x-run w (lanes 3w, 3w + 1, 3w + 2): its candidate total decides whether masks fit
         const uint32_t runEnd = __shfl_sync(0xffffffffu, incl, min(3u * lane + 2u, 31u));
         const uint32_t runBeg = __shfl_sync(0xffffffffu, excl, min(3u * lane, 31u));
-        const bool masks = d.MASK != nullptr &&
-                           !__any_sync(0xffffffffu, lane < 9u && runEnd - runBeg > kRunMax);
-        const uint32_t rowFlag = (d.MASK != nullptr && !masks) ? kRowPath : 0u;
+        const bool compact = d.NBRC != nullptr &&
+                             !__any_sync(0xffffffffu, lane < 9u && runEnd - runBeg > kRunMax);
+        const uint32_t rowFlag = (d.NBRC != nullptr && !compact) ? kRowPath : 0u;
         uint32_t mx = 0u;
         for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
             const uint32_t kk = min(32u, cnt - k0);
             __syncwarp();
             if (lane < kk) sx[w][lane] = d.X[start + k0 + lane];
-            if (masks)
-                for (uint32_t t = lane; t < kk * kMaskWords; t += 32u) smask[w][t] = 0ull;
             __syncwarp();
             uint32_t count = 0u;  // neighbours so far of particle start + k0 + lane
             for (uint32_t base = 0; base < ncand; base += 32u) {
@@ -374,9 +371,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                 const bool valid = i < ncand;
                 const uint32_t q = checked_index(d.status, __shfl_sync(0xffffffffu, cs, j) +
                                                  (i - __shfl_sync(0xffffffffu, excl, j)), valid ? d.n : 0xFFFFFFFFu);
-                // mask word and bit of this candidate: its x-run and place in the run
+                // stencil position of this candidate: its x-run and place in the run
                 const uint32_t run = j / 3u;
-                const uint32_t bit = i - __shfl_sync(0xffffffffu, excl, 3u * run);
+                const uint32_t entry = (run << 6) | (i - __shfl_sync(0xffffffffu, excl, 3u * run));
                 const float4 xq = valid ? d.X[q] : make_float4(0.f, 0.f, 0.f, 0.f);
                 for (uint32_t k = 0; k < kk; k++) {
                     const float3 e = pair_r<REL>(d, xq, sx[w][k]);
@@ -387,15 +384,10 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
                     const uint32_t at = ck + __popc(bits & below);
                     if (hit && at < kMaxNeighbors) {
                         d.NBR[(size_t)(start + k0 + k) * kRow + at] = q;
-                        if (masks) atomicOr(&smask[w][k * kMaskWords + run], 1ull << bit);
+                        if (compact) d.NBRC[(size_t)(start + k0 + k) * kRow + at] = (uint16_t)entry;
                     }
                     if (lane == k) count = min(kMaxNeighbors, ck + __popc(bits));
                 }
-            }
-            __syncwarp();
-            if (masks) {  // the chunk's rows are consecutive slots: one coalesced copy
-                unsigned long long* out = d.MASK + (size_t)(start + k0) * kMaskWords;
-                for (uint32_t t = lane; t < kk * kMaskWords; t += 32u) out[t] = smask[w][t];
             }
             if (lane < kk) {
                 d.NCNT[start + k0 + lane] = count | rowFlag;

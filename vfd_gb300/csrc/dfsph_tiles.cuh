@@ -2,24 +2,25 @@
 // Jacobi update K6/K19 and the viscosity CG product K14, DFSPHKernels.cu:317-432 and
 // :758-842), the passes a step repeats tens of times.
 //
-// A block takes a tile of 2^L consecutive Morton cells (a 2x2x2, 4x2x2 or 4x4x2 cube of
-// cells of edge h), stages the positions and the pass's neighbour field of every particle
-// in the tile's halo (the tile grown by one cell on every side) into shared memory, and
-// walks each particle's neighbours there. The halo is staged in z, y, x cell order, so
-// the candidates of the three cells (x-1, x, x+1) of one (y, z) row are contiguous: a
-// particle's neighbours are then exactly the set bits of its nine MASK words (one per
-// x-run, written by the neighbour search), bit b of word w being entry b of run w. No
-// per-pair index or gradient is read from memory; gradW / r is recomputed from the table
-// (the same midpoint lookup the row loops use). Each particle's data is read from L2 once
-// per tile whose halo holds it ((TX+2)(TY+2)(TZ+2) / (TX TY TZ) times per pass, 8x for a
-// 2x2x2 tile) instead of once per neighbour.
+// A block takes a tile of 2^L consecutive Morton cells (a 2x2x2 or 4x2x2 block of cells of
+// edge h), stages the positions and the pass's neighbour field of every particle in the
+// tile's halo (the tile grown by one cell on every side) into shared memory, and walks each
+// particle's neighbours there. The halo is staged in z, y, x cell order, so the candidates
+// of the three cells (x-1, x, x+1) of one (y, z) row -- an x-run -- are contiguous; the
+// search gives every neighbour its stencil position (x-run w, place b in the run), stored
+// as a 16-bit NBRC row beside the slot row, and the neighbour's staged index is then the
+// run's first staged index (nine per particle, kept in shared memory) plus b. No per-pair
+// slot or gradient is read from memory; gradW / r is recomputed from the table (the same
+// midpoint lookup the row loops use). Each particle's data is read from L2 once per tile
+// whose halo holds it ((TX+2)(TY+2)(TZ+2) / (TX TY TZ) times per pass, 8x for a 2x2x2
+// tile, 6x for 4x2x2) instead of once per neighbour.
 //
-// G lanes share a particle; lane l takes the mask bits at positions l, l + G, ... of every
-// word, which spreads the neighbours evenly, and the group's partial sums meet in a
-// shuffle tree, lane 0 writing the results. Particles flagged kRowPath by the search
-// (an x-run of more than 64 candidates), and every particle of a tile whose halo holds
-// more than the shared-memory capacity, walk their neighbour rows from global memory
-// instead; both walks evaluate the same pair terms.
+// G lanes share a particle and walk its row in lockstep rounds: lane l takes entries
+// l, l + G, ..., U entries per round (as the row loops do), so no lane runs a loop of its
+// own length; the group's partial sums meet in a shuffle tree and lane 0 writes the
+// results. Particles flagged kRowPath by the search (an x-run of more than 64 candidates),
+// and every particle of a tile whose halo holds more than the shared-memory capacity, walk
+// their slot rows from global memory instead; both walks evaluate the same pair terms.
 //
 // Reductions (Jacobi residual, p . Ap): each lane 0 accumulates its particles' FP32 terms
 // as an FP32 pair across the block's tiles; the block folds them (warp_sum_pair
@@ -38,21 +39,10 @@ struct TileShape {
     static constexpr uint32_t T = 1u << L;
     static constexpr uint32_t TX = 1u << ((L + 2u) / 3u), TY = 1u << ((L + 1u) / 3u), TZ = 1u << (L / 3u);
     static constexpr uint32_t HX = TX + 2u, HY = TY + 2u, HZ = TZ + 2u, HALO = HX * HY * HZ;
-    // staged particles: 16 per halo cell (the densest cells of the configurations hold
-    // ~10 on average and 18 at most)
-    static constexpr uint32_t CAP = 16u * HALO;
+    // staged particles: 12 per halo cell on average (cells of the configurations hold ~10
+    // on average and 18 at most; a halo sums 64-96 of them); a fuller halo walks rows
+    static constexpr uint32_t CAP = 12u * HALO;
 };
-
-// Lane selection of mask bits: positions congruent to `lane` modulo G.
-template <uint32_t G>
-__device__ __forceinline__ unsigned long long lane_bits(uint32_t lane) {
-    constexpr unsigned long long pat = G == 1u ? ~0ull
-                                     : G == 2u ? 0x5555555555555555ull
-                                     : G == 4u ? 0x1111111111111111ull
-                                     : G == 8u ? 0x0101010101010101ull
-                                               : 0x0001000100010001ull;
-    return pat << lane;
-}
 
 // Per-thread FP32-pair accumulation of a pass's reduction term across tiles, folded per
 // scene into the FP64 buckets (one atomic per block and scene).
@@ -83,7 +73,8 @@ struct TileSum {
     }
 };
 
-// The tile loop (the calling kernel counts its launch). Op supplies, as static device functions and members:
+// The tile loop (the calling kernel counts its launch). Op supplies, as static device
+// functions and members:
 //   kField            whether a per-particle float4 field is staged beside the position
 //   kReduce, kSlot    whether finish() returns a term summed into accumulator kSlot
 //   active(S)         whether scene S runs this pass
@@ -97,16 +88,20 @@ template <class Op, uint32_t L, uint32_t G, bool REL>
 __device__ __forceinline__ void tile_pass(const Dev& d) {
     using TS = TileShape<L>;
     constexpr uint32_t CAP = TS::CAP;
+    constexpr uint32_t U = 4u;                   // row entries per lane and round
+    constexpr uint32_t PER = kTileBlock / G;     // particles per chunk
+    static_assert(TS::HALO <= 255u, "staged cell index is one byte");
     extern __shared__ float4 tileSmem[];
     float4* sx = tileSmem;
     float4* sf = tileSmem + CAP;
     __shared__ uint32_t hStart[TS::HALO], hOff[TS::HALO + 1u];
-    __shared__ uint32_t tInfo[4];  // first, last, scene, skip
+    __shared__ uint8_t cellOf[CAP];              // halo cell of each staged particle
+    __shared__ uint32_t runBase[PER][9];         // first staged index of each x-run, per particle
+    __shared__ uint32_t tInfo[4];                // first, last, scene, skip
     if (is_aborted(d)) return;
     const uint32_t nTiles = d.status[2] >> L;
-    const uint32_t gl = threadIdx.x % G;
+    const uint32_t gl = threadIdx.x % G, pp = threadIdx.x / G;
     const uint32_t gmask = G == 32u ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(G - 1u)));
-    const unsigned long long sel = lane_bits<G>(gl);
     TileSum sum;
     for (uint32_t tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
         const uint32_t k0 = tile << L;
@@ -175,62 +170,61 @@ __device__ __forceinline__ void tile_pass(const Dev& d) {
         const uint32_t staged = hOff[TS::HALO];
         const bool fits = staged <= CAP;
         if (fits) {
+            // each halo cell marks its staged range, then every thread copies its elements
+            for (uint32_t t = threadIdx.x; t < TS::HALO; t += kTileBlock)
+                for (uint32_t i = hOff[t]; i < hOff[t + 1u]; i++) cellOf[i] = (uint8_t)t;
+            __syncthreads();
             for (uint32_t i = threadIdx.x; i < staged; i += kTileBlock) {
-                uint32_t lo = 0u, hi = TS::HALO - 1u;  // last halo cell with hOff <= i
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi + 1u) >> 1;
-                    if (hOff[mid] <= i) lo = mid;
-                    else hi = mid - 1u;
-                }
-                const uint32_t q = checked_index(d.status, hStart[lo] + (i - hOff[lo]), d.n);
+                const uint32_t c = cellOf[i];
+                const uint32_t q = checked_index(d.status, hStart[c] + (i - hOff[c]), d.n);
                 sx[i] = d.X[q];
                 if (Op::kField) sf[i] = Op::field(d, q);
             }
         }
         __syncthreads();
-        for (uint32_t pb = first; pb < last; pb += kTileBlock / G) {
-            const uint32_t p = pb + threadIdx.x / G;
-            if (p >= last) continue;  // whole groups leave together
-            typename Op::Own own;
-            Op::load(d, p, S, own);
-            typename Op::Acc acc{};
-            const uint32_t ncnt = d.NCNT[p];
-            if (fits && !(ncnt & kRowPath)) {
-                const uint32_t m = d.KEYS[p] - k0;  // local Morton index of the particle's cell
-                const uint32_t lx = compact3(m), ly = compact3(m >> 1), lz = compact3(m >> 2);
-                const ulonglong2* mrow = reinterpret_cast<const ulonglong2*>(d.MASK + (size_t)p * kMaskWords);
-                // words two at a time (16-byte loads), each lane keeping only its own bits
+        for (uint32_t pb = first; pb < last; pb += PER) {
+            const uint32_t p = pb + pp;
+            if (p < last) {  // whole groups take this branch together
+                typename Op::Own own;
+                Op::load(d, p, S, own);
+                typename Op::Acc acc{};
+                const uint32_t ncnt = d.NCNT[p];
+                const uint32_t cnt = ncnt & kCountMask;
+                if (fits && !(ncnt & kRowPath)) {
+                    const uint32_t m = d.KEYS[p] - k0;  // local Morton index of the particle's cell
+                    const uint32_t lx = compact3(m), ly = compact3(m >> 1), lz = compact3(m >> 2);
+                    for (uint32_t w = gl; w < 9u; w += G)
+                        runBase[pp][w] = hOff[((lz + w / 3u) * TS::HY + ly + w % 3u) * TS::HX + lx];
+                    __syncwarp(gmask);
+                    const uint16_t* row = d.NBRC + (size_t)p * kRow;
+                    for (uint32_t base = 0; base < cnt; base += U * G) {
+                        uint32_t e[U];
 #pragma unroll
-                for (uint32_t k = 0; k < kMaskWords / 2u; k++) {
-                    const ulonglong2 v = __ldcs(mrow + k);
+                        for (uint32_t u = 0; u < U; u++) {
+                            const uint32_t j = base + gl + u * G;
+                            e[u] = j < cnt ? (uint32_t)__ldcs(row + j) : 0xFFFFu;
+                        }
 #pragma unroll
-                    for (uint32_t h = 0; h < 2u; h++) {
-                        const uint32_t w = 2u * k + h;
-                        if (w >= 9u) break;
-                        const uint32_t hy = ly + w % 3u, hz = lz + w / 3u;
-                        const uint32_t base = hOff[(hz * TS::HY + hy) * TS::HX + lx];
-                        unsigned long long bits = (h ? v.y : v.x) & sel;
-                        while (bits) {
-                            const uint32_t j = base + (uint32_t)(__ffsll((long long)bits) - 1);
-                            bits &= bits - 1ull;
-                            const uint32_t jj = checked_index(d.status, j, staged);
+                        for (uint32_t u = 0; u < U; u++) {
+                            if (e[u] == 0xFFFFu) continue;
+                            const uint32_t jj = checked_index(d.status, runBase[pp][e[u] >> 6] + (e[u] & 63u), staged);
                             Op::pair(d, own, sx[jj], Op::kField ? sf[jj] : make_float4(0.f, 0.f, 0.f, 0.f), acc);
                         }
                     }
+                } else {
+                    const uint32_t* row = d.NBR + (size_t)p * kRow;
+                    for (uint32_t j = gl; j < cnt; j += G) {
+                        const uint32_t q = checked_index(d.status, __ldg(row + j), d.n);
+                        Op::pair(d, own, d.X[q], Op::kField ? Op::field(d, q) : make_float4(0.f, 0.f, 0.f, 0.f), acc);
+                    }
                 }
-            } else {
-                const uint32_t cnt = ncnt & kCountMask;
-                const uint32_t* row = d.NBR + (size_t)p * kRow;
-                for (uint32_t j = gl; j < cnt; j += G) {
-                    const uint32_t q = checked_index(d.status, __ldg(row + j), d.n);
-                    Op::pair(d, own, d.X[q], Op::kField ? Op::field(d, q) : make_float4(0.f, 0.f, 0.f, 0.f), acc);
+                acc = group_sum<G>(gmask, acc);
+                if (gl == 0u) {
+                    const float term = Op::finish(d, p, S, own, acc, ncnt);
+                    if (Op::kReduce) sum.add(term);
                 }
             }
-            acc = group_sum<G>(gmask, acc);
-            if (gl == 0u) {
-                const float term = Op::finish(d, p, S, own, acc, ncnt);
-                if (Op::kReduce) sum.add(term);
-            }
+            __syncwarp();  // runBase of this chunk is reused by the next
         }
         __syncthreads();  // the halo and tInfo are rewritten by the next tile
     }
