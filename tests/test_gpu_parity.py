@@ -327,3 +327,37 @@ def test_search_equals_reference_kernels():
                for k in golden[name]["sha256"]}
         assert got == golden[name]["sha256"], name
         g.close()
+
+
+@pytest.mark.parametrize("tiles", [3, 4])
+def test_tile_passes_match_oracle(tiles):
+    """The solver-loop passes on cell tiles (2x2x2 or 4x2x2 cells staged in shared memory,
+    neighbours walked by stencil position) hold the same one-step tolerances against the
+    FP32 oracle as the neighbour-row passes, with viscosity and surface tension on."""
+    s = scenes.small_dam_break(n_side=12, viscosity=0.02, surface_tension=0.05)
+    g, o = pair(s, 32)
+    g.SetTiles([tiles] * len(V.TUNED_KERNELS))
+    assert set(g.GetTiles().values()) == {tiles}
+    h = 4 * s["desc"]["ParticleRadius"]
+    for k in range(3):
+        _compare_step(g, o, h, median_tol=1e-6 * (k + 1) ** 2)
+
+
+def test_tile_passes_in_a_batch_match_single_scenes():
+    sc = [scenes.small_dam_break(n_side=n, viscosity=vv, seed=sd) for n, vv, sd in
+          [(8, 0.0, 1), (11, 0.02, 2), (9, 0.2, 3)]]
+    maps = [gpu_maps(s) for s in sc]
+    batch = V.batch_simulation(sc, maps)
+    batch.SetTiles([3] * len(V.TUNED_KERNELS))
+    singles = [V.scene_simulation(s, maps=maps[k]) for k, s in enumerate(sc)]
+    for one in singles:
+        one.SetTiles([3] * len(V.TUNED_KERNELS))
+    for _ in range(4):
+        batch.Steps(1)
+        for one in singles:
+            one.OnUpdate()
+    for k, one in enumerate(singles):
+        xb, vb, _ = batch.GetState(scene=k)
+        xs, vs, _ = one.GetState()
+        np.testing.assert_allclose(xb, xs, atol=1e-6)
+        np.testing.assert_allclose(vb, vs, atol=1e-5)

@@ -542,13 +542,15 @@ class DFSPHSimulation:
         return list(arr)[:len(TUNED_KERNELS)]
 
     def SetTiles(self, tiles):
-        """log2 of the cells per tile of the cell-tile kernels, in TUNED_KERNELS order
-        (3 = 2x2x2, 4 = 4x2x2; entries of other kernels are ignored)."""
+        """Per solver-loop pass, in TUNED_KERNELS order: 0 = walk neighbour rows, 3 or 4 =
+        log2 of the cells per shared-memory tile (2x2x2, 4x2x2); entries of other kernels
+        are ignored."""
         arr = (C.c_uint8 * len(tiles))(*tiles)
         _check(lib().vfd_set_tiles(self._h, arr, len(tiles)), "vfd_set_tiles")
 
     def GetTiles(self) -> dict:
-        """Tile sizes (log2 of the cells) of the three cell-tile kernels."""
+        """Tile choice of the three solver-loop passes (0 = neighbour rows, 3 or 4 = log2
+        of the cells per tile)."""
         arr = (C.c_uint8 * 16)()
         _check(lib().vfd_get_tiles(self._h, arr, 16), "vfd_get_tiles")
         return {k: arr[i] for i, k in enumerate(TUNED_KERNELS) if k in TILE_KERNELS}

@@ -313,6 +313,7 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.RES, st));
     TRY(dalloc(s, &base.XB, st * std::max<uint32_t>(1u, maxBodies)));
     TRY(dalloc(s, &base.NBR, st * kRow));
+    TRY(dalloc(s, &base.NG, st * kRow));
     TRY(dalloc(s, &base.NBRC, st * kRow));
     TRY(dalloc(s, &base.NCNT, st));
     TRY(dalloc(s, &base.KEY, st));
@@ -354,6 +355,7 @@ int allocate(vfd_sim* s) {
         base.batchBlocks = (uint32_t)std::max(1, sms) * (2048u / kBlock);
     }
     std::memcpy(base.tiles, s->tiles, sizeof(base.tiles));
+    base.compactRows = uses_tiles(s->tiles) ? 1u : 0u;
     CK(prepare_tile_kernels());
     TRY(dalloc(s, &s->dWM, kTableRes));
     TRY(dalloc(s, &s->dGM, kTableRes));
@@ -397,6 +399,7 @@ int allocate(vfd_sim* s) {
         CK(cudaMemcpy(s->dBodies, bodies.data(), sizeof(BodyDev) * bodies.size(), cudaMemcpyHostToDevice));
     CK(cudaMemset(base.NCNT, 0, sizeof(uint32_t) * st));
     CK(cudaMemset(base.NBR, 0, sizeof(uint32_t) * st * kRow));
+    CK(cudaMemset(base.NG, 0, sizeof(uint2) * st * kRow));
     CK(cudaMemset(base.NBRC, 0, sizeof(uint16_t) * st * kRow));
     CK(cudaMemset(base.A, 0, sizeof(float4) * st));
     CK(cudaMemset(base.AP, 0, sizeof(float4) * st));
@@ -1956,9 +1959,13 @@ int vfd_set_tiles(vfd_sim* s, const uint8_t* tiles, uint32_t count) {
     TRY(check_sim(s));
     if (!tiles || count == 0 || count > kTunedCount) return fail(VFD_E_ARG, "tiles: 1..%d values", (int)kTunedCount);
     for (uint32_t k = 0; k < count; k++)
-        if (tiles[k] != 3 && tiles[k] != 4) return fail(VFD_E_ARG, "tile size must be 3 (2x2x2) or 4 (4x2x2)");
+        if (tiles[k] != 0 && tiles[k] != 3 && tiles[k] != 4)
+            return fail(VFD_E_ARG, "tile size must be 0 (neighbour rows), 3 (2x2x2) or 4 (4x2x2)");
     std::memcpy(s->tiles, tiles, count);
-    for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+    for (int k = 0; k < 2; k++) {
+        std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+        s->dev[k].compactRows = uses_tiles(s->tiles) ? 1u : 0u;
+    }
     s->releaseGraphs();
     return VFD_OK;
 }
@@ -2022,16 +2029,18 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
         return fail(VFD_E_CUDA, "autotune snapshot: %s", cudaGetErrorString(e));
     }
     // every lane count with every tile size of the cell-tile kernels (the others ignore it)
-    const uint8_t tileCand[2] = {3, 4};
-    double times[kTunedCount][3][2] = {};
+    const uint8_t tileCand[3] = {0, 3, 4};  // neighbour rows, 2x2x2 tiles, 4x2x2 tiles
+    double times[kTunedCount][3][3] = {};
     int rc = VFD_OK;
-    for (int ct = 0; ct < 6 && rc == VFD_OK; ct++) {
+    for (int ct = 0; ct < 9 && rc == VFD_OK; ct++) {
         const int c = ct % 3, tl = ct / 3;
-        for (int k = 0; k < 2; k++)
+        for (int k = 0; k < 2; k++) {
             for (int t = 0; t < kTunedCount; t++) {
                 s->dev[k].lanes[t] = cand[c];
                 s->dev[k].tiles[t] = tileCand[tl];
             }
+            s->dev[k].compactRows = tileCand[tl] != 0 ? 1u : 0u;
+        }
         EventProfiler prof;
         g_profiler = &prof;
         for (uint32_t k = 0; k < steps && rc == VFD_OK; k++) {
@@ -2058,17 +2067,21 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
         for (int k = 0; k < 2; k++) {
             std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
             std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+            s->dev[k].compactRows = uses_tiles(s->tiles) ? 1u : 0u;
         }
         return rc;
     }
     for (int t = 0; t < kTunedCount; t++) {
+        const bool tileable = t == kTPAccel || t == kTJacobi || t == kTSpmv;
+        // kernels without tiles ran the same code in all three tile runs: their sum
+        auto cost = [&](int c, int tl) {
+            return tileable ? times[t][c][tl] : times[t][c][0] + times[t][c][1] + times[t][c][2];
+        };
         int best = 1, bestTile = 0;
-        double bt = times[t][1][0] + times[t][1][1];  // lanes alone: both tile runs summed
-        const bool tiled = t == kTPAccel || t == kTJacobi || t == kTSpmv;
-        if (tiled) bt = times[t][1][0];
+        double bt = cost(1, 0);
         for (int c = 0; c < 3; c++)
-            for (int tl = 0; tl < (tiled ? 2 : 1); tl++) {
-                const double v = tiled ? times[t][c][tl] : times[t][c][0] + times[t][c][1];
+            for (int tl = 0; tl < (tileable ? 3 : 1); tl++) {
+                const double v = cost(c, tl);
                 if (v > 0.0 && v < bt) {
                     bt = v;
                     best = c;
@@ -2076,11 +2089,12 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
                 }
             }
         s->lanes[t] = cand[best];
-        s->tiles[t] = tileCand[bestTile];
+        s->tiles[t] = tileable ? tileCand[bestTile] : 0;
     }
     for (int k = 0; k < 2; k++) {
         std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
         std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+        s->dev[k].compactRows = uses_tiles(s->tiles) ? 1u : 0u;
     }
     s->releaseGraphs();
     if (lanes_out) std::memcpy(lanes_out, s->lanes, std::min<uint32_t>(count, 16));

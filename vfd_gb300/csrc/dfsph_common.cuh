@@ -14,7 +14,11 @@
 //   NBR  u32 [slot][72] neighbour slots, one row per particle in the reference's
 //        z, y, x cell order (at most 70 used), read by groups of G lanes
 //   NCNT u32 [slot] neighbour count | flag bits
-//   NBRC u16 [slot][72] the same row as stencil positions: entry (w << 6) | b is the b-th
+//   NG   (u32, f32) [slot][72] the row again with gradW / r of each pair beside each
+//        index, written once per step by the density pass and streamed (one 8-byte load
+//        per pair) by the later row loops instead of a table lookup
+//   NBRC u16 [slot][72] the same row as stencil positions (only while a pass runs on
+//        cell tiles, Dev::compactRows): entry (w << 6) | b is the b-th
 //        candidate, in cell order, of x-run w = 3 (dz + 1) + (dy + 1) of the 27-cell
 //        stencil (cells x-1, x, x+1 at y+dy, z+dz); read by the cell-tile kernels of the
 //        solver loops, which stage each run contiguously in shared memory
@@ -127,6 +131,7 @@ struct Dev {
     float *RHO, *ALPHA, *RHOADV, *KAPPA, *KAPPAV, *RES;
     float4* XB;
     uint32_t *NBR, *NCNT;
+    uint2* NG;                 // [slot][72] (neighbour slot, gradW factor bits) of each pair (row layout)
     uint16_t* NBRC;            // [slot][kRow] stencil-position rows (null: not kept)
     // search scratch
     uint32_t *KEY, *KEYS, *TMP, *CELL_START, *CELL_COUNT, *FILL, *SCAN;
@@ -158,9 +163,11 @@ struct Dev {
     uint32_t* WORK;
     uint32_t workStride, batchBlocks;
     // Cell tiles of the solver-loop kernels (pressure acceleration, Jacobi update, CG
-    // product), per TunedKernel: 2^tiles[k] consecutive Morton cells (3: a 2x2x2 block,
-    // 4: 4x2x2).
+    // product), per TunedKernel: 0 = the pass walks neighbour rows, else 2^tiles[k]
+    // consecutive Morton cells per tile (3: a 2x2x2 block, 4: 4x2x2). compactRows: some
+    // pass runs on tiles, so the search writes the NBRC rows.
     uint8_t tiles[16];
+    uint32_t compactRows;
     // 1: the CG product walks the neighbour rows instead of cell tiles (the adjoint's CG
     // runs on recorded rows of a past step, whose cell tables are no longer current)
     uint32_t rowLoops;

@@ -96,6 +96,7 @@ __device__ __forceinline__ int chunk_scene(const Dev& d, int loop, uint32_t base
 
 struct Nbr {
     const uint32_t* row;
+    const uint2* ng;
     uint32_t count, flags;
 #ifdef VFD_BOUNDS_CHECK
     uint32_t n;
@@ -109,9 +110,9 @@ struct Nbr {
 __device__ __forceinline__ Nbr neighbors(const Dev& d, uint32_t p) {
     const uint32_t w = d.NCNT[p];
 #ifdef VFD_BOUNDS_CHECK
-    return Nbr{d.NBR + (size_t)p * kRow, w & kCountMask, w, d.n, d.status};
+    return Nbr{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w, d.n, d.status};
 #else
-    return Nbr{d.NBR + (size_t)p * kRow, w & kCountMask, w};
+    return Nbr{d.NBR + (size_t)p * kRow, d.NG + (size_t)p * kRow, w & kCountMask, w};
 #endif
 }
 
@@ -124,38 +125,53 @@ __device__ __forceinline__ void set_kappa(const Dev& d, uint32_t p, float k) {
 // Row entries per lane and round of a neighbour loop (other depths measured slower).
 constexpr uint32_t kUnroll = 4u;
 
-// Neighbour loop of one group over the particle's row (the solver-loop kernels use the
-// cell tiles instead, dfsph_tiles.cuh; this path serves the once-per-step kernels and
-// the particles whose candidate runs are too long for masks). In a round the group
-// covers U*G consecutive row entries and lane l takes entries l, l + G, ...,
-// l + (U-1)G, so at each step the group's lanes read consecutive entries -- usually
-// consecutive slots of one cell, which the gathers then fetch in one or two sectors.
-// The first round's index loads do not wait for the count (rows have 72 slots, entries
-// past the count are masked), so the count, the indices and the particle's own fields
-// are fetched together; within a round the U gathers per lane are independent. Masked
-// entries use the particle itself as a stand-in index. The row is read once per pass,
-// so it is loaded with the evict-first hint (ld.global.cs) to leave L2 to the gathered
-// fields. f(q, j, ok): neighbour slot, row position, valid.
-template <uint32_t G, class F>
+// Neighbour loop of one group. In a round the group covers U*G consecutive row
+// entries and lane l takes entries l, l + G, ..., l + (U-1)G, so at each step the
+// group's lanes read consecutive entries -- usually consecutive slots of one cell,
+// which the gathers then fetch in one or two sectors. The first round's index loads do
+// not wait for the count (rows have 72 slots, entries past the count are masked), so
+// the count, the indices and the particle's own fields are fetched together; within a
+// round the U gathers per lane are independent. Masked entries use the particle itself
+// as a stand-in index. The row and gradient streams are read once per pass, so they
+// are loaded with the evict-first hint (ld.global.cs) to leave L2 to the gathered
+// fields.
+template <uint32_t G, bool WITH_GS, class F>
 __device__ __forceinline__ void for_neighbors(const Group<G>& grp, const Nbr& nb, uint32_t self, F&& f) {
     constexpr uint32_t U = kUnroll;
     static_assert(U * G <= kRow, "first round must stay inside the row");
     uint32_t q[U];
+    float g[U];
 #pragma unroll
-    for (uint32_t u = 0; u < U; u++) q[u] = __ldcs(nb.row + grp.lane + u * G);
+    for (uint32_t u = 0; u < U; u++) {
+        if (WITH_GS) {
+            const uint2 e = __ldcs(nb.ng + grp.lane + u * G);
+            q[u] = e.x;
+            g[u] = __uint_as_float(e.y);
+        } else {
+            q[u] = __ldcs(nb.row + grp.lane + u * G);
+            g[u] = 0.0f;
+        }
+    }
     for (uint32_t base = 0; base < nb.count; base += U * G) {
         if (base > 0) {
 #pragma unroll
             for (uint32_t u = 0; u < U; u++) {
                 const uint32_t j = base + grp.lane + u * G;
-                q[u] = j < nb.count ? __ldcs(nb.row + j) : self;
+                if (WITH_GS) {
+                    const uint2 e = j < nb.count ? __ldcs(nb.ng + j) : make_uint2(self, 0u);
+                    q[u] = e.x;
+                    g[u] = __uint_as_float(e.y);
+                } else {
+                    q[u] = j < nb.count ? __ldcs(nb.row + j) : self;
+                    g[u] = 0.0f;
+                }
             }
         }
 #pragma unroll
         for (uint32_t u = 0; u < U; u++) {
             const uint32_t j = base + grp.lane + u * G;
             const bool ok = j < nb.count;
-            f(ok ? nb.check(q[u]) : self, j, ok);
+            f(ok ? nb.check(q[u]) : self, g[u], j, ok);
         }
     }
 }
@@ -208,12 +224,14 @@ __global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
     const float V = S.volume;
     const bool div = DIV && S.enableDiv;
     const float3 vi = div ? f3(d.V[p]) : make_float3(0.f, 0.f, 0.f);
-    for_neighbors<G>(grp, nb, p, [&](uint32_t q, uint32_t, bool ok) {
+    uint2* ngRow = d.NG + (size_t)p * kRow;
+    for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t j, bool ok) {
         const float3 r = pair_r<REL>(d, xi4, d.X[q]);
         float w, gs;
         kernel_wg(d, r, w, gs);
         const float3 vq = div ? f3(d.V[q]) : make_float3(0.f, 0.f, 0.f);
         if (!ok) return;
+        __stcs(ngRow + j, make_uint2(q, __float_as_uint(gs)));
         wsum += w;
         const float3 gj = (-V * gs) * r;
         g2 += dot3(gj, gj);
@@ -264,9 +282,8 @@ template <uint32_t G, bool REL>
 __device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
                                                      const Nbr& nb, float4 xi, float3 vi) {
     float s = 0.0f;
-    for_neighbors<G>(grp, nb, p, [&](uint32_t q, uint32_t, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float3 r = pair_r<REL>(d, xi, d.X[q]);
-        const float gs = grad_factor(d, r);
         const float3 vq = f3(d.V[q]);
         const float t = dot3(vi - vq, gs * r);
         if (ok) s += t;
@@ -286,11 +303,10 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
     const float4 xi = d.X[p];
     const float V = S.volume;
     float3 a = make_float3(0.f, 0.f, 0.f);
-    for_neighbors<G>(grp, nb, p, [&](uint32_t q, uint32_t, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float4 xq = d.X[q];
         const float sum = ki + (REL ? kap[q] : xq.w);
         const float3 r = pair_r<REL>(d, xi, xq);
-        const float gs = grad_factor(d, r);
         if (ok && fabsf(sum) > kEps) a += (sum * (-V * gs)) * r;
     });
     a = grp.sum(a);
@@ -298,115 +314,58 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
     return a;
 }
 
-// 3x3 matrices of the viscosity solve (block-Jacobi preconditioner, boundary term).
-struct Mat3 {
-    float3 r0, r1, r2;
-};
-__device__ __forceinline__ float3 mul(const Mat3& m, float3 v) {
-    return make_float3(dot3(m.r0, v), dot3(m.r1, v), dot3(m.r2, v));
-}
-__device__ __forceinline__ void add_outer(Mat3& m, float c, float3 a, float3 b) {  // m += c a b^T
-    m.r0 += (c * a.x) * b;
-    m.r1 += (c * a.y) * b;
-    m.r2 += (c * a.z) * b;
-}
-__device__ __forceinline__ Mat3 load_mat(const float4* M, size_t stride, uint32_t p) {
-    Mat3 m;
-    m.r0 = f3(M[p]);
-    m.r1 = f3(M[stride + p]);
-    m.r2 = f3(M[2 * stride + p]);
-    return m;
-}
-__device__ __forceinline__ void store_mat(float4* M, size_t stride, uint32_t p, const Mat3& m) {
-    M[p] = f4(m.r0, 0.f);
-    M[stride + p] = f4(m.r1, 0.f);
-    M[2 * stride + p] = f4(m.r2, 0.f);
-}
-__device__ __forceinline__ Mat3 inverse3(const Mat3& a) {  // cofactors / determinant
-    const float c00 = a.r1.y * a.r2.z - a.r1.z * a.r2.y;
-    const float c01 = a.r1.z * a.r2.x - a.r1.x * a.r2.z;
-    const float c02 = a.r1.x * a.r2.y - a.r1.y * a.r2.x;
-    const float det = a.r0.x * c00 + a.r0.y * c01 + a.r0.z * c02;
-    const float id = 1.0f / det;
-    Mat3 r;
-    r.r0 = make_float3(c00 * id, (a.r0.z * a.r2.y - a.r0.y * a.r2.z) * id, (a.r0.y * a.r1.z - a.r0.z * a.r1.y) * id);
-    r.r1 = make_float3(c01 * id, (a.r0.x * a.r2.z - a.r0.z * a.r2.x) * id, (a.r0.z * a.r1.x - a.r0.x * a.r1.z) * id);
-    r.r2 = make_float3(c02 * id, (a.r0.y * a.r2.x - a.r0.x * a.r2.y) * id, (a.r0.x * a.r1.y - a.r0.y * a.r1.x) * id);
-    return r;
+// K5 / K18.
+template <bool DIV, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    GROUP_PROLOGUE(G)
+    const SceneDev& S = d.scenes[scene_of(d, p)];
+    if (!(DIV ? S.div.active : S.pres.active)) return;
+    const Nbr nb = neighbors(d, p);
+    const float3 a = pressure_accel<DIV, G, REL>(d, grp, p, S, nb);
+    if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
 }
 
-// ---------------------------------------------------------------------------
-// The solver-loop passes as cell-tile kernels (dfsph_tiles.cuh). Each Op states one
-// pass's pair term and epilogue; the tile loop walks the neighbours (shared-memory halo
-// and masks, or the row for kRowPath particles) and sums the terms over the group.
+// K5 / K18 of a batch: the scenes still iterating, from the loop's work list.
+template <bool DIV, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kBlock) k_pressure_accel_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    const int L = DIV ? kLoopDiv : kLoopPres;
+    BATCH_LOOP(L, G) {
+        const uint32_t vp = base_ + threadIdx.x / G;
+        if (vp >= total_) continue;
+        uint32_t sid;
+        const uint32_t p = work_slot(d, L, vp, sid);
+        const Group<G> grp(p);
+        const Nbr nb = neighbors(d, p);
+        const float3 a = pressure_accel<DIV, G, REL>(d, grp, p, d.scenes[sid], nb);
+        if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
+    }
+}
 
-// K5 DivergenceSolveIterationKernel's force part / K18 (:388-432, :342-386): pressure
-// acceleration a_p = -V sum_j (k_i + k_j) gradW_ij - k_i GB_i (kappa in X.w, or staged
-// with cell-relative positions).
-template <bool DIV, bool REL>
-struct PressureAccelOp {
-    static constexpr bool kField = REL;
-    static constexpr bool kReduce = false;
-    static constexpr int kSlot = 0;
-    struct Own {
-        float4 xi;
-        float ki, V;
-    };
-    using Acc = float3;
-    __device__ static bool active(const SceneDev& S) { return (DIV ? S.div.active : S.pres.active) != 0u; }
-    __device__ static float4 field(const Dev& d, uint32_t q) {
-        return make_float4((DIV ? d.KAPPAV : d.KAPPA)[q], 0.f, 0.f, 0.f);
-    }
-    __device__ static void load(const Dev& d, uint32_t p, const SceneDev& S, Own& o) {
-        o.xi = d.X[p];
-        o.ki = (DIV ? d.KAPPAV : d.KAPPA)[p];
-        o.V = S.volume;
-    }
-    __device__ static void pair(const Dev& d, const Own& o, float4 xq, float4 fq, Acc& a) {
-        const float sum = o.ki + (REL ? fq.x : xq.w);
-        const float3 r = pair_r<REL>(d, o.xi, xq);
-        const float gs = grad_factor(d, r);
-        if (fabsf(sum) > kEps) a += (sum * (-o.V * gs)) * r;
-    }
-    __device__ static float finish(const Dev& d, uint32_t p, const SceneDev&, const Own& o, Acc a, uint32_t ncnt) {
-        if (fabsf(o.ki) > kEps && (ncnt & kHasBoundary)) a += o.ki * (-f3(d.GB[p]));
-        d.AP[p] = f4(a, 0.0f);
-        return 0.0f;
-    }
-};
-
-// K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel
-// (:317-340), each with ComputeDensityPressureForce (:280-315): the density change of
-// the pressure accelerations, the clamped residual, the kappa update, and the residual
-// into the FP64-accurate sum.
-template <bool DIV, bool REL>
-struct JacobiOp {
-    static constexpr bool kField = true;
-    static constexpr bool kReduce = true;
-    static constexpr int kSlot = 0;
-    struct Own {
-        float4 xi;
-        float3 ai;
-    };
-    using Acc = float;
-    __device__ static bool active(const SceneDev& S) { return (DIV ? S.div.active : S.pres.active) != 0u; }
-    __device__ static float4 field(const Dev& d, uint32_t q) { return d.AP[q]; }
-    __device__ static void load(const Dev& d, uint32_t p, const SceneDev&, Own& o) {
-        o.xi = d.X[p];
-        o.ai = f3(d.AP[p]);
-    }
-    __device__ static void pair(const Dev& d, const Own& o, float4 xq, float4 aq, Acc& f) {
-        const float3 r = pair_r<REL>(d, o.xi, xq);
-        const float gs = grad_factor(d, r);
-        f += dot3(o.ai - f3(aq), gs * r);
-    }
-    __device__ static float finish(const Dev& d, uint32_t p, const SceneDev& S, const Own& o, Acc f, uint32_t ncnt) {
-        f *= S.volume;
-        if (ncnt & kHasBoundary) f += dot3(o.ai, f3(d.GB[p]));
+// K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
+// each with ComputeDensityPressureForce (:280-315) and the FP64-accurate residual sum.
+template <bool DIV, uint32_t G, bool REL>
+__device__ __forceinline__ float jacobi_item(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S) {
+    float res = 0.0f;
+    const Nbr nb = neighbors(d, p);
+    const float4 xi = d.X[p];
+    const float3 ai = f3(d.AP[p]);
+    float f = 0.0f;
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
+        const float3 r = pair_r<REL>(d, xi, d.X[q]);
+        const float3 aq = f3(d.AP[q]);
+        const float t = dot3(ai - aq, gs * r);
+        if (ok) f += t;
+    });
+    f = grp.sum(f) * S.volume;
+    if (grp.lane == 0) {
+        if (nb.flags & kHasBoundary) f += dot3(ai, f3(d.GB[p]));
         float r;
         if (DIV) {
             f *= S.dt;
-            r = (ncnt & kCountMask) < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
+            r = nb.count < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
             const float k = d.KAPPAV[p] - r * d.ALPHA[p];
             d.KAPPAV[p] = k;
             set_kappa(d, p, k);
@@ -418,60 +377,47 @@ struct JacobiOp {
             set_kappa(d, p, k);
         }
         d.RES[p] = r;
-        return r;
+        res = r;
     }
-};
-
-// ComputeMatrixVecProdFunctionKernel (:758-842) on the CG direction p (p.w = m / rho) and
-// the p . Ap term of the step length (:695-720).
-template <bool REL>
-struct SpmvOp {
-    static constexpr bool kField = true;
-    static constexpr bool kReduce = true;
-    static constexpr int kSlot = 0;
-    struct Own {
-        float4 xi;
-        float3 vi;
-        float cmu, eps2;
-    };
-    using Acc = float3;
-    __device__ static bool active(const SceneDev& S) { return S.cgActive != 0u; }
-    __device__ static float4 field(const Dev& d, uint32_t q) { return d.CP[q]; }
-    __device__ static void load(const Dev& d, uint32_t p, const SceneDev& S, Own& o) {
-        o.xi = d.X[p];
-        o.vi = f3(d.CP[p]);
-        o.cmu = 10.0f * S.dynVisc;
-        o.eps2 = 0.01f * S.h2;
-    }
-    __device__ static void pair(const Dev& d, const Own& o, float4 xq, float4 vq, Acc& acc) {
-        const float3 r = pair_r<REL>(d, o.xi, xq);
-        const float r2 = dot3(r, r);
-        const float gs = grad_factor_r2(d, r2);
-        acc += (__fdividef(o.cmu * vq.w * dot3(o.vi - f3(vq), r), r2 + o.eps2) * gs) * r;
-    }
-    __device__ static float finish(const Dev& d, uint32_t p, const SceneDev& S, const Own& o, Acc acc, uint32_t ncnt) {
-        if (ncnt & kHasBoundaryVisc) acc += mul(load_mat(d.BVM, d.stride, p), o.vi);
-        const float3 ap = o.vi - (S.dt / d.RHO[p]) * acc;
-        d.CAP[p] = f4(ap, 0.0f);
-        return dot_term(o.vi, ap);
-    }
-};
-
-// The tile kernels, one name per pass for profilers.
-template <bool DIV, uint32_t L, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kTileBlock) k_pressure_accel(Dev d) {
-    VFD_COUNT_LAUNCH(d);
-    tile_pass<PressureAccelOp<DIV, REL>, L, G, REL>(d);
+    return res;
 }
-template <bool DIV, uint32_t L, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kTileBlock) k_jacobi_iter(Dev d) {
+
+template <bool DIV, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
     VFD_COUNT_LAUNCH(d);
-    tile_pass<JacobiOp<DIV, REL>, L, G, REL>(d);
+    const Group<G> grp;
+    const uint32_t p = grp.p;
+    const bool inRange = p < d.n && !aborted_p(d);
+    const uint32_t sid = inRange ? scene_of(d, p) : 0u;
+    const SceneDev& S = d.scenes[sid];
+    const bool active = inRange && (DIV ? S.div.active : S.pres.active);
+    float res = 0.0f;
+    if (active) res = jacobi_item<DIV, G, REL>(d, grp, p, S);
+    const float v[1] = {res};
+    const int slot[1] = {0};
+    scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
 }
-template <uint32_t L, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kTileBlock) k_cg_spmv(Dev d) {
+
+// The same for a batch (work list of the loop).
+template <bool DIV, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
-    tile_pass<SpmvOp<REL>, L, G, REL>(d);
+    if (aborted_p(d)) return;
+    const int L = DIV ? kLoopDiv : kLoopPres;
+    BATCH_LOOP(L, G) {
+        const uint32_t vp = base_ + threadIdx.x / G;
+        const bool in = vp < total_;
+        uint32_t sid = 0;
+        const uint32_t p = in ? work_slot(d, L, vp, sid) : 0u;
+        float res = 0.0f;
+        if (in) {
+            const Group<G> grp(p);
+            res = jacobi_item<DIV, G, REL>(d, grp, p, d.scenes[sid]);
+        }
+        const float v[1] = {res};
+        const int slot[1] = {0};
+        scene_accumulate_core<1, G>(d, chunk_scene(d, L, base_, per_, total_), sid, in && threadIdx.x % G == 0u, v, slot);
+    }
 }
 
 // Loop start: the reference's while condition evaluated with error 0, iteration 0
@@ -638,7 +584,7 @@ __global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
     const float4 xi = d.X[p];
     float3 nc = make_float3(0.f, 0.f, 0.f);
     float cc = 0.0f, cf = 0.0f;
-    for_neighbors<G>(grp, nb, p, [&](uint32_t q, uint32_t, bool ok) {
+    for_neighbors<G, false>(grp, nb, p, [&](uint32_t q, float, uint32_t, bool ok) {
         const float4 nj = d.STN[q];
         const float3 dx = pair_r<REL>(d, d.X[q], xi);
         if (ok && nonzero3(nj)) {
@@ -681,6 +627,42 @@ __global__ void __launch_bounds__(kBlock) k_st_blend(Dev d, uint32_t pass) {
 
 // ---------------------------------------------------------------------------
 // Viscosity (Weiler 2018 implicit, block-Jacobi PCG), DFSPHImplementation.cu:577-808.
+struct Mat3 {
+    float3 r0, r1, r2;
+};
+__device__ __forceinline__ float3 mul(const Mat3& m, float3 v) {
+    return make_float3(dot3(m.r0, v), dot3(m.r1, v), dot3(m.r2, v));
+}
+__device__ __forceinline__ void add_outer(Mat3& m, float c, float3 a, float3 b) {  // m += c a b^T
+    m.r0 += (c * a.x) * b;
+    m.r1 += (c * a.y) * b;
+    m.r2 += (c * a.z) * b;
+}
+__device__ __forceinline__ Mat3 load_mat(const float4* M, size_t stride, uint32_t p) {
+    Mat3 m;
+    m.r0 = f3(M[p]);
+    m.r1 = f3(M[stride + p]);
+    m.r2 = f3(M[2 * stride + p]);
+    return m;
+}
+__device__ __forceinline__ void store_mat(float4* M, size_t stride, uint32_t p, const Mat3& m) {
+    M[p] = f4(m.r0, 0.f);
+    M[stride + p] = f4(m.r1, 0.f);
+    M[2 * stride + p] = f4(m.r2, 0.f);
+}
+__device__ __forceinline__ Mat3 inverse3(const Mat3& a) {  // cofactors / determinant
+    const float c00 = a.r1.y * a.r2.z - a.r1.z * a.r2.y;
+    const float c01 = a.r1.z * a.r2.x - a.r1.x * a.r2.z;
+    const float c02 = a.r1.x * a.r2.y - a.r1.y * a.r2.x;
+    const float det = a.r0.x * c00 + a.r0.y * c01 + a.r0.z * c02;
+    const float id = 1.0f / det;
+    Mat3 r;
+    r.r0 = make_float3(c00 * id, (a.r0.z * a.r2.y - a.r0.y * a.r2.z) * id, (a.r0.y * a.r1.z - a.r0.z * a.r1.y) * id);
+    r.r1 = make_float3(c01 * id, (a.r0.x * a.r2.z - a.r0.z * a.r2.x) * id, (a.r0.z * a.r1.x - a.r0.x * a.r1.z) * id);
+    r.r2 = make_float3(c02 * id, (a.r0.y * a.r2.x - a.r0.x * a.r2.y) * id, (a.r0.x * a.r1.y - a.r0.y * a.r1.x) * id);
+    return r;
+}
+
 // K12 ComputeViscosityPreconditionerKernel (:604-684) + K13 ComputeViscosityGradientKernel
 // (:686-756, whose boundary term dots a zero vector: b = v) + the boundary matrix BV of
 // the SpMV's boundary term (:793-839): BV p_i = sum_k c_k (p_i . d_k) gradW_k.
@@ -697,9 +679,8 @@ __global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     Mat3 m = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    for_neighbors<G>(grp, nb, p, [&](uint32_t q, uint32_t, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float3 r = pair_r<REL>(d, xi4, d.X[q]);
-        const float gs = grad_factor(d, r);
         const float rho = d.RHO[q];
         if (!ok) return;
         const float3 g = gs * r;
@@ -765,9 +746,8 @@ __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp,
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    for_neighbors<G>(grp, nb, p, [&](uint32_t q, uint32_t, bool ok) {
+    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
         const float3 r = pair_r<REL>(d, xi, d.X[q]);
-        const float gs = grad_factor(d, r);
         const float4 vq = vec[q];
         const float r2 = dot3(r, r);
         const float3 t = (__fdividef(cmu * vq.w * dot3(vi - f3(vq), r), r2 + eps2) * gs) * r;
@@ -902,11 +882,9 @@ __global__ void k_ctrl_cg1(Dev d) {
     if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
 }
 
-// Loop body 1 from the neighbour rows (Dev::rowLoops): Ap and p . Ap. The adjoint's CG
-// runs the forward CG on a recorded step, whose rows are restored but whose cell tables
-// (and thus tiles and masks) belong to another step.
+// Loop body 1: Ap and p . Ap (:695-720).
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv_rows(Dev d) {
+__global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
     const uint32_t p = grp.p;
@@ -926,6 +904,33 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_rows(Dev d) {
     const float v[1] = {pap};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, valid && grp.lane == 0, v, slot);
+}
+
+// Loop body 1 of a batch.
+template <uint32_t G, bool REL>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    if (aborted_p(d)) return;
+    BATCH_LOOP(kLoopCG, G) {
+        const uint32_t vp = base_ + threadIdx.x / G;
+        const bool in = vp < total_;
+        uint32_t sid = 0;
+        const uint32_t p = in ? work_slot(d, kLoopCG, vp, sid) : 0u;
+        float pap = 0.0f;
+        if (in) {
+            const Group<G> grp(p);
+            const float3 pv = f3(d.CP[p]);
+            const float3 ap = visc_matvec<G, REL>(d, grp, p, d.scenes[sid], d.CP, pv);
+            if (grp.lane == 0) {
+                d.CAP[p] = f4(ap, 0.0f);
+                pap = dot_term(pv, ap);
+            }
+        }
+        const float v[1] = {pap};
+        const int slot[1] = {0};
+        scene_accumulate_core<1, G>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in && threadIdx.x % G == 0u,
+                                 v, slot);
+    }
 }
 
 // alpha = |r . z| / (p . Ap) (:714-720).
@@ -1192,37 +1197,143 @@ __global__ void k_ctrl_end(Dev d) {
     }
 }
 
-// ---------------------------------------------------------------- launchers
-// The instantiation for the position storage mode (K and its _R variant).
-#define VFD_LAUNCH_MODE(LAUNCHER, name, id, K) \
-    do {                                       \
-        if (d.cellRel) LAUNCHER(name, id, K##_R); \
-        else LAUNCHER(name, id, K);           \
-    } while (0)
-#define K_DENSITY(G) k_density_factor<G, false>
-#define K_DENSITY_R(G) k_density_factor<G, true>
-#define K_DENSITY_DIV(G) k_density_factor<G, false, true>
-#define K_DENSITY_DIV_R(G) k_density_factor<G, true, true>
-#define K_DIV_FINISH(G) k_div_finish<G, false>
-#define K_DIV_FINISH_R(G) k_div_finish<G, true>
-#define K_ST_CLASSIFY(G) k_st_classify<G, false>
-#define K_ST_CLASSIFY_R(G) k_st_classify<G, true>
-#define K_ST_SMOOTH(G) k_st_smooth<G, false>
-#define K_ST_SMOOTH_R(G) k_st_smooth<G, true>
-#define K_VISC_PRECOND(G) k_visc_precond<G, false>
-#define K_VISC_PRECOND_R(G) k_visc_precond<G, true>
-#define K_VISC_SETUP(G) k_visc_setup<G, false>
-#define K_VISC_SETUP_R(G) k_visc_setup<G, true>
-#define K_PRES_INIT(G) k_pres_init<G, false>
-#define K_PRES_INIT_R(G) k_pres_init<G, true>
-#define K_PRES_FINISH(G) k_pres_finish<G, false>
-#define K_PRES_FINISH_R(G) k_pres_finish<G, true>
+// ---------------------------------------------------------------------------
+// The solver-loop passes as cell-tile kernels (dfsph_tiles.cuh). Each Op states one
+// pass's pair term and epilogue; the tile loop walks the neighbours (shared-memory halo
+// and masks, or the row for kRowPath particles) and sums the terms over the group.
 
-void launch_density(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY); }
-// K2 + K3 + K4 in one pass, then the divergence loop's start.
-void launch_density_div_init(const Dev& d, cudaStream_t s) {
-    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY_DIV);
-    VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d));
+// K5 DivergenceSolveIterationKernel's force part / K18 (:388-432, :342-386): pressure
+// acceleration a_p = -V sum_j (k_i + k_j) gradW_ij - k_i GB_i (kappa in X.w, or staged
+// with cell-relative positions).
+template <bool DIV, bool REL>
+struct PressureAccelOp {
+    static constexpr bool kField = REL;
+    static constexpr bool kReduce = false;
+    static constexpr int kSlot = 0;
+    struct Own {
+        float4 xi;
+        float ki, V;
+    };
+    using Acc = float3;
+    __device__ static bool active(const SceneDev& S) { return (DIV ? S.div.active : S.pres.active) != 0u; }
+    __device__ static float4 field(const Dev& d, uint32_t q) {
+        return make_float4((DIV ? d.KAPPAV : d.KAPPA)[q], 0.f, 0.f, 0.f);
+    }
+    __device__ static void load(const Dev& d, uint32_t p, const SceneDev& S, Own& o) {
+        o.xi = d.X[p];
+        o.ki = (DIV ? d.KAPPAV : d.KAPPA)[p];
+        o.V = S.volume;
+    }
+    __device__ static void pair(const Dev& d, const Own& o, float4 xq, float4 fq, Acc& a) {
+        const float sum = o.ki + (REL ? fq.x : xq.w);
+        const float3 r = pair_r<REL>(d, o.xi, xq);
+        const float gs = grad_factor(d, r);
+        if (fabsf(sum) > kEps) a += (sum * (-o.V * gs)) * r;
+    }
+    __device__ static float finish(const Dev& d, uint32_t p, const SceneDev&, const Own& o, Acc a, uint32_t ncnt) {
+        if (fabsf(o.ki) > kEps && (ncnt & kHasBoundary)) a += o.ki * (-f3(d.GB[p]));
+        d.AP[p] = f4(a, 0.0f);
+        return 0.0f;
+    }
+};
+
+// K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel
+// (:317-340), each with ComputeDensityPressureForce (:280-315): the density change of
+// the pressure accelerations, the clamped residual, the kappa update, and the residual
+// into the FP64-accurate sum.
+template <bool DIV, bool REL>
+struct JacobiOp {
+    static constexpr bool kField = true;
+    static constexpr bool kReduce = true;
+    static constexpr int kSlot = 0;
+    struct Own {
+        float4 xi;
+        float3 ai;
+    };
+    using Acc = float;
+    __device__ static bool active(const SceneDev& S) { return (DIV ? S.div.active : S.pres.active) != 0u; }
+    __device__ static float4 field(const Dev& d, uint32_t q) { return d.AP[q]; }
+    __device__ static void load(const Dev& d, uint32_t p, const SceneDev&, Own& o) {
+        o.xi = d.X[p];
+        o.ai = f3(d.AP[p]);
+    }
+    __device__ static void pair(const Dev& d, const Own& o, float4 xq, float4 aq, Acc& f) {
+        const float3 r = pair_r<REL>(d, o.xi, xq);
+        const float gs = grad_factor(d, r);
+        f += dot3(o.ai - f3(aq), gs * r);
+    }
+    __device__ static float finish(const Dev& d, uint32_t p, const SceneDev& S, const Own& o, Acc f, uint32_t ncnt) {
+        f *= S.volume;
+        if (ncnt & kHasBoundary) f += dot3(o.ai, f3(d.GB[p]));
+        float r;
+        if (DIV) {
+            f *= S.dt;
+            r = (ncnt & kCountMask) < 20u ? 0.0f : fminf(-d.RHOADV[p] - f, 0.0f);
+            const float k = d.KAPPAV[p] - r * d.ALPHA[p];
+            d.KAPPAV[p] = k;
+            set_kappa(d, p, k);
+        } else {
+            f *= S.dt2;
+            r = fminf(1.0f - d.RHOADV[p] - f, 0.0f);
+            const float k = d.KAPPA[p] - r * d.ALPHA[p];
+            d.KAPPA[p] = k;
+            set_kappa(d, p, k);
+        }
+        d.RES[p] = r;
+        return r;
+    }
+};
+
+// ComputeMatrixVecProdFunctionKernel (:758-842) on the CG direction p (p.w = m / rho) and
+// the p . Ap term of the step length (:695-720).
+template <bool REL>
+struct SpmvOp {
+    static constexpr bool kField = true;
+    static constexpr bool kReduce = true;
+    static constexpr int kSlot = 0;
+    struct Own {
+        float4 xi;
+        float3 vi;
+        float cmu, eps2;
+    };
+    using Acc = float3;
+    __device__ static bool active(const SceneDev& S) { return S.cgActive != 0u; }
+    __device__ static float4 field(const Dev& d, uint32_t q) { return d.CP[q]; }
+    __device__ static void load(const Dev& d, uint32_t p, const SceneDev& S, Own& o) {
+        o.xi = d.X[p];
+        o.vi = f3(d.CP[p]);
+        o.cmu = 10.0f * S.dynVisc;
+        o.eps2 = 0.01f * S.h2;
+    }
+    __device__ static void pair(const Dev& d, const Own& o, float4 xq, float4 vq, Acc& acc) {
+        const float3 r = pair_r<REL>(d, o.xi, xq);
+        const float r2 = dot3(r, r);
+        const float gs = grad_factor_r2(d, r2);
+        acc += (__fdividef(o.cmu * vq.w * dot3(o.vi - f3(vq), r), r2 + o.eps2) * gs) * r;
+    }
+    __device__ static float finish(const Dev& d, uint32_t p, const SceneDev& S, const Own& o, Acc acc, uint32_t ncnt) {
+        if (ncnt & kHasBoundaryVisc) acc += mul(load_mat(d.BVM, d.stride, p), o.vi);
+        const float3 ap = o.vi - (S.dt / d.RHO[p]) * acc;
+        d.CAP[p] = f4(ap, 0.0f);
+        return dot_term(o.vi, ap);
+    }
+};
+
+// The tile kernels, one name per pass for profilers.
+template <bool DIV, uint32_t L, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kTileBlock) k_pressure_accel_tile(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    tile_pass<PressureAccelOp<DIV, REL>, L, G, REL>(d);
+}
+template <bool DIV, uint32_t L, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kTileBlock) k_jacobi_iter_tile(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    tile_pass<JacobiOp<DIV, REL>, L, G, REL>(d);
+}
+template <uint32_t L, uint32_t G, bool REL>
+__global__ void __launch_bounds__(kTileBlock) k_cg_spmv_tile(Dev d) {
+    VFD_COUNT_LAUNCH(d);
+    tile_pass<SpmvOp<REL>, L, G, REL>(d);
 }
 
 // ---------------------------------------------------------------- tile launches
@@ -1267,11 +1378,11 @@ constexpr size_t tile_smem() { return (Op::kField ? 2u : 1u) * TileShape<L>::CAP
 #define VFD_TILE_PREPARE(K, OPT, L) \
     if (e == cudaSuccess) e = prepare_tile<K, tile_smem<OPT, L>()>();
 
-#define FN_PACC_D(L, G, R) k_pressure_accel<true, L, G, R>
-#define FN_PACC_P(L, G, R) k_pressure_accel<false, L, G, R>
-#define FN_JAC_D(L, G, R) k_jacobi_iter<true, L, G, R>
-#define FN_JAC_P(L, G, R) k_jacobi_iter<false, L, G, R>
-#define FN_SPMV(L, G, R) k_cg_spmv<L, G, R>
+#define FN_PACC_D(L, G, R) k_pressure_accel_tile<true, L, G, R>
+#define FN_PACC_P(L, G, R) k_pressure_accel_tile<false, L, G, R>
+#define FN_JAC_D(L, G, R) k_jacobi_iter_tile<true, L, G, R>
+#define FN_JAC_P(L, G, R) k_jacobi_iter_tile<false, L, G, R>
+#define FN_SPMV(L, G, R) k_cg_spmv_tile<L, G, R>
 #define OP_PACC_D(R) PressureAccelOp<true, R>
 #define OP_PACC_P(R) PressureAccelOp<false, R>
 #define OP_JAC_D(R) JacobiOp<true, R>
@@ -1316,12 +1427,74 @@ cudaError_t prepare_tile_kernels() {
         }                                                                                     \
     } while (0)
 
-// The solver-loop passes run as cell-tile kernels for single scenes and batches alike
-// (tiles of scenes that stopped iterating are skipped); batches keep their work lists
-// for the CG's element-wise kernels.
+
+// ---------------------------------------------------------------- launchers
+// The instantiation for the position storage mode (K and its _R variant).
+#define VFD_LAUNCH_MODE(LAUNCHER, name, id, K) \
+    do {                                       \
+        if (d.cellRel) LAUNCHER(name, id, K##_R); \
+        else LAUNCHER(name, id, K);           \
+    } while (0)
+#define K_DENSITY(G) k_density_factor<G, false>
+#define K_DENSITY_R(G) k_density_factor<G, true>
+#define K_DENSITY_DIV(G) k_density_factor<G, false, true>
+#define K_DENSITY_DIV_R(G) k_density_factor<G, true, true>
+#define K_PACCEL_D(G) k_pressure_accel<true, G, false>
+#define K_PACCEL_D_R(G) k_pressure_accel<true, G, true>
+#define K_PACCEL_P(G) k_pressure_accel<false, G, false>
+#define K_PACCEL_P_R(G) k_pressure_accel<false, G, true>
+#define K_JACOBI_D(G) k_jacobi_iter<true, G, false>
+#define K_JACOBI_D_R(G) k_jacobi_iter<true, G, true>
+#define K_JACOBI_P(G) k_jacobi_iter<false, G, false>
+#define K_JACOBI_P_R(G) k_jacobi_iter<false, G, true>
+#define K_DIV_FINISH(G) k_div_finish<G, false>
+#define K_DIV_FINISH_R(G) k_div_finish<G, true>
+#define K_ST_CLASSIFY(G) k_st_classify<G, false>
+#define K_ST_CLASSIFY_R(G) k_st_classify<G, true>
+#define K_ST_SMOOTH(G) k_st_smooth<G, false>
+#define K_ST_SMOOTH_R(G) k_st_smooth<G, true>
+#define K_VISC_PRECOND(G) k_visc_precond<G, false>
+#define K_VISC_PRECOND_R(G) k_visc_precond<G, true>
+#define K_VISC_SETUP(G) k_visc_setup<G, false>
+#define K_VISC_SETUP_R(G) k_visc_setup<G, true>
+#define K_SPMV(G) k_cg_spmv<G, false>
+#define K_SPMV_R(G) k_cg_spmv<G, true>
+#define K_PRES_INIT(G) k_pres_init<G, false>
+#define K_PRES_INIT_R(G) k_pres_init<G, true>
+#define K_PRES_FINISH(G) k_pres_finish<G, false>
+#define K_PRES_FINISH_R(G) k_pres_finish<G, true>
+
+void launch_density(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY); }
+// K2 + K3 + K4 in one pass, then the divergence loop's start.
+void launch_density_div_init(const Dev& d, cudaStream_t s) {
+    VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_density_factor", kTDensity, K_DENSITY_DIV);
+    VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<true><<<1, 256, 0, s>>>(d));
+}
+#define K_PACCEL_DB(G) k_pressure_accel_b<true, G, false>
+#define K_PACCEL_DB_R(G) k_pressure_accel_b<true, G, true>
+#define K_PACCEL_PB(G) k_pressure_accel_b<false, G, false>
+#define K_PACCEL_PB_R(G) k_pressure_accel_b<false, G, true>
+#define K_JACOBI_DB(G) k_jacobi_iter_b<true, G, false>
+#define K_JACOBI_DB_R(G) k_jacobi_iter_b<true, G, true>
+#define K_JACOBI_PB(G) k_jacobi_iter_b<false, G, false>
+#define K_JACOBI_PB_R(G) k_jacobi_iter_b<false, G, true>
+#define K_SPMV_B(G) k_cg_spmv_b<G, false>
+#define K_SPMV_B_R(G) k_cg_spmv_b<G, true>
+
+// Whether a solver-loop pass runs on cell tiles (vfd_set_tiles / the autotuner) rather
+// than the neighbour rows; the adjoint's CG always walks rows (Dev::rowLoops).
+inline bool tiled(const Dev& d, int id) { return d.tiles[id] != 0u && d.compactRows && !d.rowLoops; }
+
+// Row path: batches run the solver-loop kernels over their work lists (the scenes still
+// iterating) with a fixed grid; a single scene keeps one group per particle. Tile path:
+// single scenes and batches alike (tiles of scenes that stopped iterating are skipped).
 void launch_div_iter(const Dev& d, cudaStream_t s) {
-    VFD_TILE_DISPATCH("k_pressure_accel", kTPAccel, FN_PACC_D, OP_PACC_D);
-    VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_D, OP_JAC_D);
+    if (tiled(d, kTPAccel)) VFD_TILE_DISPATCH("k_pressure_accel", kTPAccel, FN_PACC_D, OP_PACC_D);
+    else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_pressure_accel", kTPAccel, K_PACCEL_DB);
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_D);
+    if (tiled(d, kTJacobi)) VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_D, OP_JAC_D);
+    else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_DB);
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_D);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
 }
 void launch_div_finish(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_div_finish", kTDivFinish, K_DIV_FINISH); }
@@ -1338,11 +1511,10 @@ void launch_visc_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_cg_p0", s, k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_ctrl_cg1", s, k_ctrl_cg1<<<1, 256, 0, s>>>(d));
 }
-#define K_SPMV_ROWS(G) k_cg_spmv_rows<G, false>
-#define K_SPMV_ROWS_R(G) k_cg_spmv_rows<G, true>
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
-    if (d.rowLoops) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV_ROWS);
-    else VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
+    if (tiled(d, kTSpmv)) VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
+    else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_cg_spmv", kTSpmv, K_SPMV_B);
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV);
     VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     if (d.nscenes > 1) {
         VFD_LAUNCH("k_cg_update", s, k_cg_update_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
@@ -1364,8 +1536,12 @@ void launch_pres_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_ctrl_jacobi_init", s, k_ctrl_jacobi_init<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_iter(const Dev& d, cudaStream_t s) {
-    VFD_TILE_DISPATCH("k_pressure_accel", kTPAccel, FN_PACC_P, OP_PACC_P);
-    VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_P, OP_JAC_P);
+    if (tiled(d, kTPAccel)) VFD_TILE_DISPATCH("k_pressure_accel", kTPAccel, FN_PACC_P, OP_PACC_P);
+    else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_pressure_accel", kTPAccel, K_PACCEL_PB);
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_P);
+    if (tiled(d, kTJacobi)) VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_P, OP_JAC_P);
+    else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_PB);
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_P);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_finish(const Dev& d, cudaStream_t s) {

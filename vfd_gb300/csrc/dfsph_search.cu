@@ -349,9 +349,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbors(Dev d) {
         // x-run w (lanes 3w, 3w + 1, 3w + 2): its candidate total decides whether masks fit
         const uint32_t runEnd = __shfl_sync(0xffffffffu, incl, min(3u * lane + 2u, 31u));
         const uint32_t runBeg = __shfl_sync(0xffffffffu, excl, min(3u * lane, 31u));
-        const bool compact = d.NBRC != nullptr &&
-                             !__any_sync(0xffffffffu, lane < 9u && runEnd - runBeg > kRunMax);
-        const uint32_t rowFlag = (d.NBRC != nullptr && !compact) ? kRowPath : 0u;
+        const bool want = d.NBRC != nullptr && d.compactRows != 0u;
+        const bool compact = want && !__any_sync(0xffffffffu, lane < 9u && runEnd - runBeg > kRunMax);
+        const uint32_t rowFlag = (want && !compact) ? kRowPath : 0u;
         uint32_t mx = 0u;
         for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
             const uint32_t kk = min(32u, cnt - k0);

@@ -31,6 +31,10 @@ void launch_pres_iter(const Dev& d, cudaStream_t s);
 void launch_pres_finish(const Dev& d, cudaStream_t s);
 // Occupancy and shared-memory limits of the cell-tile kernels (once, before any capture).
 cudaError_t prepare_tile_kernels();
+// Whether any solver-loop pass runs on cell tiles (then the search writes NBRC rows).
+inline bool uses_tiles(const uint8_t* tiles) {
+    return tiles[kTPAccel] != 0 || tiles[kTJacobi] != 0 || tiles[kTSpmv] != 0;
+}
 void box_map_sizes(const uint32_t res[3], uint32_t& nodes, uint32_t& cells);
 int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, float padding, const uint32_t res[3],
                       float r, const float* table, float wZero, float invStep, float* nodes, uint32_t* cells,
@@ -164,8 +168,9 @@ struct vfd_sim {
     bool analyticKernel = false;  // VFD_KERNEL_ANALYTIC
     bool graphFailed = false;
     uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
-    // cell tiles of the solver-loop kernels per TunedKernel: log2 of the cells in a tile
-    uint8_t tiles[16] = {3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3};
+    // cell tiles of the solver-loop kernels per TunedKernel: 0 = neighbour rows, else log2
+    // of the cells in a tile (vfd_set_tiles, vfd_autotune)
+    uint8_t tiles[16] = {};
 
     // layout
     bool allocated = false, uploaded = false;
