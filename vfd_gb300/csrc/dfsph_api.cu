@@ -52,6 +52,15 @@ __global__ void k_export1(const uint32_t* pid, const float* src, const float4* s
     if (o >= count) return;
     out[o] = src4 ? (&src4[p].x)[comp] : src[p];
 }
+// Sets *bad when any of the n values is not finite (inputs checked on the device after
+// their copy, before they are imported).
+__global__ void k_check_finite(const float* a, size_t n, uint32_t* bad) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (!isfinite(a[i])) {
+            *bad = 1u;
+            return;
+        }
+}
 // Original-order import into a float4 field (w kept).
 __global__ void k_import3(const uint32_t* pid, const float* in, float4* dst, uint32_t begin, uint32_t count) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,6 +349,7 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &s->dBodies, std::max<uint32_t>(1u, bodyTotal)));
     TRY(dalloc(s, &s->dStatus, 16));
     TRY(dalloc(s, &s->dStage, 3 * st));
+    TRY(dalloc(s, &s->dStage2, 3 * st));
     TRY(dalloc(s, &base.ACCB, (size_t)base.nscenes * kAccSlots * kBuckets * 16u));
     TRY(dalloc(s, &base.MAXB, (size_t)base.nscenes * 2u * kBuckets * 32u));
     TRY(dalloc(s, &base.MMB, (size_t)base.nscenes * 6u * kBuckets * 32u));
@@ -1423,13 +1433,32 @@ int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
     TRY(check_sim(s));
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
-    const size_t cnt3 = 3 * (size_t)s->scenes[0].count();
-    for (size_t i = 0; i < cnt3; i++)
-        if ((x && !std::isfinite(x[i])) || (v && !std::isfinite(v[i])))
-            return fail(VFD_E_NAN, "non-finite input at element %zu", i);
+    const uint32_t cnt = s->scenes[0].count();
+    if (cnt == 0) return VFD_OK;
+    const size_t bytes = sizeof(float) * 3 * (size_t)cnt;
+    // both arrays are copied and checked on the device before either is imported
+    uint32_t* bad = s->dStatus + 10;
+    CK(cudaMemsetAsync(bad, 0, sizeof(uint32_t), s->stream));
+    if (x) {
+        CK(cudaMemcpyAsync(s->dStage, x, bytes, cudaMemcpyHostToDevice, s->stream));
+        k_check_finite<<<blocks_for(3 * cnt, 256), 256, 0, s->stream>>>(s->dStage, 3 * (size_t)cnt, bad);
+    }
+    if (v) {
+        CK(cudaMemcpyAsync(s->dStage2, v, bytes, cudaMemcpyHostToDevice, s->stream));
+        k_check_finite<<<blocks_for(3 * cnt, 256), 256, 0, s->stream>>>(s->dStage2, 3 * (size_t)cnt, bad);
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(s->hStatus + 10, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (s->hStatus[10]) return fail(VFD_E_NAN, "non-finite input");
     const Dev& d = s->dev[s->cs];
-    if (x) TRY(gather_pos(s, 0, x, d.XN));
-    if (v) TRY(gather_vec(s, 0, v, d.Vc));
+    const uint32_t b = s->sceneBegin[0];
+    if (x) {
+        if (s->cellRel) k_import_pos<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d, s->dStage, d.XN, b, cnt);
+        else k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d.PIDc, s->dStage, d.XN, b, cnt);
+    }
+    if (v) k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d.PIDc, s->dStage2, d.Vc, b, cnt);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }

@@ -182,6 +182,7 @@ struct vfd_sim {
     int cs = 0;  // set holding the current carried state
     float4* XB = nullptr;
     float* dStage = nullptr;     // 3 floats per particle, original order
+    float* dStage2 = nullptr;    // a second one (velocities beside positions in vfd_set_state)
     vfd::SceneDev* dScenes = nullptr;
     vfd::BodyDev* dBodies = nullptr;
     uint32_t* dStatus = nullptr;
