@@ -398,6 +398,57 @@ def jet_form(V, scenes, steps: int = 8, warmup: int = 2):
     return out
 
 
+def fp64_precision_form(V, scenes, steps: int = 10, pool=(400, 50, 400)):
+    """Precision of the FP32 step against the FP64 GPU path on the jet-coiling scene: the
+    8M-particle pool with the jet column already flowing (no emitter, so all modes keep
+    the same particles), `steps` steps each of FP64 (vfd_set_precision), FP32 absolute and
+    FP32 cell-relative positions, and the FP32 modes again with the scene translated by
+    (1000, 200, -300) m. Per step: the mean density error at the pressure solve's exit
+    (-rho0 sum(res)/N, % of rho0) of every mode; after the last step: each FP32 mode's
+    position difference from the FP64 trajectory (translated back), and the step rate.
+    Surface tension as in the jet form (sigma scaled by (r / 25 mm)^3)."""
+    out = {}
+    far = np.array([1000.0, 200.0, -300.0])
+    ref = None
+    for mode, offset in (("fp64", None), ("fp32_absolute", None), ("fp32_cell_relative", None),
+                         ("fp32_absolute_far", far), ("fp32_cell_relative_far", far)):
+        s = scenes.jet_column_8m(pool=pool, offset=(0.0, 0.0, 0.0) if offset is None else tuple(offset))
+        r = s["desc"]["ParticleRadius"]
+        s["desc"]["SurfaceTension"] = 0.07 * (r / 0.025) ** 3
+        sim = V.scene_simulation(s)
+        if mode == "fp64":
+            sim.SetPrecision(True)
+        elif "cell_relative" in mode:
+            sim.SetPositionMode(True)
+            sim.SetFluidObjects(s["x"], s["v"])
+        errs, its = [], []
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            st = sim.OnUpdate()
+            errs.append(100.0 * st["PressureSolverError"] / 1000.0)
+            its.append([st["DivergenceSolverIterationCount"], st["PressureSolverIterationCount"],
+                        st["ViscositySolverIterationCount"]])
+        el = time.perf_counter() - t0
+        n = len(s["x"])
+        if mode == "fp64":
+            ref, _ = sim.GetStateF64()
+            rec = {}
+        else:
+            x, _, _ = sim.GetState()
+            e = np.linalg.norm(x.astype(np.float64) - (far if offset is not None else 0.0) - ref, axis=1)
+            rec = {"mean_position_error_m": float(e.mean()), "max_position_error_m": float(e.max()),
+                   "p99_position_error_m": float(np.quantile(e, 0.99))}
+        rec.update({"particle_steps_per_s": n * steps / el, "mean_density_error_pct_per_step": errs,
+                    "iterations_per_step": its})
+        out[mode] = rec
+        sim.close()
+        del sim
+    out["workload"] = (f"jet column onto a pool: {n} particles (pool {pool[0]}x{pool[1]}x{pool[2]}, r = 1.5 mm), "
+                       f"{steps} steps per mode; FP32 modes against the FP64 GPU path, also translated by "
+                       f"(1000, 200, -300) m")
+    return out
+
+
 def legacy_sph_form(steps: int = 100, warmup: int = 5):
     """The reference's legacy SPH pipeline (vfd_sph_*): a 100^3 block (1M particles,
     r = 4 mm, h = 1 cm) falling in a 1.6 x 1.2 x 1.6 m world box, `steps` steps with the
@@ -607,6 +658,10 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched-scene measurement")
     ap.add_argument("--no-jet", action="store_true", help="skip the 8M-particle jet-coiling form")
     ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--precision-steps", type=int, default=5,
+                    help="steps per mode of the FP64-vs-FP32 precision form on the 8M jet scene")
+    ap.add_argument("--precision-only", action="store_true",
+                    help="run only the FP64-vs-FP32 precision form (with --precision-steps) and print its JSON")
     ap.add_argument("--eager", action="store_true",
                     help="launch the timed steps kernel by kernel instead of as CUDA graphs (same kernels, same "
                          "results); profilers cannot see the kernels inside graphs with conditional nodes")
@@ -630,6 +685,12 @@ def main():
         return profile_case(args)
     if args.dry_run:
         return dry_run(args)
+    if args.precision_only:
+        import vfd_gb300 as V
+        from vfd_gb300 import scenes
+        V.lib().vfd_set_device(0)
+        print(json.dumps({"fp64_precision": fp64_precision_form(V, scenes, args.precision_steps)}), flush=True)
+        return
 
     import torch
     import torch.distributed as dist
@@ -764,6 +825,7 @@ def main():
             line["forms"]["precision"] = precision_form(V, scenes)
             if not args.no_jet:
                 line["forms"]["jet_8m"] = jet_form(V, scenes)
+                line["forms"]["fp64_precision"] = fp64_precision_form(V, scenes, args.precision_steps)
             line["forms"]["legacy_sph"] = legacy_sph_form()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, el, nc, cores = cpu_baseline(40, args.cpu_steps, 2)

@@ -54,6 +54,10 @@ enum {
 #define VFD_POSITIONS_ABSOLUTE       0  /* FP32 absolute coordinates, as the reference stores them */
 #define VFD_POSITIONS_CELL_RELATIVE  1  /* FP32 offsets within anchor cells of edge h             */
 
+/* Arithmetic of the step (vfd_set_precision). */
+#define VFD_PRECISION_FP32  0  /* FP32 state and neighbour sums, FP64 reductions (the default) */
+#define VFD_PRECISION_FP64  1  /* the whole step in FP64 on the GPU (a reference trajectory)   */
+
 /* SPH kernel evaluation modes (vfd_set_kernel_mode). */
 #define VFD_KERNEL_TABLE     0  /* midpoint of two 10000-entry table values, as the reference */
 #define VFD_KERNEL_ANALYTIC  1  /* the cubic spline evaluated at |r| (smooth in r)            */
@@ -510,6 +514,23 @@ int vfd_set_position_mode(vfd_sim* sim, int32_t mode);
  * vfd_set_position_mode it drops the device state.
  */
 int vfd_set_kernel_mode(vfd_sim* sim, int32_t mode);
+
+/*
+ * Arithmetic of the step. No counterpart in the reference, whose step is FP32 throughout.
+ * VFD_PRECISION_FP64 runs the whole step -- search, boundary, density, the three solves,
+ * surface tension, CFL step, integration -- in double precision on the GPU, one thread per
+ * particle with the solver loops driven from the host: the reference trajectory against
+ * which the FP32 paths (absolute and cell-relative positions) are measured on scenes of
+ * millions of particles. Single scene; restarts the simulation from its fluid objects.
+ * In FP64 mode vfd_step / vfd_steps / vfd_get_state / vfd_get_debug_info and
+ * vfd_get_field(VFD_FIELD_DENSITY) work as usual (values rounded to float), and
+ * vfd_get_state_f64 returns the double positions and velocities (n*3 doubles each, original
+ * order, either may be NULL); the calls that act on the FP32 state (vfd_set_state,
+ * checkpoints, vfd_emit, vfd_simulate, the adjoint, the profiler and autotuner,
+ * vfd_find_neighbors) return VFD_E_STATE.
+ */
+int vfd_set_precision(vfd_sim* sim, int32_t mode);
+int vfd_get_state_f64(vfd_sim* sim, double* x, double* v);
 
 /*
  * Appends `count` particles (xyz, and velocities or NULL for zero) to the running state

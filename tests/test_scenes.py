@@ -50,3 +50,16 @@ def test_config4_viscous_drop():
     assert np.linalg.norm(x - c, axis=1).max() <= 0.1 + 0.01  # a sphere of radius 0.1 m
     assert abs(np.linalg.norm(v, axis=1).max() - 0.5) < 1e-6  # Fourier modes scaled to 0.5 m/s
     assert np.array_equal(scenes.viscous_drop_33k()["v"], s["v"])
+
+
+def test_jet_column_scene_has_pool_and_falling_column():
+    s = scenes.jet_column_8m(pool=(20, 5, 20))
+    pool = scenes.jet_coiling_8m(pool=(20, 5, 20))
+    n0 = len(pool["x"])
+    assert len(s["x"]) > n0
+    np.testing.assert_array_equal(s["x"][:n0], pool["x"])
+    col = s["x"][n0:]
+    assert np.all(s["v"][n0:, 1] == -1.0) and np.all(s["v"][:n0] == 0.0)
+    assert col[:, 1].max() <= 0.5 + 1e-6 and col[:, 1].min() > pool["x"][:, 1].max()
+    far = scenes.jet_column_8m(pool=(20, 5, 20), offset=(1000.0, 0.0, 0.0))
+    np.testing.assert_allclose(far["x"][:, 0] - 1000.0, s["x"][:, 0], atol=1e-3)

@@ -36,7 +36,7 @@ EXPORTS = [
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
     "vfd_emit", "vfd_get_graph_mode", "vfd_checkpoint_size", "vfd_checkpoint", "vfd_restore",
-    "vfd_set_tiles", "vfd_get_tiles",
+    "vfd_set_tiles", "vfd_get_tiles", "vfd_set_precision", "vfd_get_state_f64",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -120,6 +120,8 @@ def lib() -> C.CDLL:
                 "vfd_set_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_get_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_set_tiles": [P, C.POINTER(C.c_uint8), C.c_uint32],
+                "vfd_set_precision": [P, C.c_int32],
+                "vfd_get_state_f64": [P, C.POINTER(C.c_double), C.POINTER(C.c_double)],
                 "vfd_get_tiles": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_autotune": [P, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_find_neighbors_noalloc": [C.c_void_p, C.c_uint32, C.c_float, C.c_void_p, C.c_void_p,
@@ -540,6 +542,20 @@ class DFSPHSimulation:
         arr = (C.c_uint8 * 16)()
         _check(lib().vfd_get_lanes(self._h, arr, 16), "vfd_get_lanes")
         return list(arr)[:len(TUNED_KERNELS)]
+
+    def SetPrecision(self, fp64: bool):
+        """FP64 (the whole step in double on the GPU, a reference trajectory) or the
+        default FP32 step; restarts from the fluid objects."""
+        _check(lib().vfd_set_precision(self._h, 1 if fp64 else 0), "vfd_set_precision")
+
+    def GetStateF64(self):
+        """Positions and velocities of the FP64 path as float64 arrays (n, 3)."""
+        n = self._n(0)
+        x = np.zeros((n, 3), np.float64)
+        v = np.zeros((n, 3), np.float64)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        _check(lib().vfd_get_state_f64(self._h, dp(x), dp(v)), "vfd_get_state_f64")
+        return x, v
 
     def SetTiles(self, tiles):
         """Per solver-loop pass, in TUNED_KERNELS order: 0 = walk neighbour rows, 3 or 4 =

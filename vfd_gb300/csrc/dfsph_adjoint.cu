@@ -1257,6 +1257,7 @@ extern "C" {
 
 int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, vfd_step_stats* stats) {
     if (!s) return fail(VFD_E_ARG, "null handle");
+    if (s->fp64Mode) return fail(VFD_E_STATE, "the adjoint differentiates the FP32 step (VFD_PRECISION_FP32)");
     if (steps == 0 || checkpoint_every == 0) return fail(VFD_E_ARG, "adjoint: steps and checkpoint_every must be positive");
     TRY(check_adjoint_scene(s));
     TRY(ensure_ready(s));

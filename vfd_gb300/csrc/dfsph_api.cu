@@ -558,6 +558,7 @@ int upload(vfd_sim* s) {
     CK(cudaDeviceSynchronize());
     s->uploaded = true;
     s->generation++;
+    if (s->fp64Mode) TRY(fp64_upload(s));
     return VFD_OK;
 }
 
@@ -825,6 +826,10 @@ int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
     if (!s) return fail(VFD_E_ARG, "null handle");
     TRY(ensure_ready(s));
     if (s->n == 0) return VFD_OK;
+    if (s->fp64Mode) {  // the FP64 path steps synchronously
+        for (uint32_t k = 0; k < count; k++) TRY(fp64_step(s, stats));
+        return VFD_OK;
+    }
     uint32_t remaining = count;
     for (int attempt = 0; remaining > 0 && attempt < 16; attempt++) {
         const int cs0 = s->cs;
@@ -1279,6 +1284,7 @@ int vfd_set_position_mode(vfd_sim* s, int32_t mode) {
 
 int vfd_emit(vfd_sim* s, const float* xyz, const float* vel, uint32_t count) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_emit is not available in the FP64 path");
     if (s->scenes.size() != 1) return fail(VFD_E_ARG, "vfd_emit adds to single-scene simulations");
     if (count == 0) return VFD_OK;
     if (!xyz) return fail(VFD_E_ARG, "null positions");
@@ -1360,6 +1366,26 @@ int vfd_set_kernel_mode(vfd_sim* s, int32_t mode) {
     return VFD_OK;
 }
 
+int vfd_set_precision(vfd_sim* s, int32_t mode) {
+    TRY(check_sim(s));
+    if (mode != VFD_PRECISION_FP32 && mode != VFD_PRECISION_FP64) return fail(VFD_E_ARG, "unknown precision %d", mode);
+    if (mode == VFD_PRECISION_FP64 && s->scenes.size() != 1)
+        return fail(VFD_E_STATE, "the FP64 path runs single-scene simulations");
+    CK(cudaSetDevice(s->device));
+    s->fp64Mode = mode == VFD_PRECISION_FP64;
+    fp64_release(s);
+    s->uploaded = false;  // the next call restarts from the fluid objects in the chosen precision
+    return VFD_OK;
+}
+
+int vfd_get_state_f64(vfd_sim* s, double* x, double* v) {
+    TRY(check_sim(s));
+    if (!s->fp64Mode) return fail(VFD_E_STATE, "vfd_get_state_f64 needs VFD_PRECISION_FP64");
+    CK(cudaSetDevice(s->device));
+    TRY(ensure_ready(s));
+    return fp64_get_state(s, x, v, nullptr, nullptr, nullptr);
+}
+
 int vfd_set_graph_mode(vfd_sim* s, int32_t enabled) {
     TRY(check_sim(s));
     s->graphMode = enabled != 0;
@@ -1404,6 +1430,10 @@ int vfd_synchronize(vfd_sim* s, vfd_step_stats* stats) {
     TRY(check_sim(s));
     CK(cudaSetDevice(s->device));
     if (!s->uploaded) return VFD_OK;
+    if (s->fp64Mode) {
+        if (stats) fp64_stats(s, stats);
+        return VFD_OK;
+    }
     uint32_t flags = 0;
     TRY(finish_steps(s, stats, flags));
     CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), s->stream));
@@ -1422,6 +1452,7 @@ int vfd_scene_get_state(vfd_sim* s, uint32_t scene, float* x, float* v, float* a
     if (scene >= s->scenes.size()) return fail(VFD_E_ARG, "scene %u out of range", scene);
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
+    if (s->fp64Mode) return fp64_get_state(s, nullptr, nullptr, x, v, a);
     const Dev& d = s->dev[s->cs];
     if (x) TRY(scatter_pos(s, scene, d.XN, d.XN, x));
     if (v) TRY(scatter_vec(s, scene, d.Vc, v));
@@ -1431,6 +1462,7 @@ int vfd_scene_get_state(vfd_sim* s, uint32_t scene, float* x, float* v, float* a
 
 int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_set_state is not available in the FP64 path");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     const uint32_t cnt = s->scenes[0].count();
@@ -1484,6 +1516,7 @@ uint64_t checkpoint_bytes(const vfd_sim* s) {
 
 int vfd_checkpoint_size(vfd_sim* s, uint64_t* bytes) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_checkpoint is not available in the FP64 path");
     if (!bytes) return fail(VFD_E_ARG, "null output");
     TRY(ensure_ready(s));
     *bytes = checkpoint_bytes(s);
@@ -1492,6 +1525,7 @@ int vfd_checkpoint_size(vfd_sim* s, uint64_t* bytes) {
 
 int vfd_checkpoint(vfd_sim* s, void* buffer, uint64_t bytes) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_checkpoint is not available in the FP64 path");
     if (!buffer) return fail(VFD_E_ARG, "null buffer");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
@@ -1528,6 +1562,7 @@ int vfd_checkpoint(vfd_sim* s, void* buffer, uint64_t bytes) {
 
 int vfd_restore(vfd_sim* s, const void* buffer, uint64_t bytes) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_restore is not available in the FP64 path");
     if (!buffer) return fail(VFD_E_ARG, "null buffer");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
@@ -1592,6 +1627,10 @@ int vfd_get_field(vfd_sim* s, int32_t field, uint32_t body, float* out) {
     if (!out) return fail(VFD_E_ARG, "null output");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
+    if (s->fp64Mode) {
+        if (field == VFD_FIELD_DENSITY) return fp64_get_density(s, out);
+        return fail(VFD_E_STATE, "the FP64 path exports positions, velocities, accelerations and densities");
+    }
     CK(cudaStreamSynchronize(s->stream));
     const Dev& d = s->dev[s->cs];
     const uint32_t cnt = s->scenes[0].count();
@@ -1622,6 +1661,7 @@ int vfd_get_field(vfd_sim* s, int32_t field, uint32_t body, float* out) {
 
 int vfd_find_neighbors(vfd_sim* s) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_find_neighbors is not available in the FP64 path");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     if (s->n == 0) return VFD_OK;
@@ -1739,6 +1779,10 @@ int vfd_scene_get_stats(vfd_sim* s, uint32_t scene, vfd_step_stats* st) {
     CK(cudaSetDevice(s->device));
     std::memset(st, 0, sizeof(*st));
     if (!s->uploaded) return VFD_OK;
+    if (s->fp64Mode) {
+        fp64_stats(s, st);
+        return VFD_OK;
+    }
     CK(cudaStreamSynchronize(s->stream));
     SceneDev S;
     CK(cudaMemcpy(&S, s->dScenes + scene, sizeof(SceneDev), cudaMemcpyDeviceToHost));
@@ -1815,6 +1859,7 @@ struct FramePipe {
 // the calling thread, in frame order, once its copy has landed.
 int vfd_simulate(vfd_sim* s, vfd_frame_callback cb, void* user) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_simulate is not available in the FP64 path");
     if (s->scenes.size() != 1) return fail(VFD_E_ARG, "vfd_simulate runs single-scene simulations");
     CK(cudaSetDevice(s->device));
     TRY(upload(s));
@@ -1927,6 +1972,7 @@ int vfd_simulate(vfd_sim* s, vfd_frame_callback cb, void* user) {
 
 int vfd_profile_kernels(vfd_sim* s, uint32_t steps, vfd_kernel_time* out, uint32_t capacity, uint32_t* count) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_profile_kernels is not available in the FP64 path");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     if (count) *count = 0;
@@ -2008,6 +2054,7 @@ int vfd_get_tiles(const vfd_sim* s, uint8_t* tiles, uint32_t count) {
 
 int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count) {
     TRY(check_sim(s));
+    if (s->fp64Mode) return fail(VFD_E_STATE, "vfd_autotune is not available in the FP64 path");
     CK(cudaSetDevice(s->device));
     TRY(ensure_ready(s));
     if (s->n == 0 || steps == 0) return VFD_OK;

@@ -155,6 +155,15 @@ struct SceneHost {
 namespace vfd {
 struct AdjointState;
 void adjoint_release(vfd_sim* s);  // frees the recorded forward run of the adjoint
+// The FP64 GPU path (vfd_set_precision): its state, built from the scene's initial
+// particles at upload, one step, and its outputs.
+struct Fp64State;
+int fp64_upload(vfd_sim* s);
+int fp64_step(vfd_sim* s, vfd_step_stats* out);
+int fp64_get_state(vfd_sim* s, double* x, double* v, float* xf, float* vf, float* af);
+int fp64_get_density(vfd_sim* s, float* out);
+void fp64_stats(const vfd_sim* s, vfd_step_stats* out);
+void fp64_release(vfd_sim* s);
 }  // namespace vfd
 
 struct vfd_sim {
@@ -166,6 +175,8 @@ struct vfd_sim {
     bool graphMode = true;
     bool cellRel = false;  // VFD_POSITIONS_CELL_RELATIVE
     bool analyticKernel = false;  // VFD_KERNEL_ANALYTIC
+    bool fp64Mode = false;        // VFD_PRECISION_FP64: steps run the FP64 GPU path
+    vfd::Fp64State* fp64 = nullptr;
     bool graphFailed = false;
     uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
     // cell tiles of the solver-loop kernels per TunedKernel: 0 = neighbour rows, else log2
@@ -239,6 +250,7 @@ struct vfd_sim {
     }
     void release() {
         vfd::adjoint_release(this);
+        vfd::fp64_release(this);
         releaseBuffers();
         for (auto& s : scenes)
             for (auto& b : s.bodies) b.release();

@@ -250,3 +250,24 @@ def small_dam_break(n_side: int = 12, r: float = 0.025, viscosity: float = 0.0, 
                 SurfaceTension=surface_tension, MaxViscositySolverError=0.01, **SOLVER)
     return dict(name=f"small_dam_break_{len(x)}", x=x, v=np.zeros_like(x), desc=desc,
                 boxes=[container((0, 0, 0), box, r, map_resolution)])
+
+
+def jet_column_8m(pool=(400, 50, 400), r: float = 0.0015, offset=(0.0, 0.0, 0.0), seed: int | None = None) -> dict:
+    """The jet-coiling scene with its jet already flowing: the resting pool of
+    jet_coiling_8m plus the column the inflow would have emitted, disk layers of spacing
+    2r from the inflow disk (0.5 m) down to 4r above the pool, moving at the inflow
+    velocity (1 m/s down). It needs no emitter, so every arithmetic mode (FP32 absolute,
+    FP32 cell-relative, FP64) starts from the same particles and keeps them. `offset`
+    translates the whole scene (boxes included)."""
+    from .emitter import InflowEmitter
+    s = jet_coiling_8m(pool=pool, r=r, seed=seed)
+    f = s["inflow"]
+    em = InflowEmitter(f["center"], f["direction"], f["radius"], f["speed"], r)
+    top = float(s["x"][:, 1].max()) + 4.0 * r
+    layers = int((f["center"][1] - top) / (2.0 * r))
+    xs, vs = zip(*(em.layer(k * 2.0 * r) for k in range(layers)))
+    off = np.asarray(offset, np.float64)
+    x = (np.concatenate([s["x"], *xs]).astype(np.float64) + off).astype(np.float32)
+    v = np.concatenate([s["v"], *vs]).astype(np.float32)
+    boxes = [dict(b, min=tuple(np.asarray(b["min"]) + off), max=tuple(np.asarray(b["max"]) + off)) for b in s["boxes"]]
+    return dict(s, name=f"jet_column_{len(x)}", x=x, v=v, boxes=boxes)
