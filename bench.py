@@ -402,21 +402,22 @@ def fp64_precision_form(V, scenes, steps: int = 10, pool=(400, 50, 400)):
     """Precision of the FP32 step against the FP64 GPU path on the jet-coiling scene: the
     8M-particle pool with the jet column already flowing (no emitter, so all modes keep
     the same particles), `steps` steps each of FP64 (vfd_set_precision), FP32 absolute and
-    FP32 cell-relative positions, and the FP32 modes again with the scene translated by
-    (1000, 200, -300) m. Per step: the mean density error at the pressure solve's exit
-    (-rho0 sum(res)/N, % of rho0) of every mode; after the last step: each FP32 mode's
-    position difference from the FP64 trajectory (translated back), and the step rate.
+    FP32 cell-relative positions, and all three again with the scene translated by
+    (1000, 200, -300) m (its FP32 inputs there are the FP64 run's inputs too). Per step:
+    the mean density error at the pressure solve's exit (-rho0 sum(res)/N, % of rho0) of
+    every mode; after the last step: each FP32 mode's position difference from the FP64
+    trajectory of the same inputs, and the step rate.
     Surface tension as in the jet form (sigma scaled by (r / 25 mm)^3)."""
     out = {}
     far = np.array([1000.0, 200.0, -300.0])
-    ref = None
+    refs = {}
     for mode, offset in (("fp64", None), ("fp32_absolute", None), ("fp32_cell_relative", None),
-                         ("fp32_absolute_far", far), ("fp32_cell_relative_far", far)):
+                         ("fp64_far", far), ("fp32_absolute_far", far), ("fp32_cell_relative_far", far)):
         s = scenes.jet_column_8m(pool=pool, offset=(0.0, 0.0, 0.0) if offset is None else tuple(offset))
         r = s["desc"]["ParticleRadius"]
         s["desc"]["SurfaceTension"] = 0.07 * (r / 0.025) ** 3
         sim = V.scene_simulation(s)
-        if mode == "fp64":
+        if mode.startswith("fp64"):
             sim.SetPrecision(True)
         elif "cell_relative" in mode:
             sim.SetPositionMode(True)
@@ -430,12 +431,12 @@ def fp64_precision_form(V, scenes, steps: int = 10, pool=(400, 50, 400)):
                         st["ViscositySolverIterationCount"]])
         el = time.perf_counter() - t0
         n = len(s["x"])
-        if mode == "fp64":
-            ref, _ = sim.GetStateF64()
+        if mode.startswith("fp64"):  # the reference of the FP32 runs from the same (FP32) inputs
+            refs[offset is not None], _ = sim.GetStateF64()
             rec = {}
         else:
             x, _, _ = sim.GetState()
-            e = np.linalg.norm(x.astype(np.float64) - (far if offset is not None else 0.0) - ref, axis=1)
+            e = np.linalg.norm(x.astype(np.float64) - refs[offset is not None], axis=1)
             rec = {"mean_position_error_m": float(e.mean()), "max_position_error_m": float(e.max()),
                    "p99_position_error_m": float(np.quantile(e, 0.99))}
         rec.update({"particle_steps_per_s": n * steps / el, "mean_density_error_pct_per_step": errs,
