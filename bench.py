@@ -575,6 +575,8 @@ def profile_case(args):
         sim.SetLanes(vals * len(V.TUNED_KERNELS) if len(vals) == 1 else vals)
     else:
         log("lanes", sim.Autotune(1))
+    if args.tiles >= 0:
+        sim.SetTiles([args.tiles] * len(V.TUNED_KERNELS))
     sim.Steps(args.graph_steps)
     sim.SetGraphMode(False)
     import torch
@@ -670,6 +672,8 @@ def main():
                     help="profiling run instead of the benchmark: the viscous dam break at N_SIDE^3 particles, "
                          "--graph-steps steps as CUDA graphs, then --eager-steps steps with every kernel launched "
                          "from the host (what a profiler filtering by kernel name captures)")
+    ap.add_argument("--tiles", type=int, default=-1, help="cell tiles of the three solver-loop passes instead of "
+                    "the autotuner's choice: 0 = neighbour rows, 3 = 2x2x2 cells, 4 = 4x2x2 cells")
     ap.add_argument("--graph-steps", type=int, default=4)
     ap.add_argument("--eager-steps", type=int, default=2)
     ap.add_argument("--dry-run", action="store_true",
@@ -716,6 +720,8 @@ def main():
         lanes = dict(zip(V.TUNED_KERNELS, vals))
     else:
         lanes = sim.Autotune(2)  # per-kernel lanes per particle and tile sizes, state restored
+    if args.tiles >= 0:
+        sim.SetTiles([args.tiles] * len(V.TUNED_KERNELS))
     sim.SetGraphMode(not args.eager)
     sim.Steps(args.warmup)
     stream = torch.cuda.ExternalStream(sim.GetStream())
