@@ -819,7 +819,7 @@ def main():
         "config": dict(dam_break_config(args.n_side), launch="eager" if args.eager else "cuda graph per step"),
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
         "roofline": roof, "step_roofline": step_roof, "kernel_shares": shares, "lanes_per_particle": lanes,
-        "tile_log2_cells": sim.GetTiles(),
+        "tile_log2_cells": sim.GetTiles(), "threads_per_block": sim.GetBlocks(),
         "solver": {k: st[k] for k in ("DivergenceSolverIterationCount", "PressureSolverIterationCount",
                                       "ViscositySolverIterationCount", "PressureSolverError", "TimeStepSize",
                                       "MaxNeighborCount", "Flags")},

@@ -437,9 +437,18 @@ int vfd_set_tiles(vfd_sim* sim, const uint8_t* tiles, uint32_t count);
 int vfd_get_tiles(const vfd_sim* sim, uint8_t* tiles, uint32_t count);
 
 /*
+ * Threads per block (64, 128 = the default, or 256) of the neighbour-row kernels, in the
+ * order of vfd_set_lanes. No counterpart in the reference, which launches 256 threads
+ * (ComputeHelper.cpp:18). vfd_autotune picks them with the lanes and tiles.
+ */
+int vfd_set_blocks(vfd_sim* sim, const uint16_t* blocks, uint32_t count);
+int vfd_get_blocks(const vfd_sim* sim, uint16_t* blocks, uint32_t count);
+
+/*
  * Autotuner: runs `steps` steps from a snapshot of the current state once per
- * lane count and tile size, times every neighbour-loop kernel with CUDA events, keeps the
- * fastest lane count (and tile size, vfd_set_tiles) per kernel and restores the state exactly (positions,
+ * lane count, tile size and block size, times every neighbour-loop kernel with CUDA events,
+ * keeps the fastest lane count (and tile size, vfd_set_tiles, and block size,
+ * vfd_set_blocks) per kernel and restores the state exactly (positions,
  * velocities, accelerations and all carried solver state; the simulation does not
  * advance). Per-step diagnostics (vfd_get_field, vfd_get_neighbors) reflect the
  * last tuning step until the next step. lanes_out (may be NULL) receives the choice.

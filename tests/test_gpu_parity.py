@@ -361,3 +361,16 @@ def test_tile_passes_in_a_batch_match_single_scenes():
         xs, vs, _ = one.GetState()
         np.testing.assert_allclose(xb, xs, atol=1e-6)
         np.testing.assert_allclose(vb, vs, atol=1e-5)
+
+
+@pytest.mark.parametrize("block", [64, 256])
+def test_block_sizes_agree(block):
+    """Other block sizes of the neighbour-row kernels (the autotuner's choices) keep the
+    one-step tolerances against the FP32 oracle."""
+    s = scenes.small_dam_break(n_side=10, viscosity=0.02, surface_tension=0.05)
+    g, o = pair(s, 32)
+    g.SetBlocks([block] * len(V.TUNED_KERNELS))
+    assert set(g.GetBlocks().values()) == {block}
+    h = 4 * s["desc"]["ParticleRadius"]
+    for k in range(2):
+        _compare_step(g, o, h, median_tol=1e-6 * (k + 1) ** 2)

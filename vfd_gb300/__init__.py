@@ -36,7 +36,7 @@ EXPORTS = [
     "vfd_find_neighbors_noalloc", "vfd_adjoint_forward", "vfd_adjoint_backward", "vfd_adjoint_release",
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
     "vfd_emit", "vfd_get_graph_mode", "vfd_checkpoint_size", "vfd_checkpoint", "vfd_restore",
-    "vfd_set_tiles", "vfd_get_tiles", "vfd_set_precision", "vfd_get_state_f64",
+    "vfd_set_tiles", "vfd_get_tiles", "vfd_set_precision", "vfd_get_state_f64", "vfd_set_blocks", "vfd_get_blocks",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -121,6 +121,8 @@ def lib() -> C.CDLL:
                 "vfd_get_lanes": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_set_tiles": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_set_precision": [P, C.c_int32],
+                "vfd_set_blocks": [P, C.POINTER(C.c_uint16), C.c_uint32],
+                "vfd_get_blocks": [P, C.POINTER(C.c_uint16), C.c_uint32],
                 "vfd_get_state_f64": [P, C.POINTER(C.c_double), C.POINTER(C.c_double)],
                 "vfd_get_tiles": [P, C.POINTER(C.c_uint8), C.c_uint32],
                 "vfd_autotune": [P, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32],
@@ -570,6 +572,16 @@ class DFSPHSimulation:
         arr = (C.c_uint8 * 16)()
         _check(lib().vfd_get_tiles(self._h, arr, 16), "vfd_get_tiles")
         return {k: arr[i] for i, k in enumerate(TUNED_KERNELS) if k in TILE_KERNELS}
+
+    def SetBlocks(self, blocks):
+        """Threads per block (64, 128, 256) of the neighbour-row kernels, TUNED_KERNELS order."""
+        arr = (C.c_uint16 * len(blocks))(*blocks)
+        _check(lib().vfd_set_blocks(self._h, arr, len(blocks)), "vfd_set_blocks")
+
+    def GetBlocks(self) -> dict:
+        arr = (C.c_uint16 * 16)()
+        _check(lib().vfd_get_blocks(self._h, arr, 16), "vfd_get_blocks")
+        return {k: arr[i] for i, k in enumerate(TUNED_KERNELS)}
 
     def GetStream(self) -> int:
         p = C.c_void_p()

@@ -365,6 +365,7 @@ int allocate(vfd_sim* s) {
         base.batchBlocks = (uint32_t)std::max(1, sms) * (2048u / kBlock);
     }
     std::memcpy(base.tiles, s->tiles, sizeof(base.tiles));
+    std::memcpy(base.blocks, s->blocks, sizeof(base.blocks));
     base.compactRows = uses_tiles(s->tiles) ? 1u : 0u;
     CK(prepare_tile_kernels());
     TRY(dalloc(s, &s->dWM, kTableRes));
@@ -2045,6 +2046,25 @@ int vfd_set_tiles(vfd_sim* s, const uint8_t* tiles, uint32_t count) {
     return VFD_OK;
 }
 
+int vfd_set_blocks(vfd_sim* s, const uint16_t* blocks, uint32_t count) {
+    TRY(check_sim(s));
+    if (!blocks || count == 0 || count > kTunedCount) return fail(VFD_E_ARG, "blocks: 1..%d values", (int)kTunedCount);
+    for (uint32_t k = 0; k < count; k++)
+        if (blocks[k] != 64 && blocks[k] != 128 && blocks[k] != 256)
+            return fail(VFD_E_ARG, "threads per block must be 64, 128 or 256");
+    std::memcpy(s->blocks, blocks, count * sizeof(uint16_t));
+    for (int k = 0; k < 2; k++) std::memcpy(s->dev[k].blocks, s->blocks, sizeof(s->blocks));
+    s->releaseGraphs();
+    return VFD_OK;
+}
+
+int vfd_get_blocks(const vfd_sim* s, uint16_t* blocks, uint32_t count) {
+    TRY(check_sim(s));
+    if (!blocks) return fail(VFD_E_ARG, "null output");
+    for (uint32_t k = 0; k < std::min<uint32_t>(count, 16); k++) blocks[k] = s->blocks[k] ? s->blocks[k] : (uint16_t)kBlock;
+    return VFD_OK;
+}
+
 int vfd_get_tiles(const vfd_sim* s, uint8_t* tiles, uint32_t count) {
     TRY(check_sim(s));
     if (!tiles) return fail(VFD_E_ARG, "null output");
@@ -2105,15 +2125,17 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
         return fail(VFD_E_CUDA, "autotune snapshot: %s", cudaGetErrorString(e));
     }
     // every lane count with every tile size of the cell-tile kernels (the others ignore it)
-    const uint8_t tileCand[3] = {0, 3, 4};  // neighbour rows, 2x2x2 tiles, 4x2x2 tiles
-    double times[kTunedCount][3][3] = {};
+    const uint8_t tileCand[3] = {0, 3, 4};        // neighbour rows, 2x2x2 tiles, 4x2x2 tiles
+    const uint16_t blockCand[3] = {128, 64, 256};  // threads per block of the row kernels
+    double times[kTunedCount][3][3][3] = {};       // [kernel][lanes][tiles][block]
     int rc = VFD_OK;
-    for (int ct = 0; ct < 9 && rc == VFD_OK; ct++) {
-        const int c = ct % 3, tl = ct / 3;
+    for (int ct = 0; ct < 27 && rc == VFD_OK; ct++) {
+        const int c = ct % 3, tl = (ct / 3) % 3, bs = ct / 9;
         for (int k = 0; k < 2; k++) {
             for (int t = 0; t < kTunedCount; t++) {
                 s->dev[k].lanes[t] = cand[c];
                 s->dev[k].tiles[t] = tileCand[tl];
+                s->dev[k].blocks[t] = blockCand[bs];
             }
             s->dev[k].compactRows = tileCand[tl] != 0 ? 1u : 0u;
         }
@@ -2132,7 +2154,7 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
             float ms = 0.0f;
             if (rc == VFD_OK && cudaEventElapsedTime(&ms, rec.a, rec.b) == cudaSuccess)
                 for (int t = 0; t < kTunedCount; t++)
-                    if (rec.name == names[t]) times[t][c][tl] += ms;
+                    if (rec.name == names[t]) times[t][c][tl][bs] += ms;
         }
         s->cs = cs0;
         e = copy_all(false);
@@ -2143,33 +2165,40 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
         for (int k = 0; k < 2; k++) {
             std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
             std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+            std::memcpy(s->dev[k].blocks, s->blocks, sizeof(s->blocks));
             s->dev[k].compactRows = uses_tiles(s->tiles) ? 1u : 0u;
         }
         return rc;
     }
     for (int t = 0; t < kTunedCount; t++) {
         const bool tileable = t == kTPAccel || t == kTJacobi || t == kTSpmv;
-        // kernels without tiles ran the same code in all three tile runs: their sum
-        auto cost = [&](int c, int tl) {
-            return tileable ? times[t][c][tl] : times[t][c][0] + times[t][c][1] + times[t][c][2];
+        // A configuration is (lanes c, tiles tl, block bs). Kernels without tiles ran the same
+        // code in all three tile runs: their cost is the sum of those; tile kernels run
+        // kTileBlock threads whatever bs, so their block choice stays the default.
+        auto cost = [&](int c, int tl, int bs) {
+            return tileable ? times[t][c][tl][bs] : times[t][c][0][bs] + times[t][c][1][bs] + times[t][c][2][bs];
         };
-        int best = 1, bestTile = 0;
-        double bt = cost(1, 0);
+        int best = 1, bestTile = 0, bestBlock = 0;
+        double bt = cost(1, 0, 0);
         for (int c = 0; c < 3; c++)
-            for (int tl = 0; tl < (tileable ? 3 : 1); tl++) {
-                const double v = cost(c, tl);
-                if (v > 0.0 && v < bt) {
-                    bt = v;
-                    best = c;
-                    bestTile = tl;
+            for (int tl = 0; tl < (tileable ? 3 : 1); tl++)
+                for (int bs = 0; bs < 3; bs++) {
+                    const double v = cost(c, tl, bs);
+                    if (v > 0.0 && v < bt) {
+                        bt = v;
+                        best = c;
+                        bestTile = tl;
+                        bestBlock = bs;
+                    }
                 }
-            }
         s->lanes[t] = cand[best];
         s->tiles[t] = tileable ? tileCand[bestTile] : 0;
+        s->blocks[t] = bestTile == 0 ? blockCand[bestBlock] : 0;
     }
     for (int k = 0; k < 2; k++) {
         std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));
         std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
+        std::memcpy(s->dev[k].blocks, s->blocks, sizeof(s->blocks));
         s->dev[k].compactRows = uses_tiles(s->tiles) ? 1u : 0u;
     }
     s->releaseGraphs();

@@ -36,7 +36,8 @@ namespace vfd {
 constexpr uint32_t kMaxNeighbors = 70u;      // ParticleSearchKernels.cuh:7
 constexpr uint32_t kTableRes = 10000u;       // Kernel/DFSPHKernels.h:143
 constexpr uint32_t kHaltonCount = 49152u;    // HaltonVec323.cuh:4
-constexpr uint32_t kBlock = 128u;            // threads per particle kernel
+constexpr uint32_t kBlock = 128u;            // threads per particle kernel (default)
+constexpr uint32_t kMaxBlock = 256u;         // largest block a neighbour-loop kernel is launched with
 constexpr uint32_t kRow = 72u;               // neighbour row length (70 rounded up to 8)
 constexpr uint32_t kGroup = 8u;              // lanes per particle in neighbour loops
 constexpr uint32_t kBuckets = 32u;           // reduction buckets per scene and quantity
@@ -156,6 +157,7 @@ struct Dev {
     int32_t* MMB;              // [scene][6][kBuckets] x32: min cell xyz, max cell xyz
     unsigned long long condHandle[3];  // while-node handles (div, cg, pres); 0 = eager
     uint8_t lanes[16];                 // lanes per particle of each TunedKernel
+    uint16_t blocks[16];               // threads per block of each TunedKernel's row kernels (0 = kBlock)
     // Batches: per solver loop (div, cg, pres) the controllers list the scenes still
     // iterating, [0] particles in them, [1] their count, then prefix[nscenes] (first
     // virtual index of each listed scene) and begin[nscenes] (its first slot); the loop
@@ -600,19 +602,22 @@ extern LaunchProfiler* g_profiler;
 // The same for a batch loop kernel: a fixed grid of d.batchBlocks blocks.
 #define VFD_LAUNCH_LANES_BATCH(name, id, KERNEL)                                                     \
     do {                                                                                            \
+        const uint32_t B_ = d.blocks[id] ? d.blocks[id] : kBlock;                                   \
+        const uint32_t NB_ = d.batchBlocks * kBlock / B_;                                           \
         switch (d.lanes[id]) {                                                                      \
-            case 4: VFD_LAUNCH(name, s, KERNEL(4)<<<d.batchBlocks, kBlock, 0, s>>>(d)); break;      \
-            case 16: VFD_LAUNCH(name, s, KERNEL(16)<<<d.batchBlocks, kBlock, 0, s>>>(d)); break;    \
-            default: VFD_LAUNCH(name, s, KERNEL(8)<<<d.batchBlocks, kBlock, 0, s>>>(d)); break;     \
+            case 4: VFD_LAUNCH(name, s, KERNEL(4)<<<NB_, B_, 0, s>>>(d)); break;                    \
+            case 16: VFD_LAUNCH(name, s, KERNEL(16)<<<NB_, B_, 0, s>>>(d)); break;                  \
+            default: VFD_LAUNCH(name, s, KERNEL(8)<<<NB_, B_, 0, s>>>(d)); break;                   \
         }                                                                                           \
     } while (0)
 
 #define VFD_LAUNCH_LANES(name, id, KERNEL)                                                          \
     do {                                                                                            \
+        const uint32_t B_ = d.blocks[id] ? d.blocks[id] : kBlock;                                   \
         switch (d.lanes[id]) {                                                                      \
-            case 4: VFD_LAUNCH(name, s, KERNEL(4)<<<blocks_for(d.n * 4u), kBlock, 0, s>>>(d)); break;   \
-            case 16: VFD_LAUNCH(name, s, KERNEL(16)<<<blocks_for(d.n * 16u), kBlock, 0, s>>>(d)); break; \
-            default: VFD_LAUNCH(name, s, KERNEL(8)<<<blocks_for(d.n * 8u), kBlock, 0, s>>>(d)); break;  \
+            case 4: VFD_LAUNCH(name, s, KERNEL(4)<<<blocks_for(d.n * 4u, B_), B_, 0, s>>>(d)); break;   \
+            case 16: VFD_LAUNCH(name, s, KERNEL(16)<<<blocks_for(d.n * 16u, B_), B_, 0, s>>>(d)); break; \
+            default: VFD_LAUNCH(name, s, KERNEL(8)<<<blocks_for(d.n * 8u, B_), B_, 0, s>>>(d)); break;  \
         }                                                                                           \
     } while (0)
 

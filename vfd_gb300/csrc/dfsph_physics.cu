@@ -212,7 +212,7 @@ __device__ __forceinline__ void kernel_wg(const Dev& d, float3 r, float& w, floa
 // and boundary gradient and each pair's gradW, so it rides along (the terms and order of
 // velocity_divergence, which K17 uses).
 template <uint32_t G, bool REL, bool DIV = false>
-__global__ void __launch_bounds__(kBlock) k_density_factor(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_density_factor(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -316,7 +316,7 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
 
 // K5 / K18.
 template <bool DIV, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_pressure_accel(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(kBlock) k_pressure_accel(Dev d) {
 
 // K5 / K18 of a batch: the scenes still iterating, from the loop's work list.
 template <bool DIV, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_pressure_accel_b(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_pressure_accel_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted_p(d)) return;
     const int L = DIV ? kLoopDiv : kLoopPres;
@@ -383,7 +383,7 @@ __device__ __forceinline__ float jacobi_item(const Dev& d, const Group<G>& grp, 
 }
 
 template <bool DIV, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_jacobi_iter(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
     const uint32_t p = grp.p;
@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_iter(Dev d) {
 
 // The same for a batch (work list of the loop).
 template <bool DIV, uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_jacobi_iter_b(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_jacobi_iter_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted_p(d)) return;
     const int L = DIV ? kLoopDiv : kLoopPres;
@@ -498,7 +498,7 @@ __global__ void k_ctrl_jacobi(Dev d) {
 
 // K7 ComputePressureAccelerationAndFactorKernel (:555-602) + K8 ClearAccelerationKernel (:24-37).
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_div_finish(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_div_finish(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(kBlock) k_div_finish(Dev d) {
 // K9: ComputeSurfaceTensionClassificationKernel (DFSPHKernels.cu:881-958); the
 // Monte-Carlo samples are split over the group's lanes.
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_st_classify(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_st_classify(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -573,7 +573,7 @@ __device__ __forceinline__ bool nonzero3(float4 a) { return a.x != 0.0f || a.y !
 
 // K10: ComputeSurfaceTensionNormalsAndCurvatureKernel (:960-1006).
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_st_smooth(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_st_smooth(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -668,7 +668,7 @@ __device__ __forceinline__ Mat3 inverse3(const Mat3& a) {  // cofactors / determ
 // the SpMV's boundary term (:793-839): BV p_i = sum_k c_k (p_i . d_k) gradW_k.
 // CG.w and CP.w hold m / rho (read by the SpMV's neighbours) from here on.
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_visc_precond(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_visc_precond(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -760,7 +760,7 @@ __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp,
 
 // Initial residual r = b - A g and the norms |b|^2, |r|^2 (:627-669).
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_visc_setup(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_visc_setup(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
     const uint32_t p = grp.p;
@@ -884,7 +884,7 @@ __global__ void k_ctrl_cg1(Dev d) {
 
 // Loop body 1: Ap and p . Ap (:695-720).
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_cg_spmv(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
     const uint32_t p = grp.p;
@@ -908,7 +908,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(Dev d) {
 
 // Loop body 1 of a batch.
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv_b(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_cg_spmv_b(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (aborted_p(d)) return;
     BATCH_LOOP(kLoopCG, G) {
@@ -1130,7 +1130,7 @@ __global__ void __launch_bounds__(kBlock) k_velocity(Dev d) {
 
 // K17 ComputeDensityAdvectionKernel (:233-278).
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_pres_init(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
@@ -1149,7 +1149,7 @@ __global__ void __launch_bounds__(kBlock) k_pres_init(Dev d) {
 // K20 ComputePressureAccelerationAndVelocityKernel (:434-481) + K21 ComputePositionKernel (:54-67);
 // positions go to XN so that the neighbours' positions read here stay unchanged.
 template <uint32_t G, bool REL>
-__global__ void __launch_bounds__(kBlock) k_pres_finish(Dev d) {
+__global__ void __launch_bounds__(kMaxBlock) k_pres_finish(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];

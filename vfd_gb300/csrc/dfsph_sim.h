@@ -182,6 +182,8 @@ struct vfd_sim {
     // cell tiles of the solver-loop kernels per TunedKernel: 0 = neighbour rows, else log2
     // of the cells in a tile (vfd_set_tiles, vfd_autotune)
     uint8_t tiles[16] = {};
+    // threads per block of each TunedKernel's neighbour-row kernels (vfd_autotune; 0 = 128)
+    uint16_t blocks[16] = {};
 
     // layout
     bool allocated = false, uploaded = false;
