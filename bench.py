@@ -398,55 +398,121 @@ def jet_form(V, scenes, steps: int = 8, warmup: int = 2):
     return out
 
 
-def fp64_precision_form(V, scenes, steps: int = 10, pool=(400, 50, 400)):
+def fp64_precision_form(V, scenes, steps: int = 10, pool=(400, 50, 400), sigma: float | None = None,
+                        far: bool = True, compare_every: int = 0):
     """Precision of the FP32 step against the FP64 GPU path on the jet-coiling scene: the
     8M-particle pool with the jet column already flowing (no emitter, so all modes keep
-    the same particles), `steps` steps each of FP64 (vfd_set_precision), FP32 absolute and
-    FP32 cell-relative positions, and all three again with the scene translated by
-    (1000, 200, -300) m (its FP32 inputs there are the FP64 run's inputs too). Per step:
-    the mean density error at the pressure solve's exit (-rho0 sum(res)/N, % of rho0) of
-    every mode; after the last step: each FP32 mode's position difference from the FP64
-    trajectory of the same inputs, and the step rate.
-    Surface tension as in the jet form (sigma scaled by (r / 25 mm)^3)."""
+    the same particles). FP64 (vfd_set_precision), FP32 absolute and FP32 cell-relative
+    positions run `steps` steps in lockstep from the same FP32 inputs, and again with the
+    scene translated by (1000, 200, -300) m unless `far` is off. Per step and mode: the
+    mean density error at the pressure solve's exit (-rho0 sum(res)/N, % of rho0), the
+    solver iteration counts and the viscosity CG's relative residual |r|/|b| where it
+    stopped. Every `compare_every` steps (and after the last): each FP32 mode's position
+    difference from the FP64 trajectory (mean, p99, max). Surface tension sigma, by
+    default the jet form's 0.07 x (r / 25 mm)^3."""
     out = {}
-    far = np.array([1000.0, 200.0, -300.0])
-    refs = {}
-    for mode, offset in (("fp64", None), ("fp32_absolute", None), ("fp32_cell_relative", None),
-                         ("fp64_far", far), ("fp32_absolute_far", far), ("fp32_cell_relative_far", far)):
-        s = scenes.jet_column_8m(pool=pool, offset=(0.0, 0.0, 0.0) if offset is None else tuple(offset))
+    far_offset = (1000.0, 200.0, -300.0)
+    modes = ("fp64", "fp32_absolute", "fp32_cell_relative")
+    for suffix, offset in (("", (0.0, 0.0, 0.0)), ("_far", far_offset))[:2 if far else 1]:
+        s = scenes.jet_column_8m(pool=pool, offset=offset)
         r = s["desc"]["ParticleRadius"]
-        s["desc"]["SurfaceTension"] = 0.07 * (r / 0.025) ** 3
-        sim = V.scene_simulation(s)
-        if mode.startswith("fp64"):
-            sim.SetPrecision(True)
-        elif "cell_relative" in mode:
-            sim.SetPositionMode(True)
-            sim.SetFluidObjects(s["x"], s["v"])
-        errs, its = [], []
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            st = sim.OnUpdate()
-            errs.append(100.0 * st["PressureSolverError"] / 1000.0)
-            its.append([st["DivergenceSolverIterationCount"], st["PressureSolverIterationCount"],
-                        st["ViscositySolverIterationCount"]])
-        el = time.perf_counter() - t0
+        s["desc"]["SurfaceTension"] = 0.07 * (r / 0.025) ** 3 if sigma is None else sigma
         n = len(s["x"])
-        if mode.startswith("fp64"):  # the reference of the FP32 runs from the same (FP32) inputs
-            refs[offset is not None], _ = sim.GetStateF64()
-            rec = {}
-        else:
-            x, _, _ = sim.GetState()
-            e = np.linalg.norm(x.astype(np.float64) - refs[offset is not None], axis=1)
-            rec = {"mean_position_error_m": float(e.mean()), "max_position_error_m": float(e.max()),
-                   "p99_position_error_m": float(np.quantile(e, 0.99))}
-        rec.update({"particle_steps_per_s": n * steps / el, "mean_density_error_pct_per_step": errs,
-                    "iterations_per_step": its})
-        out[mode] = rec
-        sim.close()
-        del sim
+        sims = {}
+        for mode in modes:
+            sim = V.scene_simulation(s)
+            if mode == "fp64":
+                sim.SetPrecision(True)
+            elif mode == "fp32_cell_relative":
+                sim.SetPositionMode(True)
+                sim.SetFluidObjects(s["x"], s["v"])
+            sims[mode] = sim
+        recs = {m: {"mean_density_error_pct_per_step": [], "iterations_per_step": [],
+                    "viscosity_residual_per_step": [], "_s": 0.0} for m in modes}
+        for m in modes[1:]:
+            recs[m]["position_error_m_by_step"] = []
+        for k in range(steps):
+            for m in modes:
+                t0 = time.perf_counter()
+                st = sims[m].OnUpdate()
+                recs[m]["_s"] += time.perf_counter() - t0
+                recs[m]["mean_density_error_pct_per_step"].append(100.0 * st["PressureSolverError"] / 1000.0)
+                recs[m]["iterations_per_step"].append([st["DivergenceSolverIterationCount"],
+                                                       st["PressureSolverIterationCount"],
+                                                       st["ViscositySolverIterationCount"]])
+                recs[m]["viscosity_residual_per_step"].append(st["ViscositySolverError"])
+            if (compare_every and (k + 1) % compare_every == 0) or k + 1 == steps:
+                ref, _ = sims["fp64"].GetStateF64()  # the FP64 trajectory of the same (FP32) inputs
+                for m in modes[1:]:
+                    x, _, _ = sims[m].GetState()
+                    e = np.linalg.norm(x.astype(np.float64) - ref, axis=1)
+                    recs[m]["position_error_m_by_step"].append(
+                        [k + 1, float(e.mean()), float(np.quantile(e, 0.99)), float(e.max())])
+        for m in modes:
+            rec = recs[m]
+            rec["particle_steps_per_s"] = n * steps / rec.pop("_s")
+            if m != "fp64":
+                _, mean, p99, mx = rec["position_error_m_by_step"][-1]
+                rec.update(mean_position_error_m=mean, p99_position_error_m=p99, max_position_error_m=mx)
+                if not compare_every:
+                    del rec["position_error_m_by_step"]
+            out[m + suffix] = rec
+            sims[m].close()
+        del sims
     out["workload"] = (f"jet column onto a pool: {n} particles (pool {pool[0]}x{pool[1]}x{pool[2]}, r = 1.5 mm), "
-                       f"{steps} steps per mode; FP32 modes against the FP64 GPU path, also translated by "
-                       f"(1000, 200, -300) m")
+                       f"surface tension {s['desc']['SurfaceTension']:.3g}, {steps} steps per mode in lockstep; "
+                       f"FP32 modes against the FP64 GPU path" +
+                       (", also translated by (1000, 200, -300) m" if far else ""))
+    return out
+
+
+def config_table(V, scenes):
+    """Step rates of each benchmark scene on the GPU (FP32 graph step and FP64 path) and on
+    the host (FP32 and FP64 oracle, all host threads), for the per-scene comparison table.
+    Each rate is particles x steps / host wall time around synchronised step calls, after
+    two warm-up steps; the 1M dam break runs on the host as its 64k (40^3) sample with
+    the same parameters."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cases = [
+        ("c1_dam_break_8k", scenes.dam_break_8k(), 200, 20),
+        ("c1b_dam_break_8k_2x1x1", scenes.dam_break_8k(box_scale=(2.0, 1.0, 1.0)), 200, 20),
+        ("c2_viscous_dam_break_1M", scenes.viscous_dam_break(), 50, 0),
+        ("c2_sample_viscous_dam_break_64k", scenes.viscous_dam_break(n_side=40), 50, 5),
+        ("c4_viscous_drop_33k", scenes.viscous_drop_33k(), 60, 10),
+    ]
+    out = {"cpu": {"cores": O.get_threads(), "cpu_model": cpu_model()}}
+
+    def rate(steps, n, k):
+        steps(2)
+        t0 = time.perf_counter()
+        steps(k)
+        return n * k / (time.perf_counter() - t0)
+
+    def oracle_steps(orc):
+        def run(k):
+            for _ in range(k):
+                orc.step()
+        return run
+
+    for name, s, gpu_steps, cpu_steps in cases:
+        n = len(s["x"])
+        rec = {"particles": n}
+        for prec in ("fp32", "fp64"):
+            sim = V.scene_simulation(s)
+            if prec == "fp64":
+                sim.SetPrecision(True)
+            k = gpu_steps if prec == "fp32" else max(5, gpu_steps // 5)
+            rec[f"gpu_{prec}"] = rate(sim.Steps, n, k)
+            sim.close()
+            del sim
+        if cpu_steps:
+            for bits in (32, 64):
+                orc = O.scene_oracle(s, bits)
+                rec[f"cpu_fp{bits}"] = rate(oracle_steps(orc), n, cpu_steps)
+                del orc
+        out[name] = rec
     return out
 
 
@@ -665,6 +731,13 @@ def main():
                     help="steps per mode of the FP64-vs-FP32 precision form on the 8M jet scene")
     ap.add_argument("--precision-only", action="store_true",
                     help="run only the FP64-vs-FP32 precision form (with --precision-steps) and print its JSON")
+    ap.add_argument("--precision-sigma", type=float, default=None,
+                    help="surface tension of the precision form (default 0.07 x (r / 25 mm)^3; 0.07 is the literal value)")
+    ap.add_argument("--precision-no-far", action="store_true", help="precision form at the origin only")
+    ap.add_argument("--precision-compare-every", type=int, default=0,
+                    help="compare positions with the FP64 run every this many steps (default: after the last)")
+    ap.add_argument("--config-table", action="store_true",
+                    help="print only the per-scene step rates (GPU FP32 and FP64, host oracle FP32 and FP64)")
     ap.add_argument("--eager", action="store_true",
                     help="launch the timed steps kernel by kernel instead of as CUDA graphs (same kernels, same "
                          "results); profilers cannot see the kernels inside graphs with conditional nodes")
@@ -694,7 +767,15 @@ def main():
         import vfd_gb300 as V
         from vfd_gb300 import scenes
         V.lib().vfd_set_device(0)
-        print(json.dumps({"fp64_precision": fp64_precision_form(V, scenes, args.precision_steps)}), flush=True)
+        print(json.dumps({"fp64_precision": fp64_precision_form(
+            V, scenes, args.precision_steps, sigma=args.precision_sigma, far=not args.precision_no_far,
+            compare_every=args.precision_compare_every)}), flush=True)
+        return
+    if args.config_table:
+        import vfd_gb300 as V
+        from vfd_gb300 import scenes
+        V.lib().vfd_set_device(0)
+        print(json.dumps({"config_table": config_table(V, scenes)}), flush=True)
         return
 
     import torch
