@@ -502,6 +502,29 @@ int vfd_adjoint_backward(vfd_sim* sim, const float* x_bar, const float* v_bar, f
 int vfd_adjoint_release(vfd_sim* sim);
 
 /*
+ * Initial guess of each backward step's viscosity solve A lambda = g_bar (the steps
+ * are walked from the last to the first): VFD_WARM_COLD starts from g_bar, as the
+ * forward solve starts from its right-hand side; VFD_WARM_PREVIOUS from the lambda of
+ * the step after; VFD_WARM_EXTRAPOLATE (default) from 2 lambda(t+1) - lambda(t+2), the
+ * linear extrapolation of the last two solutions, once two exist. Every choice solves to
+ * the same tolerance; they differ in iteration count. No counterpart in the reference.
+ */
+#define VFD_WARM_COLD 0
+#define VFD_WARM_PREVIOUS 1
+#define VFD_WARM_EXTRAPOLATE 2
+int vfd_adjoint_set_warm_start(vfd_sim* sim, int32_t mode);
+
+/* Counters of the last vfd_adjoint_backward. */
+typedef struct vfd_adjoint_stats {
+    uint32_t Steps;                      /* steps differentiated                          */
+    uint32_t ReplayedSteps;              /* steps re-run from checkpoints                 */
+    uint32_t ViscositySolves;            /* adjoint viscosity solves                      */
+    uint32_t ViscositySolverIterations;  /* their CG iterations, summed                   */
+    uint32_t MaxViscositySolverIterations;
+} vfd_adjoint_stats;
+int vfd_adjoint_get_stats(vfd_sim* sim, vfd_adjoint_stats* stats);
+
+/*
  * Position storage. No counterpart in the reference, which stores absolute FP32
  * coordinates (VFD_POSITIONS_ABSOLUTE, the default). VFD_POSITIONS_CELL_RELATIVE stores
  * each position as its FP32 offset within an anchor cell (a cube of edge h, the support

@@ -48,7 +48,7 @@ def _c_layout(struct_name, fields):
 
 
 @pytest.mark.parametrize("cls", [_abi.vfd_desc, _abi.vfd_volume_map, _abi.vfd_step_stats, _abi.vfd_info,
-                                 sph.vfd_sph_desc, sph.vfd_sph_params])
+                                 _abi.vfd_adjoint_stats, sph.vfd_sph_desc, sph.vfd_sph_params])
 def test_struct_layout_matches_header(tmp_path, cls):
     names = [n for n, _ in cls._fields_]
     src = tmp_path / "layout.c"

@@ -157,6 +157,45 @@ def test_adjoint_matches_fp64_reference_analytic_kernel(full_analytic):
     _check("dL/dBoundaryViscosity (analytic kernel)", gpu["pb"][1], ref["pb"][1], 1e-3)
 
 
+def test_warm_start_modes_agree_and_count():
+    """The three initial guesses of the adjoint viscosity solves (cold, previous lambda,
+    extrapolated) give the same gradients to the solve's tolerance; the counters report
+    every step's solve and the replayed segments (the last is recorded in the forward run)."""
+    sc = _floor_scene(div=True)
+    run = GpuRun(sc, 12, 4, analytic=True)
+    out = {}
+    for mode in (V._abi.WARM_COLD, V._abi.WARM_PREVIOUS, V._abi.WARM_EXTRAPOLATE):
+        run.sim.AdjointSetWarmStart(mode)
+        out[mode] = (run.gradient(), run.sim.AdjointStats())
+    ref, st0 = out[V._abi.WARM_COLD]
+    assert st0["Steps"] == 12 and st0["ReplayedSteps"] == 8 and st0["ViscositySolves"] == 12
+    assert 0 < st0["MaxViscositySolverIterations"] <= st0["ViscositySolverIterations"]
+    for mode, (g, st) in out.items():
+        print(f"warm start {mode}: {st}")
+        for key in ("v0b", "x0b"):
+            rel = np.linalg.norm(g[key] - ref[key]) / np.linalg.norm(ref[key])
+            assert rel < 1e-4, (mode, key, rel)
+        assert np.abs(g["pb"] - ref["pb"]).max() <= 1e-4 * np.abs(ref["pb"]).max()
+    with pytest.raises(V.VFDError):
+        run.sim.AdjointSetWarmStart(3)
+
+
+def test_backward_graph_matches_host_launches():
+    """The backward pass as one graph per step (device-side loops) and launched kernel by
+    kernel from the host (loops counted on the host) run the same kernels: the gradients
+    agree to the last bits the FP64 atomics of the parameter sums leave free."""
+    sc = _floor_scene(div=True)
+    out = []
+    for graph in (True, False):
+        run = GpuRun(sc, 10, 4)
+        run.sim.SetGraphMode(graph)
+        out.append(run.gradient())
+    g, e = out
+    for key in ("v0b", "x0b"):
+        np.testing.assert_allclose(g[key], e[key], rtol=1e-5, atol=1e-6 * np.abs(e[key]).max())
+    np.testing.assert_allclose(g["pb"], e["pb"], rtol=1e-5)
+
+
 # ------------------------------------------------------------ finite differences, smooth step
 @pytest.fixture(scope="module")
 def smooth():

@@ -37,6 +37,7 @@ EXPORTS = [
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
     "vfd_emit", "vfd_get_graph_mode", "vfd_checkpoint_size", "vfd_checkpoint", "vfd_restore",
     "vfd_set_tiles", "vfd_get_tiles", "vfd_set_precision", "vfd_get_state_f64", "vfd_set_blocks", "vfd_get_blocks",
+    "vfd_adjoint_set_warm_start", "vfd_adjoint_get_stats",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -131,6 +132,8 @@ def lib() -> C.CDLL:
                 "vfd_adjoint_forward": [P, C.c_uint32, C.c_uint32, C.POINTER(vfd_step_stats)],
                 "vfd_adjoint_backward": [P, f32p, f32p, f32p, f32p, f32p],
                 "vfd_adjoint_release": [P],
+                "vfd_adjoint_set_warm_start": [P, C.c_int32],
+                "vfd_adjoint_get_stats": [P, C.POINTER(_abi.vfd_adjoint_stats)],
                 "vfd_set_position_mode": [P, C.c_int32],
                 "vfd_set_kernel_mode": [P, C.c_int32],
                 "vfd_emit": [P, f32p, f32p, C.c_uint32],
@@ -521,6 +524,18 @@ class DFSPHSimulation:
 
     def AdjointRelease(self):
         _check(lib().vfd_adjoint_release(self._h), "vfd_adjoint_release")
+
+    def AdjointSetWarmStart(self, mode: int):
+        """Initial guess of the adjoint viscosity solves: _abi.WARM_COLD, WARM_PREVIOUS or
+        WARM_EXTRAPOLATE (the default)."""
+        _check(lib().vfd_adjoint_set_warm_start(self._h, int(mode)), "vfd_adjoint_set_warm_start")
+
+    def AdjointStats(self) -> dict:
+        """Counters of the last AdjointBackward (steps, replayed steps, viscosity solves and
+        their CG iterations)."""
+        st = _abi.vfd_adjoint_stats()
+        _check(lib().vfd_adjoint_get_stats(self._h, C.byref(st)), "vfd_adjoint_get_stats")
+        return st.as_dict()
 
     def ProfileKernels(self, steps: int) -> dict:
         """{kernel name: (launches, total ms)} over `steps` eagerly launched steps."""

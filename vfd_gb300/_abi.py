@@ -15,6 +15,10 @@ VFD_POSITIONS_ABSOLUTE = 0
 VFD_POSITIONS_CELL_RELATIVE = 1
 VFD_KERNEL_TABLE = 0
 VFD_KERNEL_ANALYTIC = 1
+VFD_WARM_COLD = 0
+VFD_WARM_PREVIOUS = 1
+VFD_WARM_EXTRAPOLATE = 2
+WARM_COLD, WARM_PREVIOUS, WARM_EXTRAPOLATE = VFD_WARM_COLD, VFD_WARM_PREVIOUS, VFD_WARM_EXTRAPOLATE
 VFD_SAMPLE_MIN_DENSITY = 0
 VFD_SAMPLE_MEDIUM_DENSITY = 1
 VFD_SAMPLE_MAX_DENSITY = 2
@@ -138,6 +142,19 @@ class vfd_step_stats(C.Structure):
         ("MaxNeighborCount", C.c_uint32),
         ("Flags", C.c_uint32),
         ("SurfaceTensionSampleCount", C.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class vfd_adjoint_stats(C.Structure):
+    _fields_ = [
+        ("Steps", C.c_uint32),
+        ("ReplayedSteps", C.c_uint32),
+        ("ViscositySolves", C.c_uint32),
+        ("ViscositySolverIterations", C.c_uint32),
+        ("MaxViscositySolverIterations", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:

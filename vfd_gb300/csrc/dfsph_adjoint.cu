@@ -35,9 +35,14 @@
 // them by a constant 0.1 r along n (identity Jacobian) and zeroes their velocity.
 //
 // Memory: states are checkpointed every `checkpoint_every` steps during the
-// forward run; the backward pass re-runs each segment eagerly from its checkpoint,
-// recording per step the neighbour rows, four velocity fields and the Jacobi
-// iterates, and then walks the segment's steps in reverse.
+// forward run (whose last segment is recorded as it runs); the backward pass re-runs
+// each other segment from its checkpoint, recording per step the neighbour rows, four
+// velocity fields and the Jacobi iterates, and then walks the segment's steps in
+// reverse. Each backward step is one launch of a graph built once: its kernels read the
+// step's arrays, time steps, iteration counts and decisions from the tape slot a device
+// counter names, and its Jacobi loops and the adjoint CG are conditional WHILE nodes.
+// The viscosity solves start from the linear extrapolation of the two solutions after
+// them (vfd_adjoint_set_warm_start).
 // Limits: one scene, surface tension off; neighbour sets must be symmetric, so a
 // particle at the 70-neighbour cap is rejected.
 #include <cuda_runtime.h>
@@ -57,6 +62,26 @@ namespace {
 
 constexpr uint32_t kAG = 8;  // lanes per particle of the adjoint neighbour loops
 
+// One recorded step: written by the tape kernels at the tape points of the step
+// (TapePoint), so that one recording graph serves every step: the slot of the current
+// step is steps[*cur], advanced by the step's last tape point.
+struct TapeStep {
+    float4 *Xpre, *V0, *V1, *G, *V2;
+    uint32_t *PID, *NCNT, *NBR;
+    float *RAD, *RAP;
+    float *KD, *RD, *KP, *RP;   // kappa^0..cap, res^0..cap-1 (stride floats each) of each solve
+    uint32_t capD, capP;
+    // written on the device
+    SceneDev pre;               // scene state at the start of the step
+    uint32_t kd, kp, overflow, zeroG, maxNbr, aborted;
+    float dto, dtn, maxV2;
+};
+struct TapeSet {
+    TapeStep* steps;
+    uint32_t* cur;
+    uint32_t count;
+};
+
 // Cotangent arrays of the backward pass (slot order unless stated).
 struct AdjDev {
     float4 *XBAR, *VBAR;      // x and v of the point of the step being differentiated
@@ -65,12 +90,21 @@ struct AdjDev {
     float4* BD;               // [3][body][stride]: (n, Vb), (grad pd, pd), (grad Vb, -)
     float *KBAR, *U, *RABAR, *APBAR, *DBAR, *RHOBAR, *ALBAR;
     float2* KU;               // (kappa^k, U) of the Jacobi iteration being differentiated
-    float4* LAM;              // last adjoint viscosity solution (initial guess of the next solve)
+    float4 *LAM, *LAM2;       // the last two adjoint viscosity solutions (initial guesses of the next)
+    uint32_t* ACNT;           // [0] adjoint CG iterations, [1] their maximum per solve, [2] solves,
+                              // [3] solutions held in LAM / LAM2 (0..2)
     uint32_t* STOP;           // 1 where the boundary zeroed the velocity
     double* SC;               // [0] dt_o bar, [1] dt_n bar, [2] Viscosity bar, [3] BoundaryViscosity bar
     uint32_t* CLAIM;          // [0] largest recomputed CFL |w|^2 (bits), [1] argmax claimed
     float4 *XBO, *VBO;        // x and v cotangents in original particle order
+    const TapeSet* ts;        // the recorded steps; BW[0] is the slot of the step being differentiated
+    uint32_t* BW;             // [0] that slot, [1] Jacobi iterations of the current solve left to differentiate
+    unsigned long long hLoop[2];  // conditional handles of the pressure [0] and divergence [1] Jacobi
+                                  // loops of the backward graph (0: launched from the host)
 };
+
+// The recorded step being differentiated.
+__device__ __forceinline__ const TapeStep& bstep(const AdjDev& a) { return a.ts->steps[a.BW[0]]; }
 
 // The reference's cubic spline (Kernel/DFSPHKernels.h:86-131) and its derivatives.
 struct Spline {
@@ -222,11 +256,25 @@ __global__ void k_adj_bdata(Dev d, AdjDev a) {
 }
 
 // ---------------------------------------------------------------- Jacobi passes
+// The kappa iterate a Jacobi pass of the recorded step works on: with U the iteration
+// being differentiated (BW[1] - 1), else the solve's last iterate; and the scale c of
+// the pass (dt_o for the divergence solve, dt_n^2 for the pressure solve).
+template <bool HAS_U, bool DIV>
+__device__ __forceinline__ const float* jacobi_kappa(const Dev& d, const AdjDev& a, const TapeStep& T) {
+    const uint32_t k = HAS_U ? a.BW[1] - 1u : (DIV ? T.kd : T.kp);
+    return (DIV ? T.KD : T.KP) + (size_t)k * d.stride;
+}
+template <bool DIV>
+__device__ __forceinline__ float jacobi_scale(const TapeStep& T) { return DIV ? T.dto : T.dtn * T.dtn; }
+
 // AK = P(kap) as the forward computes it (masks |k_i + k_j| > eps, |k_i| > eps);
 // with U: ABAR = c D^T(U) = c (V sum_j (u_i + u_j) gradW_ij + u_i GB_i).
-template <bool HAS_U>
-__global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const float* __restrict__ kap, float c) {
+template <bool HAS_U, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a) {
     ADJ_GROUP
+    const TapeStep& T = bstep(a);
+    const float* __restrict__ kap = jacobi_kappa<HAS_U, DIV>(d, a, T);
+    const float c = jacobi_scale<DIV>(T);
     const SceneDev& S = d.scenes[0];
     const float V = S.volume;
     float3 acc = make_float3(0.f, 0.f, 0.f), ab = acc;
@@ -273,9 +321,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a, const flo
 // KBAR += P^T(ABAR) (masked like P); XBAR += XP(kap, ABAR) + c XD(AK, U), where
 // XP(k, ab)_i = -V sum_j e_ij (k_i + k_j) H_ij (ab_i - ab_j) - k_i J_GB^T ab_i and
 // XD(w, u)_i = V sum_j H_ij (w_i - w_j)(u_i + u_j) + u_i J_GB^T w_i.
-template <bool HAS_U>
-__global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a, const float* __restrict__ kap, float c) {
+template <bool HAS_U, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a) {
     ADJ_GROUP
+    const TapeStep& T = bstep(a);
+    const float* __restrict__ kap = jacobi_kappa<HAS_U, DIV>(d, a, T);
+    const float c = jacobi_scale<DIV>(T);
     const SceneDev& S = d.scenes[0];
     const Spline sp(d.radius);
     const float V = S.volume;
@@ -331,8 +382,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a, const flo
 
 // VBAR += D^T(DBAR); XBAR += XD(w, DBAR); with DT also SC[1] += sum RABAR_i D_i(w).
 template <bool DT>
-__global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a, const float4* __restrict__ w) {
+__global__ void __launch_bounds__(kBlock) k_adj_div_b(Dev d, AdjDev a) {
     ADJ_GROUP
+    const TapeStep& T = bstep(a);
+    const float4* __restrict__ w = DT ? T.V2 : T.V0;  // v2 for the pressure solve's D, v0 for the divergence solve's
     const SceneDev& S = d.scenes[0];
     const Spline sp(d.radius);
     const float V = S.volume;
@@ -465,8 +518,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_density(Dev d, AdjDev a) {
 //   SC[0] += lambda_i . Q_i / rho_i, SC[2] += rho0 lt_i . dQ_i/d mu, SC[3] += rho0 lt_i . dQ_i/d mu_b,
 // where T_ij = cmu (m / rho_j)(g_ij . r) phi(|r|) r, phi = gs / (|r|^2 + eps2) and
 // R(r, g, w) = phi ((r . w) g + (g . r) w) + (g . r)(r . w)(phi' / |r|) r.
-__global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const float4* __restrict__ G, float dt) {
-    if (d.scenes[0].cgZeroG) return;  // lambda = 0
+__global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a) {
+    const TapeStep& T = bstep(a);
+    if (T.zeroG || d.scenes[0].cgZeroG) return;  // g = 0 in the forward step, or lambda = 0
+    const float4* __restrict__ G = T.G;
+    const float dt = T.dto;
     ADJ_GROUP
     const SceneDev& S = d.scenes[0];
     const Spline sp(d.radius);
@@ -566,10 +622,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a, const floa
 }
 
 // ---------------------------------------------------------------- element-wise steps
-__global__ void k_adj_load(Dev d, AdjDev a, const uint32_t* pid) {
+__global__ void k_adj_load(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n) return;
-    const uint32_t o = pid[p];
+    const uint32_t o = bstep(a).PID[p];
     a.XBAR[p] = a.XBO[o];
     a.VBAR[p] = a.VBO[o];
     a.RHOBAR[p] = 0.f;
@@ -577,17 +633,20 @@ __global__ void k_adj_load(Dev d, AdjDev a, const uint32_t* pid) {
 }
 
 // The boundary's velocity reset, then back to original order.
-__global__ void k_adj_store(Dev d, AdjDev a, const uint32_t* pid) {
+__global__ void k_adj_store(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n) return;
-    const uint32_t o = pid[p];
+    const uint32_t o = bstep(a).PID[p];
     a.XBO[o] = a.XBAR[p];
     a.VBO[o] = a.STOP[p] ? make_float4(0.f, 0.f, 0.f, 0.f) : a.VBAR[p];
 }
 
 // x' = x + dt_n v3, v3 = v2 + dt_n a_p (K20 + K21): v3 bar, dt_n bar; ABAR = dt_n v3 bar.
-__global__ void k_adj_pres_out(Dev d, AdjDev a, const float4* V2, float dtn) {
+__global__ void k_adj_pres_out(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const TapeStep& T = bstep(a);
+    const float4* V2 = T.V2;
+    const float dtn = T.dtn;
     float acc = 0.0f;
     if (p < d.n) {
         const float3 ap = f3(a.AK[p]);
@@ -605,8 +664,9 @@ __global__ void k_adj_pres_out(Dev d, AdjDev a, const float4* V2, float dtn) {
 }
 
 // v1 = v0 + dt_o a_d (K7): dt_o bar; ABAR = dt_o v1 bar.
-__global__ void k_adj_div_out(Dev d, AdjDev a, float dto) {
+__global__ void k_adj_div_out(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const float dto = bstep(a).dto;
     float acc = 0.0f;
     if (p < d.n) {
         const float3 vb = f3(a.VBAR[p]);
@@ -623,9 +683,15 @@ __global__ void k_adj_div_out(Dev d, AdjDev a, float dto) {
 // 1 pressure; r = 0 where skipped): U = [r < 0] alpha' k_bar; rho_adv bar += U,
 // alpha' bar += -r k_bar; f = scale * D(P(k)) gives SC[slot] += fdt * U f.
 template <bool DIV>
-__global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, const float* kap, float alphaScale,
-                        float fdt) {
+__global__ void k_adj_u(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const TapeStep& T = bstep(a);
+    const uint32_t k = a.BW[1] - 1u;
+    const float* res = (DIV ? T.RD : T.RP) + (size_t)k * d.stride;
+    const float* rhoadv = DIV ? T.RAD : T.RAP;
+    const float* kap = (DIV ? T.KD : T.KP) + (size_t)k * d.stride;
+    const float alphaScale = DIV ? 1.0f / T.dto : 1.0f / (T.dtn * T.dtn);
+    const float fdt = DIV ? 1.0f / T.dto : 2.0f / T.dtn;
     float acc = 0.0f;
     if (p < d.n) {
         const float r = res[p];
@@ -645,8 +711,11 @@ __global__ void k_adj_u(Dev d, AdjDev a, const float* res, const float* rhoadv, 
 
 // Pressure solve start (K17): k0 = max(rho_adv - 1, 0) alpha'', rho_adv = rho / rho0 + dt_n D(v2),
 // alpha'' = alpha / dt_n^2.
-__global__ void k_adj_pres_init(Dev d, AdjDev a, const float* rhoadv, float dtn) {
+__global__ void k_adj_pres_init(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const TapeStep& T = bstep(a);
+    const float* rhoadv = T.RAP;
+    const float dtn = T.dtn;
     float acc = 0.0f;
     if (p < d.n) {
         const SceneDev& S = d.scenes[0];
@@ -667,8 +736,11 @@ __global__ void k_adj_pres_init(Dev d, AdjDev a, const float* rhoadv, float dtn)
 
 // Divergence solve start (K4): k0 = rho_adv alpha', rho_adv = [n >= 20] max(D(v0), 0),
 // alpha' = alpha / dt_o.
-__global__ void k_adj_div_init(Dev d, AdjDev a, const float* rhoadv, float dto) {
+__global__ void k_adj_div_init(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const TapeStep& T = bstep(a);
+    const float* rhoadv = T.RAD;
+    const float dto = T.dto;
     float acc = 0.0f;
     if (p < d.n) {
         const float ra = rhoadv[p];
@@ -684,10 +756,19 @@ __global__ void k_adj_div_init(Dev d, AdjDev a, const float* rhoadv, float dto) 
     block_add(a.SC + 0, acc);
 }
 
+// Viscosity mode of the recorded step: 0 no viscosity, 1 viscosity, 2 viscosity with g = 0
+// (the forward CG's right-hand side was zero).
+__device__ __forceinline__ int visc_mode(const TapeStep& T, int visc) { return !visc ? 0 : (T.zeroG ? 2 : 1); }
+
 // v2 = v1 + dt_n a with a = gravity (+ (g - v1) / dt_o with viscosity; g = 0 when the CG
-// right-hand side was zero). mode: 0 no viscosity, 1 viscosity, 2 viscosity with g = 0.
-__global__ void k_adj_velocity(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, float dtn, int mode) {
+// right-hand side was zero).
+__global__ void k_adj_velocity(Dev d, AdjDev a, int visc) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const TapeStep& T = bstep(a);
+    const float4* V1 = T.V1;
+    const float4* G = T.G;
+    const float dto = T.dto, dtn = T.dtn;
+    const int mode = visc_mode(T, visc);
     float sn = 0.0f, so = 0.0f;
     if (p < d.n) {
         const SceneDev& S = d.scenes[0];
@@ -712,7 +793,12 @@ __global__ void k_adj_velocity(Dev d, AdjDev a, const float4* V1, const float4* 
 
 // CFL (k_visc_finish + k_ctrl_dt): dt_n = 0.4 d / sqrt(|w*|^2) for the particle with the
 // largest |w|^2 = |v1 + a dt_o|^2; d dt_n / d w = -dt_n w / |w|^2. The first kernel finds
-// the largest recomputed |w|^2, the second gives its particle the derivative.
+// the largest recomputed |w|^2, the second gives its particle the derivative. Both do
+// nothing when dt_n was not the CFL value (clamped to its bounds, or |w|^2 <= 0.1): the
+// forward's own expression, evaluated again on the device, decides.
+__device__ __forceinline__ bool cfl_active(const TapeStep& T) {
+    return T.maxV2 > 0.1f && 0.4f * (T.pre.diam / sqrtf(T.maxV2)) == T.dtn;
+}
 __device__ __forceinline__ float3 cfl_w(const Dev& d, const float4* V1, const float4* G, uint32_t p, float dto,
                                         int mode) {
     const SceneDev& S = d.scenes[0];
@@ -724,17 +810,20 @@ __device__ __forceinline__ float3 cfl_w(const Dev& d, const float4* V1, const fl
     }
     return v1 + acc * dto;
 }
-__global__ void k_adj_cfl_max(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, int mode) {
+__global__ void k_adj_cfl_max(Dev d, AdjDev a, int visc) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
-    const float3 w = cfl_w(d, V1, G, p, dto, mode);
+    const TapeStep& T = bstep(a);
+    if (p >= d.n || !cfl_active(T)) return;
+    const float3 w = cfl_w(d, T.V1, T.G, p, T.dto, visc_mode(T, visc));
     atomicMax(a.CLAIM, __float_as_uint(dot3(w, w)));
 }
-__global__ void k_adj_cfl(Dev d, AdjDev a, const float4* V1, const float4* G, float dto, float dtn, float maxV2,
-                          int mode) {
+__global__ void k_adj_cfl(Dev d, AdjDev a, int visc) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
-    const float3 w = cfl_w(d, V1, G, p, dto, mode);
+    const TapeStep& T = bstep(a);
+    if (p >= d.n || !cfl_active(T)) return;
+    const int mode = visc_mode(T, visc);
+    const float dtn = T.dtn, maxV2 = T.maxV2;
+    const float3 w = cfl_w(d, T.V1, T.G, p, T.dto, mode);
     if (__float_as_uint(dot3(w, w)) != a.CLAIM[0]) return;
     if (atomicExch(a.CLAIM + 1, 1u) != 0u) return;
     const SceneDev& S = d.scenes[0];
@@ -746,57 +835,104 @@ __global__ void k_adj_cfl(Dev d, AdjDev a, const float4* V1, const float4* G, fl
     else if (mode == 0) a.VBAR[p] = f4(f3(a.VBAR[p]) + wb, 0.f);
 }
 
-// v1 bar += lambda, unless the adjoint solve's right-hand side was zero (lambda = 0).
+// v1 bar += lambda, unless the adjoint solve's right-hand side was zero (lambda = 0) or the
+// forward step's was (g = 0, no solve to differentiate).
 __global__ void k_adj_add_lambda(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || d.scenes[0].cgZeroG) return;
+    if (p >= d.n || bstep(a).zeroG || d.scenes[0].cgZeroG) return;
     a.VBAR[p] = f4(f3(a.VBAR[p]) + f3(d.CG[p]), 0.f);
 }
 
-// Initial guess lambda_0 = lambda of the step after this one (kept in LAM: the forward
-// CG of replayed steps reuses CG): the CG starts from V + DV with V = g_bar, so DV = LAM - V.
-__global__ void k_adj_warm(Dev d, AdjDev a) {
+// Right-hand side and initial guess lambda_0 of the adjoint viscosity solve (mode:
+// VFD_WARM_*). The forward CG solves A g = V from V + DV, so V = g_bar (0 when the forward
+// step's right-hand side was zero: the CG then stops at once) and DV = lambda_0 - V. LAM
+// holds the lambda of the step after this one, LAM2 the one after that (the forward CG of
+// replayed steps reuses CG, so they are kept apart). Cold: lambda_0 = g_bar (DV = 0);
+// previous: LAM; extrapolate: 2 LAM - LAM2, the linear extrapolation in time of the
+// sequence of solutions, once two exist.
+__global__ void k_adj_visc_start(Dev d, AdjDev a, int mode) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n) return;
-    d.DV[p] = f4(f3(a.LAM[p]) - f3(d.V[p]), 0.f);
+    const bool zero = bstep(a).zeroG != 0u;
+    d.V[p] = zero ? make_float4(0.f, 0.f, 0.f, 0.f) : a.GBAR[p];
+    const uint32_t have = a.ACNT[3];
+    if (zero || mode == 0 || have == 0) {
+        d.DV[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float3 l1 = f3(a.LAM[p]);
+    const float3 x0 = (mode == 2 && have >= 2) ? 2.0f * l1 - f3(a.LAM2[p]) : l1;
+    d.DV[p] = f4(x0 - f3(a.GBAR[p]), 0.f);
 }
 
-// Keeps this step's lambda for the next solve.
+// Keeps this step's lambda for the next solves and counts the solve's iterations.
 __global__ void k_adj_keep(Dev d, AdjDev a) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || d.scenes[0].cgZeroG) return;
+    const SceneDev& S = d.scenes[0];
+    if (bstep(a).zeroG) return;  // no solve in this step
+    if (p == 0) {
+        const uint32_t it = S.cgIt;
+        a.ACNT[0] += it;
+        a.ACNT[1] = max(a.ACNT[1], it);
+        a.ACNT[2] += 1u;
+        if (!S.cgZeroG) a.ACNT[3] = min(a.ACNT[3] + 1u, 2u);
+    }
+    if (p >= d.n || S.cgZeroG) return;
+    a.LAM2[p] = a.LAM[p];
     a.LAM[p] = d.CG[p];
 }
 
-// dt_o of this step is dt_n of the step before.
+// dt_o of this step is dt_n of the step before; the next step to differentiate is the
+// one before (the slot below).
 __global__ void k_adj_carry(AdjDev a) {
     a.SC[1] = a.SC[0];
     a.SC[0] = 0.0;
     a.CLAIM[0] = 0u;
     a.CLAIM[1] = 0u;
+    if (a.BW[0] > 0u) a.BW[0] -= 1u;
 }
 
-// ---------------------------------------------------------------- tape
-// One recorded step: written by the tape kernels at the tape points of the step
-// (TapePoint), so that one recording graph serves every step: the slot of the current
-// step is steps[*cur], advanced by the step's last tape point.
-struct TapeStep {
-    float4 *Xpre, *V0, *V1, *G, *V2;
-    uint32_t *PID, *NCNT, *NBR;
-    float *RAD, *RAP;
-    float *KD, *RD, *KP, *RP;   // kappa^0..cap, res^0..cap-1 (stride floats each) of each solve
-    uint32_t capD, capP;
-    // written on the device
-    SceneDev pre;               // scene state at the start of the step
-    uint32_t kd, kp, overflow, zeroG, maxNbr, aborted;
-    float dto, dtn, maxV2;
-};
-struct TapeSet {
-    TapeStep* steps;
-    uint32_t* cur;
-    uint32_t count;
-};
+// The slot of the first step a backward segment differentiates (its last recorded step).
+__global__ void k_adj_set_slot(AdjDev a, uint32_t slot) { a.BW[0] = slot; }
 
+// The forward arrays of the recorded step: positions before the step, neighbour counts and
+// rows, and the scene state at its start (the first block copies it word by word).
+__global__ void k_adj_fetch(Dev d, AdjDev a) {
+    const TapeStep& T = bstep(a);
+    if (blockIdx.x == 0) {
+        static_assert(sizeof(SceneDev) % 4 == 0, "SceneDev is copied in 32-bit words");
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(&T.pre);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(d.scenes);
+        for (uint32_t w = threadIdx.x; w < sizeof(SceneDev) / 4; w += blockDim.x) dst[w] = src[w];
+    }
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.n) return;
+    d.X[p] = T.Xpre[p];
+    d.NCNT[p] = T.NCNT[p];
+    const uint4* rs = reinterpret_cast<const uint4*>(T.NBR + (size_t)p * kRow);
+    uint4* rd = reinterpret_cast<uint4*>(d.NBR + (size_t)p * kRow);
+#pragma unroll
+    for (uint32_t k = 0; k < kRow / 4u; k++) rd[k] = rs[k];
+}
+
+// Jacobi loop control of the backward pass: the recorded solve's iterations are
+// differentiated last to first, BW[1] counting those left; in a graph the loop's
+// conditional handle follows it.
+template <bool DIV>
+__global__ void k_adj_loop_init(AdjDev a) {
+    const TapeStep& T = bstep(a);
+    const uint32_t left = DIV ? T.kd : T.kp;
+    a.BW[1] = left;
+    if (a.hLoop[DIV]) cudaGraphSetConditional((cudaGraphConditionalHandle)a.hLoop[DIV], left > 0u ? 1u : 0u);
+}
+template <bool DIV>
+__global__ void k_adj_loop_next(AdjDev a) {
+    const uint32_t left = a.BW[1] - 1u;
+    a.BW[1] = left;
+    if (a.hLoop[DIV]) cudaGraphSetConditional((cudaGraphConditionalHandle)a.hLoop[DIV], left > 0u ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------- tape points
 __device__ __forceinline__ TapeStep& tape_step(const TapeSet* ts) { return ts->steps[*ts->cur]; }
 
 __global__ void k_tape_begin(Dev d, const TapeSet* ts) {
@@ -894,8 +1030,6 @@ void tape_point(const Dev& d, const void* rec, int point, cudaStream_t st) {
 
 namespace {
 
-#define ADJ_LAUNCH(kernel, grid, ...) kernel<<<(grid), kBlock, 0, st>>>(__VA_ARGS__)
-
 struct Checkpoint {
     float4 *XN = nullptr, *V = nullptr, *DV = nullptr;
     float* DK = nullptr;
@@ -916,7 +1050,7 @@ struct AdjointState {
     TapeStep* dsteps = nullptr;
     uint32_t* dcur = nullptr;
     bool lastRecorded = false;     // the forward run recorded its last segment
-    bool warm = false;             // CG holds the last adjoint viscosity solution
+    uint32_t replayed = 0;         // steps re-run by the last backward pass
     std::vector<void*> allocs;
     AdjDev a{};
     ~AdjointState() {
@@ -1025,8 +1159,6 @@ int restore_checkpoint(vfd_sim* s, const Checkpoint& c) {
     return VFD_OK;
 }
 
-#define COPY(dst, src, bytes) CK(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st))
-
 // `count` steps from the current state, recorded into the tape slots 0..count-1, as CUDA
 // graphs (one per parity) unless graphs are off; then the slots' device-written fields
 // are read back and checked.
@@ -1065,130 +1197,200 @@ int record_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
     return VFD_OK;
 }
 
-// The adjoint solve A lambda = g_bar: the forward CG (precondition, setup, loop) on the
-// backward's working set, as one graph with a device-side while loop.
-int build_cg_graph(vfd_sim* s, AdjointState* A) {
+// ---------------------------------------------------------------- backward pass of one step
+// The backward pass of recorded step BW[0] in stages, shared by the backward graph (one
+// per simulation, launched once per step, its loops conditional nodes) and the host-driven
+// path (loops counted on the host). Every kernel reads what it needs of the step (arrays,
+// time steps, iteration counts, decisions) from its tape slot, so the same launches serve
+// every step; a.hLoop / d.condHandle are the graph's conditional handles, or 0.
+struct BwdLaunch {
+    Dev d;
+    AdjDev a;
+    cudaStream_t st;
+    uint32_t g1, gG;
+    int visc, warm;
+};
+
+// Step inputs, boundary data, density and factor; the pressure solve's output (K20 + K21,
+// v3 and x') and the start of its Jacobi iterations.
+void bwd_head(const BwdLaunch& L, uint32_t* dStatus) {
+    cudaMemsetAsync(dStatus, 0, 16 * sizeof(uint32_t), L.st);
+    k_adj_fetch<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_bdata<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    launch_boundary(L.d, L.st);
+    launch_density(L.d, L.st);
+    k_adj_load<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_jac_a<false, false><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_pres_out<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_jac_b<false, false><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_loop_init<false><<<1, 1, 0, L.st>>>(L.a);
+}
+
+// One Jacobi iteration of a solve, differentiated (the last first).
+template <bool DIV>
+void bwd_jacobi(const BwdLaunch& L) {
+    k_adj_u<DIV><<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_jac_a<true, DIV><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_jac_b<true, DIV><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_loop_next<DIV><<<1, 1, 0, L.st>>>(L.a);
+}
+
+// Pressure solve start (K17), K16 velocity update and the CFL time step; with viscosity the
+// start of the adjoint solve A lambda = g_bar with the forward's CG.
+void bwd_mid(const BwdLaunch& L) {
+    k_adj_pres_init<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_div_b<true><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_velocity<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc);
+    k_adj_cfl_max<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc);
+    k_adj_cfl<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc);
+    if (L.visc) {
+        k_adj_visc_start<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.warm);
+        launch_visc_init(L.d, L.st);
+    }
+}
+
+// After the adjoint viscosity solve: v1 bar += lambda, and the derivative of A g = v1.
+void bwd_visc_tail(const BwdLaunch& L) {
+    k_adj_add_lambda<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_keep<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_visc<<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+}
+
+// Divergence solve (K4-K7): its output v1 = v0 + dt_o a_d, then its iterations.
+void bwd_div_head(const BwdLaunch& L) {
+    k_adj_jac_a<false, true><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_div_out<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_jac_b<false, true><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_loop_init<true><<<1, 1, 0, L.st>>>(L.a);
+}
+void bwd_div_tail(const BwdLaunch& L) {
+    k_adj_div_init<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_div_b<false><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+}
+
+// Density and factor (K2 + K3), the boundary's velocity reset and original order; the
+// step before is next.
+void bwd_end(const BwdLaunch& L) {
+    k_adj_gsum<<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_density<<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_store<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
+    k_adj_carry<<<1, 1, 0, L.st>>>(L.a);
+}
+
+BwdLaunch bwd_launch(vfd_sim* s, const AdjointState* A, cudaStream_t st) {
+    BwdLaunch L{};
+    L.d = s->dev[0];
+    L.d.rowLoops = 1u;  // the recorded rows; the cell tables are not the recorded step's
+    for (auto& h : L.d.condHandle) h = 0ull;
+    L.a = A->a;
+    L.a.hLoop[0] = L.a.hLoop[1] = 0ull;
+    L.st = st;
+    L.g1 = blocks_for(s->n);
+    L.gG = blocks_for(s->n * kAG);
+    L.visc = s->anyVisc ? 1 : 0;
+    L.warm = s->adjWarm;
+    return L;
+}
+
+// The backward pass of one step as a graph: the Jacobi loops and the adjoint CG as
+// conditional WHILE nodes whose handles the loop-control kernels set.
+int build_backward_graph(vfd_sim* s, AdjointState* A) {
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h;
-    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+    const bool div = s->anyDiv, visc = s->anyVisc;
+    cudaGraphConditionalHandle hP = 0, hD = 0, hC = 0;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&hP, g, 0, 0);
+    if (e == cudaSuccess && div) e = cudaGraphConditionalHandleCreate(&hD, g, 0, 0);
+    if (e == cudaSuccess && visc) e = cudaGraphConditionalHandleCreate(&hC, g, 0, 0);
     if (e != cudaSuccess) {
         cudaGraphDestroy(g);
         return fail(VFD_E_CUDA, "adjoint: cudaGraphConditionalHandleCreate: %s", cudaGetErrorString(e));
     }
-    Dev d = s->dev[0];
-    d.condHandle[1] = (unsigned long long)h;
-    d.rowLoops = 1u;  // the recorded rows; the cell tables are not the recorded step's
+    BwdLaunch L = bwd_launch(s, A, s->stream);
+    L.a.hLoop[0] = (unsigned long long)hP;
+    L.a.hLoop[1] = (unsigned long long)hD;
+    L.d.condHandle[1] = (unsigned long long)hC;  // the CG loop's (set_condition of the forward's CG kernels)
+    uint32_t* dStatus = s->dStatus;
     std::vector<cudaGraphNode_t> leaves;
-    e = add_segment(s->stream, g, leaves, [&](cudaStream_t st) { launch_visc_init(d, st); });
-    if (e == cudaSuccess) e = add_while(s->stream, g, h, leaves, [&](cudaStream_t st) { launch_cg_iter(d, st); });
+    cudaStream_t cap = s->stream;
+    e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        L.st = st;
+        bwd_head(L, dStatus);
+    });
+    if (e == cudaSuccess) e = add_while(cap, g, hP, leaves, [&](cudaStream_t st) {
+        L.st = st;
+        bwd_jacobi<false>(L);
+    });
+    if (e == cudaSuccess) e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        L.st = st;
+        bwd_mid(L);
+    });
+    if (e == cudaSuccess && visc) e = add_while(cap, g, hC, leaves, [&](cudaStream_t st) { launch_cg_iter(L.d, st); });
+    if (e == cudaSuccess) e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        L.st = st;
+        if (visc) bwd_visc_tail(L);
+        if (div) bwd_div_head(L);
+    });
+    if (e == cudaSuccess && div) e = add_while(cap, g, hD, leaves, [&](cudaStream_t st) {
+        L.st = st;
+        bwd_jacobi<true>(L);
+    });
+    if (e == cudaSuccess) e = add_segment(cap, g, leaves, [&](cudaStream_t st) {
+        L.st = st;
+        if (div) bwd_div_tail(L);
+        bwd_end(L);
+    });
     cudaGraphExec_t exec = nullptr;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
     if (e != cudaSuccess) {
         cudaGetLastError();
         cudaGraphDestroy(g);
-        return fail(VFD_E_CUDA, "adjoint: CG graph construction failed: %s", cudaGetErrorString(e));
+        return fail(VFD_E_CUDA, "adjoint: backward graph construction failed: %s", cudaGetErrorString(e));
     }
-    s->adjCgGraph = g;
-    s->adjCgExec = exec;
+    s->adjBwdGraph = g;
+    s->adjBwdExec = exec;
     return VFD_OK;
 }
 
-// Backward pass of recorded step t (tape slot t); A->a.XBO / VBO hold the cotangents of
-// its outputs on entry and of its inputs on return. No host synchronisation.
-int backward_step(vfd_sim* s, AdjointState* A, uint32_t t) {
-    cudaStream_t st = s->stream;
-    const Dev& d = s->dev[0];
-    AdjDev& a = A->a;
+// Backward pass of recorded step t (tape slot t, which BW[0] holds) from the host: the
+// loops run the recorded iteration counts, the CG reads its flag once per iteration.
+// A->a.XBO / VBO hold the cotangents of the step's outputs on entry and of its inputs
+// on return.
+int backward_step_eager(vfd_sim* s, AdjointState* A, uint32_t t) {
     const TapeStep& T = A->host[t];
-    const uint32_t n = s->n;
-    const uint32_t g1 = blocks_for(n), gG = blocks_for(n * kAG);
-    const size_t sd = s->stride;
-    auto KD = [&](uint32_t k) { return T.KD + (size_t)k * sd; };
-    auto RD = [&](uint32_t k) { return T.RD + (size_t)k * sd; };
-    auto KP = [&](uint32_t k) { return T.KP + (size_t)k * sd; };
-    auto RP = [&](uint32_t k) { return T.RP + (size_t)k * sd; };
-    // the forward arrays of this step
-    COPY(s->dScenes, &A->dsteps[t].pre, sizeof(SceneDev));
-    COPY(d.X, T.Xpre, sizeof(float4) * sd);
-    COPY(d.NCNT, T.NCNT, sizeof(uint32_t) * sd);
-    COPY(d.NBR, T.NBR, sizeof(uint32_t) * sd * kRow);
-    CK(cudaMemsetAsync(s->dStatus, 0, 16 * sizeof(uint32_t), st));
-    ADJ_LAUNCH(k_adj_bdata, g1, d, a);
-    launch_boundary(d, st);
-    launch_density(d, st);
-    ADJ_LAUNCH(k_adj_load, g1, d, a, T.PID);
-
-    // pressure solve, K20 + K21 (v3 and x')
-    const float dtn = T.dtn, dto = T.dto;
-    const uint32_t kp = T.kp;
-    ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, KP(kp), 0.0f);
-    ADJ_LAUNCH(k_adj_pres_out, g1, d, a, T.V2, dtn);
-    ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, KP(kp), 0.0f);
-    for (uint32_t k = kp; k-- > 0;) {
-        ADJ_LAUNCH(k_adj_u<false>, g1, d, a, RP(k), T.RAP, KP(k), 1.0f / (dtn * dtn), 2.0f / dtn);
-        ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, KP(k), dtn * dtn);
-        ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, KP(k), dtn * dtn);
-    }
-    ADJ_LAUNCH(k_adj_pres_init, g1, d, a, T.RAP, dtn);
-    ADJ_LAUNCH(k_adj_div_b<true>, gG, d, a, T.V2);
-
-    // K16 velocity update and the CFL time step
-    const bool visc = s->anyVisc, div = s->anyDiv;
-    const int mode = !visc ? 0 : (T.zeroG ? 2 : 1);
-    ADJ_LAUNCH(k_adj_velocity, g1, d, a, T.V1, T.G, dto, dtn, mode);
-    const float raw = 0.4f * (T.pre.diam / sqrtf(T.maxV2));
-    if (T.maxV2 > 0.1f && raw == T.dtn) {
-        ADJ_LAUNCH(k_adj_cfl_max, g1, d, a, T.V1, T.G, dto, mode);
-        ADJ_LAUNCH(k_adj_cfl, g1, d, a, T.V1, T.G, dto, dtn, T.maxV2, mode);
-    }
-
-    // viscosity: A lambda = g_bar with the forward's CG, then the derivative of A g = v1
-    if (mode == 1) {
-        COPY(d.V, a.GBAR, sizeof(float4) * sd);
-        // initial guess: the previous backward step's lambda (still in CG) when there is one
-        if (A->warm) ADJ_LAUNCH(k_adj_warm, g1, d, a);
-        else CK(cudaMemsetAsync(d.DV, 0, sizeof(float4) * sd, st));
-        if (s->graphMode && !s->graphFailed) {
-            if (!s->adjCgExec) TRY(build_cg_graph(s, A));
-            CK(cudaGraphLaunch(s->adjCgExec, st));
-        } else {  // eager: one flag read per CG iteration
-            uint32_t more = 0;
-            Dev dr = d;
-            dr.rowLoops = 1u;  // the recorded rows; the cell tables are not the recorded step's
-            launch_visc_init(dr, st);
+    const BwdLaunch L = bwd_launch(s, A, s->stream);
+    bwd_head(L, s->dStatus);
+    for (uint32_t k = 0; k < T.kp; k++) bwd_jacobi<false>(L);
+    bwd_mid(L);
+    if (L.visc) {
+        uint32_t more = 0;
+        TRY(read_flag(s, 5, more));
+        for (uint32_t guard = 0; more && guard < 100000u; guard++) {
+            launch_cg_iter(L.d, L.st);
             TRY(read_flag(s, 5, more));
-            for (uint32_t guard = 0; more && guard < 100000u; guard++) {
-                launch_cg_iter(dr, st);
-                TRY(read_flag(s, 5, more));
-            }
         }
-        A->warm = true;
-        ADJ_LAUNCH(k_adj_add_lambda, g1, d, a);
-        ADJ_LAUNCH(k_adj_keep, g1, d, a);
-        ADJ_LAUNCH(k_adj_visc, gG, d, a, T.G, dto);
+        bwd_visc_tail(L);
     }
-
-    // divergence solve, K4-K7
-    if (div) {
-        const uint32_t kd = T.kd;
-        ADJ_LAUNCH(k_adj_jac_a<false>, gG, d, a, KD(kd), 0.0f);
-        ADJ_LAUNCH(k_adj_div_out, g1, d, a, dto);
-        ADJ_LAUNCH(k_adj_jac_b<false>, gG, d, a, KD(kd), 0.0f);
-        for (uint32_t k = kd; k-- > 0;) {
-            ADJ_LAUNCH(k_adj_u<true>, g1, d, a, RD(k), T.RAD, KD(k), 1.0f / dto, 1.0f / dto);
-            ADJ_LAUNCH(k_adj_jac_a<true>, gG, d, a, KD(k), dto);
-            ADJ_LAUNCH(k_adj_jac_b<true>, gG, d, a, KD(k), dto);
-        }
-        ADJ_LAUNCH(k_adj_div_init, g1, d, a, T.RAD, dto);
-        ADJ_LAUNCH(k_adj_div_b<false>, gG, d, a, T.V0);
+    if (s->anyDiv) {
+        bwd_div_head(L);
+        for (uint32_t k = 0; k < T.kd; k++) bwd_jacobi<true>(L);
+        bwd_div_tail(L);
     }
+    bwd_end(L);
+    CK(cudaGetLastError());
+    return VFD_OK;
+}
 
-    // density and factor (K2 + K3), then the boundary's velocity reset and original order
-    ADJ_LAUNCH(k_adj_gsum, gG, d, a);
-    ADJ_LAUNCH(k_adj_density, gG, d, a);
-    ADJ_LAUNCH(k_adj_store, g1, d, a, T.PID);
-    k_adj_carry<<<1, 1, 0, st>>>(a);
+// The backward pass of a recorded segment of `count` steps, the last first.
+int backward_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
+    cudaStream_t st = s->stream;
+    k_adj_set_slot<<<1, 1, 0, st>>>(A->a, count - 1u);
+    const bool graphs = s->graphMode && !s->graphFailed;
+    if (graphs && !s->adjBwdExec) TRY(build_backward_graph(s, A));
+    for (uint32_t t = count; t-- > 0;) {
+        if (graphs) CK(cudaGraphLaunch(s->adjBwdExec, st));
+        else TRY(backward_step_eager(s, A, t));
+    }
     CK(cudaGetLastError());
     return VFD_OK;
 }
@@ -1215,6 +1417,9 @@ int alloc_cotangents(vfd_sim* s, AdjointState* A) {
     TRY(aalloc(A, &a.U, st));
     TRY(aalloc(A, &a.KU, st));
     TRY(aalloc(A, &a.LAM, st));
+    TRY(aalloc(A, &a.LAM2, st));
+    TRY(aalloc(A, &a.ACNT, 4));
+    TRY(aalloc(A, &a.BW, 2));
     TRY(aalloc(A, &a.RABAR, st));
     TRY(aalloc(A, &a.APBAR, st));
     TRY(aalloc(A, &a.DBAR, st));
@@ -1243,7 +1448,16 @@ __global__ void k_adj_unpack(float* dst, const float4* src, uint32_t n) {
 
 }  // namespace
 
+// The backward graph addresses the adjoint state's arrays: it goes with them.
+void drop_backward_graph(vfd_sim* s) {
+    if (s->adjBwdExec) cudaGraphExecDestroy(s->adjBwdExec);
+    if (s->adjBwdGraph) cudaGraphDestroy(s->adjBwdGraph);
+    s->adjBwdExec = nullptr;
+    s->adjBwdGraph = nullptr;
+}
+
 void adjoint_release(vfd_sim* s) {
+    drop_backward_graph(s);
     delete s->adjoint;
     s->adjoint = nullptr;
 }
@@ -1272,6 +1486,7 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
                A->host[0].capD == capD && A->host[0].capP == capP))
         A.reset();
     if (!A) {
+        drop_backward_graph(s);
         A = std::make_unique<AdjointState>();
         A->every = every;
         A->n = s->n;
@@ -1285,7 +1500,6 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
     }
     A->steps = steps;
     A->lastRecorded = false;
-    A->warm = false;
     const uint32_t segs = (steps + A->every - 1) / A->every;
     A->ckpt.resize(segs + 1);
     for (uint32_t k = 0; k < segs; k++) {
@@ -1331,6 +1545,10 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
     cudaStream_t st = s->stream;
     if (!A->a.XBAR) TRY(alloc_cotangents(s, A));
     AdjDev& a = A->a;
+    if (a.ts != A->dset) {  // the tape set moved (new buffers): graphs addressing the old one are gone
+        drop_backward_graph(s);
+        a.ts = A->dset;
+    }
     // cotangents of the final state, original order
     CK(cudaMemcpyAsync(s->dStage, x_bar, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
     k_adj_pack<<<blocks_for(n, 256), 256, 0, st>>>(a.XBO, s->dStage, n);
@@ -1338,15 +1556,18 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
     k_adj_pack<<<blocks_for(n, 256), 256, 0, st>>>(a.VBO, s->dStage, n);
     CK(cudaMemsetAsync(a.SC, 0, 8 * sizeof(double), st));
     CK(cudaMemsetAsync(a.CLAIM, 0, 2 * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(a.ACNT, 0, 4 * sizeof(uint32_t), st));
     const uint32_t segs = (uint32_t)A->ckpt.size() - 1;
     int rc = VFD_OK;
+    A->replayed = 0;
     for (uint32_t k = segs; k-- > 0 && rc == VFD_OK;) {
         const uint32_t cnt = std::min(A->every, A->steps - k * A->every);
         if (!(k + 1 == segs && A->lastRecorded)) {
             rc = restore_checkpoint(s, A->ckpt[k]);
             if (rc == VFD_OK) rc = record_segment(s, A, cnt);
+            A->replayed += cnt;
         }
-        for (uint32_t t = cnt; t-- > 0 && rc == VFD_OK;) rc = backward_step(s, A, t);
+        if (rc == VFD_OK) rc = backward_segment(s, A, cnt);
     }
     // the tape now holds the first segment; leave the simulation where the forward run ended
     A->lastRecorded = false;
@@ -1377,6 +1598,32 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
 int vfd_adjoint_release(vfd_sim* s) {
     if (!s) return fail(VFD_E_ARG, "null handle");
     adjoint_release(s);
+    return VFD_OK;
+}
+
+int vfd_adjoint_set_warm_start(vfd_sim* s, int32_t mode) {
+    if (!s) return fail(VFD_E_ARG, "null handle");
+    if (mode < VFD_WARM_COLD || mode > VFD_WARM_EXTRAPOLATE) return fail(VFD_E_ARG, "unknown warm-start mode %d", mode);
+    if (mode != s->adjWarm) drop_backward_graph(s);  // the backward graph carries the mode
+    s->adjWarm = mode;
+    return VFD_OK;
+}
+
+int vfd_adjoint_get_stats(vfd_sim* s, vfd_adjoint_stats* out) {
+    if (!s || !out) return fail(VFD_E_ARG, "null argument");
+    *out = vfd_adjoint_stats{};
+    const AdjointState* A = s->adjoint;
+    if (!A) return fail(VFD_E_STATE, "adjoint: no recorded forward run (call vfd_adjoint_forward first)");
+    out->Steps = A->steps;
+    if (!A->a.ACNT) return VFD_OK;  // no backward pass yet
+    uint32_t c[4];
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemcpyAsync(c, A->a.ACNT, sizeof(c), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    out->ReplayedSteps = A->replayed;
+    out->ViscositySolverIterations = c[0];
+    out->MaxViscositySolverIterations = c[1];
+    out->ViscositySolves = c[2];
     return VFD_OK;
 }
 

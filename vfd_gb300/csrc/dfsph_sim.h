@@ -213,14 +213,15 @@ struct vfd_sim {
     // adjoint: checkpoints and tapes of the last vfd_adjoint_forward; `generation`
     // counts uploads, so a reset after the recorded run is detected
     vfd::AdjointState* adjoint = nullptr;
+    int adjWarm = 2;  // VFD_WARM_* of the adjoint viscosity solves
     uint64_t generation = 0;
     // kept across adjoint runs while the buffers live: the device tape set that recording
-    // graphs address, those graphs (one per parity) and the adjoint CG solve's graph
+    // graphs address, those graphs (one per parity) and the backward graph of one step
     void* adjTapeSet = nullptr;
     cudaGraph_t adjRecGraph[2] = {nullptr, nullptr};
     cudaGraphExec_t adjRecExec[2] = {nullptr, nullptr};
-    cudaGraph_t adjCgGraph = nullptr;
-    cudaGraphExec_t adjCgExec = nullptr;
+    cudaGraph_t adjBwdGraph = nullptr;
+    cudaGraphExec_t adjBwdExec = nullptr;
 
     ~vfd_sim() { release(); }
 
@@ -235,10 +236,10 @@ struct vfd_sim {
             adjRecExec[k] = nullptr;
             adjRecGraph[k] = nullptr;
         }
-        if (adjCgExec) cudaGraphExecDestroy(adjCgExec);
-        if (adjCgGraph) cudaGraphDestroy(adjCgGraph);
-        adjCgExec = nullptr;
-        adjCgGraph = nullptr;
+        if (adjBwdExec) cudaGraphExecDestroy(adjBwdExec);
+        if (adjBwdGraph) cudaGraphDestroy(adjBwdGraph);
+        adjBwdExec = nullptr;
+        adjBwdGraph = nullptr;
     }
     void releaseBuffers() {
         releaseGraphs();
