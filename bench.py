@@ -281,6 +281,7 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
     xb = (2.0 / n) * (x.astype(np.float64) - target)
     x0b, v0b, pb = sim.AdjointBackward(xb.astype(np.float32), np.zeros_like(v))
     t_adj = time.perf_counter() - t0
+    adj_stats = sim.AdjointStats()
     # the same run with every step recorded in the forward pass (no segment replays):
     # what 280 GB of HBM allows at this size
     restart()
@@ -339,6 +340,9 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
             "forward": n * steps / t_fwd, "fwd_adjoint": n * steps / t_adj, "adjoint_over_forward": t_adj / t_fwd,
             "forward_s": t_fwd, "fwd_adjoint_s": t_adj,
             "every_step_recorded": {"fwd_adjoint_s": t_all, "adjoint_over_forward": t_all / t_fwd},
+            "backward": {"replayed_steps": adj_stats["ReplayedSteps"],
+                         "viscosity_cg_iterations": adj_stats["ViscositySolverIterations"],
+                         "max_viscosity_cg_iterations": adj_stats["MaxViscositySolverIterations"]},
             "grad_check": {"variant": "same scene, fixed dt 1 ms, divergence solve off, pressure iterations "
                                       "pinned to 3, analytic kernel" if analytic_check else
                                       "same scene, fixed dt 1 ms, divergence solve off, pressure iterations "

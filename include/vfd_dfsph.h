@@ -503,11 +503,13 @@ int vfd_adjoint_release(vfd_sim* sim);
 
 /*
  * Initial guess of each backward step's viscosity solve A lambda = g_bar (the steps
- * are walked from the last to the first): VFD_WARM_COLD starts from g_bar, as the
- * forward solve starts from its right-hand side; VFD_WARM_PREVIOUS from the lambda of
- * the step after; VFD_WARM_EXTRAPOLATE (default) from 2 lambda(t+1) - lambda(t+2), the
- * linear extrapolation of the last two solutions, once two exist. Every choice solves to
- * the same tolerance; they differ in iteration count. No counterpart in the reference.
+ * are walked from the last to the first): VFD_WARM_COLD (default) starts from g_bar;
+ * VFD_WARM_PREVIOUS from the lambda of the step after; VFD_WARM_EXTRAPOLATE from
+ * 2 lambda(t+1) - lambda(t+2), the linear extrapolation of the last two solutions, once
+ * two exist. Every choice solves to the same tolerance and differs in iteration count
+ * (the cotangents change too much from step to step for the earlier solutions to help:
+ * on a 33k-particle viscous drop, 60 steps, 1113 / 1229 / 1280 iterations). No
+ * counterpart in the reference.
  */
 #define VFD_WARM_COLD 0
 #define VFD_WARM_PREVIOUS 1

@@ -526,8 +526,8 @@ class DFSPHSimulation:
         _check(lib().vfd_adjoint_release(self._h), "vfd_adjoint_release")
 
     def AdjointSetWarmStart(self, mode: int):
-        """Initial guess of the adjoint viscosity solves: _abi.WARM_COLD, WARM_PREVIOUS or
-        WARM_EXTRAPOLATE (the default)."""
+        """Initial guess of the adjoint viscosity solves: _abi.WARM_COLD (the default),
+        WARM_PREVIOUS or WARM_EXTRAPOLATE."""
         _check(lib().vfd_adjoint_set_warm_start(self._h, int(mode)), "vfd_adjoint_set_warm_start")
 
     def AdjointStats(self) -> dict:

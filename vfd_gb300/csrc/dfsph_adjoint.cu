@@ -41,8 +41,6 @@
 // reverse. Each backward step is one launch of a graph built once: its kernels read the
 // step's arrays, time steps, iteration counts and decisions from the tape slot a device
 // counter names, and its Jacobi loops and the adjoint CG are conditional WHILE nodes.
-// The viscosity solves start from the linear extrapolation of the two solutions after
-// them (vfd_adjoint_set_warm_start).
 // Limits: one scene, surface tension off; neighbour sets must be symmetric, so a
 // particle at the 70-neighbour cap is rejected.
 #include <cuda_runtime.h>
@@ -97,7 +95,7 @@ struct AdjDev {
     double* SC;               // [0] dt_o bar, [1] dt_n bar, [2] Viscosity bar, [3] BoundaryViscosity bar
     uint32_t* CLAIM;          // [0] largest recomputed CFL |w|^2 (bits), [1] argmax claimed
     float4 *XBO, *VBO;        // x and v cotangents in original particle order
-    const TapeSet* ts;        // the recorded steps; BW[0] is the slot of the step being differentiated
+    TapeSet* ts;              // the recorded steps; BW[0] is the slot of the step being differentiated
     uint32_t* BW;             // [0] that slot, [1] Jacobi iterations of the current solve left to differentiate
     unsigned long long hLoop[2];  // conditional handles of the pressure [0] and divergence [1] Jacobi
                                   // loops of the backward graph (0: launched from the host)
@@ -892,8 +890,11 @@ __global__ void k_adj_carry(AdjDev a) {
     if (a.BW[0] > 0u) a.BW[0] -= 1u;
 }
 
-// The slot of the first step a backward segment differentiates (its last recorded step).
-__global__ void k_adj_set_slot(AdjDev a, uint32_t slot) { a.BW[0] = slot; }
+// The bank a backward segment reads and the slot of its first step (the segment's last).
+__global__ void k_adj_set_slot(AdjDev a, TapeStep* steps, uint32_t slot) {
+    a.ts->steps = steps;
+    a.BW[0] = slot;
+}
 
 // The forward arrays of the recorded step: positions before the step, neighbour counts and
 // rows, and the scene state at its start (the first block copies it word by word).
@@ -1041,19 +1042,49 @@ struct Checkpoint {
 
 }  // namespace
 
+// One segment's recorded steps: `every` device slots and host copies of them (the
+// device-written fields after record_segment reads them back).
+struct TapeBank {
+    std::vector<TapeStep> host;
+    TapeStep* dsteps = nullptr;
+    uint32_t* dcur = nullptr;
+};
+
+// The settings a replaying copy of the simulation must share with it.
+struct ShadowKey {
+    vfd_desc desc{};
+    uint8_t lanes[16] = {}, tiles[16] = {};
+    uint16_t blocks[16] = {};
+    uint32_t n = 0, graphs = 0, analytic = 0;
+    bool operator==(const ShadowKey& o) const {
+        return std::memcmp(&desc, &o.desc, sizeof(desc)) == 0 && std::memcmp(lanes, o.lanes, sizeof(lanes)) == 0 &&
+               std::memcmp(tiles, o.tiles, sizeof(tiles)) == 0 && std::memcmp(blocks, o.blocks, sizeof(blocks)) == 0 &&
+               n == o.n && graphs == o.graphs && analytic == o.analytic;
+    }
+};
+
 struct AdjointState {
     uint32_t steps = 0, every = 0, n = 0, stride = 0;
     uint64_t generation = 0;
     std::vector<Checkpoint> ckpt;  // ckpt[k]: before step k * every; back(): after the last step
-    std::vector<TapeStep> host;    // host copy of one segment's tape slots
-    TapeSet* dset = nullptr;       // device tape set (steps, cur): the handle's adjTapeSet
-    TapeStep* dsteps = nullptr;
-    uint32_t* dcur = nullptr;
+    // bank[0]: what the simulation itself records (the forward run's last segment, replays
+    // without a shadow); bank[1]: what the shadow records while a backward pass reads the other
+    TapeBank bank[2];
+    TapeSet* dset = nullptr;       // the simulation's recording tape set (its adjTapeSet): bank 0
+    TapeSet* bset = nullptr;       // the backward pass's tape set: the bank of the segment it walks
+    // A copy of the simulation (its own buffers and stream; the volume maps borrowed) that
+    // replays the segment before the one the backward pass walks, into the other bank.
+    vfd_sim* shadow = nullptr;
+    ShadowKey shadowKey{};
+    cudaEvent_t bankRead[2] = {nullptr, nullptr};  // the backward pass has finished reading bank k
     bool lastRecorded = false;     // the forward run recorded its last segment
     uint32_t replayed = 0;         // steps re-run by the last backward pass
     std::vector<void*> allocs;
     AdjDev a{};
     ~AdjointState() {
+        for (cudaEvent_t& e : bankRead)
+            if (e) cudaEventDestroy(e);
+        delete shadow;
         for (void* p : allocs) cudaFree(p);
     }
 };
@@ -1073,20 +1104,22 @@ int aalloc(AdjointState* A, T** p, size_t count) {
     return VFD_OK;
 }
 
-// Tape slots for `every` steps, iterates sized by the scene's iteration caps.
-int alloc_tape(vfd_sim* s, AdjointState* A) {
+// Bytes of one tape slot (one recorded step), iterates sized by the scene's iteration caps.
+size_t tape_step_bytes(vfd_sim* s) {
     const size_t st = s->stride;
     const vfd_desc& dd = s->scenes[0].desc;
     const uint32_t capD = s->anyDiv ? dd.MaxDivergenceSolverIterations : 0u, capP = dd.MaxPressureSolverIterations;
-    const size_t per = st * (5 * sizeof(float4) + (2 + kRow) * sizeof(uint32_t) + 2 * sizeof(float)) +
-                       st * sizeof(float) * (2 * (size_t)capD + 1 + 2 * (size_t)capP + 1);
-    size_t freeB = 0, totalB = 0;
-    CK(cudaMemGetInfo(&freeB, &totalB));
-    if (per * A->every > freeB / 2)
-        return fail(VFD_E_NOMEM, "adjoint: %zu bytes of tape for %u steps exceed half the free device memory; "
-                                 "use a smaller checkpoint_every", per * A->every, A->every);
-    A->host.assign(A->every, TapeStep{});
-    for (auto& T : A->host) {
+    return st * (5 * sizeof(float4) + (2 + kRow) * sizeof(uint32_t) + 2 * sizeof(float)) +
+           st * sizeof(float) * (2 * (size_t)capD + 1 + 2 * (size_t)capP + 1);
+}
+
+// `every` tape slots.
+int alloc_bank(vfd_sim* s, AdjointState* A, TapeBank& B) {
+    const size_t st = s->stride;
+    const vfd_desc& dd = s->scenes[0].desc;
+    const uint32_t capD = s->anyDiv ? dd.MaxDivergenceSolverIterations : 0u, capP = dd.MaxPressureSolverIterations;
+    B.host.assign(A->every, TapeStep{});
+    for (auto& T : B.host) {
         TRY(aalloc(A, &T.Xpre, st));
         TRY(aalloc(A, &T.V0, st));
         TRY(aalloc(A, &T.V1, st));
@@ -1104,16 +1137,28 @@ int alloc_tape(vfd_sim* s, AdjointState* A) {
         T.capD = capD;
         T.capP = capP;
     }
-    TRY(aalloc(A, &A->dsteps, A->every));
-    TRY(aalloc(A, &A->dcur, 1));
+    TRY(aalloc(A, &B.dsteps, A->every));
+    TRY(aalloc(A, &B.dcur, 1));
+    CK(cudaMemcpy(B.dsteps, B.host.data(), sizeof(TapeStep) * A->every, cudaMemcpyHostToDevice));
+    return VFD_OK;
+}
+
+// Bank 0 and the simulation's recording tape set, which addresses it.
+int alloc_tape(vfd_sim* s, AdjointState* A) {
+    size_t freeB = 0, totalB = 0;
+    CK(cudaMemGetInfo(&freeB, &totalB));
+    const size_t per = tape_step_bytes(s);
+    if (per * A->every > freeB / 2)
+        return fail(VFD_E_NOMEM, "adjoint: %zu bytes of tape for %u steps exceed half the free device memory; "
+                                 "use a smaller checkpoint_every", per * A->every, A->every);
+    TRY(alloc_bank(s, A, A->bank[0]));
     if (!s->adjTapeSet) {
         TapeSet* p = nullptr;
         TRY(dalloc(s, &p, 1));
         s->adjTapeSet = p;
     }
     A->dset = static_cast<TapeSet*>(s->adjTapeSet);
-    CK(cudaMemcpy(A->dsteps, A->host.data(), sizeof(TapeStep) * A->every, cudaMemcpyHostToDevice));
-    TapeSet ts{A->dsteps, A->dcur, A->every};
+    TapeSet ts{A->bank[0].dsteps, A->bank[0].dcur, A->every};
     CK(cudaMemcpy(A->dset, &ts, sizeof(ts), cudaMemcpyHostToDevice));
     return VFD_OK;
 }
@@ -1159,26 +1204,28 @@ int restore_checkpoint(vfd_sim* s, const Checkpoint& c) {
     return VFD_OK;
 }
 
-// `count` steps from the current state, recorded into the tape slots 0..count-1, as CUDA
-// graphs (one per parity) unless graphs are off; then the slots' device-written fields
-// are read back and checked.
-int record_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
-    cudaStream_t st = s->stream;
-
-    CK(cudaMemsetAsync(A->dcur, 0, sizeof(uint32_t), st));
-    const bool graphs = s->graphMode && !s->graphFailed;
+// `count` steps of simulation `sim` from its current state, recorded into bank B's slots
+// 0..count-1 through the recording tape set `rec` (sim's own: its recording graphs address
+// it), as CUDA graphs (one per parity) unless graphs are off; then the slots'
+// device-written fields are read back and checked. Runs on sim's stream.
+int record_segment(vfd_sim* sim, AdjointState* A, TapeSet* rec, TapeBank& B, uint32_t count) {
+    cudaStream_t st = sim->stream;
+    const TapeSet ts{B.dsteps, B.dcur, A->every};
+    CK(cudaMemcpyAsync(rec, &ts, sizeof(ts), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(B.dcur, 0, sizeof(uint32_t), st));
+    const bool graphs = sim->graphMode && !sim->graphFailed;
     for (uint32_t t = 0; t < count; t++) {
-        if (graphs && !s->adjRecExec[s->cs])
-            TRY(build_graph(s, s->cs, A->dset, &s->adjRecGraph[s->cs], &s->adjRecExec[s->cs]));
-        if (graphs) CK(cudaGraphLaunch(s->adjRecExec[s->cs], st));
-        else TRY(launch_eager(s, A->dset));
-        s->cs = 1 - s->cs;
+        if (graphs && !sim->adjRecExec[sim->cs])
+            TRY(build_graph(sim, sim->cs, rec, &sim->adjRecGraph[sim->cs], &sim->adjRecExec[sim->cs]));
+        if (graphs) CK(cudaGraphLaunch(sim->adjRecExec[sim->cs], st));
+        else TRY(launch_eager(sim, rec));
+        sim->cs = 1 - sim->cs;
     }
     std::vector<TapeStep> dev(count);
-    CK(cudaMemcpyAsync(dev.data(), A->dsteps, sizeof(TapeStep) * count, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(dev.data(), B.dsteps, sizeof(TapeStep) * count, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
-    CK(cudaMemsetAsync(s->dStatus + 7, 0, sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(sim->dStatus + 7, 0, sizeof(uint32_t), st));
     for (uint32_t t = 0; t < count; t++) {
         const TapeStep& T = dev[t];
         if (T.aborted) return fail(VFD_E_STATE, "adjoint: a recorded step aborted (grid capacity or non-finite position)");
@@ -1186,15 +1233,73 @@ int record_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
         if (T.maxNbr >= kMaxNeighbors)
             return fail(VFD_E_CAPACITY, "adjoint: a particle reached the %u-neighbour cap (neighbour sets must be "
                                         "symmetric)", kMaxNeighbors);
-        A->host[t].pre = T.pre;
-        A->host[t].kd = T.kd;
-        A->host[t].kp = T.kp;
-        A->host[t].zeroG = T.zeroG;
-        A->host[t].dto = T.dto;
-        A->host[t].dtn = T.dtn;
-        A->host[t].maxV2 = T.maxV2;
+        TapeStep& H = B.host[t];
+        H.pre = T.pre;
+        H.kd = T.kd;
+        H.kp = T.kp;
+        H.zeroG = T.zeroG;
+        H.dto = T.dto;
+        H.dtn = T.dtn;
+        H.maxV2 = T.maxV2;
     }
     return VFD_OK;
+}
+
+ShadowKey shadow_key(const vfd_sim* s) {
+    ShadowKey k;
+    k.desc = s->scenes[0].desc;
+    std::memcpy(k.lanes, s->lanes, sizeof(k.lanes));
+    std::memcpy(k.tiles, s->tiles, sizeof(k.tiles));
+    std::memcpy(k.blocks, s->blocks, sizeof(k.blocks));
+    k.n = s->n;
+    k.graphs = s->graphMode && !s->graphFailed ? 1u : 0u;
+    k.analytic = s->analyticKernel ? 1u : 0u;
+    return k;
+}
+
+// The shadow simulation and bank 1, made (or remade, when the simulation's settings
+// changed) for a backward pass over more than one segment. Returns false, with nothing
+// made, when the second bank does not fit in half the free device memory or the copy
+// cannot be set up: the backward pass then replays on the simulation itself.
+bool ensure_shadow(vfd_sim* s, AdjointState* A) {
+    const ShadowKey key = shadow_key(s);
+    if (A->shadow && A->shadowKey == key) return true;
+    delete A->shadow;
+    A->shadow = nullptr;
+    if (A->bank[1].host.empty()) {
+        size_t freeB = 0, totalB = 0;
+        if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess || tape_step_bytes(s) * A->every > freeB / 2) return false;
+        if (alloc_bank(s, A, A->bank[1]) != VFD_OK) return false;
+    }
+    for (cudaEvent_t& e : A->bankRead)
+        if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    vfd_sim* t = new (std::nothrow) vfd_sim();
+    if (!t) return false;
+    t->device = s->device;
+    if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete t;
+        return false;
+    }
+    t->scenes = s->scenes;
+    t->borrowedBodies = true;  // the volume maps stay the simulation's
+    t->table = s->table;
+    t->halton = s->halton;
+    t->graphMode = key.graphs != 0u;
+    t->analyticKernel = s->analyticKernel;
+    t->reserve = s->reserve;
+    std::memcpy(t->lanes, s->lanes, sizeof(t->lanes));
+    std::memcpy(t->tiles, s->tiles, sizeof(t->tiles));
+    std::memcpy(t->blocks, s->blocks, sizeof(t->blocks));
+    TapeSet* rec = nullptr;
+    if (ensure_ready(t) != VFD_OK || dalloc(t, &rec, 1) != VFD_OK || t->n != s->n || t->stride != s->stride) {
+        delete t;
+        cudaGetLastError();
+        return false;
+    }
+    t->adjTapeSet = rec;
+    A->shadow = t;
+    A->shadowKey = key;
+    return true;
 }
 
 // ---------------------------------------------------------------- backward pass of one step
@@ -1356,8 +1461,8 @@ int build_backward_graph(vfd_sim* s, AdjointState* A) {
 // loops run the recorded iteration counts, the CG reads its flag once per iteration.
 // A->a.XBO / VBO hold the cotangents of the step's outputs on entry and of its inputs
 // on return.
-int backward_step_eager(vfd_sim* s, AdjointState* A, uint32_t t) {
-    const TapeStep& T = A->host[t];
+int backward_step_eager(vfd_sim* s, AdjointState* A, const TapeBank& B, uint32_t t) {
+    const TapeStep& T = B.host[t];
     const BwdLaunch L = bwd_launch(s, A, s->stream);
     bwd_head(L, s->dStatus);
     for (uint32_t k = 0; k < T.kp; k++) bwd_jacobi<false>(L);
@@ -1381,15 +1486,16 @@ int backward_step_eager(vfd_sim* s, AdjointState* A, uint32_t t) {
     return VFD_OK;
 }
 
-// The backward pass of a recorded segment of `count` steps, the last first.
-int backward_segment(vfd_sim* s, AdjointState* A, uint32_t count) {
+// The backward pass of a segment of `count` steps recorded in bank B, the last first, on
+// the simulation's stream (asynchronous with graphs).
+int backward_segment(vfd_sim* s, AdjointState* A, const TapeBank& B, uint32_t count) {
     cudaStream_t st = s->stream;
-    k_adj_set_slot<<<1, 1, 0, st>>>(A->a, count - 1u);
+    k_adj_set_slot<<<1, 1, 0, st>>>(A->a, B.dsteps, count - 1u);
     const bool graphs = s->graphMode && !s->graphFailed;
     if (graphs && !s->adjBwdExec) TRY(build_backward_graph(s, A));
     for (uint32_t t = count; t-- > 0;) {
         if (graphs) CK(cudaGraphLaunch(s->adjBwdExec, st));
-        else TRY(backward_step_eager(s, A, t));
+        else TRY(backward_step_eager(s, A, B, t));
     }
     CK(cudaGetLastError());
     return VFD_OK;
@@ -1420,6 +1526,8 @@ int alloc_cotangents(vfd_sim* s, AdjointState* A) {
     TRY(aalloc(A, &a.LAM2, st));
     TRY(aalloc(A, &a.ACNT, 4));
     TRY(aalloc(A, &a.BW, 2));
+    TRY(aalloc(A, &A->bset, 1));
+    a.ts = A->bset;
     TRY(aalloc(A, &a.RABAR, st));
     TRY(aalloc(A, &a.APBAR, st));
     TRY(aalloc(A, &a.DBAR, st));
@@ -1482,8 +1590,8 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
     const uint32_t capD = s->anyDiv ? dd.MaxDivergenceSolverIterations : 0u, capP = dd.MaxPressureSolverIterations;
     std::unique_ptr<AdjointState> A(s->adjoint);
     s->adjoint = nullptr;
-    if (A && !(A->n == s->n && A->stride == s->stride && A->every == every && !A->host.empty() &&
-               A->host[0].capD == capD && A->host[0].capP == capP))
+    if (A && !(A->n == s->n && A->stride == s->stride && A->every == every && !A->bank[0].host.empty() &&
+               A->bank[0].host[0].capD == capD && A->bank[0].host[0].capP == capP))
         A.reset();
     if (!A) {
         drop_backward_graph(s);
@@ -1492,11 +1600,11 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
         A->n = s->n;
         A->stride = s->stride;
         TRY(alloc_tape(s, A.get()));
-    } else {
-        TapeSet ts{A->dsteps, A->dcur, A->every};
-        A->dset = static_cast<TapeSet*>(s->adjTapeSet);
-        if (!A->dset) TRY(alloc_tape(s, A.get()));  // buffers were reallocated since
-        else CK(cudaMemcpy(A->dset, &ts, sizeof(ts), cudaMemcpyHostToDevice));
+    } else if (!s->adjTapeSet) {  // buffers were reallocated since: a new recording tape set
+        TapeSet* p = nullptr;
+        TRY(dalloc(s, &p, 1));
+        s->adjTapeSet = p;
+        A->dset = p;
     }
     A->steps = steps;
     A->lastRecorded = false;
@@ -1512,7 +1620,7 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
         // the last segment is recorded as it runs, so the backward pass starts on it
         // without a replay; a step the search had to abort (grid growth) falls back to a
         // plain run and a replay
-        const int rc = record_segment(s, A.get(), cnt);
+        const int rc = record_segment(s, A.get(), A->dset, A->bank[0], cnt);
         if (rc == VFD_OK) {
             A->lastRecorded = true;
             if (stats) {
@@ -1545,10 +1653,6 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
     cudaStream_t st = s->stream;
     if (!A->a.XBAR) TRY(alloc_cotangents(s, A));
     AdjDev& a = A->a;
-    if (a.ts != A->dset) {  // the tape set moved (new buffers): graphs addressing the old one are gone
-        drop_backward_graph(s);
-        a.ts = A->dset;
-    }
     // cotangents of the final state, original order
     CK(cudaMemcpyAsync(s->dStage, x_bar, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
     k_adj_pack<<<blocks_for(n, 256), 256, 0, st>>>(a.XBO, s->dStage, n);
@@ -1557,17 +1661,42 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
     CK(cudaMemsetAsync(a.SC, 0, 8 * sizeof(double), st));
     CK(cudaMemsetAsync(a.CLAIM, 0, 2 * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.ACNT, 0, 4 * sizeof(uint32_t), st));
+    // The segments are walked from the last to the first. The last was recorded by the
+    // forward run into bank 0 (else it is replayed now). With a shadow, the backward pass
+    // of segment k (on the simulation's stream) runs while the shadow replays segment k - 1
+    // into the other bank on its own stream; the shadow waits for the backward pass that
+    // read that bank before overwriting it. Without one, each segment is replayed on the
+    // simulation itself after the backward pass of the segment after it.
     const uint32_t segs = (uint32_t)A->ckpt.size() - 1;
+    const bool overlap = segs > 1 && ensure_shadow(s, A);
     int rc = VFD_OK;
     A->replayed = 0;
+    if (!A->lastRecorded) {
+        const uint32_t cnt = A->steps - (segs - 1) * A->every;
+        rc = restore_checkpoint(s, A->ckpt[segs - 1]);
+        if (rc == VFD_OK) rc = record_segment(s, A, A->dset, A->bank[0], cnt);
+        A->replayed += cnt;
+    }
+    int b = 0;  // the bank holding segment k
     for (uint32_t k = segs; k-- > 0 && rc == VFD_OK;) {
         const uint32_t cnt = std::min(A->every, A->steps - k * A->every);
-        if (!(k + 1 == segs && A->lastRecorded)) {
-            rc = restore_checkpoint(s, A->ckpt[k]);
-            if (rc == VFD_OK) rc = record_segment(s, A, cnt);
-            A->replayed += cnt;
+        rc = backward_segment(s, A, A->bank[b], cnt);
+        if (rc != VFD_OK || k == 0) break;
+        if (overlap) {
+            CK(cudaEventRecord(A->bankRead[b], st));
+            const int nb = 1 - b;
+            vfd_sim* t = A->shadow;
+            rc = restore_checkpoint(t, A->ckpt[k - 1]);
+            if (rc == VFD_OK) {
+                CK(cudaStreamWaitEvent(t->stream, A->bankRead[nb], 0));
+                rc = record_segment(t, A, static_cast<TapeSet*>(t->adjTapeSet), A->bank[nb], A->every);
+            }
+            b = nb;
+        } else {
+            rc = restore_checkpoint(s, A->ckpt[k - 1]);
+            if (rc == VFD_OK) rc = record_segment(s, A, A->dset, A->bank[0], A->every);
         }
-        if (rc == VFD_OK) rc = backward_segment(s, A, cnt);
+        A->replayed += A->every;
     }
     // the tape now holds the first segment; leave the simulation where the forward run ended
     A->lastRecorded = false;

@@ -353,8 +353,6 @@ int allocate(vfd_sim* s) {
     TRY(dalloc(s, &base.ACCB, (size_t)base.nscenes * kAccSlots * kBuckets * 16u));
     TRY(dalloc(s, &base.MAXB, (size_t)base.nscenes * 2u * kBuckets * 32u));
     TRY(dalloc(s, &base.MMB, (size_t)base.nscenes * 6u * kBuckets * 32u));
-    TRY(dalloc(s, &base.TICKET, kTicketCount));
-    CK(cudaMemset(base.TICKET, 0, kTicketCount * sizeof(uint32_t)));
     base.cellRel = s->cellRel ? 1u : 0u;
     base.analytic = s->analyticKernel ? 1u : 0u;
     base.splK = s->table.K;

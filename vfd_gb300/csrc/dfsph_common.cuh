@@ -155,7 +155,6 @@ struct Dev {
     double* ACCB;              // [scene][kAccSlots][kBuckets] x16: FP64 sums
     uint32_t* MAXB;            // [scene][2][kBuckets] x32: max |v + a dt|^2 bits, max neighbours
     int32_t* MMB;              // [scene][6][kBuckets] x32: min cell xyz, max cell xyz
-    uint32_t* TICKET;          // [TicketId] blocks finished of a pass that ends with its controller
     unsigned long long condHandle[3];  // while-node handles (div, cg, pres); 0 = eager
     uint8_t lanes[16];                 // lanes per particle of each TunedKernel
     uint16_t blocks[16];               // threads per block of each TunedKernel's row kernels (0 = kBlock)
@@ -370,27 +369,6 @@ __device__ __forceinline__ uint32_t fold_max(const Dev& d, uint32_t s, int k) {
 #pragma unroll
     for (uint32_t b = 0; b < kBuckets; b++) q[(size_t)b * 32u] = 0u;
     return t;
-}
-
-// Single-scene solver passes that end with their loop controller (instead of a separate
-// one-block launch): each block takes a ticket after its accumulator atomics, fencing
-// first, so the block that takes the last ticket sees every block's sums and runs the
-// controller; it resets the ticket for the next launch. True in that block only. Every
-// thread of every block must call it, after scene_accumulate (1-D grids).
-enum TicketId : uint32_t { kTicketSpmv = 0, kTicketCgUpdate = 1, kTicketJacobi = 2, kTicketCount = 4 };
-__device__ __forceinline__ bool last_block_done(const Dev& d, TicketId which) {
-    __shared__ uint32_t isLast;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const uint32_t t = atomicAdd(d.TICKET + which, 1u);
-        isLast = t == gridDim.x - 1u ? 1u : 0u;
-    }
-    __syncthreads();
-    if (!isLast) return false;
-    __threadfence();
-    if (threadIdx.x == 0) d.TICKET[which] = 0u;
-    return true;
 }
 
 // Warp sum of the FP32 values v over the lanes that are multiples of `step` (the others

@@ -382,10 +382,6 @@ __device__ __forceinline__ float jacobi_item(const Dev& d, const Group<G>& grp, 
     return res;
 }
 
-template <bool DIV>
-__device__ void jacobi_control_single(const Dev& d, uint32_t lane);
-
-// The last block to finish runs the loop's controller (single scene; no separate launch).
 template <bool DIV, uint32_t G, bool REL>
 __global__ void __launch_bounds__(kMaxBlock) k_jacobi_iter(Dev d) {
     VFD_COUNT_LAUNCH(d);
@@ -400,7 +396,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_jacobi_iter(Dev d) {
     const float v[1] = {res};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
-    if (last_block_done(d, kTicketJacobi) && threadIdx.x < 32u) jacobi_control_single<DIV>(d, threadIdx.x);
 }
 
 // The same for a batch (work list of the loop).
@@ -473,21 +468,17 @@ __device__ __forceinline__ bool jacobi_control(SceneDev& S, double sum) {
 // buckets together (fold_acc_warp) and lane 0 takes the decisions; a batch gives each
 // scene a thread.
 template <bool DIV>
-__device__ void jacobi_control_single(const Dev& d, uint32_t lane) {
-    SceneDev& S = d.scenes[0];
-    const bool act = (DIV ? S.div.active : S.pres.active) != 0u;
-    const double sum = act ? fold_acc_warp(d, 0, 0, lane) : 0.0;
-    if (lane == 0) {
-        const bool again = act && jacobi_control<DIV>(S, sum);
-        set_condition(d, DIV ? kLoopDiv : kLoopPres, (again && !aborted_p(d)) ? 1u : 0u);
-    }
-}
-
-template <bool DIV>
 __global__ void k_ctrl_jacobi(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (d.nscenes == 1) {
-        if (threadIdx.x < 32u) jacobi_control_single<DIV>(d, threadIdx.x);
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        const bool act = (DIV ? S.div.active : S.pres.active) != 0u;
+        const double sum = act ? fold_acc_warp(d, 0, 0, threadIdx.x) : 0.0;
+        if (threadIdx.x == 0) {
+            const bool again = act && jacobi_control<DIV>(S, sum);
+            set_condition(d, DIV ? kLoopDiv : kLoopPres, (again && !aborted_p(d)) ? 1u : 0u);
+        }
         return;
     }
     __shared__ uint32_t any;
@@ -891,9 +882,7 @@ __global__ void k_ctrl_cg1(Dev d) {
     if (threadIdx.x == 0) set_condition(d, kLoopCG, any);
 }
 
-__device__ void cg_alpha_single(const Dev& d, uint32_t lane);
-
-// Loop body 1: Ap and p . Ap (:695-720); single scene: the last block to finish forms alpha.
+// Loop body 1: Ap and p . Ap (:695-720).
 template <uint32_t G, bool REL>
 __global__ void __launch_bounds__(kMaxBlock) k_cg_spmv(Dev d) {
     VFD_COUNT_LAUNCH(d);
@@ -915,7 +904,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_cg_spmv(Dev d) {
     const float v[1] = {pap};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, valid && grp.lane == 0, v, slot);
-    if (last_block_done(d, kTicketSpmv) && threadIdx.x < 32u) cg_alpha_single(d, threadIdx.x);  // alpha (single scene)
 }
 
 // Loop body 1 of a batch.
@@ -946,17 +934,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_cg_spmv_b(Dev d) {
 }
 
 // alpha = |r . z| / (p . Ap) (:714-720).
-__device__ void cg_alpha_single(const Dev& d, uint32_t lane) {
-    SceneDev& S = d.scenes[0];
-    if (!S.cgActive) return;
-    const double pap = fold_acc_warp(d, 0, 0, lane);
-    if (lane == 0) S.cgAlpha = (float)(S.cgAbsNew / pap);
-}
-
 __global__ void k_ctrl_cg_alpha(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (d.nscenes == 1) {
-        if (threadIdx.x < 32u) cg_alpha_single(d, threadIdx.x);
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        if (!S.cgActive) return;
+        const double pap = fold_acc_warp(d, 0, 0, threadIdx.x);
+        if (threadIdx.x == 0) S.cgAlpha = (float)(S.cgAbsNew / pap);
         return;
     }
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
@@ -981,9 +966,6 @@ __device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const S
     rz = dot_term(r, z);
 }
 
-__device__ void cg_control_single(const Dev& d, uint32_t lane);
-
-// Single scene: the last block to finish runs the loop control (no separate launch).
 __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -996,7 +978,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     const float v[2] = {rr, rz};
     const int slot[2] = {1, 2};
     scene_accumulate<2>(d, sid, valid, v, slot);
-    if (last_block_done(d, kTicketCgUpdate) && threadIdx.x < 32u) cg_control_single(d, threadIdx.x);
 }
 
 __global__ void __launch_bounds__(kBlock) k_cg_update_b(Dev d) {
@@ -1034,24 +1015,21 @@ __device__ __forceinline__ bool cg_control(const Dev& d, SceneDev& S, double rr,
     return again;
 }
 
-__device__ void cg_control_single(const Dev& d, uint32_t lane) {
-    SceneDev& S = d.scenes[0];
-    const bool act = S.cgActive != 0u;
-    double rr = 0.0, rz = 0.0;
-    if (act) {
-        rr = fold_acc_warp(d, 0, 1, lane);
-        rz = fold_acc_warp(d, 0, 2, lane);
-    }
-    if (lane == 0) {
-        S.cgUpdateP = 0;
-        set_condition(d, kLoopCG, (act && cg_control(d, S, rr, rz)) ? 1u : 0u);
-    }
-}
-
 __global__ void k_ctrl_cg(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (d.nscenes == 1) {
-        if (threadIdx.x < 32u) cg_control_single(d, threadIdx.x);
+        if (threadIdx.x >= 32u) return;
+        SceneDev& S = d.scenes[0];
+        const bool act = S.cgActive != 0u;
+        double rr = 0.0, rz = 0.0;
+        if (act) {
+            rr = fold_acc_warp(d, 0, 1, threadIdx.x);
+            rz = fold_acc_warp(d, 0, 2, threadIdx.x);
+        }
+        if (threadIdx.x == 0) {
+            S.cgUpdateP = 0;
+            set_condition(d, kLoopCG, (act && cg_control(d, S, rr, rz)) ? 1u : 0u);
+        }
         return;
     }
     __shared__ uint32_t any;
@@ -1516,10 +1494,7 @@ void launch_div_iter(const Dev& d, cudaStream_t s) {
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_D);
     if (tiled(d, kTJacobi)) VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_D, OP_JAC_D);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_DB);
-    else {
-        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_D);  // ends with the controller
-        return;
-    }
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_D);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
 }
 void launch_div_finish(const Dev& d, cudaStream_t s) { VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_div_finish", kTDivFinish, K_DIV_FINISH); }
@@ -1536,19 +1511,11 @@ void launch_visc_init(const Dev& d, cudaStream_t s) {
     VFD_LAUNCH("k_cg_p0", s, k_cg_p0<<<blocks_for(d.n), kBlock, 0, s>>>(d));
     VFD_LAUNCH("k_ctrl_cg1", s, k_ctrl_cg1<<<1, 256, 0, s>>>(d));
 }
-// One CG iteration. A single scene's row product and update end with their controllers
-// (alpha; convergence, beta and the loop condition): three launches per iteration; the
-// tiled product and batches keep the one-block controller launches.
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
-    if (tiled(d, kTSpmv)) {
-        VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
-        VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
-    } else if (d.nscenes > 1) {
-        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_cg_spmv", kTSpmv, K_SPMV_B);
-        VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
-    } else {
-        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV);
-    }
+    if (tiled(d, kTSpmv)) VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
+    else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_cg_spmv", kTSpmv, K_SPMV_B);
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV);
+    VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     if (d.nscenes > 1) {
         VFD_LAUNCH("k_cg_update", s, k_cg_update_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
         VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
@@ -1556,6 +1523,7 @@ void launch_cg_iter(const Dev& d, cudaStream_t s) {
         return;
     }
     VFD_LAUNCH("k_cg_update", s, k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
     VFD_LAUNCH("k_cg_p", s, k_cg_p<<<blocks_for(d.n), kBlock, 0, s>>>(d));
 }
 void launch_visc_finish_dt(const Dev& d, cudaStream_t s) {
@@ -1573,10 +1541,7 @@ void launch_pres_iter(const Dev& d, cudaStream_t s) {
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_P);
     if (tiled(d, kTJacobi)) VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_P, OP_JAC_P);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_PB);
-    else {
-        VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_P);  // ends with the controller
-        return;
-    }
+    else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_P);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
 }
 void launch_pres_finish(const Dev& d, cudaStream_t s) {

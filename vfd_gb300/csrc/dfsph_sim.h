@@ -176,6 +176,7 @@ struct vfd_sim {
     bool cellRel = false;  // VFD_POSITIONS_CELL_RELATIVE
     bool analyticKernel = false;  // VFD_KERNEL_ANALYTIC
     bool fp64Mode = false;        // VFD_PRECISION_FP64: steps run the FP64 GPU path
+    bool borrowedBodies = false;  // the scenes' volume maps belong to another simulation (an adjoint's replay copy)
     vfd::Fp64State* fp64 = nullptr;
     bool graphFailed = false;
     uint8_t lanes[16] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
@@ -213,7 +214,7 @@ struct vfd_sim {
     // adjoint: checkpoints and tapes of the last vfd_adjoint_forward; `generation`
     // counts uploads, so a reset after the recorded run is detected
     vfd::AdjointState* adjoint = nullptr;
-    int adjWarm = 2;  // VFD_WARM_* of the adjoint viscosity solves
+    int adjWarm = 0;  // VFD_WARM_* of the adjoint viscosity solves
     uint64_t generation = 0;
     // kept across adjoint runs while the buffers live: the device tape set that recording
     // graphs address, those graphs (one per parity) and the backward graph of one step
@@ -255,8 +256,9 @@ struct vfd_sim {
         vfd::adjoint_release(this);
         vfd::fp64_release(this);
         releaseBuffers();
-        for (auto& s : scenes)
-            for (auto& b : s.bodies) b.release();
+        if (!borrowedBodies)
+            for (auto& s : scenes)
+                for (auto& b : s.bodies) b.release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
