@@ -503,18 +503,29 @@ int vfd_adjoint_release(vfd_sim* sim);
 
 /*
  * Initial guess of each backward step's viscosity solve A lambda = g_bar (the steps
- * are walked from the last to the first): VFD_WARM_COLD (default) starts from g_bar;
- * VFD_WARM_PREVIOUS from the lambda of the step after; VFD_WARM_EXTRAPOLATE from
- * 2 lambda(t+1) - lambda(t+2), the linear extrapolation of the last two solutions, once
- * two exist. Every choice solves to the same tolerance and differs in iteration count
- * (the cotangents change too much from step to step for the earlier solutions to help:
- * on a 33k-particle viscous drop, 60 steps, 1113 / 1229 / 1280 iterations). No
- * counterpart in the reference.
+ * are walked from the last to the first): VFD_WARM_COLD starts from g_bar;
+ * VFD_WARM_PREVIOUS (default) from the lambda of the step after; VFD_WARM_EXTRAPOLATE
+ * from 2 lambda(t+1) - lambda(t+2), the linear extrapolation of the last two solutions,
+ * once two exist. Every choice stops at the same residual; they differ in iteration count
+ * and in the error left in lambda (the residual bounds it loosely, see
+ * vfd_adjoint_set_tolerance): the previous solution carries the components of lambda that
+ * change slowly from step to step, which the CG resolves last. No counterpart in the
+ * reference.
  */
 #define VFD_WARM_COLD 0
 #define VFD_WARM_PREVIOUS 1
 #define VFD_WARM_EXTRAPOLATE 2
 int vfd_adjoint_set_warm_start(vfd_sim* sim, int32_t mode);
+
+/*
+ * Tolerance of the backward viscosity solves relative to the forward's: they stop at a
+ * relative residual of `factor` x (MaxViscositySolverError / 100), factor in (0, 1],
+ * default 1. The cotangent g_bar of a viscous step can be dominated by components the
+ * viscosity damps, so that lambda = A^-1 g_bar is much smaller than g_bar and a residual
+ * relative to g_bar bounds lambda's relative error only loosely; a smaller factor buys
+ * gradient accuracy with iterations. No counterpart in the reference.
+ */
+int vfd_adjoint_set_tolerance(vfd_sim* sim, float factor);
 
 /* Counters of the last vfd_adjoint_backward. */
 typedef struct vfd_adjoint_stats {

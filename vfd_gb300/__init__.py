@@ -37,7 +37,7 @@ EXPORTS = [
     "vfd_set_position_mode", "vfd_build_mesh_map", "vfd_sample_mesh_volume", "vfd_set_kernel_mode",
     "vfd_emit", "vfd_get_graph_mode", "vfd_checkpoint_size", "vfd_checkpoint", "vfd_restore",
     "vfd_set_tiles", "vfd_get_tiles", "vfd_set_precision", "vfd_get_state_f64", "vfd_set_blocks", "vfd_get_blocks",
-    "vfd_adjoint_set_warm_start", "vfd_adjoint_get_stats",
+    "vfd_adjoint_set_warm_start", "vfd_adjoint_get_stats", "vfd_adjoint_set_tolerance",
     # include/vfd_sph.h: the legacy SPH pipeline (vfd_gb300.sph)
     "vfd_sph_create", "vfd_sph_destroy", "vfd_sph_on_update", "vfd_sph_steps", "vfd_sph_reset",
     "vfd_sph_update_description", "vfd_sph_get_params", "vfd_sph_get_state", "vfd_sph_set_velocities",
@@ -133,6 +133,7 @@ def lib() -> C.CDLL:
                 "vfd_adjoint_backward": [P, f32p, f32p, f32p, f32p, f32p],
                 "vfd_adjoint_release": [P],
                 "vfd_adjoint_set_warm_start": [P, C.c_int32],
+                "vfd_adjoint_set_tolerance": [P, C.c_float],
                 "vfd_adjoint_get_stats": [P, C.POINTER(_abi.vfd_adjoint_stats)],
                 "vfd_set_position_mode": [P, C.c_int32],
                 "vfd_set_kernel_mode": [P, C.c_int32],
@@ -526,9 +527,13 @@ class DFSPHSimulation:
         _check(lib().vfd_adjoint_release(self._h), "vfd_adjoint_release")
 
     def AdjointSetWarmStart(self, mode: int):
-        """Initial guess of the adjoint viscosity solves: _abi.WARM_COLD (the default),
-        WARM_PREVIOUS or WARM_EXTRAPOLATE."""
+        """Initial guess of the adjoint viscosity solves: _abi.WARM_COLD, WARM_PREVIOUS (the
+        default) or WARM_EXTRAPOLATE."""
         _check(lib().vfd_adjoint_set_warm_start(self._h, int(mode)), "vfd_adjoint_set_warm_start")
+
+    def AdjointSetTolerance(self, factor: float):
+        """Tolerance of the adjoint viscosity solves relative to the forward's (0, 1]; default 1."""
+        _check(lib().vfd_adjoint_set_tolerance(self._h, float(factor)), "vfd_adjoint_set_tolerance")
 
     def AdjointStats(self) -> dict:
         """Counters of the last AdjointBackward (steps, replayed steps, viscosity solves and

@@ -99,10 +99,22 @@ struct AdjDev {
     uint32_t* BW;             // [0] that slot, [1] Jacobi iterations of the current solve left to differentiate
     unsigned long long hLoop[2];  // conditional handles of the pressure [0] and divergence [1] Jacobi
                                   // loops of the backward graph (0: launched from the host)
+    float tolScale;               // the adjoint viscosity solves' tolerance relative to the forward's
 };
 
 // The recorded step being differentiated.
 __device__ __forceinline__ const TapeStep& bstep(const AdjDev& a) { return a.ts->steps[a.BW[0]]; }
+
+// Jacobi loop control of the backward pass: a solve's recorded iterations are
+// differentiated last to first, BW[1] counting those left; in a graph the loop's
+// conditional handle follows it (loop_start from one thread of the pass before the loop,
+// k_adj_loop_next at the end of each iteration).
+template <bool DIV>
+__device__ __forceinline__ void loop_start(const AdjDev& a, const TapeStep& T) {
+    const uint32_t left = DIV ? T.kd : T.kp;
+    a.BW[1] = left;
+    if (a.hLoop[DIV]) cudaGraphSetConditional((cudaGraphConditionalHandle)a.hLoop[DIV], left > 0u ? 1u : 0u);
+}
 
 // The reference's cubic spline (Kernel/DFSPHKernels.h:86-131) and its derivatives.
 struct Spline {
@@ -214,11 +226,7 @@ __device__ __forceinline__ double dot3d(float3 a, float3 b) {
 // The boundary kernel's decisions (k_boundary, ComputeVolumeAndBoundaryKernel
 // DFSPHKernels.cu:69-150) replayed on the positions before it ran, keeping what the
 // adjoint needs: per body (n, Vb), (grad pd, pd), (grad Vb), and the velocity reset.
-__global__ void k_adj_bdata(Dev d, AdjDev a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
-    const SceneDev& S = d.scenes[0];
-    float3 x = f3(d.X[p]);
+__device__ void bdata_item(const Dev& d, const AdjDev& a, const SceneDev& S, uint32_t p, float3 x) {
     uint32_t stop = 0;
     for (uint32_t b = 0; b < S.bodyCount; b++) {
         const BodyDev& m = d.bodies[S.bodyBegin + b];
@@ -265,8 +273,36 @@ __device__ __forceinline__ const float* jacobi_kappa(const Dev& d, const AdjDev&
 template <bool DIV>
 __device__ __forceinline__ float jacobi_scale(const TapeStep& T) { return DIV ? T.dto : T.dtn * T.dtn; }
 
+// The output of a solve, for particle p with its recomputed acceleration ap, and the
+// cotangent arrays of the solve's iterations set up; returns its term of the dt bar sum.
+//   pressure (K20 + K21): x' = x + dt_n v3, v3 = v2 + dt_n a_p: v3 bar, dt_n bar;
+//                         ABAR = dt_n v3 bar;
+//   divergence (K7):      v1 = v0 + dt_o a_d: dt_o bar; ABAR = dt_o v1 bar.
+template <bool DIV>
+__device__ __forceinline__ float solve_output(const AdjDev& a, const TapeStep& T, uint32_t p, float3 ap) {
+    float term;
+    if (DIV) {
+        const float3 vb = f3(a.VBAR[p]);
+        term = dot3(ap, vb);
+        a.ABAR[p] = f4(T.dto * vb, 0.f);
+    } else {
+        const float dtn = T.dtn;
+        const float3 v3 = f3(T.V2[p]) + dtn * ap;
+        const float3 xb = f3(a.XBAR[p]);
+        const float3 vb = f3(a.VBAR[p]) + dtn * xb;
+        term = dot3(v3, xb) + dot3(ap, vb);
+        a.VBAR[p] = f4(vb, 0.f);
+        a.ABAR[p] = f4(dtn * vb, 0.f);
+    }
+    a.KBAR[p] = 0.f;
+    a.RABAR[p] = 0.f;
+    a.APBAR[p] = 0.f;
+    return term;
+}
+
 // AK = P(kap) as the forward computes it (masks |k_i + k_j| > eps, |k_i| > eps);
-// with U: ABAR = c D^T(U) = c (V sum_j (u_i + u_j) gradW_ij + u_i GB_i).
+// with U: ABAR = c D^T(U) = c (V sum_j (u_i + u_j) gradW_ij + u_i GB_i). Without U (the
+// solve's last iterate) it also takes the solve's output (solve_output).
 template <bool HAS_U, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a) {
     ADJ_GROUP
@@ -308,12 +344,16 @@ __global__ void __launch_bounds__(kBlock) k_adj_jac_a(Dev d, AdjDev a) {
     }
     acc = grp.sum(acc);
     if (HAS_U) ab = grp.sum(ab);
-    if (!live || grp.lane != 0) return;
-    const float3 gb = f3(d.GB[p]);
-    if (fabsf(ki) > kEps && (rw.flags & kHasBoundary)) acc += ki * (-gb);
-    // .w: U and kappa, for the neighbours' gathers in k_adj_jac_b
-    a.AK[p] = f4(acc, ui);
-    if (HAS_U) a.ABAR[p] = f4(c * (ab + ui * gb), ki);
+    float term = 0.0f;
+    if (live && grp.lane == 0) {
+        const float3 gb = f3(d.GB[p]);
+        if (fabsf(ki) > kEps && (rw.flags & kHasBoundary)) acc += ki * (-gb);
+        // .w: U and kappa, for the neighbours' gathers in k_adj_jac_b
+        a.AK[p] = f4(acc, ui);
+        if (HAS_U) a.ABAR[p] = f4(c * (ab + ui * gb), ki);
+        else term = solve_output<DIV>(a, T, p, acc);
+    }
+    if (!HAS_U) block_add(a.SC + (DIV ? 0 : 1), term);
 }
 
 // KBAR += P^T(ABAR) (masked like P); XBAR += XP(kap, ABAR) + c XD(AK, U), where
@@ -323,6 +363,7 @@ template <bool HAS_U, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_adj_jac_b(Dev d, AdjDev a) {
     ADJ_GROUP
     const TapeStep& T = bstep(a);
+    if (!HAS_U && blockIdx.x == 0 && threadIdx.x == 0) loop_start<DIV>(a, T);  // the solve's iterations next
     const float* __restrict__ kap = jacobi_kappa<HAS_U, DIV>(d, a, T);
     const float c = jacobi_scale<DIV>(T);
     const SceneDev& S = d.scenes[0];
@@ -505,7 +546,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_density(Dev d, AdjDev a) {
         }
         acc += jgb_t(d, a, sp, S.bodyCount, p, gbi);
     }
-    a.XBAR[p] = f4(f3(a.XBAR[p]) + acc, 0.0f);
+    // the step's input cotangents, back in original order (the boundary's velocity reset)
+    const uint32_t o = bstep(a).PID[p];
+    a.XBO[o] = f4(f3(a.XBAR[p]) + acc, 0.0f);
+    a.VBO[o] = a.STOP[p] ? make_float4(0.f, 0.f, 0.f, 0.f) : a.VBAR[p];
 }
 
 // ---------------------------------------------------------------- viscosity
@@ -516,9 +560,20 @@ __global__ void __launch_bounds__(kBlock) k_adj_density(Dev d, AdjDev a) {
 //   SC[0] += lambda_i . Q_i / rho_i, SC[2] += rho0 lt_i . dQ_i/d mu, SC[3] += rho0 lt_i . dQ_i/d mu_b,
 // where T_ij = cmu (m / rho_j)(g_ij . r) phi(|r|) r, phi = gs / (|r|^2 + eps2) and
 // R(r, g, w) = phi ((r . w) g + (g . r) w) + (g . r)(r . w)(phi' / |r|) r.
+// Also: v1 bar += lambda, this step's lambda kept for the next solves' initial guesses,
+// and the solve's iterations counted.
 __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a) {
     const TapeStep& T = bstep(a);
-    if (T.zeroG || d.scenes[0].cgZeroG) return;  // g = 0 in the forward step, or lambda = 0
+    if (T.zeroG) return;  // g = 0 in the forward step: no solve to differentiate
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const SceneDev& S0 = d.scenes[0];
+        const uint32_t it = S0.cgIt;
+        a.ACNT[0] += it;
+        a.ACNT[1] = max(a.ACNT[1], it);
+        a.ACNT[2] += 1u;
+        if (!S0.cgZeroG) a.ACNT[3] = min(a.ACNT[3] + 1u, 2u);
+    }
+    if (d.scenes[0].cgZeroG) return;  // lambda = 0
     const float4* __restrict__ G = T.G;
     const float dt = T.dto;
     ADJ_GROUP
@@ -610,6 +665,9 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a) {
         racc += -dot3(lti, Q) / rhoi;
         a.XBAR[p] = f4(f3(a.XBAR[p]) + xacc, 0.0f);
         a.RHOBAR[p] += racc;
+        a.VBAR[p] = f4(f3(a.VBAR[p]) + li, 0.f);
+        a.LAM2[p] = a.LAM[p];
+        a.LAM[p] = f4(li, 0.f);
         s0 = dot3(li, Q) / rhoi;
         s2v = S.rho0 * dot3(lti, q1);
         s3v = S.rho0 * dot3(lti, b1);
@@ -620,62 +678,6 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(Dev d, AdjDev a) {
 }
 
 // ---------------------------------------------------------------- element-wise steps
-__global__ void k_adj_load(Dev d, AdjDev a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
-    const uint32_t o = bstep(a).PID[p];
-    a.XBAR[p] = a.XBO[o];
-    a.VBAR[p] = a.VBO[o];
-    a.RHOBAR[p] = 0.f;
-    a.ALBAR[p] = 0.f;
-}
-
-// The boundary's velocity reset, then back to original order.
-__global__ void k_adj_store(Dev d, AdjDev a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
-    const uint32_t o = bstep(a).PID[p];
-    a.XBO[o] = a.XBAR[p];
-    a.VBO[o] = a.STOP[p] ? make_float4(0.f, 0.f, 0.f, 0.f) : a.VBAR[p];
-}
-
-// x' = x + dt_n v3, v3 = v2 + dt_n a_p (K20 + K21): v3 bar, dt_n bar; ABAR = dt_n v3 bar.
-__global__ void k_adj_pres_out(Dev d, AdjDev a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const TapeStep& T = bstep(a);
-    const float4* V2 = T.V2;
-    const float dtn = T.dtn;
-    float acc = 0.0f;
-    if (p < d.n) {
-        const float3 ap = f3(a.AK[p]);
-        const float3 v3 = f3(V2[p]) + dtn * ap;
-        const float3 xb = f3(a.XBAR[p]);
-        const float3 vb = f3(a.VBAR[p]) + dtn * xb;
-        acc = dot3(v3, xb) + dot3(ap, vb);
-        a.VBAR[p] = f4(vb, 0.f);
-        a.ABAR[p] = f4(dtn * vb, 0.f);
-        a.KBAR[p] = 0.f;
-        a.RABAR[p] = 0.f;
-        a.APBAR[p] = 0.f;
-    }
-    block_add(a.SC + 1, acc);
-}
-
-// v1 = v0 + dt_o a_d (K7): dt_o bar; ABAR = dt_o v1 bar.
-__global__ void k_adj_div_out(Dev d, AdjDev a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const float dto = bstep(a).dto;
-    float acc = 0.0f;
-    if (p < d.n) {
-        const float3 vb = f3(a.VBAR[p]);
-        acc = dot3(f3(a.AK[p]), vb);
-        a.ABAR[p] = f4(dto * vb, 0.f);
-        a.KBAR[p] = 0.f;
-        a.RABAR[p] = 0.f;
-        a.APBAR[p] = 0.f;
-    }
-    block_add(a.SC + 0, acc);
-}
 
 // One Jacobi update k <- k - r alpha', r = min(c0 - rho_adv - f, 0) (c0 = 0 divergence,
 // 1 pressure; r = 0 where skipped): U = [r < 0] alpha' k_bar; rho_adv bar += U,
@@ -758,6 +760,34 @@ __global__ void k_adj_div_init(Dev d, AdjDev a) {
 // (the forward CG's right-hand side was zero).
 __device__ __forceinline__ int visc_mode(const TapeStep& T, int visc) { return !visc ? 0 : (T.zeroG ? 2 : 1); }
 
+// CFL (k_visc_finish + k_ctrl_dt): dt_n = 0.4 d / sqrt(|w*|^2) for the particle with the
+// largest |w|^2 = |v1 + a dt_o|^2; d dt_n / d w = -dt_n w / |w|^2. k_adj_velocity finds
+// the largest recomputed |w|^2, k_adj_cfl_visc gives its particle the derivative. Both do
+// nothing when dt_n was not the CFL value (clamped to its bounds, or |w|^2 <= 0.1): the
+// forward's own expression, evaluated again on the device, decides.
+__device__ __forceinline__ bool cfl_active(const TapeStep& T) {
+    return T.maxV2 > 0.1f && 0.4f * (T.pre.diam / sqrtf(T.maxV2)) == T.dtn;
+}
+// |w|^2 of particle p, rounded operation by operation (no contraction into fused
+// multiply-adds), so that the kernel finding the maximum and the kernel matching it compute
+// the same bits whatever the compiler does with their surroundings.
+__device__ __forceinline__ float cfl_w2(const Dev& d, const float4* V1, const float4* G, uint32_t p, float dto,
+                                        int mode, float3& w) {
+    const SceneDev& S = d.scenes[0];
+    const float3 v1 = f3(V1[p]);
+    float3 acc = make_float3(S.g[0], S.g[1], S.g[2]);
+    if (mode != 0) {
+        const float3 g = mode == 1 ? f3(G[p]) : make_float3(0.f, 0.f, 0.f);
+        const float inv = __fdiv_rn(1.0f, dto);
+        acc.x = __fadd_rn(acc.x, __fmul_rn(inv, __fsub_rn(g.x, v1.x)));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(inv, __fsub_rn(g.y, v1.y)));
+        acc.z = __fadd_rn(acc.z, __fmul_rn(inv, __fsub_rn(g.z, v1.z)));
+    }
+    w = make_float3(__fadd_rn(v1.x, __fmul_rn(acc.x, dto)), __fadd_rn(v1.y, __fmul_rn(acc.y, dto)),
+                    __fadd_rn(v1.z, __fmul_rn(acc.z, dto)));
+    return __fadd_rn(__fadd_rn(__fmul_rn(w.x, w.x), __fmul_rn(w.y, w.y)), __fmul_rn(w.z, w.z));
+}
+
 // v2 = v1 + dt_n a with a = gravity (+ (g - v1) / dt_o with viscosity; g = 0 when the CG
 // right-hand side was zero).
 __global__ void k_adj_velocity(Dev d, AdjDev a, int visc) {
@@ -784,61 +814,13 @@ __global__ void k_adj_velocity(Dev d, AdjDev a, int visc) {
             a.GBAR[p] = mode == 1 ? f4((dtn / dto) * vb, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
             a.VBAR[p] = f4((1.0f - dtn / dto) * vb, 0.f);
         }
+        if (cfl_active(T)) {  // the largest recomputed |w|^2
+            float3 w;
+            atomicMax(a.CLAIM, __float_as_uint(cfl_w2(d, V1, G, p, dto, mode, w)));
+        }
     }
     block_add(a.SC + 1, sn);
     block_add(a.SC + 0, so);
-}
-
-// CFL (k_visc_finish + k_ctrl_dt): dt_n = 0.4 d / sqrt(|w*|^2) for the particle with the
-// largest |w|^2 = |v1 + a dt_o|^2; d dt_n / d w = -dt_n w / |w|^2. The first kernel finds
-// the largest recomputed |w|^2, the second gives its particle the derivative. Both do
-// nothing when dt_n was not the CFL value (clamped to its bounds, or |w|^2 <= 0.1): the
-// forward's own expression, evaluated again on the device, decides.
-__device__ __forceinline__ bool cfl_active(const TapeStep& T) {
-    return T.maxV2 > 0.1f && 0.4f * (T.pre.diam / sqrtf(T.maxV2)) == T.dtn;
-}
-__device__ __forceinline__ float3 cfl_w(const Dev& d, const float4* V1, const float4* G, uint32_t p, float dto,
-                                        int mode) {
-    const SceneDev& S = d.scenes[0];
-    const float3 v1 = f3(V1[p]);
-    float3 acc = make_float3(S.g[0], S.g[1], S.g[2]);
-    if (mode != 0) {
-        const float3 g = mode == 1 ? f3(G[p]) : make_float3(0.f, 0.f, 0.f);
-        acc += 1.0f / dto * (g - v1);
-    }
-    return v1 + acc * dto;
-}
-__global__ void k_adj_cfl_max(Dev d, AdjDev a, int visc) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const TapeStep& T = bstep(a);
-    if (p >= d.n || !cfl_active(T)) return;
-    const float3 w = cfl_w(d, T.V1, T.G, p, T.dto, visc_mode(T, visc));
-    atomicMax(a.CLAIM, __float_as_uint(dot3(w, w)));
-}
-__global__ void k_adj_cfl(Dev d, AdjDev a, int visc) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const TapeStep& T = bstep(a);
-    if (p >= d.n || !cfl_active(T)) return;
-    const int mode = visc_mode(T, visc);
-    const float dtn = T.dtn, maxV2 = T.maxV2;
-    const float3 w = cfl_w(d, T.V1, T.G, p, T.dto, mode);
-    if (__float_as_uint(dot3(w, w)) != a.CLAIM[0]) return;
-    if (atomicExch(a.CLAIM + 1, 1u) != 0u) return;
-    const SceneDev& S = d.scenes[0];
-    const float3 grav = make_float3(S.g[0], S.g[1], S.g[2]);
-    const float dtnb = (float)a.SC[1];
-    const float3 wb = (-dtnb * dtn / maxV2) * w;
-    atomicAdd(a.SC + 0, dot3d(wb, grav));
-    if (mode == 1) a.GBAR[p] = f4(f3(a.GBAR[p]) + wb, 0.f);
-    else if (mode == 0) a.VBAR[p] = f4(f3(a.VBAR[p]) + wb, 0.f);
-}
-
-// v1 bar += lambda, unless the adjoint solve's right-hand side was zero (lambda = 0) or the
-// forward step's was (g = 0, no solve to differentiate).
-__global__ void k_adj_add_lambda(Dev d, AdjDev a) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n || bstep(a).zeroG || d.scenes[0].cgZeroG) return;
-    a.VBAR[p] = f4(f3(a.VBAR[p]) + f3(d.CG[p]), 0.f);
 }
 
 // Right-hand side and initial guess lambda_0 of the adjoint viscosity solve (mode:
@@ -848,10 +830,8 @@ __global__ void k_adj_add_lambda(Dev d, AdjDev a) {
 // replayed steps reuses CG, so they are kept apart). Cold: lambda_0 = g_bar (DV = 0);
 // previous: LAM; extrapolate: 2 LAM - LAM2, the linear extrapolation in time of the
 // sequence of solutions, once two exist.
-__global__ void k_adj_visc_start(Dev d, AdjDev a, int mode) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.n) return;
-    const bool zero = bstep(a).zeroG != 0u;
+__device__ __forceinline__ void visc_start_item(const Dev& d, const AdjDev& a, const TapeStep& T, uint32_t p, int mode) {
+    const bool zero = T.zeroG != 0u;
     d.V[p] = zero ? make_float4(0.f, 0.f, 0.f, 0.f) : a.GBAR[p];
     const uint32_t have = a.ACNT[3];
     if (zero || mode == 0 || have == 0) {
@@ -863,21 +843,28 @@ __global__ void k_adj_visc_start(Dev d, AdjDev a, int mode) {
     d.DV[p] = f4(x0 - f3(a.GBAR[p]), 0.f);
 }
 
-// Keeps this step's lambda for the next solves and counts the solve's iterations.
-__global__ void k_adj_keep(Dev d, AdjDev a) {
+// The CFL derivative for the particle with the largest recomputed |w|^2 (it claims it; ties
+// go to one), then, with viscosity, the adjoint solve's start for every particle.
+__global__ void k_adj_cfl_visc(Dev d, AdjDev a, int visc, int warm) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const SceneDev& S = d.scenes[0];
-    if (bstep(a).zeroG) return;  // no solve in this step
-    if (p == 0) {
-        const uint32_t it = S.cgIt;
-        a.ACNT[0] += it;
-        a.ACNT[1] = max(a.ACNT[1], it);
-        a.ACNT[2] += 1u;
-        if (!S.cgZeroG) a.ACNT[3] = min(a.ACNT[3] + 1u, 2u);
+    if (p >= d.n) return;
+    const TapeStep& T = bstep(a);
+    const int mode = visc_mode(T, visc);
+    if (cfl_active(T)) {
+        const float dtn = T.dtn, maxV2 = T.maxV2;
+        float3 w;
+        const float w2 = cfl_w2(d, T.V1, T.G, p, T.dto, mode, w);
+        if (__float_as_uint(w2) == a.CLAIM[0] && atomicExch(a.CLAIM + 1, 1u) == 0u) {
+            const SceneDev& S = d.scenes[0];
+            const float3 grav = make_float3(S.g[0], S.g[1], S.g[2]);
+            const float dtnb = (float)a.SC[1];
+            const float3 wb = (-dtnb * dtn / maxV2) * w;
+            atomicAdd(a.SC + 0, dot3d(wb, grav));
+            if (mode == 1) a.GBAR[p] = f4(f3(a.GBAR[p]) + wb, 0.f);
+            else if (mode == 0) a.VBAR[p] = f4(f3(a.VBAR[p]) + wb, 0.f);
+        }
     }
-    if (p >= d.n || S.cgZeroG) return;
-    a.LAM2[p] = a.LAM[p];
-    a.LAM[p] = d.CG[p];
+    if (visc) visc_start_item(d, a, T, p, warm);
 }
 
 // dt_o of this step is dt_n of the step before; the next step to differentiate is the
@@ -897,7 +884,8 @@ __global__ void k_adj_set_slot(AdjDev a, TapeStep* steps, uint32_t slot) {
 }
 
 // The forward arrays of the recorded step: positions before the step, neighbour counts and
-// rows, and the scene state at its start (the first block copies it word by word).
+// rows, and the scene state at its start (the first block copies it word by word; the
+// adjoint viscosity solve's tolerance is the forward's scaled by tolScale).
 __global__ void k_adj_fetch(Dev d, AdjDev a) {
     const TapeStep& T = bstep(a);
     if (blockIdx.x == 0) {
@@ -905,27 +893,29 @@ __global__ void k_adj_fetch(Dev d, AdjDev a) {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(&T.pre);
         uint32_t* dst = reinterpret_cast<uint32_t*>(d.scenes);
         for (uint32_t w = threadIdx.x; w < sizeof(SceneDev) / 4; w += blockDim.x) dst[w] = src[w];
+        __syncthreads();
+        if (threadIdx.x == 0) d.scenes[0].maxErrV = T.pre.maxErrV * a.tolScale;
     }
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.n) return;
-    d.X[p] = T.Xpre[p];
+    const float4 x = T.Xpre[p];
+    d.X[p] = x;
     d.NCNT[p] = T.NCNT[p];
     const uint4* rs = reinterpret_cast<const uint4*>(T.NBR + (size_t)p * kRow);
     uint4* rd = reinterpret_cast<uint4*>(d.NBR + (size_t)p * kRow);
 #pragma unroll
     for (uint32_t k = 0; k < kRow / 4u; k++) rd[k] = rs[k];
+    // the boundary data on the positions before the boundary kernel moves them (the scene
+    // constants it reads are those of the step's start), and the step's output cotangents
+    // in slot order
+    bdata_item(d, a, T.pre, p, f3(x));
+    const uint32_t o = T.PID[p];
+    a.XBAR[p] = a.XBO[o];
+    a.VBAR[p] = a.VBO[o];
+    a.RHOBAR[p] = 0.f;
+    a.ALBAR[p] = 0.f;
 }
 
-// Jacobi loop control of the backward pass: the recorded solve's iterations are
-// differentiated last to first, BW[1] counting those left; in a graph the loop's
-// conditional handle follows it.
-template <bool DIV>
-__global__ void k_adj_loop_init(AdjDev a) {
-    const TapeStep& T = bstep(a);
-    const uint32_t left = DIV ? T.kd : T.kp;
-    a.BW[1] = left;
-    if (a.hLoop[DIV]) cudaGraphSetConditional((cudaGraphConditionalHandle)a.hLoop[DIV], left > 0u ? 1u : 0u);
-}
 template <bool DIV>
 __global__ void k_adj_loop_next(AdjDev a) {
     const uint32_t left = a.BW[1] - 1u;
@@ -1321,14 +1311,10 @@ struct BwdLaunch {
 void bwd_head(const BwdLaunch& L, uint32_t* dStatus) {
     cudaMemsetAsync(dStatus, 0, 16 * sizeof(uint32_t), L.st);
     k_adj_fetch<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_bdata<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     launch_boundary(L.d, L.st);
     launch_density(L.d, L.st);
-    k_adj_load<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_jac_a<false, false><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_pres_out<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_jac_b<false, false><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_loop_init<false><<<1, 1, 0, L.st>>>(L.a);
 }
 
 // One Jacobi iteration of a solve, differentiated (the last first).
@@ -1346,27 +1332,19 @@ void bwd_mid(const BwdLaunch& L) {
     k_adj_pres_init<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_div_b<true><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_velocity<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc);
-    k_adj_cfl_max<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc);
-    k_adj_cfl<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc);
-    if (L.visc) {
-        k_adj_visc_start<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.warm);
-        launch_visc_init(L.d, L.st);
-    }
+    k_adj_cfl_visc<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a, L.visc, L.warm);
+    if (L.visc) launch_visc_init(L.d, L.st);
 }
 
 // After the adjoint viscosity solve: v1 bar += lambda, and the derivative of A g = v1.
 void bwd_visc_tail(const BwdLaunch& L) {
-    k_adj_add_lambda<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_keep<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_visc<<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
 }
 
 // Divergence solve (K4-K7): its output v1 = v0 + dt_o a_d, then its iterations.
 void bwd_div_head(const BwdLaunch& L) {
     k_adj_jac_a<false, true><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_div_out<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_jac_b<false, true><<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_loop_init<true><<<1, 1, 0, L.st>>>(L.a);
 }
 void bwd_div_tail(const BwdLaunch& L) {
     k_adj_div_init<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
@@ -1378,7 +1356,6 @@ void bwd_div_tail(const BwdLaunch& L) {
 void bwd_end(const BwdLaunch& L) {
     k_adj_gsum<<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_density<<<L.gG, kBlock, 0, L.st>>>(L.d, L.a);
-    k_adj_store<<<L.g1, kBlock, 0, L.st>>>(L.d, L.a);
     k_adj_carry<<<1, 1, 0, L.st>>>(L.a);
 }
 
@@ -1394,6 +1371,7 @@ BwdLaunch bwd_launch(vfd_sim* s, const AdjointState* A, cudaStream_t st) {
     L.gG = blocks_for(s->n * kAG);
     L.visc = s->anyVisc ? 1 : 0;
     L.warm = s->adjWarm;
+    L.a.tolScale = s->adjTol;
     return L;
 }
 
@@ -1735,6 +1713,14 @@ int vfd_adjoint_set_warm_start(vfd_sim* s, int32_t mode) {
     if (mode < VFD_WARM_COLD || mode > VFD_WARM_EXTRAPOLATE) return fail(VFD_E_ARG, "unknown warm-start mode %d", mode);
     if (mode != s->adjWarm) drop_backward_graph(s);  // the backward graph carries the mode
     s->adjWarm = mode;
+    return VFD_OK;
+}
+
+int vfd_adjoint_set_tolerance(vfd_sim* s, float factor) {
+    if (!s) return fail(VFD_E_ARG, "null handle");
+    if (!(factor > 0.0f && factor <= 1.0f)) return fail(VFD_E_ARG, "adjoint tolerance factor must be in (0, 1]");
+    if (factor != s->adjTol) drop_backward_graph(s);  // the backward graph carries it
+    s->adjTol = factor;
     return VFD_OK;
 }
 

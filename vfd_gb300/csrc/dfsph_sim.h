@@ -214,7 +214,8 @@ struct vfd_sim {
     // adjoint: checkpoints and tapes of the last vfd_adjoint_forward; `generation`
     // counts uploads, so a reset after the recorded run is detected
     vfd::AdjointState* adjoint = nullptr;
-    int adjWarm = 0;  // VFD_WARM_* of the adjoint viscosity solves
+    int adjWarm = 1;      // VFD_WARM_* of the adjoint viscosity solves
+    float adjTol = 1.0f;  // adjoint viscosity solves' tolerance relative to the forward's
     uint64_t generation = 0;
     // kept across adjoint runs while the buffers live: the device tape set that recording
     // graphs address, those graphs (one per parity) and the backward graph of one step
