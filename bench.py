@@ -749,8 +749,9 @@ def main():
                     help="profiling run instead of the benchmark: the viscous dam break at N_SIDE^3 particles, "
                          "--graph-steps steps as CUDA graphs, then --eager-steps steps with every kernel launched "
                          "from the host (what a profiler filtering by kernel name captures)")
-    ap.add_argument("--tiles", type=int, default=-1, help="cell tiles of the three solver-loop passes instead of "
-                    "the autotuner's choice: 0 = neighbour rows, 3 = 2x2x2 cells, 4 = 4x2x2 cells")
+    ap.add_argument("--tiles", type=int, default=-1, help="form of the three solver-loop passes instead of the "
+                    "autotuner's choice: 0 = neighbour rows, 1 = rows with gradW recomputed, 3 = 2x2x2 cell tiles, "
+                    "4 = 4x2x2 cell tiles")
     ap.add_argument("--graph-steps", type=int, default=4)
     ap.add_argument("--eager-steps", type=int, default=2)
     ap.add_argument("--dry-run", action="store_true",

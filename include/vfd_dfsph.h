@@ -424,14 +424,16 @@ int vfd_set_lanes(vfd_sim* sim, const uint8_t* lanes, uint32_t count);
 int vfd_get_lanes(const vfd_sim* sim, uint8_t* lanes, uint32_t count);
 
 /*
- * Cell tiles of the solver-loop kernels (pressure acceleration, Jacobi update, CG
+ * Form of the solver-loop kernels (pressure acceleration, Jacobi update, CG
  * matrix-vector product), in the order of vfd_set_lanes (the other entries are
  * ignored): 0 (the default) = the pass walks each particle's neighbour row and gathers
  * from global memory, as the reference's kernels do (DFSPHKernels.cu:317-432,
- * :758-842); 3 or 4 = log2 of the cells per tile (a 2x2x2 or 4x2x2 block of cells): a
- * block stages the tile's halo of cells in shared memory and walks its particles'
- * neighbours there. Both give the same results to rounding. vfd_autotune picks them
- * with the lanes.
+ * :758-842), reading each pair's gradW / r from the stream the density pass wrote;
+ * 1 = the same walk over the slot rows alone, forming gradW / r from the kernel table
+ * per pair (half the streamed bytes, a table lookup per pair; single scenes); 3 or 4 =
+ * log2 of the cells per tile (a 2x2x2 or 4x2x2 block of cells): a block stages the
+ * tile's halo of cells in shared memory and walks its particles' neighbours there. All
+ * give the same results to rounding. vfd_autotune picks them with the lanes.
  */
 int vfd_set_tiles(vfd_sim* sim, const uint8_t* tiles, uint32_t count);
 int vfd_get_tiles(const vfd_sim* sim, uint8_t* tiles, uint32_t count);

@@ -329,11 +329,13 @@ def test_search_equals_reference_kernels():
         g.close()
 
 
-@pytest.mark.parametrize("tiles", [3, 4])
+@pytest.mark.parametrize("tiles", [1, 3, 4])
 def test_tile_passes_match_oracle(tiles):
-    """The solver-loop passes on cell tiles (2x2x2 or 4x2x2 cells staged in shared memory,
-    neighbours walked by stencil position) hold the same one-step tolerances against the
-    FP32 oracle as the neighbour-row passes, with viscosity and surface tension on."""
+    """The other forms of the solver-loop passes -- neighbour rows with gradW / r formed from
+    the table per pair (1), cell tiles of 2x2x2 or 4x2x2 cells staged in shared memory,
+    neighbours walked by stencil position (3, 4) -- hold the same one-step tolerances
+    against the FP32 oracle as the neighbour-row passes, with viscosity and surface
+    tension on."""
     s = scenes.small_dam_break(n_side=12, viscosity=0.02, surface_tension=0.05)
     g, o = pair(s, 32)
     g.SetTiles([tiles] * len(V.TUNED_KERNELS))

@@ -580,9 +580,10 @@ class DFSPHSimulation:
         return x, v
 
     def SetTiles(self, tiles):
-        """Per solver-loop pass, in TUNED_KERNELS order: 0 = walk neighbour rows, 3 or 4 =
-        log2 of the cells per shared-memory tile (2x2x2, 4x2x2); entries of other kernels
-        are ignored."""
+        """Per solver-loop pass, in TUNED_KERNELS order: 0 = walk neighbour rows (gradW / r
+        from the density pass's stream), 1 = walk neighbour rows forming gradW / r from the
+        table, 3 or 4 = log2 of the cells per shared-memory tile (2x2x2, 4x2x2); entries of
+        other kernels are ignored."""
         arr = (C.c_uint8 * len(tiles))(*tiles)
         _check(lib().vfd_set_tiles(self._h, arr, len(tiles)), "vfd_set_tiles")
 

@@ -2035,8 +2035,9 @@ int vfd_set_tiles(vfd_sim* s, const uint8_t* tiles, uint32_t count) {
     TRY(check_sim(s));
     if (!tiles || count == 0 || count > kTunedCount) return fail(VFD_E_ARG, "tiles: 1..%d values", (int)kTunedCount);
     for (uint32_t k = 0; k < count; k++)
-        if (tiles[k] != 0 && tiles[k] != 3 && tiles[k] != 4)
-            return fail(VFD_E_ARG, "tile size must be 0 (neighbour rows), 3 (2x2x2) or 4 (4x2x2)");
+        if (tiles[k] != 0 && tiles[k] != kRowsNoStream && tiles[k] != 3 && tiles[k] != 4)
+            return fail(VFD_E_ARG, "pass form must be 0 (neighbour rows), 1 (rows, gradW recomputed), 3 (2x2x2 tiles) "
+                                   "or 4 (4x2x2 tiles)");
     std::memcpy(s->tiles, tiles, count);
     for (int k = 0; k < 2; k++) {
         std::memcpy(s->dev[k].tiles, s->tiles, sizeof(s->tiles));
@@ -2124,20 +2125,22 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
         release();
         return fail(VFD_E_CUDA, "autotune snapshot: %s", cudaGetErrorString(e));
     }
-    // every lane count with every tile size of the cell-tile kernels (the others ignore it)
-    const uint8_t tileCand[3] = {0, 3, 4};        // neighbour rows, 2x2x2 tiles, 4x2x2 tiles
+    // every lane count with every form of the three solver-loop passes (the others ignore it)
+    constexpr int kForms = 4;
+    const uint8_t tileCand[kForms] = {0, kRowsNoStream, 3, 4};  // rows, rows without the gradient
+                                                                // stream, 2x2x2 and 4x2x2 tiles
     const uint16_t blockCand[3] = {128, 64, 256};  // threads per block of the row kernels
-    double times[kTunedCount][3][3][3] = {};       // [kernel][lanes][tiles][block]
+    double times[kTunedCount][3][kForms][3] = {};  // [kernel][lanes][form][block]
     int rc = VFD_OK;
-    for (int ct = 0; ct < 27 && rc == VFD_OK; ct++) {
-        const int c = ct % 3, tl = (ct / 3) % 3, bs = ct / 9;
+    for (int ct = 0; ct < 3 * kForms * 3 && rc == VFD_OK; ct++) {
+        const int c = ct % 3, tl = (ct / 3) % kForms, bs = ct / (3 * kForms);
         for (int k = 0; k < 2; k++) {
             for (int t = 0; t < kTunedCount; t++) {
                 s->dev[k].lanes[t] = cand[c];
                 s->dev[k].tiles[t] = tileCand[tl];
                 s->dev[k].blocks[t] = blockCand[bs];
             }
-            s->dev[k].compactRows = tileCand[tl] != 0 ? 1u : 0u;
+            s->dev[k].compactRows = tileCand[tl] >= kTileMinLog2 ? 1u : 0u;
         }
         EventProfiler prof;
         g_profiler = &prof;
@@ -2172,16 +2175,19 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
     }
     for (int t = 0; t < kTunedCount; t++) {
         const bool tileable = t == kTPAccel || t == kTJacobi || t == kTSpmv;
-        // A configuration is (lanes c, tiles tl, block bs). Kernels without tiles ran the same
-        // code in all three tile runs: their cost is the sum of those; tile kernels run
+        // A configuration is (lanes c, form tl, block bs). Kernels without forms ran the same
+        // code in all the form runs: their cost is the sum of those; tile kernels run
         // kTileBlock threads whatever bs, so their block choice stays the default.
         auto cost = [&](int c, int tl, int bs) {
-            return tileable ? times[t][c][tl][bs] : times[t][c][0][bs] + times[t][c][1][bs] + times[t][c][2][bs];
+            if (tileable) return times[t][c][tl][bs];
+            double sum = 0.0;
+            for (int f = 0; f < kForms; f++) sum += times[t][c][f][bs];
+            return sum;
         };
         int best = 1, bestTile = 0, bestBlock = 0;
         double bt = cost(1, 0, 0);
         for (int c = 0; c < 3; c++)
-            for (int tl = 0; tl < (tileable ? 3 : 1); tl++)
+            for (int tl = 0; tl < (tileable ? kForms : 1); tl++)
                 for (int bs = 0; bs < 3; bs++) {
                     const double v = cost(c, tl, bs);
                     if (v > 0.0 && v < bt) {
@@ -2193,7 +2199,7 @@ int vfd_autotune(vfd_sim* s, uint32_t steps, uint8_t* lanes_out, uint32_t count)
                 }
         s->lanes[t] = cand[best];
         s->tiles[t] = tileable ? tileCand[bestTile] : 0;
-        s->blocks[t] = bestTile == 0 ? blockCand[bestBlock] : 0;
+        s->blocks[t] = tileCand[bestTile] < kTileMinLog2 ? blockCand[bestBlock] : 0;
     }
     for (int k = 0; k < 2; k++) {
         std::memcpy(s->dev[k].lanes, s->lanes, sizeof(s->lanes));

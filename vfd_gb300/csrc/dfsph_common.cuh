@@ -56,6 +56,11 @@ enum TunedKernel {
     kTDensity = 0, kTPAccel, kTJacobi, kTDivFinish, kTStClassify, kTStSmooth, kTViscPrecond,
     kTViscSetup, kTSpmv, kTPresInit, kTPresFinish, kTunedCount
 };
+// Form of the three solver-loop passes (Dev::tiles / vfd_set_tiles): 0 = neighbour rows with
+// the per-pair gradient stream, kRowsNoStream = neighbour rows with gradW / r formed from
+// the table per pair, >= kTileMinLog2 = cell tiles of 2^value Morton cells.
+constexpr uint8_t kRowsNoStream = 1u;
+constexpr uint8_t kTileMinLog2 = 3u;
 
 // Per-scene solver loop state (one Jacobi or CG loop).
 struct LoopState {

@@ -294,8 +294,10 @@ __device__ __forceinline__ float velocity_divergence(const Dev& d, const Group<G
 }
 
 // Pressure acceleration from kappa (K5 :388-432, K7 :555-602, K18 :342-386, K20 :434-481);
-// valid on lane 0.
-template <bool DIV, uint32_t G, bool REL>
+// valid on lane 0. NS: the pass reads the slot rows only and forms each pair's gradW / r
+// from the table itself (as the density pass did), instead of reading it from the
+// per-pair stream: half the streamed bytes for a table lookup per pair.
+template <bool DIV, uint32_t G, bool REL, bool NS = false>
 __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
                                                  const Nbr& nb) {
     const float* kap = DIV ? d.KAPPAV : d.KAPPA;
@@ -303,10 +305,11 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
     const float4 xi = d.X[p];
     const float V = S.volume;
     float3 a = make_float3(0.f, 0.f, 0.f);
-    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
+    for_neighbors<G, !NS>(grp, nb, p, [&](uint32_t q, float gsStream, uint32_t, bool ok) {
         const float4 xq = d.X[q];
         const float sum = ki + (REL ? kap[q] : xq.w);
         const float3 r = pair_r<REL>(d, xi, xq);
+        const float gs = NS ? grad_factor(d, r) : gsStream;
         if (ok && fabsf(sum) > kEps) a += (sum * (-V * gs)) * r;
     });
     a = grp.sum(a);
@@ -315,14 +318,14 @@ __device__ __forceinline__ float3 pressure_accel(const Dev& d, const Group<G>& g
 }
 
 // K5 / K18.
-template <bool DIV, uint32_t G, bool REL>
+template <bool DIV, uint32_t G, bool REL, bool NS = false>
 __global__ void __launch_bounds__(kMaxBlock) k_pressure_accel(Dev d) {
     VFD_COUNT_LAUNCH(d);
     GROUP_PROLOGUE(G)
     const SceneDev& S = d.scenes[scene_of(d, p)];
     if (!(DIV ? S.div.active : S.pres.active)) return;
     const Nbr nb = neighbors(d, p);
-    const float3 a = pressure_accel<DIV, G, REL>(d, grp, p, S, nb);
+    const float3 a = pressure_accel<DIV, G, REL, NS>(d, grp, p, S, nb);
     if (grp.lane == 0) d.AP[p] = f4(a, 0.0f);
 }
 
@@ -346,15 +349,16 @@ __global__ void __launch_bounds__(kMaxBlock) k_pressure_accel_b(Dev d) {
 
 // K6 DivergenceSolveIterationKernel (:531-553) / K19 PressureSolveIterationKernel (:317-340),
 // each with ComputeDensityPressureForce (:280-315) and the FP64-accurate residual sum.
-template <bool DIV, uint32_t G, bool REL>
+template <bool DIV, uint32_t G, bool REL, bool NS = false>
 __device__ __forceinline__ float jacobi_item(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S) {
     float res = 0.0f;
     const Nbr nb = neighbors(d, p);
     const float4 xi = d.X[p];
     const float3 ai = f3(d.AP[p]);
     float f = 0.0f;
-    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
+    for_neighbors<G, !NS>(grp, nb, p, [&](uint32_t q, float gsStream, uint32_t, bool ok) {
         const float3 r = pair_r<REL>(d, xi, d.X[q]);
+        const float gs = NS ? grad_factor(d, r) : gsStream;
         const float3 aq = f3(d.AP[q]);
         const float t = dot3(ai - aq, gs * r);
         if (ok) f += t;
@@ -382,7 +386,7 @@ __device__ __forceinline__ float jacobi_item(const Dev& d, const Group<G>& grp, 
     return res;
 }
 
-template <bool DIV, uint32_t G, bool REL>
+template <bool DIV, uint32_t G, bool REL, bool NS = false>
 __global__ void __launch_bounds__(kMaxBlock) k_jacobi_iter(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
@@ -392,7 +396,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_jacobi_iter(Dev d) {
     const SceneDev& S = d.scenes[sid];
     const bool active = inRange && (DIV ? S.div.active : S.pres.active);
     float res = 0.0f;
-    if (active) res = jacobi_item<DIV, G, REL>(d, grp, p, S);
+    if (active) res = jacobi_item<DIV, G, REL, NS>(d, grp, p, S);
     const float v[1] = {res};
     const int slot[1] = {0};
     scene_accumulate<1, G>(d, sid, active && grp.lane == 0, v, slot);
@@ -738,7 +742,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_visc_precond(Dev d) {
 }
 
 // ComputeMatrixVecProdFunctionKernel (:758-842): (A x)_i with vec[q].w = m / rho_q; lane 0.
-template <uint32_t G, bool REL>
+// NS: gradW / r from the table, as in pressure_accel.
+template <uint32_t G, bool REL, bool NS = false>
 __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp, uint32_t p, const SceneDev& S,
                                               const float4* vec, float3 vi) {
     const Nbr nb = neighbors(d, p);
@@ -746,10 +751,11 @@ __device__ __forceinline__ float3 visc_matvec(const Dev& d, const Group<G>& grp,
     const float eps2 = 0.01f * S.h2;
     const float cmu = 10.0f * S.dynVisc;
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    for_neighbors<G, true>(grp, nb, p, [&](uint32_t q, float gs, uint32_t, bool ok) {
+    for_neighbors<G, !NS>(grp, nb, p, [&](uint32_t q, float gsStream, uint32_t, bool ok) {
         const float3 r = pair_r<REL>(d, xi, d.X[q]);
         const float4 vq = vec[q];
         const float r2 = dot3(r, r);
+        const float gs = NS ? grad_factor(d, r) : gsStream;
         const float3 t = (__fdividef(cmu * vq.w * dot3(vi - f3(vq), r), r2 + eps2) * gs) * r;
         if (ok) acc += t;
     });
@@ -883,7 +889,7 @@ __global__ void k_ctrl_cg1(Dev d) {
 }
 
 // Loop body 1: Ap and p . Ap (:695-720).
-template <uint32_t G, bool REL>
+template <uint32_t G, bool REL, bool NS = false>
 __global__ void __launch_bounds__(kMaxBlock) k_cg_spmv(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const Group<G> grp;
@@ -895,7 +901,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cg_spmv(Dev d) {
     float pap = 0.0f;
     if (valid) {
         const float3 pv = f3(d.CP[p]);
-        const float3 ap = visc_matvec<G, REL>(d, grp, p, S, d.CP, pv);
+        const float3 ap = visc_matvec<G, REL, NS>(d, grp, p, S, d.CP, pv);
         if (grp.lane == 0) {
             d.CAP[p] = f4(ap, 0.0f);
             pap = dot_term(pv, ap);
@@ -1459,6 +1465,16 @@ cudaError_t prepare_tile_kernels() {
 #define K_VISC_SETUP_R(G) k_visc_setup<G, true>
 #define K_SPMV(G) k_cg_spmv<G, false>
 #define K_SPMV_R(G) k_cg_spmv<G, true>
+#define K_SPMV_NS(G) k_cg_spmv<G, false, true>
+#define K_SPMV_NS_R(G) k_cg_spmv<G, true, true>
+#define K_PACCEL_D_NS(G) k_pressure_accel<true, G, false, true>
+#define K_PACCEL_D_NS_R(G) k_pressure_accel<true, G, true, true>
+#define K_PACCEL_P_NS(G) k_pressure_accel<false, G, false, true>
+#define K_PACCEL_P_NS_R(G) k_pressure_accel<false, G, true, true>
+#define K_JACOBI_D_NS(G) k_jacobi_iter<true, G, false, true>
+#define K_JACOBI_D_NS_R(G) k_jacobi_iter<true, G, true, true>
+#define K_JACOBI_P_NS(G) k_jacobi_iter<false, G, false, true>
+#define K_JACOBI_P_NS_R(G) k_jacobi_iter<false, G, true, true>
 #define K_PRES_INIT(G) k_pres_init<G, false>
 #define K_PRES_INIT_R(G) k_pres_init<G, true>
 #define K_PRES_FINISH(G) k_pres_finish<G, false>
@@ -1483,7 +1499,9 @@ void launch_density_div_init(const Dev& d, cudaStream_t s) {
 
 // Whether a solver-loop pass runs on cell tiles (vfd_set_tiles / the autotuner) rather
 // than the neighbour rows; the adjoint's CG always walks rows (Dev::rowLoops).
-inline bool tiled(const Dev& d, int id) { return d.tiles[id] != 0u && d.compactRows && !d.rowLoops; }
+inline bool tiled(const Dev& d, int id) { return d.tiles[id] >= kTileMinLog2 && d.compactRows && !d.rowLoops; }
+// Single-scene row pass without the per-pair gradient stream (tiles[id] == kRowsNoStream).
+inline bool no_stream(const Dev& d, int id) { return d.tiles[id] == kRowsNoStream && d.nscenes == 1; }
 
 // Row path: batches run the solver-loop kernels over their work lists (the scenes still
 // iterating) with a fixed grid; a single scene keeps one group per particle. Tile path:
@@ -1491,9 +1509,11 @@ inline bool tiled(const Dev& d, int id) { return d.tiles[id] != 0u && d.compactR
 void launch_div_iter(const Dev& d, cudaStream_t s) {
     if (tiled(d, kTPAccel)) VFD_TILE_DISPATCH("k_pressure_accel", kTPAccel, FN_PACC_D, OP_PACC_D);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_pressure_accel", kTPAccel, K_PACCEL_DB);
+    else if (no_stream(d, kTPAccel)) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_D_NS);
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_D);
     if (tiled(d, kTJacobi)) VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_D, OP_JAC_D);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_DB);
+    else if (no_stream(d, kTJacobi)) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_D_NS);
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_D);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<true><<<1, 256, 0, s>>>(d));
 }
@@ -1514,6 +1534,7 @@ void launch_visc_init(const Dev& d, cudaStream_t s) {
 void launch_cg_iter(const Dev& d, cudaStream_t s) {
     if (tiled(d, kTSpmv)) VFD_TILE_DISPATCH("k_cg_spmv", kTSpmv, FN_SPMV, OP_SPMV);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_cg_spmv", kTSpmv, K_SPMV_B);
+    else if (no_stream(d, kTSpmv)) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV_NS);
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV);
     VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     if (d.nscenes > 1) {
@@ -1538,9 +1559,11 @@ void launch_pres_init(const Dev& d, cudaStream_t s) {
 void launch_pres_iter(const Dev& d, cudaStream_t s) {
     if (tiled(d, kTPAccel)) VFD_TILE_DISPATCH("k_pressure_accel", kTPAccel, FN_PACC_P, OP_PACC_P);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_pressure_accel", kTPAccel, K_PACCEL_PB);
+    else if (no_stream(d, kTPAccel)) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_P_NS);
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_pressure_accel", kTPAccel, K_PACCEL_P);
     if (tiled(d, kTJacobi)) VFD_TILE_DISPATCH("k_jacobi_iter", kTJacobi, FN_JAC_P, OP_JAC_P);
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_jacobi_iter", kTJacobi, K_JACOBI_PB);
+    else if (no_stream(d, kTJacobi)) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_P_NS);
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_jacobi_iter", kTJacobi, K_JACOBI_P);
     VFD_LAUNCH("k_ctrl_jacobi", s, k_ctrl_jacobi<false><<<1, 256, 0, s>>>(d));
 }

@@ -33,7 +33,7 @@ void launch_pres_finish(const Dev& d, cudaStream_t s);
 cudaError_t prepare_tile_kernels();
 // Whether any solver-loop pass runs on cell tiles (then the search writes NBRC rows).
 inline bool uses_tiles(const uint8_t* tiles) {
-    return tiles[kTPAccel] != 0 || tiles[kTJacobi] != 0 || tiles[kTSpmv] != 0;
+    return tiles[kTPAccel] >= kTileMinLog2 || tiles[kTJacobi] >= kTileMinLog2 || tiles[kTSpmv] >= kTileMinLog2;
 }
 void box_map_sizes(const uint32_t res[3], uint32_t& nodes, uint32_t& cells);
 int build_box_map_gpu(const float bmin[3], const float bmax[3], bool inverted, float padding, const uint32_t res[3],
