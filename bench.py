@@ -42,33 +42,35 @@ if ROOT not in sys.path:
 METRIC = "particle-steps/s @1M, ≤0.1% density err: plain vs batched vs fwd+adjoint"
 UNIT = "particle-steps/s"
 
-# Algorithmic bytes per particle of each kernel: the fields it must read and write
-# once (float3 = 12 B, float = 4 B), neighbour fields assumed cache-served and the
-# neighbour list not counted (it is an implementation choice).
+# Algorithmic bytes per particle of each kernel, from the per-phase table of compulsory
+# FP32 SoA traffic (each field counted once per synchronisation phase, neighbour-field
+# gathers cache-served, neighbour-list and index traffic not counted), phase by phase
+# onto the kernels that carry it. Kernels outside that table count the fields they must
+# read and write once.
 ALGO_BYTES = {
-    "k_cg_spmv": 12 + 4 + 12 + 12,          # x, rho, p -> Ap (+ dot)
-    "k_cg_update": 12 * 4 + 36 + 12 * 3,    # p, g, r, Ap, Minv -> g, r, z
-    "k_cg_p": 12 * 2 + 12,                  # p, z -> p
-    "k_pressure_accel": 12 + 4 + 12,        # x, kappa -> a_p
-    "k_jacobi_iter": 12 + 12 + 4 + 4 + 4 + 4,  # x, a_p, rho_adv, alpha, kappa -> kappa, res
-    "k_density_factor": 12 + 12 + 4 * 4,    # x, v -> rho, alpha, rho_adv, kappa_v (K2-K4: divergence solve on)
-    "k_neighbors": 12 + 4,                  # x -> count (list excluded)
-    "k_visc_precond": 12 + 4 + 12 + 12 + 36 + 12 + 12,
-    "k_visc_setup": 12 + 4 + 12 + 12 + 12,
-    "k_st_classify": 12 + 16,
-    "k_boundary": 12 + 16,
-    "k_pres_finish": 12 + 4 + 12 + 12 + 12,
-    "k_pres_init": 12 + 12 + 4 + 4 + 4 + 4 + 4,
-    "k_div_finish": 12 + 4 + 12 + 4 + 12 + 12,
-    "k_rank_gather": 4 + 4 + 12 + 12 + 12 + 4 + 4 + 4 + 4 + 12 + 12 + 12 + 4 + 4,
-    "k_minmax": 12,
-    "k_keys": 12 + 4,
-    "k_slots": 4 + 4,
-    "k_st_smooth": 12 + 16 + 16 + 16,
-    "k_st_blend": 16 + 16 + 12,
-    "k_cg_p0": 12 + 12,
-    "k_visc_finish": 12 * 5,
-    "k_velocity": 12 * 3,
+    "k_boundary": 28,                       # K1
+    "k_density_factor": 32 + 32 + 56,       # K2 + K3, and K4 (the bench scene runs the divergence solve)
+    "k_pressure_accel": 44,                 # K5 / K18
+    "k_jacobi_iter": 60 + 4,                # K6 / K19 + the residual reduction
+    "k_div_finish": 64 + 12,                # K7 + K8
+    "k_visc_precond": 68 + 68,              # K12 + K13
+    "k_visc_setup": 68,                     # r0
+    "k_cg_p0": 60,                          # z0
+    "k_cg_spmv": 56,                        # SpMV + dot
+    "k_cg_update": 120,                     # alpha update
+    "k_cg_p": 36,                           # beta update
+    "k_visc_finish": 60 + 24,               # K15 + T1
+    "k_velocity": 36,                       # K16
+    "k_pres_init": 60,                      # K17
+    "k_pres_finish": 56 + 36,               # K20 + K21
+    "k_st_classify": 28,                    # surface tension, classification
+    "k_st_smooth": 44,                      # surface tension, smoothing
+    "k_st_blend": 60,                       # surface tension, blend
+    "k_keys": 20,                           # search: key generation
+    "k_slots": 4,                           # search: cell table
+    "k_rank_gather": 48,                    # search: reorder of x, v
+    "k_minmax": 12,                         # x -> grid bounds (outside the table)
+    "k_neighbors": 12 + 4,                  # x -> count (outside the table; the list excluded)
 }
 
 

@@ -196,6 +196,21 @@ def test_backward_graph_matches_host_launches():
     np.testing.assert_allclose(g["pb"], e["pb"], rtol=1e-5)
 
 
+def test_adjoint_after_the_boundary_changes():
+    """Replacing the volume maps releases the recorded run, with the copy of the simulation
+    that replays its segments (which borrowed the old maps): a later run on the new maps
+    matches a fresh simulation's."""
+    sc = _floor_scene(div=True)
+    run = GpuRun(sc, 8, 4)
+    run.gradient()  # two segments: the replaying copy is made
+    moved = O.build_box_map((0, 0, 0), (1.0, 0.9, 1.0), True, 0.0, (10, 10, 10), R_P)
+    run.sim.SetRigidBodies([moved])
+    g = run.gradient()
+    fresh = GpuRun(dict(sc, maps=[moved]), 8, 4).gradient()
+    for key in ("x0b", "v0b", "pb"):
+        np.testing.assert_allclose(g[key], fresh[key], rtol=1e-5, atol=1e-7 * np.abs(fresh[key]).max())
+
+
 # ------------------------------------------------------------ finite differences, smooth step
 @pytest.fixture(scope="module")
 def smooth():

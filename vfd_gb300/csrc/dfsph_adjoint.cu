@@ -1060,7 +1060,6 @@ struct AdjointState {
     // bank[0]: what the simulation itself records (the forward run's last segment, replays
     // without a shadow); bank[1]: what the shadow records while a backward pass reads the other
     TapeBank bank[2];
-    TapeSet* dset = nullptr;       // the simulation's recording tape set (its adjTapeSet): bank 0
     TapeSet* bset = nullptr;       // the backward pass's tape set: the bank of the segment it walks
     // A copy of the simulation (its own buffers and stream; the volume maps borrowed) that
     // replays the segment before the one the backward pass walks, into the other bank.
@@ -1133,7 +1132,19 @@ int alloc_bank(vfd_sim* s, AdjointState* A, TapeBank& B) {
     return VFD_OK;
 }
 
-// Bank 0 and the simulation's recording tape set, which addresses it.
+// The recording tape set of simulation `sim` (its recording graphs address it; it lives
+// with the simulation's buffers, so it is made again after they are reallocated).
+int recording_set(vfd_sim* sim, TapeSet*& rec) {
+    if (!sim->adjTapeSet) {
+        TapeSet* p = nullptr;
+        TRY(dalloc(sim, &p, 1));
+        sim->adjTapeSet = p;
+    }
+    rec = static_cast<TapeSet*>(sim->adjTapeSet);
+    return VFD_OK;
+}
+
+// Bank 0.
 int alloc_tape(vfd_sim* s, AdjointState* A) {
     size_t freeB = 0, totalB = 0;
     CK(cudaMemGetInfo(&freeB, &totalB));
@@ -1141,16 +1152,7 @@ int alloc_tape(vfd_sim* s, AdjointState* A) {
     if (per * A->every > freeB / 2)
         return fail(VFD_E_NOMEM, "adjoint: %zu bytes of tape for %u steps exceed half the free device memory; "
                                  "use a smaller checkpoint_every", per * A->every, A->every);
-    TRY(alloc_bank(s, A, A->bank[0]));
-    if (!s->adjTapeSet) {
-        TapeSet* p = nullptr;
-        TRY(dalloc(s, &p, 1));
-        s->adjTapeSet = p;
-    }
-    A->dset = static_cast<TapeSet*>(s->adjTapeSet);
-    TapeSet ts{A->bank[0].dsteps, A->bank[0].dcur, A->every};
-    CK(cudaMemcpy(A->dset, &ts, sizeof(ts), cudaMemcpyHostToDevice));
-    return VFD_OK;
+    return alloc_bank(s, A, A->bank[0]);
 }
 
 int save_checkpoint(vfd_sim* s, AdjointState* A, Checkpoint& c) {
@@ -1195,11 +1197,13 @@ int restore_checkpoint(vfd_sim* s, const Checkpoint& c) {
 }
 
 // `count` steps of simulation `sim` from its current state, recorded into bank B's slots
-// 0..count-1 through the recording tape set `rec` (sim's own: its recording graphs address
-// it), as CUDA graphs (one per parity) unless graphs are off; then the slots'
-// device-written fields are read back and checked. Runs on sim's stream.
-int record_segment(vfd_sim* sim, AdjointState* A, TapeSet* rec, TapeBank& B, uint32_t count) {
+// 0..count-1 through sim's recording tape set, as CUDA graphs (one per parity) unless
+// graphs are off; then the slots' device-written fields are read back and checked. Runs
+// on sim's stream.
+int record_segment(vfd_sim* sim, AdjointState* A, TapeBank& B, uint32_t count) {
     cudaStream_t st = sim->stream;
+    TapeSet* rec = nullptr;
+    TRY(recording_set(sim, rec));
     const TapeSet ts{B.dsteps, B.dcur, A->every};
     CK(cudaMemcpyAsync(rec, &ts, sizeof(ts), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(B.dcur, 0, sizeof(uint32_t), st));
@@ -1280,13 +1284,11 @@ bool ensure_shadow(vfd_sim* s, AdjointState* A) {
     std::memcpy(t->lanes, s->lanes, sizeof(t->lanes));
     std::memcpy(t->tiles, s->tiles, sizeof(t->tiles));
     std::memcpy(t->blocks, s->blocks, sizeof(t->blocks));
-    TapeSet* rec = nullptr;
-    if (ensure_ready(t) != VFD_OK || dalloc(t, &rec, 1) != VFD_OK || t->n != s->n || t->stride != s->stride) {
+    if (ensure_ready(t) != VFD_OK || t->n != s->n || t->stride != s->stride) {
         delete t;
         cudaGetLastError();
         return false;
     }
-    t->adjTapeSet = rec;
     A->shadow = t;
     A->shadowKey = key;
     return true;
@@ -1578,11 +1580,6 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
         A->n = s->n;
         A->stride = s->stride;
         TRY(alloc_tape(s, A.get()));
-    } else if (!s->adjTapeSet) {  // buffers were reallocated since: a new recording tape set
-        TapeSet* p = nullptr;
-        TRY(dalloc(s, &p, 1));
-        s->adjTapeSet = p;
-        A->dset = p;
     }
     A->steps = steps;
     A->lastRecorded = false;
@@ -1598,7 +1595,7 @@ int vfd_adjoint_forward(vfd_sim* s, uint32_t steps, uint32_t checkpoint_every, v
         // the last segment is recorded as it runs, so the backward pass starts on it
         // without a replay; a step the search had to abort (grid growth) falls back to a
         // plain run and a replay
-        const int rc = record_segment(s, A.get(), A->dset, A->bank[0], cnt);
+        const int rc = record_segment(s, A.get(), A->bank[0], cnt);
         if (rc == VFD_OK) {
             A->lastRecorded = true;
             if (stats) {
@@ -1652,7 +1649,7 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
     if (!A->lastRecorded) {
         const uint32_t cnt = A->steps - (segs - 1) * A->every;
         rc = restore_checkpoint(s, A->ckpt[segs - 1]);
-        if (rc == VFD_OK) rc = record_segment(s, A, A->dset, A->bank[0], cnt);
+        if (rc == VFD_OK) rc = record_segment(s, A, A->bank[0], cnt);
         A->replayed += cnt;
     }
     int b = 0;  // the bank holding segment k
@@ -1667,12 +1664,12 @@ int vfd_adjoint_backward(vfd_sim* s, const float* x_bar, const float* v_bar, flo
             rc = restore_checkpoint(t, A->ckpt[k - 1]);
             if (rc == VFD_OK) {
                 CK(cudaStreamWaitEvent(t->stream, A->bankRead[nb], 0));
-                rc = record_segment(t, A, static_cast<TapeSet*>(t->adjTapeSet), A->bank[nb], A->every);
+                rc = record_segment(t, A, A->bank[nb], A->every);
             }
             b = nb;
         } else {
             rc = restore_checkpoint(s, A->ckpt[k - 1]);
-            if (rc == VFD_OK) rc = record_segment(s, A, A->dset, A->bank[0], A->every);
+            if (rc == VFD_OK) rc = record_segment(s, A, A->bank[0], A->every);
         }
         A->replayed += A->every;
     }

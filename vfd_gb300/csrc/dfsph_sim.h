@@ -244,6 +244,9 @@ struct vfd_sim {
         adjBwdGraph = nullptr;
     }
     void releaseBuffers() {
+        // a recorded adjoint run (and the copy of the simulation that replays it, which
+        // borrows the volume maps) does not outlive the layout it was recorded on
+        vfd::adjoint_release(this);
         releaseGraphs();
         for (void* p : allocs) cudaFree(p);
         allocs.clear();
