@@ -660,6 +660,35 @@ def profile_case(args):
     log("particles", len(s["x"]), "stats", st, "tiles", sim.GetTiles())
 
 
+def adjoint_profile_case(args):
+    """The adjoint form's scene and run (the 33k viscous drop, 60 steps, a checkpoint every
+    10) with every kernel launched from the host, the forward and backward passes between
+    cudaProfilerStart / Stop, for a profiler's launch list (graphs with conditional nodes
+    hide their kernels from it)."""
+    import numpy as np
+    import vfd_gb300 as V
+    from vfd_gb300 import scenes
+    V.lib().vfd_set_device(0)
+    s = scenes.viscous_drop_33k()
+    n = len(s["x"])
+    rng = np.random.default_rng(scenes.config_seed(4))
+    target = s["x"].astype(np.float64) + np.array([0.05, -0.2, 0.0]) + 0.25 * s["desc"]["ParticleRadius"] * \
+        rng.standard_normal(s["x"].shape)
+    sim = V.scene_simulation(s)
+    sim.SetGraphMode(False)
+    sim.Steps(2)
+    sim.SetFluidObjects(s["x"], s["v"])
+    import torch
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    sim.AdjointForward(60, 10)
+    x, v, _ = sim.GetState()
+    sim.AdjointBackward(((2.0 / n) * (x.astype(np.float64) - target)).astype(np.float32), np.zeros_like(v))
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    log("particles", n, "adjoint", sim.AdjointStats())
+
+
 def free_port() -> int:
     import socket
     with socket.socket() as so:
@@ -754,6 +783,9 @@ def main():
     ap.add_argument("--tiles", type=int, default=-1, help="form of the three solver-loop passes instead of the "
                     "autotuner's choice: 0 = neighbour rows, 1 = rows with gradW recomputed, 3 = 2x2x2 cell tiles, "
                     "4 = 4x2x2 cell tiles")
+    ap.add_argument("--adjoint-profile-case", action="store_true",
+                    help="profiling run instead of the benchmark: the adjoint form's run with every kernel launched "
+                         "from the host")
     ap.add_argument("--graph-steps", type=int, default=4)
     ap.add_argument("--eager-steps", type=int, default=2)
     ap.add_argument("--dry-run", action="store_true",
@@ -768,6 +800,8 @@ def main():
         return run_reference(args)
     if args.profile_case:
         return profile_case(args)
+    if args.adjoint_profile_case:
+        return adjoint_profile_case(args)
     if args.dry_run:
         return dry_run(args)
     if args.precision_only:
