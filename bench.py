@@ -253,6 +253,7 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
         rng.standard_normal(s["x"].shape)
     sim = V.scene_simulation(s)
     sim.Steps(2)  # builds the step graphs
+    sim.Autotune(2)  # lanes and block sizes for this scene size, as for the main form
 
     def restart(x=None, v=None, nu=None):
         d = dict(s["desc"])

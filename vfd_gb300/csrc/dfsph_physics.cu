@@ -958,8 +958,8 @@ __global__ void k_ctrl_cg_alpha(Dev d) {
 }
 
 // Loop body 2: g += alpha p, r -= alpha Ap, |r|^2, z = M^-1 r, r . z (:722-784).
-__device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const SceneDev& S, float& rr, float& rz) {
-    const float alpha = S.cgAlpha;
+__device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const SceneDev& S, float& rr, float& rz,
+                                               float alpha) {
     const float3 pv = f3(d.CP[p]);
     const float4 g4 = d.CG[p];
     const float3 g = f3(g4) + pv * alpha;
@@ -972,15 +972,37 @@ __device__ __forceinline__ void cg_update_item(const Dev& d, uint32_t p, const S
     rz = dot_term(r, z);
 }
 
+// FOLD (a single scene on a small grid): every block forms alpha itself from the SpMV's
+// p . Ap buckets, folded by its first warp as k_ctrl_cg_alpha folds them (the same bits),
+// instead of a one-block launch between the two passes; k_ctrl_cg zeroes the buckets. On
+// tens of thousands of blocks the bucket reads cost more than the launch.
+template <bool FOLD>
 __global__ void __launch_bounds__(kBlock) k_cg_update(Dev d) {
     VFD_COUNT_LAUNCH(d);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool inRange = p < d.n && !aborted_p(d);
     const uint32_t sid = inRange ? scene_of(d, p) : 0u;
     const SceneDev& S = d.scenes[sid];
+    float alpha = S.cgAlpha;
+    if (FOLD) {
+        __shared__ float alphaBlock;
+        if (threadIdx.x < 32u) {
+            const double* q = acc_bucket(d, 0, 0, threadIdx.x);
+            double v = __ldcg(q);
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (threadIdx.x == 0) {
+                const SceneDev& S0 = d.scenes[0];
+                alphaBlock = S0.cgActive ? (float)(S0.cgAbsNew / v) : 0.0f;
+                if (blockIdx.x == 0 && S0.cgActive) d.scenes[0].cgAlpha = alphaBlock;
+            }
+        }
+        __syncthreads();
+        alpha = alphaBlock;
+    }
     const bool valid = inRange && S.cgActive;
     float rr = 0.0f, rz = 0.0f;
-    if (valid) cg_update_item(d, p, S, rr, rz);
+    if (valid) cg_update_item(d, p, S, rr, rz, alpha);
     const float v[2] = {rr, rz};
     const int slot[2] = {1, 2};
     scene_accumulate<2>(d, sid, valid, v, slot);
@@ -995,7 +1017,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_b(Dev d) {
         uint32_t sid = 0;
         const uint32_t p = in ? work_slot(d, kLoopCG, vp, sid) : 0u;
         float rr = 0.0f, rz = 0.0f;
-        if (in) cg_update_item(d, p, d.scenes[sid], rr, rz);
+        if (in) cg_update_item(d, p, d.scenes[sid], rr, rz, d.scenes[sid].cgAlpha);
         const float v[2] = {rr, rz};
         const int slot[2] = {1, 2};
         scene_accumulate_core<2>(d, chunk_scene(d, kLoopCG, base_, per_, total_), sid, in, v, slot);
@@ -1025,6 +1047,7 @@ __global__ void k_ctrl_cg(Dev d) {
     VFD_COUNT_LAUNCH(d);
     if (d.nscenes == 1) {
         if (threadIdx.x >= 32u) return;
+        *acc_bucket(d, 0, 0, threadIdx.x) = 0.0;  // p . Ap, read by every block of a folding update
         SceneDev& S = d.scenes[0];
         const bool act = S.cgActive != 0u;
         double rr = 0.0, rz = 0.0;
@@ -1500,6 +1523,8 @@ void launch_density_div_init(const Dev& d, cudaStream_t s) {
 // Whether a solver-loop pass runs on cell tiles (vfd_set_tiles / the autotuner) rather
 // than the neighbour rows; the adjoint's CG always walks rows (Dev::rowLoops).
 inline bool tiled(const Dev& d, int id) { return d.tiles[id] >= kTileMinLog2 && d.compactRows && !d.rowLoops; }
+// Single-scene CG updates on at most this many blocks form alpha themselves (k_cg_update<true>).
+constexpr uint32_t kFoldAlphaBlocks = 1024u;
 // Single-scene row pass without the per-pair gradient stream (tiles[id] == kRowsNoStream).
 inline bool no_stream(const Dev& d, int id) { return d.tiles[id] == kRowsNoStream && d.nscenes == 1; }
 
@@ -1536,14 +1561,20 @@ void launch_cg_iter(const Dev& d, cudaStream_t s) {
     else if (d.nscenes > 1) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES_BATCH, "k_cg_spmv", kTSpmv, K_SPMV_B);
     else if (no_stream(d, kTSpmv)) VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV_NS);
     else VFD_LAUNCH_MODE(VFD_LAUNCH_LANES, "k_cg_spmv", kTSpmv, K_SPMV);
-    VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
     if (d.nscenes > 1) {
+        VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
         VFD_LAUNCH("k_cg_update", s, k_cg_update_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
         VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
         VFD_LAUNCH("k_cg_p", s, k_cg_p_b<<<d.batchBlocks, kBlock, 0, s>>>(d));
         return;
     }
-    VFD_LAUNCH("k_cg_update", s, k_cg_update<<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    // a small grid forms alpha in the update's blocks (k_cg_update<true>): one launch fewer
+    if (blocks_for(d.n) <= kFoldAlphaBlocks) {
+        VFD_LAUNCH("k_cg_update", s, k_cg_update<true><<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    } else {
+        VFD_LAUNCH("k_ctrl_cg_alpha", s, k_ctrl_cg_alpha<<<1, 256, 0, s>>>(d));
+        VFD_LAUNCH("k_cg_update", s, k_cg_update<false><<<blocks_for(d.n), kBlock, 0, s>>>(d));
+    }
     VFD_LAUNCH("k_ctrl_cg", s, k_ctrl_cg<<<1, 256, 0, s>>>(d));
     VFD_LAUNCH("k_cg_p", s, k_cg_p<<<blocks_for(d.n), kBlock, 0, s>>>(d));
 }
