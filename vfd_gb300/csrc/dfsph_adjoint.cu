@@ -1045,11 +1045,11 @@ struct ShadowKey {
     vfd_desc desc{};
     uint8_t lanes[16] = {}, tiles[16] = {};
     uint16_t blocks[16] = {};
-    uint32_t n = 0, graphs = 0, analytic = 0;
+    uint32_t n = 0, graphs = 0, analytic = 0, cellCap = 0;
     bool operator==(const ShadowKey& o) const {
         return std::memcmp(&desc, &o.desc, sizeof(desc)) == 0 && std::memcmp(lanes, o.lanes, sizeof(lanes)) == 0 &&
                std::memcmp(tiles, o.tiles, sizeof(tiles)) == 0 && std::memcmp(blocks, o.blocks, sizeof(blocks)) == 0 &&
-               n == o.n && graphs == o.graphs && analytic == o.analytic;
+               n == o.n && graphs == o.graphs && analytic == o.analytic && cellCap == o.cellCap;
     }
 };
 
@@ -1248,6 +1248,7 @@ ShadowKey shadow_key(const vfd_sim* s) {
     k.n = s->n;
     k.graphs = s->graphMode && !s->graphFailed ? 1u : 0u;
     k.analytic = s->analyticKernel ? 1u : 0u;
+    k.cellCap = s->cellCap;
     return k;
 }
 
@@ -1281,6 +1282,7 @@ bool ensure_shadow(vfd_sim* s, AdjointState* A) {
     t->graphMode = key.graphs != 0u;
     t->analyticKernel = s->analyticKernel;
     t->reserve = s->reserve;
+    t->cellCap = s->cellCap;  // the search grid the simulation grew to, so replays do not abort on it
     std::memcpy(t->lanes, s->lanes, sizeof(t->lanes));
     std::memcpy(t->tiles, s->tiles, sizeof(t->tiles));
     std::memcpy(t->blocks, s->blocks, sizeof(t->blocks));
