@@ -71,26 +71,59 @@ __global__ void __launch_bounds__(kBlock) k_minmax(Dev d) {
 }
 
 // ParticleSearch::ComputeMinMax tail + ComputeCellInformation (ParticleSearch.cu:50-86),
-// per scene, then the scene cell bases (exclusive scan) and the capacity check.
+// per scene, then the scene cell bases (exclusive scan) and the capacity check. With one
+// scene the first warp folds the N1 buckets (lane b takes bucket b, an xor butterfly of
+// min / max) instead of one thread walking them: 192 dependent L2 round trips were ~27 us,
+// most of a small scene's search.
 __global__ void k_grid(Dev d) {
     VFD_COUNT_LAUNCH(d);
     __shared__ uint32_t total;
+    __shared__ int foldMin[3], foldMax[3];
+    const bool one = d.nscenes == 1;
+    if (one && threadIdx.x < 32u) {
+        const uint32_t b = threadIdx.x;
+        for (int k = 0; k < 3; k++) {  // fold the N1 buckets, reset them for the next step
+            int32_t* qa = mm_bucket(d, 0, k, b);
+            int32_t* qb = mm_bucket(d, 0, 3 + k, b);
+            int mn = *qa, mx = *qb;
+            *qa = INT_MAX;
+            *qb = INT_MIN;
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) {
+                mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            }
+            if (b == 0) {
+                foldMin[k] = mn;
+                foldMax[k] = mx;
+            }
+        }
+        *max_bucket(d, 0, 1, b) = 0u;
+    }
+    __syncthreads();
     for (uint32_t s = threadIdx.x; s < d.nscenes; s += blockDim.x) {
         SceneDev& S = d.scenes[s];
-        for (int k = 0; k < 3; k++) {  // fold the N1 buckets, reset them for the next step
-            int mn = INT_MAX, mx = INT_MIN;
-            for (uint32_t b = 0; b < kBuckets; b++) {
-                int32_t* qa = mm_bucket(d, s, k, b);
-                int32_t* qb = mm_bucket(d, s, 3 + k, b);
-                mn = min(mn, *qa);
-                mx = max(mx, *qb);
-                *qa = INT_MAX;
-                *qb = INT_MIN;
+        if (one) {
+            for (int k = 0; k < 3; k++) {
+                S.minCell[k] = foldMin[k];
+                S.maxCell[k] = foldMax[k];
             }
-            S.minCell[k] = mn;
-            S.maxCell[k] = mx;
+        } else {
+            for (int k = 0; k < 3; k++) {  // fold the N1 buckets, reset them for the next step
+                int mn = INT_MAX, mx = INT_MIN;
+                for (uint32_t b = 0; b < kBuckets; b++) {
+                    int32_t* qa = mm_bucket(d, s, k, b);
+                    int32_t* qb = mm_bucket(d, s, 3 + k, b);
+                    mn = min(mn, *qa);
+                    mx = max(mx, *qb);
+                    *qa = INT_MAX;
+                    *qb = INT_MIN;
+                }
+                S.minCell[k] = mn;
+                S.maxCell[k] = mx;
+            }
+            for (uint32_t b = 0; b < kBuckets; b++) *max_bucket(d, s, 1, b) = 0u;
         }
-        for (uint32_t b = 0; b < kBuckets; b++) *max_bucket(d, s, 1, b) = 0u;
         const float R = S.h;
         uint32_t cells = 1u;
         bool ok = S.count > 0;
