@@ -178,6 +178,23 @@ def test_warm_start_modes_agree_and_count():
         assert np.abs(g["pb"] - ref["pb"]).max() <= 1e-4 * np.abs(ref["pb"]).max()
     with pytest.raises(V.VFDError):
         run.sim.AdjointSetWarmStart(3)
+    for bad in (0.0, -0.1, 1.5, float("nan")):
+        with pytest.raises(V.VFDError):
+            run.sim.AdjointSetTolerance(bad)
+
+
+def test_tighter_adjoint_tolerance_converges_to_the_same_gradient():
+    """A tenth of the forward's tolerance changes the gradients by no more than the solves'
+    own tolerance allows, and costs iterations."""
+    sc = _floor_scene(div=True)
+    run = GpuRun(sc, 12, 4, analytic=True)
+    g1, st1 = run.gradient(), run.sim.AdjointStats()
+    run.sim.AdjointSetTolerance(0.1)
+    g2, st2 = run.gradient(), run.sim.AdjointStats()
+    assert st2["ViscositySolverIterations"] >= st1["ViscositySolverIterations"]
+    for key in ("v0b", "x0b"):
+        rel = np.linalg.norm(g1[key] - g2[key]) / np.linalg.norm(g2[key])
+        assert rel < 1e-4, (key, rel)
 
 
 def test_backward_graph_matches_host_launches():
