@@ -144,6 +144,42 @@ def test_steps_track_fp32_oracle():
         _compare_step(g, o, h, median_tol=1e-6 * (k + 1) ** 2)
 
 
+def test_empty_fluid_steps_and_returns_an_empty_state():
+    s = scenes.small_dam_break(n_side=4)
+    s["x"] = np.zeros((0, 3), np.float32)
+    s["v"] = np.zeros((0, 3), np.float32)
+    g = V.scene_simulation(s)
+    g.Steps(3)
+    g.OnUpdate()
+    x, v, a = g.GetState()
+    assert x.shape == v.shape == a.shape == (0, 3)
+    assert g.GetParticleCount() == 0
+
+
+@pytest.mark.parametrize("where", ["free", "wall"])
+def test_single_particle_matches_fp32_oracle(where):
+    """One particle: no fluid neighbours, density below rest, so both solves stop at
+    their minimum iteration count; near the floor and the back wall the volume map
+    pushes it away (the boundary density and gradient paths with nothing else)."""
+    s = scenes.small_dam_break(n_side=4)
+    r = s["desc"]["ParticleRadius"]
+    y = 0.15 if where == "free" else scenes.wall_gap(r) + 1.2 * r
+    s["x"] = np.array([[0.2, y, 0.1]], np.float32)
+    s["v"] = np.zeros_like(s["x"])
+    g, o = pair(s, 32)
+    h = 4 * r
+    for _ in range(8):
+        sg, so = g.OnUpdate(), o.step()
+        for k in ("PressureSolverIterationCount", "DivergenceSolverIterationCount"):
+            assert sg[k] == so[k], (k, sg[k], so[k])
+        assert sg["TimeStepSize"] == pytest.approx(so["TimeStepSize"], rel=1e-6)
+        xg, vg, _ = g.GetState()
+        xo, vo, _ = o.state()
+        assert xg.shape == (1, 3)
+        assert np.abs(xg - xo).max() < 1e-5 * h, (xg, xo)
+        assert np.abs(vg - vo).max() < 1e-4, (vg, vo)
+
+
 def test_twenty_steps_track_fp64_oracle():
     s = scenes.dam_break_8k(n_side=12, box_scale=(2, 1, 1))
     g, o = pair(s, 64)
