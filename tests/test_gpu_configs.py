@@ -174,6 +174,45 @@ def test_viscous_dam_break_64k_20_steps():
     assert_within_fp32_gap(g, o32, o64, h, "viscous_dam_break_64k_20", per_particle=False)
 
 
+def test_viscous_dam_break_1M_full_size():
+    """The 1M configuration at its full size (100^3 = 1,000,000 particles), 60 steps on the
+    GPU: one-step parity with the FP32 oracle from the GPU's carried state at steps 0 and
+    59 (the checks of one_step_parity), and along the whole run the pressure solve's exit
+    error <= 0.1 % of rho0 (PressureSolverError <= 1), every particle finite and inside
+    the box."""
+    s = scenes.viscous_dam_break()
+    assert len(s["x"]) == 1_000_000
+    gm, om = maps_for(s)
+    g = V.scene_simulation(s, maps=gm)
+    checks = {}
+    for k in range(60):
+        if k in (0, 59):
+            st, sg, _ = one_step_parity(g, s, om, surface_tension=True)
+            checks[k] = st
+        else:
+            sg = g.OnUpdate()
+        assert sg["PressureSolverError"] <= 1.0 + 1e-6
+    x, v, _ = g.GetState()
+    box = np.asarray(s["boxes"][0]["max"], np.float64)
+    assert np.isfinite(x).all() and np.isfinite(v).all()
+    assert (x > -1e-3).all() and (x < box + 1e-3).all()
+    report("viscous_dam_break_1M_one_step", {str(k): v for k, v in checks.items()})
+
+
+def test_jet_column_8m_full_size():
+    """The jet-coiling configuration at its full size (the 8.0M-particle pool with the jet
+    column in place, 8,015,618 particles; surface tension scaled as in the bench), one-step
+    parity with the FP32 oracle from the GPU's carried state after 3 GPU steps."""
+    s = scenes.jet_column_8m()
+    assert len(s["x"]) > 8_000_000
+    gm, om = maps_for(s)
+    g = V.scene_simulation(s, maps=gm)
+    for _ in range(3):
+        assert g.OnUpdate()["PressureSolverError"] <= 1.0 + 1e-6
+    st, sg, so = one_step_parity(g, s, om, surface_tension=True)
+    report("jet_column_8m_one_step", {"3": st, "iterations": {k: [int(sg[k]), int(so[k])] for k in ITER_KEYS}})
+
+
 def test_viscous_dam_break_64k_without_surface_tension_tracks_fp64():
     """The same 64,000 particles with surface tension off, 12 steps: smooth enough
     that positions compare particle by particle with the FP64 oracle (mean and 99th
