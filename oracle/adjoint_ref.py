@@ -17,7 +17,8 @@ adjoint:
   * divergence and pressure Jacobi solves (DFSPHImplementation.cu:443-575) with the
     reference's loop conditions, unrolled in the derivative;
   * the Weiler viscosity system A g = v (DFSPHImplementation.cu:577-808) solved exactly
-    by a sparse direct solve, differentiated by the implicit function theorem;
+    by a sparse direct solve (on large scenes by CG to a relative residual of 1e-13; A is
+    symmetric), differentiated by the implicit function theorem;
   * the CFL step (DFSPHImplementation.cu:395-441) through its argmax particle.
 The reference itself ships no derivative, so this module is pinned by its own
 central differences in FP64 (tests/test_adjoint_ref.py).
@@ -32,6 +33,43 @@ from . import oracle as O
 
 EPS = 1.0e-5           # Core/Math/Math.h:6
 FLT_MAX = float(np.finfo(np.float32).max)
+
+
+# Above these sizes the all-pairs distance matrix and the direct solve give way to a k-d
+# tree and CG (the same pair set and the same solution to rounding).
+_ALL_PAIRS_MAX = 4096
+_DIRECT_MAX = 30000
+
+
+def _pairs(x, h):
+    """(I, J) of every pair with 0 < |x_i - x_j|^2 < h^2, row-major order."""
+    if len(x) <= _ALL_PAIRS_MAX:
+        d2 = np.sum((x[:, None, :] - x[None, :, :]) ** 2, axis=2)
+        return np.nonzero((d2 > 0) & (d2 < h * h))
+    from scipy.spatial import cKDTree
+    pr = cKDTree(x).query_pairs(h * (1.0 + 1e-9), output_type="ndarray")
+    I = np.concatenate([pr[:, 0], pr[:, 1]])
+    J = np.concatenate([pr[:, 1], pr[:, 0]])
+    d2 = np.sum((x[I] - x[J]) ** 2, axis=1)
+    keep = (d2 > 0) & (d2 < h * h)
+    I, J = I[keep], J[keep]
+    order = np.lexsort((J, I))
+    return I[order], J[order]
+
+
+def _solve_spd(A, b):
+    """A x = b for the symmetric positive definite viscosity matrix."""
+    if A.shape[0] <= _DIRECT_MAX:
+        return spla.spsolve(A.tocsc(), b)
+    A = A.tocsr()
+    M = sp.diags(1.0 / A.diagonal())
+    try:
+        x, info = spla.cg(A, b, rtol=1e-13, atol=0.0, maxiter=10000, M=M)
+    except TypeError:  # scipy < 1.12
+        x, info = spla.cg(A, b, tol=1e-13, atol=0.0, maxiter=10000, M=M)
+    if info != 0:
+        raise RuntimeError(f"viscosity CG did not converge ({info})")
+    return x
 
 
 class Kernel:
@@ -194,8 +232,7 @@ class Step:
         P, k = self.P, self.k
         n = self.n = len(x_in)
         # neighbour search on the positions before the boundary kernel
-        d2 = np.sum((x_in[:, None, :] - x_in[None, :, :]) ** 2, axis=2)
-        I, J = np.nonzero((d2 > 0) & (d2 < P.h * P.h))
+        I, J = _pairs(x_in, P.h)
         self.I, self.J = I, J
         self.cnt = np.bincount(I, minlength=n)
         if self.cnt.max() >= 70:
@@ -256,7 +293,7 @@ class Step:
                 self.zeroG = True
             else:
                 A = self._visc_matrix(dt_o)
-                g = spla.spsolve(A.tocsc(), b.reshape(-1)).reshape(n, 3)
+                g = _solve_spd(A, b.reshape(-1)).reshape(n, 3)
             self.gv = g
             acc = P.g[None, :] + (g - v1) / dt_o
         else:
@@ -407,7 +444,7 @@ class Step:
         # viscosity: A lambda = g_bar
         if P.visc and not self.zeroG:
             A = self._visc_matrix(dto)
-            lam = spla.spsolve(A.T.tocsc(), gbar.reshape(-1)).reshape(n, 3)
+            lam = _solve_spd(A.T, gbar.reshape(-1)).reshape(n, 3)
             vbar += lam
             X_, rho_, dtob_, nub, nubb = self._visc_derivative(lam, dto)
             X += X_
