@@ -69,3 +69,24 @@ def test_reference_viscosity_gradient(problem, k, name):
     lo[name], hi[name] = nu - eps, nu + eps
     fd = (_loss(problem, desc=hi) - _loss(problem, desc=lo)) / (2 * eps)
     assert _rel(float(problem["pb"][k]), fd) < 1e-5
+
+
+def test_large_scene_paths_match_the_exact_ones(problem, monkeypatch):
+    """The k-d tree pair search gives the all-pairs search's pairs in the same order, and
+    the CG solve of the viscosity system the direct solve's solution (to 1e-10), on the
+    scene above with the size thresholds lowered so both paths run."""
+    rng = np.random.default_rng(11)
+    x = rng.random((1500, 3)) * 0.4
+    h = 0.05
+    exact = R._pairs(x, h)
+    monkeypatch.setattr(R, "_ALL_PAIRS_MAX", 100)
+    tree = R._pairs(x, h)
+    for a, b in zip(exact, tree):
+        np.testing.assert_array_equal(a, b)
+    step = problem["roll"].steps[-1]
+    A = step._visc_matrix(step.dto)
+    b = rng.standard_normal(A.shape[0])
+    direct = R._solve_spd(A, b)
+    monkeypatch.setattr(R, "_DIRECT_MAX", 10)
+    cg = R._solve_spd(A, b)
+    assert np.linalg.norm(cg - direct) <= 1e-10 * np.linalg.norm(direct)
