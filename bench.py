@@ -280,6 +280,7 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
     restart()
     t0 = time.perf_counter()
     sim.AdjointForward(steps, every)
+    t_rec = time.perf_counter() - t0  # the forward run with its checkpoints and tape (synchronous)
     x, v, _ = sim.GetState()
     xb = (2.0 / n) * (x.astype(np.float64) - target)
     x0b, v0b, pb = sim.AdjointBackward(xb.astype(np.float32), np.zeros_like(v))
@@ -342,6 +343,8 @@ def adjoint_form(V, scenes, steps: int = 60, every: int = 10, analytic_check: bo
                         f"checkpoint every {every}",
             "forward": n * steps / t_fwd, "fwd_adjoint": n * steps / t_adj, "adjoint_over_forward": t_adj / t_fwd,
             "forward_s": t_fwd, "fwd_adjoint_s": t_adj,
+            # the two passes apart: the recording forward run, and the reverse pass (replays included)
+            "recording_forward_s": t_rec, "backward_s": t_adj - t_rec, "backward_over_forward": (t_adj - t_rec) / t_fwd,
             "every_step_recorded": {"fwd_adjoint_s": t_all, "adjoint_over_forward": t_all / t_fwd},
             "backward": {"replayed_steps": adj_stats["ReplayedSteps"],
                          "viscosity_cg_iterations": adj_stats["ViscositySolverIterations"],
