@@ -1,19 +1,23 @@
-// Stand-in for the reference's precompiled header when its neighbour-search kernels
-// (Simulation/DFSPH/ParticleSearch/ParticleSearchKernels.cu) are compiled as plain C++
-// for the CPU. Test infrastructure only: it lets the oracle's search be checked against
-// the reference's own kernel code, run here with one emulated CUDA thread at a time.
+// Stand-in for the reference's precompiled header when its kernels -- the neighbour
+// search (Simulation/DFSPH/ParticleSearch/ParticleSearchKernels.cu) and the step
+// (Simulation/DFSPH/DFSPHKernels.cu) -- are compiled as plain C++ for the CPU. Test
+// infrastructure only: it lets the oracle be checked against the reference's own kernel
+// code, run here with one emulated CUDA thread at a time.
 //
 // Provides what those kernels use: the CUDA function qualifiers (as nothing), the
 // built-in thread indices (set by the driver before each emulated thread), the three
-// atomics they call (sequential, returning the old value), and the glm subset they and
-// the DFSPHParticle / SearchInfo structs use (glm_subset.h).
+// atomics the search calls (sequential, returning the old value), the standard headers
+// the reference's precompiled header brings in, and the glm subset (glm_subset.h).
 #ifndef VFD_REF_SEARCH_PCH_H
 #define VFD_REF_SEARCH_PCH_H
 
+#include <algorithm>
+#include <cfloat>
 #include <climits>
 #include <cmath>
 #include <cstdint>
 #include <limits>
+#include <vector>
 
 #define __global__
 #define __device__

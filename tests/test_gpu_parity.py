@@ -144,6 +144,25 @@ def test_steps_track_fp32_oracle():
         _compare_step(g, o, h, median_tol=1e-6 * (k + 1) ** 2)
 
 
+@pytest.mark.parametrize("name", ["plain", "viscous", "surface_tension"])
+def test_cuda_step_equals_reference_kernels(name):
+    """The CUDA step against the reference's own step kernels (DFSPHKernels.cu compiled for
+    the CPU, tests/golden/ref_step.npz; see tests/test_ref_step_golden.py): five steps of a
+    1,000-particle dam break from the same inputs and volume maps. Iteration counts and time
+    steps as for the oracle; positions within 2.5e-5 h at the median and 1e-3 h at the
+    maximum, the bounds of the CUDA step against the FP32 oracle over five steps."""
+    import test_ref_step_golden as T
+
+    scene = T.M.cases()[name]
+    g = V.scene_simulation(scene, maps=T.M.box_maps(scene))
+
+    def state():
+        x, v, _ = g.GetState()
+        return x, v
+
+    T.check_against_fixture(name, scene, g.OnUpdate, state, g.GetField, pos_median=2.5e-5, pos_max=1e-3)
+
+
 def test_empty_fluid_steps_and_returns_an_empty_state():
     s = scenes.small_dam_break(n_side=4)
     s["x"] = np.zeros((0, 3), np.float32)

@@ -1,0 +1,69 @@
+"""The FP32 oracle's step against the reference's own step kernels.
+
+tests/golden/ref_step.npz holds what the reference's DFSPHKernels.cu computes (compiled
+for the CPU with a CUDA/glm stand-in, its host loop restated with the oracle's
+deterministic reduction rules; tests/golden/make_ref_step.py) over five steps of three
+seeded 1,000-particle dam breaks: plain, with the viscosity solve, and with viscosity and
+surface tension. The oracle restates the same kernels, with the GPU's fast-math square
+roots and divisions where the reference's CUDA build has them (the CPU build of the
+reference rounds those exactly). Tolerances: every solver iteration count and surface-
+tension sample count equal; time steps within 1e-6 relative; densities and DFSPH factors
+after the first step within 1e-6 relative at the median, 1e-3 at the 99th percentile and
+1e-2 at the maximum (a boundary sample's table index can flip with the rounding of a square
+root, and a factor's sum of squared gradients then moves most); positions after the first
+and the last step within 1e-6 h at the median and 2e-4 h at the maximum; velocities within
+1e-4 m/s at the median. The CUDA step is held to the same fixture in
+tests/test_gpu_parity.py."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from vfd_gb300 import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_ref_step as M  # noqa: E402
+
+GOLDEN = np.load(os.path.join(HERE, "golden", "ref_step.npz"))
+ITERS = ("DivergenceSolverIterationCount", "PressureSolverIterationCount", "ViscositySolverIterationCount")
+
+
+def check_against_fixture(name, scene, step, state, field=None, pos_median=1e-6, pos_max=2e-4):
+    """Runs `step()` M.STEPS times (returning the stats dict) and compares with the
+    reference's kernels: state() -> (x, v) after a step, field(kind) -> densities or factors;
+    position tolerances in h."""
+    g = {k[len(name) + 1:]: GOLDEN[k] for k in GOLDEN.files if k.startswith(name + "/")}
+    h = 4 * scene["desc"]["ParticleRadius"]
+    for k in range(M.STEPS):
+        st = step()
+        for key in ITERS:
+            assert int(st[key]) == int(g[key][k]), (name, k, key, st[key], g[key][k])
+        assert st["TimeStepSize"] == pytest.approx(float(g["TimeStepSize"][k]), rel=1e-6)
+        if k == 0 and field is not None:
+            for kind, ref in ((_abi.FIELD_DENSITY, g["density1"]), (_abi.FIELD_FACTOR, g["factor1"])):
+                rel = np.abs(field(kind) - ref) / np.maximum(np.abs(ref), 1e-30)
+                assert np.median(rel) < 1e-6 and np.quantile(rel, 0.99) < 1e-3 and rel.max() < 1e-2, \
+                    (name, kind, np.median(rel), np.quantile(rel, 0.99), rel.max())
+        if k in (0, M.STEPS - 1):
+            x, v = state()
+            dx = np.abs(np.asarray(x, np.float64) - g[f"x{k + 1}"]).max(axis=1) / h
+            dv = np.abs(np.asarray(v, np.float64) - g[f"v{k + 1}"]).max(axis=1)
+            assert np.median(dx) < pos_median and dx.max() < pos_max, (name, k, np.median(dx), dx.max())
+            assert np.median(dv) < 1e-4, (name, k, np.median(dv))
+
+
+@pytest.mark.parametrize("name", sorted(M.cases()))
+def test_oracle_step_equals_reference_kernels(name):
+    scene = M.cases()[name]
+    o = O.scene_oracle(scene, 32, maps=M.box_maps(scene))
+
+    def state():
+        x, v, _ = o.state()
+        return x, v
+
+    check_against_fixture(name, scene, o.step, state, o.field)
+    if name == "surface_tension":
+        assert int(GOLDEN[name + "/SurfaceTensionSampleCount"][-1]) > 0
