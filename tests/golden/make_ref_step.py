@@ -3,11 +3,13 @@
 Builds oracle/_ref/libvfd_refstep.so (the reference's Simulation/DFSPH/DFSPHKernels.cu and
 its search kernels compiled for the CPU with a CUDA/glm stand-in header, beside a
 restatement of their host loop, oracle/ref_step/driver.cpp; recipe in oracle/Makefile,
-target `ref`) and runs it on three seeded 1,000-particle dam breaks -- plain, with the
-viscosity solve, and with viscosity and surface tension -- for five steps each, with the
-volume maps of the oracle's box-map builder. Writes tests/golden/ref_step.npz: per case
-and step the solver iteration counts, errors and time step, the densities and DFSPH factors
-after the first step, and the positions and velocities after the first and the last step.
+target `ref`) and runs it for five steps on three seeded 1,000-particle dam breaks -- plain, with the
+viscosity solve, and with viscosity and surface tension -- and on two benchmark workloads,
+the 8,000-particle dam break and the 1M configuration's parameters at 64,000 particles,
+with the volume maps of the oracle's box-map builder. Writes tests/golden/ref_step.npz:
+per case and step the solver iteration counts, errors and time step, the densities and
+DFSPH factors after the first step, and the positions and velocities after the first and
+the last step (of every 8th / 32nd particle in the two larger cases).
 
 Usage: python tests/golden/make_ref_step.py VFD_ROOT
 """
@@ -42,7 +44,15 @@ def cases() -> dict:
         "plain": scenes.small_dam_break(n_side=10),
         "viscous": scenes.small_dam_break(n_side=10, viscosity=0.05),
         "surface_tension": scenes.small_dam_break(n_side=10, viscosity=0.01, surface_tension=0.05),
+        # two benchmark workloads: the 8,000-particle dam break as configured, and the 1M
+        # configuration's parameters (viscosity, surface tension, CSD) at 40^3 particles
+        "dam_break_8k": scenes.dam_break_8k(),
+        "viscous_dam_break_64k": scenes.viscous_dam_break(n_side=40),
     }
+
+
+# Every STRIDE-th particle's positions and velocities are kept for the larger cases.
+STRIDE = {"dam_break_8k": 8, "viscous_dam_break_64k": 32}
 
 
 def box_maps(scene) -> list:
@@ -64,7 +74,7 @@ def load(vfd_root: str):
     return lib
 
 
-def run(lib, scene) -> dict:
+def run(lib, scene, stride: int = 1) -> dict:
     maps = box_maps(scene)
     desc = _abi.make_desc(**scene["desc"])
     h = lib.ref_step_create(C.byref(desc))
@@ -84,9 +94,9 @@ def run(lib, scene) -> dict:
             x, v = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
             rho, fac = np.zeros(n, np.float32), np.zeros(n, np.float32)
             lib.ref_step_get_state(h, x.ctypes.data, v.ctypes.data, None, rho.ctypes.data, fac.ctypes.data)
-            out[f"x{k + 1}"], out[f"v{k + 1}"] = x, v
+            out[f"x{k + 1}"], out[f"v{k + 1}"] = x[::stride], v[::stride]
             if k == 0:
-                out["density1"], out["factor1"] = rho, fac
+                out["density1"], out["factor1"] = rho[::stride], fac[::stride]
     lib.ref_step_destroy(h)
     return {k: np.asarray(v) for k, v in out.items()}
 
@@ -97,7 +107,7 @@ def main():
     lib = load(sys.argv[1])
     arrays = {}
     for name, scene in cases().items():
-        for key, val in run(lib, scene).items():
+        for key, val in run(lib, scene, STRIDE.get(name, 1)).items():
             arrays[f"{name}/{key}"] = val
     np.savez_compressed(OUT, **arrays)
     print(f"wrote {OUT} ({os.path.getsize(OUT)} bytes)")
