@@ -4,12 +4,13 @@ Builds oracle/_ref/libvfd_refstep.so (the reference's Simulation/DFSPH/DFSPHKern
 its search kernels compiled for the CPU with a CUDA/glm stand-in header, beside a
 restatement of their host loop, oracle/ref_step/driver.cpp; recipe in oracle/Makefile,
 target `ref`) and runs it for five steps on three seeded 1,000-particle dam breaks -- plain, with the
-viscosity solve, and with viscosity and surface tension -- and on two benchmark workloads,
-the 8,000-particle dam break and the 1M configuration's parameters at 64,000 particles,
+viscosity solve, and with viscosity and surface tension -- and on three benchmark
+workloads, the 8,000-particle dam break, the 1M configuration's parameters at 64,000
+particles and the 33,401-particle viscous drop,
 with the volume maps of the oracle's box-map builder. Writes tests/golden/ref_step.npz:
 per case and step the solver iteration counts, errors and time step, the densities and
 DFSPH factors after the first step, and the positions and velocities after the first and
-the last step (of every 8th / 32nd particle in the two larger cases).
+the last step (of every 8th or 32nd particle in the three larger cases).
 
 Usage: python tests/golden/make_ref_step.py VFD_ROOT
 """
@@ -48,11 +49,13 @@ def cases() -> dict:
         # configuration's parameters (viscosity, surface tension, CSD) at 40^3 particles
         "dam_break_8k": scenes.dam_break_8k(),
         "viscous_dam_break_64k": scenes.viscous_dam_break(n_side=40),
+        # the differentiable workload: the 33,401-particle viscous drop
+        "viscous_drop_33k": scenes.viscous_drop_33k(),
     }
 
 
 # Every STRIDE-th particle's positions and velocities are kept for the larger cases.
-STRIDE = {"dam_break_8k": 8, "viscous_dam_break_64k": 32}
+STRIDE = {"dam_break_8k": 8, "viscous_dam_break_64k": 32, "viscous_drop_33k": 32}
 
 
 def box_maps(scene) -> list:

@@ -144,11 +144,12 @@ def test_steps_track_fp32_oracle():
         _compare_step(g, o, h, median_tol=1e-6 * (k + 1) ** 2)
 
 
-@pytest.mark.parametrize("name", ["plain", "viscous", "surface_tension", "dam_break_8k", "viscous_dam_break_64k"])
+@pytest.mark.parametrize("name", ["plain", "viscous", "surface_tension", "dam_break_8k", "viscous_dam_break_64k",
+                                  "viscous_drop_33k"])
 def test_cuda_step_equals_reference_kernels(name):
     """The CUDA step against the reference's own step kernels (DFSPHKernels.cu compiled for
     the CPU, tests/golden/ref_step.npz; see tests/test_ref_step_golden.py): five steps of
-    three 1,000-particle dam breaks and two benchmark workloads from the same inputs and
+    three 1,000-particle dam breaks and three benchmark workloads from the same inputs and
     volume maps. Iteration counts and time steps as for the oracle; positions within 2.5e-5 h
     at the median and 1e-3 h at the maximum, the bounds of the CUDA step against the FP32
     oracle over five steps (0.05 h at the maximum with surface tension at 64k particles,

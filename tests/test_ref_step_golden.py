@@ -4,9 +4,9 @@ tests/golden/ref_step.npz holds what the reference's DFSPHKernels.cu computes (c
 for the CPU with a CUDA/glm stand-in, its host loop restated with the oracle's
 deterministic reduction rules; tests/golden/make_ref_step.py) over five steps of three
 seeded 1,000-particle dam breaks (plain, with the viscosity solve, and with viscosity and
-surface tension) and of two benchmark workloads (the 8,000-particle dam break as
-configured, and the 1M configuration's parameters at 64,000 particles; every 8th / 32nd
-particle kept). The oracle restates the same kernels, with the GPU's fast-math square
+surface tension) and of three benchmark workloads (the 8,000-particle dam break as
+configured, the 1M configuration's parameters at 64,000 particles and the 33,401-particle
+viscous drop; every 8th or 32nd particle kept). The oracle restates the same kernels, with the GPU's fast-math square
 roots and divisions where the reference's CUDA build has them (the CPU build of the
 reference rounds those exactly). Tolerances: every solver iteration count and surface-
 tension sample count equal; time steps within 1e-3 relative (the adaptive step follows
