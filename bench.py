@@ -183,7 +183,8 @@ def dam_break_config(n_side: int) -> dict:
 def batched_form(V, scenes, steps: int, warmup: int, plain_every: int, ws: int = 1, rank: int = 0):
     """The uneven-scene batch (256 scenes, 2k-64k particles each) advanced as one
     simulation, against the plain step run scene by scene on every `plain_every`-th
-    scene. Both in particle-steps/s, timed with CUDA events on the library's stream.
+    scene, each autotuned first. Both in particle-steps/s, timed with CUDA events on the
+    library's stream.
     With several ranks the scenes are split by particle count (vfd_gb300.partition),
     each rank advances its share as one batch, and the whole batch's particle-steps are
     divided by the slowest rank's time."""
@@ -208,7 +209,10 @@ def batched_form(V, scenes, steps: int, warmup: int, plain_every: int, ws: int =
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
+    # both sides autotuned (lanes, forms, block sizes), as the main form is
     sim = V.batch_simulation(batch, maps)
+    sim.Steps(2)
+    sim.Autotune(2)
     if ws > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -225,6 +229,8 @@ def batched_form(V, scenes, steps: int, warmup: int, plain_every: int, ws: int =
     plain_n, plain_ms = 0, 0.0
     for k in range(0, len(batch), plain_every):
         one = V.scene_simulation(batch[k], maps=maps[k])
+        one.Steps(2)
+        one.Autotune(2)
         plain_ms += run(one, steps)
         plain_n += counts[k]
         del one
@@ -765,7 +771,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched-scene measurement")
     ap.add_argument("--no-jet", action="store_true", help="skip the 8M-particle jet-coiling form")
-    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=200, help="steps of the uneven-scene batch (the "
+                    "configuration's 200)")
     ap.add_argument("--precision-steps", type=int, default=5,
                     help="steps per mode of the FP64-vs-FP32 precision form on the 8M jet scene")
     ap.add_argument("--precision-only", action="store_true",
