@@ -390,6 +390,7 @@ def jet_form(V, scenes, steps: int = 8, warmup: int = 2):
         f = s["inflow"]
         em = emitter.InflowEmitter(f["center"], f["direction"], f["radius"], f["speed"], r)
         em.run(sim, warmup)
+        sim.Autotune(2)  # lanes, forms and block sizes for this scene, as for the main form (state restored)
         torch.cuda.synchronize()
         errs, its = [], []
         t0 = time.perf_counter()
