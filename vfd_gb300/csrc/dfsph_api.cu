@@ -862,15 +862,18 @@ int run_steps(vfd_sim* s, uint32_t count, vfd_step_stats* stats, bool wait) {
 
 int check_sim(const vfd_sim* s) { return s ? VFD_OK : fail(VFD_E_ARG, "null handle"); }
 
-int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out) {
+// The scatters export through one staging buffer in stream order; wait = false leaves the
+// copy to a later synchronisation of the stream (the caller's).
+int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out, bool wait) {
     const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     k_export3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs].PIDc, dsrc, s->dStage, b, cnt);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, s->dStage, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    if (wait) CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
+int scatter_vec(vfd_sim* s, uint32_t scene, const float4* dsrc, float* out) { return scatter_vec(s, scene, dsrc, out, true); }
 
 int scatter_scalar(vfd_sim* s, uint32_t scene, const float* dsrc, float* out, int comp = -1, const float4* d4 = nullptr) {
     const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
@@ -892,15 +895,18 @@ int gather_vec(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
 }
 
 // Positions (absolute in the caller's frame whatever the storage mode).
-int scatter_pos(vfd_sim* s, uint32_t scene, const float4* dsrc, const float4* anchors, float* out) {
-    if (!s->cellRel) return scatter_vec(s, scene, dsrc, out);
+int scatter_pos(vfd_sim* s, uint32_t scene, const float4* dsrc, const float4* anchors, float* out, bool wait) {
+    if (!s->cellRel) return scatter_vec(s, scene, dsrc, out, wait);
     const uint32_t b = s->sceneBegin[scene], cnt = s->scenes[scene].count();
     if (cnt == 0) return VFD_OK;
     k_export_pos<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(s->dev[s->cs], dsrc, anchors, s->dStage, b, cnt);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, s->dStage, sizeof(float) * 3 * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    if (wait) CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
+}
+int scatter_pos(vfd_sim* s, uint32_t scene, const float4* dsrc, const float4* anchors, float* out) {
+    return scatter_pos(s, scene, dsrc, anchors, out, true);
 }
 
 int gather_pos(vfd_sim* s, uint32_t scene, const float* in, float4* ddst) {
@@ -1455,9 +1461,11 @@ int vfd_scene_get_state(vfd_sim* s, uint32_t scene, float* x, float* v, float* a
     TRY(ensure_ready(s));
     if (s->fp64Mode) return fp64_get_state(s, nullptr, nullptr, x, v, a);
     const Dev& d = s->dev[s->cs];
-    if (x) TRY(scatter_pos(s, scene, d.XN, d.XN, x));
-    if (v) TRY(scatter_vec(s, scene, d.Vc, v));
-    if (a) TRY(scatter_vec(s, scene, d.A, a));
+    // the three exports share the staging buffer in stream order; one wait for all
+    if (x) TRY(scatter_pos(s, scene, d.XN, d.XN, x, false));
+    if (v) TRY(scatter_vec(s, scene, d.Vc, v, false));
+    if (a) TRY(scatter_vec(s, scene, d.A, a, false));
+    CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
 
@@ -1491,8 +1499,8 @@ int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
         else k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d.PIDc, s->dStage, d.XN, b, cnt);
     }
     if (v) k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d.PIDc, s->dStage2, d.Vc, b, cnt);
+    // the inputs were read by the copies before the check; the imports run in stream order
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
 
