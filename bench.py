@@ -866,13 +866,15 @@ def main():
         if ws > 1:
             dist.barrier()
         torch.cuda.synchronize()
-        torch.cuda.profiler.start()  # `ncu --profile-from-start off` records the timed steps only
+        if args.eager:  # `ncu --profile-from-start off` then records the timed steps' kernels
+            torch.cuda.profiler.start()
         e0.record(stream)
         sim.StepsAsync(k)
         e1.record(stream)
         st = sim.Synchronize()
         torch.cuda.synchronize()
-        torch.cuda.profiler.stop()
+        if args.eager:
+            torch.cuda.profiler.stop()
         if ws > 1:
             dist.barrier()
         return e0.elapsed_time(e1), st, sim.GetLaunchCount()
@@ -914,8 +916,15 @@ def main():
     e2e = {"value": n * ws * e2e_steps / float(t.item()), "unit": UNIT, "steps": e2e_steps, "h2d_bytes_per_step": 24 * n,
            "d2h_bytes_per_step": 36 * n}
 
-    # per-kernel event timing of eager launches -> dominant kernel and roofline
+    # per-kernel event timing of eager launches -> dominant kernel and roofline; by default
+    # `ncu --profile-from-start off` records exactly these launches (the kernel shares' list)
+    torch.cuda.synchronize()
+    if not args.eager:
+        torch.cuda.profiler.start()
     prof = sim.ProfileKernels(3)
+    torch.cuda.synchronize()
+    if not args.eager:
+        torch.cuda.profiler.stop()
     tot = sum(v[1] for v in prof.values())
     name, (cnt, kms) = max(prof.items(), key=lambda kv: kv[1][1])
     peak, peak_kind = measured_peaks()
