@@ -325,8 +325,7 @@ int vfd_simulate(vfd_sim* sim, vfd_frame_callback cb, void* user);
 int vfd_get_state(vfd_sim* sim, float* x, float* v, float* a);
 
 /* Overwrites positions and velocities (original order; vel may be NULL) of the running state;
- * VFD_E_NAN for non-finite input. The arrays are read before the call returns; the
- * overwrite runs on the simulation's stream ahead of its next work. */
+ * VFD_E_NAN for non-finite input. */
 int vfd_set_state(vfd_sim* sim, const float* x, const float* v);
 
 /*

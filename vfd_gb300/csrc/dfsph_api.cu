@@ -1499,8 +1499,9 @@ int vfd_set_state(vfd_sim* s, const float* x, const float* v) {
         else k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d.PIDc, s->dStage, d.XN, b, cnt);
     }
     if (v) k_import3<<<blocks_for(cnt, 256), 256, 0, s->stream>>>(d.PIDc, s->dStage2, d.Vc, b, cnt);
-    // the inputs were read by the copies before the check; the imports run in stream order
     CK(cudaGetLastError());
+    // calls that write the state with default-stream copies (restore, upload) must find it settled
+    CK(cudaStreamSynchronize(s->stream));
     return VFD_OK;
 }
 
