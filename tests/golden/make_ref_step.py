@@ -66,6 +66,11 @@ def box_maps(scene) -> list:
 
 def load(vfd_root: str):
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={vfd_root}"], check=True)
+    return open_lib()
+
+
+def open_lib():
+    """The built reference-step library (oracle/_ref/libvfd_refstep.so) with its signatures."""
     lib = C.CDLL(LIB)
     lib.ref_step_create.restype = C.c_void_p
     lib.ref_step_create.argtypes = [C.POINTER(_abi.vfd_desc)]

@@ -44,3 +44,13 @@ def test_oracle_search_equals_reference_kernels(name):
     for i, row in ref["rows"].items():
         i = int(i)
         assert b["list"][b["offsets"][i]:b["offsets"][i] + b["counts"][i]].tolist() == row
+
+
+@pytest.mark.skipif(not os.path.exists(M.LIB), reason="the reference's search kernels are built only where its "
+                                                      "sources are (oracle/Makefile target ref)")
+@pytest.mark.parametrize("name", ["dam_break_8k", "dense_cells_and_cap"])
+def test_reference_search_library_reproduces_the_fixture(name):
+    """The committed digests are what the compiled reference kernels compute: rerun."""
+    x, h = M.cases()[name]
+    r = M.run_reference(x, h)
+    assert {k: M.digest(v) for k, v in r.items()} == GOLDEN["cases"][name]["sha256"]

@@ -83,3 +83,13 @@ def test_oracle_step_equals_reference_kernels(name):
     check_against_fixture(name, scene, o.step, state, o.field)
     if name == "surface_tension":
         assert int(GOLDEN[name + "/SurfaceTensionSampleCount"][-1]) > 0
+
+
+@pytest.mark.skipif(not os.path.exists(M.LIB), reason="the reference's step kernels are built only where its "
+                                                      "sources are (oracle/Makefile target ref)")
+@pytest.mark.parametrize("name", ["plain", "viscous"])
+def test_reference_step_library_reproduces_the_fixture(name):
+    """The committed fixture is what the compiled reference kernels compute: rerun, bit for bit."""
+    out = M.run(M.open_lib(), M.cases()[name], M.STRIDE.get(name, 1))
+    for key, val in out.items():
+        np.testing.assert_array_equal(val, GOLDEN[f"{name}/{key}"], err_msg=key)
